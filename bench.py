@@ -1,0 +1,301 @@
+"""Benchmark: Gray-Scott on the 1024 x 1024 jittered grid (1,048,576 vertices).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = the reference's Gray-Scott advance_time (CPUSolver.cpp:127-145):
+mass-weighted reaction right-hand side for u and v, then the two SPD solves
+(M/dt + D K) x = b with Jacobi-PCG, FP32 fields and FP64-accurate reductions.
+Workload (synthetic, seeded): Du 2e-5, Dv 1e-5, F 0.037, k 0.06, dt 1, Neumann,
+u = 1, v = 0 with 20 squares of side 0.05 at u = 0.5, v = 0.25, plus U(-0.01,
+0.01) noise.  Timed steps continue from the warm-up state.
+
+Prints one JSON line (rank 0).  `value` times each step on the device with
+CUDA events on the solver's stream, with the L2 cache flushed (256 MiB write)
+before every timed step; `e2e` times set_values (host -> device) +
+advance_time(1) + get_values (device -> host) through the C ABI with
+page-locked host buffers.  With --gpus N > 1 (torchrun) every rank steps its
+own replica of the workload: the path does not shard across GPUs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fea-visualizer_gb300"))
+
+GRID_N = 1024
+PARAMS = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+METRIC = "Gray-Scott 1M-vert steps/s at rel-L2<=1e-5, batched vs plain; CG SpMV HBM GB/s"
+
+
+def workload():
+    from fea_gb300 import meshgen as mg
+    xyz, tri = mg.jittered_grid(GRID_N, seed=0)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=0)
+    return xyz, tri, u0, v0
+
+
+def config(V, T, nnz, extra=None):
+    c = {"workload": f"gray-scott {GRID_N}x{GRID_N} jittered grid", "vertices": V, "triangles": T,
+         "nnz": nnz, "reaction": "mass-weighted (consistent)", "bc": "neumann", "dt": 1.0, "Du": 2e-5,
+         "Dv": 1e-5, "F": 0.037, "k": 0.06, "cg": "jacobi-pcg, tol FLT_EPSILON relative, FP64-accurate dots",
+         "l2": "flushed before every timed step (256 MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def spmv_bytes(N, nnz, nfields=2):
+    """Algorithmic bytes of one paired CSR SpMV launch: values (4 B per field)
+    and a 4 B column index per stored entry, row pointers, the gathered vector
+    read once and the product written once (4 B per field per row)."""
+    return nnz * (4 * nfields + 4) + 4 * (N + 1) + 2 * 4 * nfields * N
+
+
+def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads):
+    """The reference's Eigen-semantics CPU step (the oracle's FP32 port):
+    A = M/dt + D K rebuilt every step, zero initial guess, tol = FLT_EPSILON."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    S = O.System(xyz, tri, bc=O.NEUMANN, dtype="float32")
+    p = O.params(O.REACTION_DIFFUSION, 1.0, Du=2e-5, Dv=1e-5, F=0.037, k=0.06, reaction_mode=1,
+                 tol=1.1920928955078125e-07, warm_start=0, nthreads=nthreads)
+    u, v = S.gather(u0), S.gather(v0)
+    u, v, *_ = S.step(p, u, v, nsteps=1)  # warm-up (page-in)
+    t0 = time.perf_counter()
+    u, v, _, it, _ = S.step(p, u, v, nsteps=nsteps)
+    dt = time.perf_counter() - t0
+    return nsteps / dt, it, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU path timed on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    xyz, tri, u0, v0 = workload()
+    nthreads = os.cpu_count() or 1
+    sps, _, _ = cpu_sample(xyz, tri, u0, v0, max(1, args.warmup), nthreads)  # warm-up steps
+    t0 = time.perf_counter()
+    sps, it, dt = cpu_sample(xyz, tri, u0, v0, args.steps, nthreads)
+    value = args.steps / dt
+    nnz = None
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(int(xyz.shape[0]), int(tri.shape[0]), nnz, {"parallelism": "cpu threads"}),
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{args.steps} full steps of the workload, oracle FP32 port "
+                                       f"(Eigen semantics: zero guess, per-step operator build), OpenMP"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+    import fea_gb300 as F
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    xyz, tri, u0, v0 = workload()
+    p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, **PARAMS)
+    s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=F.FP32, params=p)
+    lanes = s.autotune()
+    info = s.info
+    N, nnz, V = info.num_unknowns, info.nnz, info.num_vertices
+    s.set_fields(u0, v0)
+    stream = torch.cuda.ExternalStream(s.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # warm-up
+    s.advance_time(args.warmup)
+    s.synchronize()
+    st0 = s.status()
+
+    # timed: K steps, L2 flushed before each, CUDA events on the solver stream
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                ev[k][0].record(stream)
+                s.advance_time(1)
+                ev[k][1].record(stream)
+        s.synchronize()
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    st1 = s.status()
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    iters = st1.total_iterations - st0.total_iterations
+    launches = args.steps * 3 + 3 * iters + 2 * args.steps  # rhs/refine/stepctl + 3 per CG iteration + start/check
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # one K-step graph launch (no flush between steps) for reference
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        s.advance_time(args.steps)
+        e1.record(stream)
+    s.synchronize()
+    one_launch_ms = e0.elapsed_time(e1)
+
+    # dominant kernel: the paired SpMV, timed alone on the same operator
+    spmv_ms = s.time_spmv(reps=20, flush_l2=True)
+    spmv_warm_ms = s.time_spmv(reps=20, flush_l2=False)
+    peak, peak_kind = measured_peak_hbm()
+    bytes_spmv = spmv_bytes(N, nnz)
+    achieved = bytes_spmv / (spmv_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with host buffers (values = v, CPUSolver.cpp:130,144)
+    hv = torch.empty(V, dtype=torch.float32).pin_memory()
+    hout = torch.empty(V, dtype=torch.float32).pin_memory()
+    _, vv = s.get_fields()
+    hv.numpy()[:] = vv
+    vals = hv.numpy()
+    outv = hout.numpy()
+    s.set_values(vals)
+    s.advance_time(1)
+    s.synchronize()
+    lib = F.load()
+    import ctypes as C
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        F.binding.check(lib.fea_set_values(s._h, C.c_void_p(vals.ctypes.data)))
+        F.binding.check(lib.fea_advance_time(s._h, 1))
+        F.binding.check(lib.fea_get_values(s._h, C.c_void_p(outv.ctypes.data)))
+        vals[:] = outv
+    e2e_s = time.perf_counter() - t0
+    e2e = world * args.steps / e2e_s
+
+    flags = s.status().flags
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        cps, cit, cdt = cpu_sample(xyz, tri, u0, v0, args.cpu_steps, nthreads)
+        cpu = {"value": cps, "unit": "steps/s", "cores": nthreads, "kind": "port",
+               "sample": f"{args.cpu_steps} full steps of the same workload ({cdt:.1f} s), oracle FP32 port "
+                         f"with Eigen semantics (zero guess, per-step operator build, tol FLT_EPSILON), "
+                         f"{cit} CG iterations"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(int(V), int(tri.shape[0]), int(nnz),
+                             {"parallelism": "replicas" if world > 1 else "single gpu", "lanes_per_row": lanes,
+                              "cg_iterations_per_step": iters / args.steps,
+                              "one_launch_ms_per_step": one_launch_ms / args.steps}),
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": 4 * V},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_cg_spmv (paired u,v SpMV + p.q)",
+                         "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": spmv_ms,
+                         "ms_per_launch_l2_warm": spmv_warm_ms, "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "status_flags": int(flags),
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,706 @@
+// cg.cu -- the per-step hot path: fused right-hand side, Jacobi-preconditioned
+// CG and the step loop, all inside one CUDA graph.
+//
+// Reference semantics: CPUSolver::advance_time (CPUSolver.cpp:64-146) solves
+// A x = b with Eigen::ConjugateGradient<.., Lower|Upper> and its diagonal
+// preconditioner (:65): stop when |r|^2 < tol^2 |b|^2, at most max_iter
+// iterations.  The compute-shader path (cgm.glsl:104-149, GPUSolver.cpp:326-361)
+// runs the same recurrences with a host round trip per stage; here the loop is
+// a CUDA graph WHILE node whose condition the update kernel sets on the device.
+//
+// Per CG iteration, three kernels:
+//   k_cg_spmv    q = A p (CSR, `LANES` lanes per row) and p.q
+//   k_cg_update  x += alpha p, r -= alpha q, z = D^-1 r, r.z and r.r,
+//                convergence test and the loop condition
+//   k_cg_dir     p = z + beta p
+// Inner products: FP32 products are accumulated exactly as float-float pairs
+// per thread and per warp, then in FP64 across warps and blocks (the GB300's
+// FP64 pipe is narrow, so FP64 arithmetic is kept off the per-element path).
+// The block partials are combined by the last block to finish, in a fixed
+// order, so every reduction is deterministic.
+#include <cmath>
+
+#include "fea_internal.cuh"
+
+namespace fea {
+
+namespace {
+
+// ---- accumulators -------------------------------------------------------------
+template <typename R>
+struct Acc;
+
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ void sub(const Acc& o) { s -= o.s; }
+    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ void shfl_add(int off) { s += __shfl_xor_sync(0xffffffffu, s, off); }
+};
+
+// float-float: value = hi + lo with |lo| <= ulp(hi)/2 (Knuth two-sum plus the
+// exact product error from fma); intrinsics keep the compiler from fusing.
+template <>
+struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        const float l = __fadd_rn(lo, err);
+        hi = __fadd_rn(s, l);
+        lo = __fsub_rn(l, __fsub_rn(hi, s));
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        const float e = __fmaf_rn(a, b, -p);
+        add(p);
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ void sub(const Acc& o) {
+        add(-o.hi);
+        lo = __fsub_rn(lo, o.lo);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ void shfl_add(int off) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+        add(oh);
+        lo = __fadd_rn(lo, ol);
+    }
+};
+
+// Block reduction of NV accumulators, then the grid-wide last-block step.
+// Returns true in the last block, with totals in out[] valid in thread 0.
+template <typename R, int NV>
+__device__ __forceinline__ bool grid_reduce(Acc<R> (&acc)[NV], double* part, int stride, unsigned int* ticket,
+                                            double (&out)[NV]) {
+    __shared__ double sm[32 * NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
+        if (lane == 0) sm[wid * NV + k] = acc[k].value();
+    }
+    __syncthreads();
+    double x[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) x[k] = 0.0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < nw; w++)
+#pragma unroll
+            for (int k = 0; k < NV; k++) x[k] += sm[w * NV + k];
+    }
+    __syncthreads();
+    // x[] holds the block totals in thread 0; the last block sums them.
+    return last_block_commit<NV>(x, part, stride, ticket, sm, out);
+}
+
+__device__ __forceinline__ void raise_flags(RunState* run, unsigned int f) {
+    const unsigned int w = __reduce_or_sync(0xffffffffu, f);
+    if (w && (threadIdx.x & 31) == 0) {
+        atomicOr(&run->flags, w);
+        __threadfence();
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ unsigned int check_value(R x) {
+    unsigned int f = 0;
+    if (x > (R)1e4f) f |= FEA_STATUS_BLOWUP;  // CPUSolver.cpp:43
+    if (!isfinite(x)) f |= FEA_STATUS_NONFINITE;
+    return f;
+}
+
+template <typename R>
+__device__ __forceinline__ R ldg(const R* p) {
+    return __ldg(p);
+}
+template <typename R, int NF>
+__device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
+    if constexpr (sizeof(FV<R, NF>) == 4) {
+        const float t = __ldg(reinterpret_cast<const float*>(p));
+        FV<R, NF> o;
+        memcpy(&o, &t, 4);
+        return o;
+    } else if constexpr (sizeof(FV<R, NF>) == 8) {
+        const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+        FV<R, NF> o;
+        memcpy(&o, &t, 8);
+        return o;
+    } else {
+        const double2 t = __ldg(reinterpret_cast<const double2*>(p));
+        FV<R, NF> o;
+        memcpy(&o, &t, 16);
+        return o;
+    }
+}
+
+// Threads are grouped LANES per CSR row; a warp covers 32/LANES consecutive
+// rows per pass, so its loads of values and column indices are contiguous.
+template <int LANES>
+struct RowMap {
+    static constexpr int RPW = 32 / LANES;
+    int sub, grp;
+    int64_t warp, nwarps;
+    __device__ __forceinline__ RowMap() {
+        const int lane = threadIdx.x & 31;
+        sub = lane & (LANES - 1);
+        grp = lane / LANES;
+        warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    }
+};
+
+// ---- kernels --------------------------------------------------------------------
+
+template <typename R, int NF, int LANES>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(StepArgs<R, NF> a) {
+    CgState* cg = a.cg;
+    int act[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) act[f] = cg->active[f];
+    Acc<R> acc[NF];
+    RowMap<LANES> m;
+    for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
+        const int64_t row = base + m.grp;
+        R s[NF];
+#pragma unroll
+        for (int f = 0; f < NF; f++) s[f] = 0;
+        if (row < a.N) {
+            const int32_t e1 = ldg(a.rp + row + 1);
+            for (int32_t e = ldg(a.rp + row) + m.sub; e < e1; e += LANES) {
+                const FV<R, NF> av = ldfv(a.A + e);
+                const FV<R, NF> pv = ldfv(a.p + ldg(a.col + e));
+#pragma unroll
+                for (int f = 0; f < NF; f++) s[f] = fma(av.v[f], pv.v[f], s[f]);
+            }
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int f = 0; f < NF; f++) s[f] += __shfl_xor_sync(0xffffffffu, s[f], o);
+        if (m.sub == 0 && row < a.N) {
+            FV<R, NF> qv;
+            const FV<R, NF> pr = a.p[row];
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                qv.v[f] = s[f];
+                acc[f].add_prod(pr.v[f], s[f]);
+            }
+            a.q[row] = qv;
+        }
+    }
+    double tot[NF];
+    if (grid_reduce<R, NF>(acc, a.part, a.part_stride, a.tickets + 0, tot) && threadIdx.x == 0) {
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            if (!act[f]) continue;
+            cg->pq[f] = tot[f];
+            const double al = cg->rz[f] / tot[f];
+            if (!(tot[f] > 0.0) || !isfinite(al)) {
+                cg->active[f] = 0;
+                cg->iters[f] = cg->iter;
+                atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            } else {
+                cg->alpha[f] = al;
+            }
+        }
+    }
+}
+
+template <typename R, int NF>
+__global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
+    CgState* cg = a.cg;
+    int act[NF];
+    R alpha[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        act[f] = cg->active[f];
+        alpha[f] = act[f] ? (R)cg->alpha[f] : (R)0;
+    }
+    Acc<R> acc[2 * NF];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        FV<R, NF> x = a.x[i], r = a.r[i];
+        const FV<R, NF> p = a.p[i], q = a.q[i], d = ldfv(a.dinv + i);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            if (act[f]) {
+                x.v[f] = fma(alpha[f], p.v[f], x.v[f]);
+                r.v[f] = fma(-alpha[f], q.v[f], r.v[f]);
+            }
+            const R z = d.v[f] * r.v[f];
+            acc[f].add_prod(r.v[f], z);
+            acc[NF + f].add_prod(r.v[f], r.v[f]);
+        }
+        a.x[i] = x;
+        a.r[i] = r;
+    }
+    double tot[2 * NF];
+    if (grid_reduce<R, 2 * NF>(acc, a.part, a.part_stride, a.tickets + 1, tot) && threadIdx.x == 0) {
+        const int it = cg->iter + 1;
+        cg->iter = it;
+        int any = 0;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            if (!act[f]) continue;
+            const double rz = tot[f], rr = tot[NF + f];
+            cg->rr[f] = rr;
+            if (!isfinite(rr)) {
+                cg->active[f] = 0;
+                cg->iters[f] = it;
+                atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            } else if (rr < cg->thr[f]) {
+                cg->active[f] = 0;
+                cg->iters[f] = it;
+            } else {
+                cg->beta[f] = rz / cg->rz[f];
+                cg->rz[f] = rz;
+                any = 1;
+            }
+        }
+        const int cont = any && it < cg->max_iter;
+        if (any && !cont) {
+            atomicOr(&a.run->flags, FEA_STATUS_NOT_CONVERGED);
+#pragma unroll
+            for (int f = 0; f < NF; f++)
+                if (cg->active[f]) {
+                    cg->active[f] = 0;
+                    cg->iters[f] = it;
+                }
+        }
+        cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+    }
+}
+
+template <typename R, int NF>
+__global__ void __launch_bounds__(kBlock) k_cg_dir(StepArgs<R, NF> a) {
+    const CgState* cg = a.cg;
+    int act[NF];
+    R beta[NF];
+    bool any = false;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        act[f] = cg->active[f];
+        beta[f] = (R)cg->beta[f];
+        any = any || act[f];
+    }
+    if (!any) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        const FV<R, NF> r = a.r[i], d = ldfv(a.dinv + i);
+        FV<R, NF> p = a.p[i];
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            if (act[f]) p.v[f] = fma(beta[f], p.v[f], d.v[f] * r.v[f]);
+        a.p[i] = p;
+    }
+}
+
+// Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
+// previous solution), z = D^-1 r, p = z, and the CG set-up scalars.  Also the
+// has_numerical_instability test of the state entering the step.
+template <typename R, int NF, int EQ, int LANES>
+__global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
+    const StepParams P = *a.prm;
+    const R dt = (R)P.dt;
+    Acc<R> dots[3 * NF];  // |b|^2, |r|^2, r.z per field
+    unsigned int flags = 0;
+    RowMap<LANES> m;
+    for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
+        const int64_t row = base + m.grp;
+        Acc<R> bs[NF], ax[NF];
+        if (row < a.N) {
+            const int32_t e1 = ldg(a.rp + row + 1);
+            for (int32_t e = ldg(a.rp + row) + m.sub; e < e1; e += LANES) {
+                const int32_t c = ldg(a.col + e);
+                const FV<R, NF> av = ldfv(a.A + e);
+                const FV<R, NF> xc = a.x[c];
+                const R me = ldg(a.M + e);
+                if constexpr (EQ == EQ_HEAT) {
+                    bs[0].add_prod(div_rn(me, dt), xc.v[0]);
+                } else if constexpr (EQ == EQ_ADV_EXPLICIT) {
+                    bs[0].add_prod(div_rn(me, dt), xc.v[0]);
+                    bs[0].add_prod((R)P.adv_sign * ldg(a.Adv + e), xc.v[0]);
+                } else if constexpr (EQ == EQ_WAVE_REF) {
+                    bs[0].add_prod(div_rn(me, dt), xc.v[0]);
+                    bs[0].add_prod(-(R)P.c2 * ldg(a.K + e), a.u[c]);
+                } else if constexpr (EQ == EQ_WAVE_NEWMARK) {
+                    const R uc = a.u[c], vc = a.v[c];
+                    const R ut = uc + dt * vc + dt * dt * ((R)0.5 - (R)P.beta) * xc.v[0];
+                    bs[0].add_prod(-(R)P.c2 * ldg(a.K + e), ut);
+                } else if constexpr (EQ == EQ_NEWMARK_INIT) {
+                    bs[0].add_prod(-(R)P.c2 * ldg(a.K + e), a.u[c]);
+                } else if constexpr (EQ == EQ_GS_REF) {
+#pragma unroll
+                    for (int f = 0; f < NF; f++) bs[f].add_prod(div_rn(me, dt), xc.v[f]);
+                } else {  // EQ_GS_CONSISTENT
+                    const R u = xc.v[0], v = xc.v[NF - 1];
+                    const R uvv = u * (v * v);
+                    const R wu = u / dt - uvv + (R)P.F * ((R)1 - u);
+                    const R wv = v / dt + uvv - ((R)P.F + (R)P.k) * v;
+                    bs[0].add_prod(me, wu);
+                    bs[NF - 1].add_prod(me, wv);
+                }
+#pragma unroll
+                for (int f = 0; f < NF; f++) ax[f].add_prod(av.v[f], xc.v[f]);
+            }
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                bs[f].shfl_add(o);
+                ax[f].shfl_add(o);
+            }
+        if (m.sub == 0 && row < a.N) {
+            const FV<R, NF> xr = a.x[row];
+            if constexpr (EQ == EQ_GS_REF) {  // nodal reaction, CPUSolver.cpp:134,137
+                const R u = xr.v[0], v = xr.v[NF - 1];
+                const R uvv = u * (v * v);
+                bs[0].add(-uvv);
+                bs[0].add((R)P.F * ((R)1 - u));
+                bs[NF - 1].add(uvv);
+                bs[NF - 1].add(-((R)P.F + (R)P.k) * v);
+            }
+            if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_NEWMARK_INIT) {
+                flags |= check_value(a.u[row]) | check_value(a.v[row]);
+            } else if constexpr (EQ == EQ_WAVE_NEWMARK) {
+                const R ur = a.u[row], vr = a.v[row], ar = xr.v[0];
+                flags |= check_value(ur) | check_value(vr);
+                a.ut[row] = ur + dt * vr + dt * dt * ((R)0.5 - (R)P.beta) * ar;
+                a.vt[row] = vr + dt * ((R)1 - (R)P.gamma) * ar;
+            } else {
+#pragma unroll
+                for (int f = 0; f < NF; f++) flags |= check_value(xr.v[f]);
+            }
+            const FV<R, NF> d = ldfv(a.dinv + row);
+            FV<R, NF> bv, rv, pv;
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                bv.v[f] = (R)bs[f].value();
+                bs[f].sub(ax[f]);
+                rv.v[f] = (R)bs[f].value();
+                pv.v[f] = d.v[f] * rv.v[f];
+                dots[f].add_prod(bv.v[f], bv.v[f]);
+                dots[NF + f].add_prod(rv.v[f], rv.v[f]);
+                dots[2 * NF + f].add_prod(rv.v[f], pv.v[f]);
+            }
+            a.b[row] = bv;
+            a.r[row] = rv;
+            a.p[row] = pv;
+        }
+    }
+    raise_flags(a.run, flags);
+    double tot[3 * NF];
+    if (grid_reduce<R, 3 * NF>(dots, a.part, a.part_stride, a.tickets + 2, tot) && threadIdx.x == 0) {
+        CgState* cg = a.cg;
+        RunState* run = a.run;
+        const int stop = (atomicOr(&run->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
+        cg->stop = stop;
+        cg->iter = 0;
+        cg->max_iter = run->max_iter;
+        int any = 0;
+        const double tiny = sizeof(R) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            const double bb = tot[f], rr = tot[NF + f], rz = tot[2 * NF + f];
+            double thr = run->tol * run->tol * bb;
+            cg->bb[f] = bb;
+            cg->thr[f] = thr < tiny ? tiny : thr;
+            cg->rr[f] = rr;
+            cg->rz[f] = rz;
+            cg->iters[f] = 0;
+            cg->active[f] = (!stop && bb > 0.0 && rr >= cg->thr[f]) ? 1 : 0;
+            any |= cg->active[f];
+        }
+        cudaGraphSetConditional(a.cond, any ? 1u : 0u);
+    }
+}
+
+// After the first CG loop: zero right-hand sides give x = 0 (Eigen's
+// early exit), then one FP64-accurate true-residual pass r = b - A x.  Fields
+// whose true residual is still above the threshold restart CG from there.
+template <typename R, int NF, int LANES>
+__global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
+    CgState* cg = a.cg;
+    const int stop = cg->stop;
+    const int refine = a.run->refine && cg->iter < cg->max_iter && !stop;
+    int zero[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) zero[f] = !stop && !(cg->bb[f] > 0.0);
+    Acc<R> dots[2 * NF];
+    RowMap<LANES> m;
+    for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
+        const int64_t row = base + m.grp;
+        Acc<R> ax[NF];
+        if (refine && row < a.N) {
+            const int32_t e1 = ldg(a.rp + row + 1);
+            for (int32_t e = ldg(a.rp + row) + m.sub; e < e1; e += LANES) {
+                const FV<R, NF> av = ldfv(a.A + e);
+                const FV<R, NF> xc = a.x[ldg(a.col + e)];
+#pragma unroll
+                for (int f = 0; f < NF; f++) ax[f].add_prod(av.v[f], xc.v[f]);
+            }
+        }
+        if (refine) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1)
+#pragma unroll
+                for (int f = 0; f < NF; f++) ax[f].shfl_add(o);
+        }
+        if (m.sub == 0 && row < a.N) {
+            bool zany = false;
+#pragma unroll
+            for (int f = 0; f < NF; f++) zany |= zero[f] != 0;
+            if (zany) {
+                FV<R, NF> xr = a.x[row];
+#pragma unroll
+                for (int f = 0; f < NF; f++)
+                    if (zero[f]) xr.v[f] = 0;
+                a.x[row] = xr;
+            }
+            if (refine) {
+                const FV<R, NF> bv = a.b[row], d = ldfv(a.dinv + row);
+                FV<R, NF> rv, pv;
+#pragma unroll
+                for (int f = 0; f < NF; f++) {
+                    Acc<R> t;
+                    t.add(bv.v[f]);
+                    t.sub(ax[f]);
+                    rv.v[f] = (R)t.value();
+                    pv.v[f] = d.v[f] * rv.v[f];
+                    dots[f].add_prod(rv.v[f], rv.v[f]);
+                    dots[NF + f].add_prod(rv.v[f], pv.v[f]);
+                }
+                a.r[row] = rv;
+                a.p[row] = pv;
+            }
+        }
+    }
+    double tot[2 * NF];
+    if (grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot) && threadIdx.x == 0) {
+        int any = 0;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            cg->active[f] = 0;
+            if (refine && !zero[f] && cg->bb[f] > 0.0) {
+                cg->rr[f] = tot[f];
+                if (tot[f] >= cg->thr[f]) {
+                    cg->rz[f] = tot[NF + f];
+                    cg->active[f] = 1;
+                    any = 1;
+                }
+            }
+        }
+        cudaGraphSetConditional(a.cond, any ? 1u : 0u);
+    }
+}
+
+// Wave updates after the solve.
+template <typename R, int NF, int EQ>
+__global__ void __launch_bounds__(kBlock) k_post(StepArgs<R, NF> a) {
+    if (a.cg->stop) return;
+    const StepParams P = *a.prm;
+    const R dt = (R)P.dt;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        if constexpr (EQ == EQ_WAVE_REF) {  // u = u + v dt, CPUSolver.cpp:118
+            a.u[i] = a.u[i] + a.x[i].v[0] * dt;
+        } else if constexpr (EQ == EQ_WAVE_NEWMARK) {
+            const R acc = a.x[i].v[0];
+            a.u[i] = a.ut[i] + (R)P.beta * dt * dt * acc;
+            a.v[i] = a.vt[i] + (R)P.gamma * dt * acc;
+        }
+    }
+}
+
+// Step bookkeeping and the outer loop condition (single thread).
+template <typename R, int NF>
+__global__ void k_stepctl(StepArgs<R, NF> a) {
+    CgState* cg = a.cg;
+    RunState* run = a.run;
+    if (!cg->stop) {
+        run->steps_done += 1;
+        run->steps_left -= 1;
+        run->total_iters += cg->iter;
+        for (int f = 0; f < NF; f++) {
+            run->last_iters[f] = cg->iters[f];
+            run->last_rel[f] = cg->bb[f] > 0.0 ? sqrt(cg->rr[f] / cg->bb[f]) : 0.0;
+        }
+    }
+    const int cont = !cg->stop && run->steps_left > 0 &&
+                     !(run->flags & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE));
+    cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+}
+
+template <typename R, int NF>
+__global__ void k_start(StepArgs<R, NF> a) {
+    cudaGraphSetConditional(a.cond, a.run->steps_left > 0 ? 1u : 0u);
+}
+
+// has_numerical_instability of the state after the last step.
+template <typename R, int NF, int EQ>
+__global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
+    unsigned int flags = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK || EQ == EQ_NEWMARK_INIT) {
+            flags |= check_value(a.u[i]) | check_value(a.v[i]);
+        } else {
+            const FV<R, NF> x = a.x[i];
+#pragma unroll
+            for (int f = 0; f < NF; f++) flags |= check_value(x.v[f]);
+        }
+    }
+    raise_flags(a.run, flags);
+}
+
+// ---- graph construction ----------------------------------------------------------
+
+template <typename... P>
+cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
+                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
+    auto local = arg;
+    void* argv[] = {(void*)&local};
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)fn;
+    kp.gridDim = dim3((unsigned)grid);
+    kp.blockDim = dim3((unsigned)block);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = argv;
+    cudaGraphNode_t n;
+    FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
+    return n;
+}
+
+cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t n;
+    FEA_CUDA_TRY(cudaGraphAddNode(&n, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, &np));
+    *body = np.conditional.phGraph_out[0];
+    return n;
+}
+
+int g_max_grid = 0;
+
+int stream_grid(int64_t n) {
+    int64_t g = ceil_div(n, kBlock);
+    if (g > max_grid_blocks()) g = max_grid_blocks();
+    return (int)(g < 1 ? 1 : g);
+}
+
+template <int LANES>
+int row_grid(int64_t n) {
+    const int64_t rpb = (kBlock / 32) * (32 / LANES);  // rows per block per pass
+    int64_t g = ceil_div(n, rpb);
+    if (g > max_grid_blocks()) g = max_grid_blocks();
+    return (int)(g < 1 ? 1 : g);
+}
+
+template <typename R, int NF, int LANES>
+void add_cg_body(cudaGraph_t body, const StepArgs<R, NF>& a) {
+    cudaGraphNode_t n1 = add_kernel(body, nullptr, k_cg_spmv<R, NF, LANES>, row_grid<LANES>(a.N), kBlock, a);
+    cudaGraphNode_t n2 = add_kernel(body, n1, k_cg_update<R, NF>, stream_grid(a.N), kBlock, a);
+    add_kernel(body, n2, k_cg_dir<R, NF>, stream_grid(a.N), kBlock, a);
+}
+
+template <typename R, int NF, int EQ, int LANES>
+void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base) {
+    cudaGraph_t top;
+    FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
+    G.graph = top;
+    cudaGraphConditionalHandle h_step;
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_step, top, 0, 0));
+    StepArgs<R, NF> a = base;
+    a.cond = h_step;
+    cudaGraphNode_t n = add_kernel(top, nullptr, k_start<R, NF>, 1, 1, a);
+    cudaGraph_t step_body;
+    n = add_while(top, n, h_step, &step_body);
+    add_kernel(top, n, k_final_check<R, NF, EQ>, stream_grid(a.N), kBlock, a);
+
+    cudaGraphConditionalHandle h_cg1, h_cg2;
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_cg1, step_body, 0, 0));
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_cg2, step_body, 0, 0));
+    StepArgs<R, NF> a1 = base, a2 = base;
+    a1.cond = h_cg1;
+    a2.cond = h_cg2;
+    cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, LANES>, row_grid<LANES>(a.N), kBlock, a1);
+    cudaGraph_t cg_body1, cg_body2;
+    s = add_while(step_body, s, h_cg1, &cg_body1);
+    add_cg_body<R, NF, LANES>(cg_body1, a1);
+    s = add_kernel(step_body, s, k_refine<R, NF, LANES>, row_grid<LANES>(a.N), kBlock, a2);
+    s = add_while(step_body, s, h_cg2, &cg_body2);
+    add_cg_body<R, NF, LANES>(cg_body2, a2);
+    if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
+        s = add_kernel(step_body, s, k_post<R, NF, EQ>, stream_grid(a.N), kBlock, a);
+    add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, a);
+    FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
+}
+
+template <typename R, int NF, int EQ>
+void build_graph_lanes(StepGraph& G, const StepArgs<R, NF>& a, int lanes) {
+    switch (lanes) {
+    case 2: build_graph_t<R, NF, EQ, 2>(G, a); break;
+    case 4: build_graph_t<R, NF, EQ, 4>(G, a); break;
+    case 16: build_graph_t<R, NF, EQ, 16>(G, a); break;
+    default: build_graph_t<R, NF, EQ, 8>(G, a); break;
+    }
+}
+
+}  // namespace
+
+int max_grid_blocks() {
+    if (g_max_grid == 0) g_max_grid = num_sms() * 8;  // 8 resident 256-thread blocks per SM
+    return g_max_grid;
+}
+
+template <typename R, int NF>
+void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int lanes) {
+    G.destroy();
+    G.kind = kind;
+    G.lanes = lanes;
+    if constexpr (NF == 1) {
+        switch (kind) {
+        case EQ_HEAT: build_graph_lanes<R, 1, EQ_HEAT>(G, a, lanes); break;
+        case EQ_ADV_EXPLICIT: build_graph_lanes<R, 1, EQ_ADV_EXPLICIT>(G, a, lanes); break;
+        case EQ_WAVE_REF: build_graph_lanes<R, 1, EQ_WAVE_REF>(G, a, lanes); break;
+        case EQ_WAVE_NEWMARK: build_graph_lanes<R, 1, EQ_WAVE_NEWMARK>(G, a, lanes); break;
+        case EQ_NEWMARK_INIT: build_graph_lanes<R, 1, EQ_NEWMARK_INIT>(G, a, lanes); break;
+        default: throw Error{FEA_ERR_UNSUPPORTED};
+        }
+    } else {
+        switch (kind) {
+        case EQ_GS_REF: build_graph_lanes<R, 2, EQ_GS_REF>(G, a, lanes); break;
+        case EQ_GS_CONSISTENT: build_graph_lanes<R, 2, EQ_GS_CONSISTENT>(G, a, lanes); break;
+        default: throw Error{FEA_ERR_UNSUPPORTED};
+        }
+    }
+}
+
+template <typename R, int NF>
+void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st) {
+    switch (lanes) {
+    case 2: k_cg_spmv<R, NF, 2><<<row_grid<2>(a.N), kBlock, 0, st>>>(a); break;
+    case 4: k_cg_spmv<R, NF, 4><<<row_grid<4>(a.N), kBlock, 0, st>>>(a); break;
+    case 16: k_cg_spmv<R, NF, 16><<<row_grid<16>(a.N), kBlock, 0, st>>>(a); break;
+    default: k_cg_spmv<R, NF, 8><<<row_grid<8>(a.N), kBlock, 0, st>>>(a); break;
+    }
+    FEA_CHECK_LAUNCH();
+}
+
+template void build_step_graph<float, 1>(StepGraph&, const StepArgs<float, 1>&, int, int);
+template void build_step_graph<float, 2>(StepGraph&, const StepArgs<float, 2>&, int, int);
+template void build_step_graph<double, 1>(StepGraph&, const StepArgs<double, 1>&, int, int);
+template void build_step_graph<double, 2>(StepGraph&, const StepArgs<double, 2>&, int, int);
+template void launch_spmv_probe<float, 1>(const StepArgs<float, 1>&, int, cudaStream_t);
+template void launch_spmv_probe<float, 2>(const StepArgs<float, 2>&, int, cudaStream_t);
+template void launch_spmv_probe<double, 1>(const StepArgs<double, 1>&, int, cudaStream_t);
+template void launch_spmv_probe<double, 2>(const StepArgs<double, 2>&, int, cudaStream_t);
+
+}  // namespace fea

@@ -1,0 +1,139 @@
+// fea_internal.cuh -- types shared by the translation units of libfea_gb300.
+#pragma once
+
+#include <vector>
+
+#include "fea_common.cuh"
+
+namespace fea {
+
+// Compressed sparsity pattern of the stiffness/mass matrices plus the data
+// that sums element entries into it in triplet order.
+struct Pattern {
+    int64_t N = 0, nnz = 0, ntrip = 0;
+    int32_t* row_ptr = nullptr;    // [N+1]
+    int32_t* col = nullptr;        // [nnz], sorted within a row
+    int32_t* seg_start = nullptr;  // [nnz+1]: first bucket position of each slot
+    int32_t* seg_id = nullptr;     // [ntrip]: triplet id (9k+3i+j) at each bucket position
+    int32_t* slot_of = nullptr;    // [9T]: slot of each triplet id, -1 if filtered out
+    int32_t* diag = nullptr;       // [N]: slot of the diagonal entry, -1 if absent
+    int32_t* tpos = nullptr;       // [nnz]: slot of the transposed entry
+    int32_t max_row = 0;
+};
+
+int launch_grid(int64_t n);
+void detect_boundary(const uint32_t* tri, int64_t T, int64_t V, uint8_t* ob, cudaStream_t st);
+bool check_triangles(const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st);
+int64_t build_idx_map(const uint8_t* ob, int64_t V, int bc, int32_t* idx, cudaStream_t st);
+void build_pattern(Pattern& P, DeviceArena& keep, const uint32_t* tri, int64_t T, const uint8_t* ob,
+                   const int32_t* idx, int bc, int64_t N, cudaStream_t st);
+
+// ---- assembly (assemble.cu) ---------------------------------------------------
+template <typename R>
+void element_matrices(const float* xyz, const uint32_t* tri, int64_t T, int vel_mode, const float vel[3],
+                      const float* elem_vel, R* Kloc, R* Mloc, R* Aloc, cudaStream_t st);
+template <typename R>
+void ordered_sum(const Pattern& P, const R* loc, const R* elem_scale, R* out, cudaStream_t st);
+template <typename R>
+void ordered_sum_adv(const Pattern& P, const R* loc, const uint32_t* tri, const uint8_t* ob, R* out,
+                     uint8_t* present, cudaStream_t st);
+
+// Operator values for NF fields: A_f = M / md_f + (k1_f * K) * k2_f + a1_f * Adv,
+// evaluated per entry with round-to-nearest operations in that order.
+template <typename R, int NF>
+struct OpCoef {
+    R md[NF], k1[NF], k2[NF], a1[NF];
+};
+template <typename R, int NF>
+void combine_operator(const Pattern& P, const R* M, const R* K, const R* Adv, const OpCoef<R, NF>& c,
+                      FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st);
+
+// ---- time stepping (cg.cu) ------------------------------------------------------
+enum StepKind : int {
+    EQ_HEAT = 0,         // b = (M/dt) u, also implicit advection-diffusion
+    EQ_ADV_EXPLICIT = 1, // b = (M/dt) u + s Adv u
+    EQ_WAVE_REF = 2,     // solve for v: b = (M/dt) v - c^2 K u; then u += dt v
+    EQ_WAVE_NEWMARK = 3, // solve for a: b = -c^2 K u~; then u, v updates
+    EQ_GS_REF = 4,       // (u, v): b = (M/dt) x + f(x) nodal
+    EQ_GS_CONSISTENT = 5, // (u, v): b = M (x/dt + f(x))
+    EQ_NEWMARK_INIT = 6   // solve M a0 = -c^2 K u0 for Newmark's starting acceleration
+};
+
+// Scalars of the step loop, device resident.
+struct StepParams {
+    double dt, F, k, c2, beta, gamma, adv_sign;
+};
+
+struct CgState {
+    double rz[2], rr[2], pq[2], thr[2], bb[2], alpha[2], beta[2];
+    int active[2];
+    int iters[2];
+    int iter;
+    int max_iter;
+    int stop;  // this step is skipped (bad state detected at its start)
+};
+
+struct RunState {
+    long long steps_left, steps_done, total_iters;
+    unsigned int flags;
+    int last_iters[2];
+    double last_rel[2];
+    double tol;
+    int max_iter;
+    int refine;
+};
+
+// Everything a step-loop kernel needs, passed by value.
+template <typename R, int NF>
+struct StepArgs {
+    int N;
+    const int32_t* rp;
+    const int32_t* col;
+    const FV<R, NF>* A;     // operator values [nnz]
+    const FV<R, NF>* dinv;  // [N]
+    const R* M;             // mass values [nnz]
+    const R* K;             // stiffness values [nnz] (diffusivity-scaled)
+    const R* Adv;           // advection values [nnz]
+    FV<R, NF>* x;           // unknown of the solve (warm start and result)
+    FV<R, NF>* b;
+    FV<R, NF>* r;
+    FV<R, NF>* p;
+    FV<R, NF>* q;
+    R* u;                   // NF == 1 equations: displacement / field
+    R* v;                   // velocity (wave)
+    R* a;                   // acceleration (Newmark)
+    R* ut;                  // Newmark predictors
+    R* vt;
+    const StepParams* prm;
+    CgState* cg;
+    RunState* run;
+    double* part;           // block partials [8 * part_stride]
+    int part_stride;
+    unsigned int* tickets;  // [8]
+    cudaGraphConditionalHandle cond;
+};
+
+// A built step-loop graph for one (precision, fields, equation, lanes) plan.
+struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int kind = -1, lanes = 0;
+    void destroy() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+};
+
+template <typename R, int NF>
+void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int lanes);
+
+// One SpMV + dot launch with the given lanes per row (autotuning probe).
+template <typename R, int NF>
+void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
+
+// FP64-accurate true residual |b - A x| / |b| of the current solve (status).
+int max_grid_blocks();
+
+}  // namespace fea

@@ -1,0 +1,947 @@
+// solver.cu -- the fea_solver handle and the C ABI of include/fea_gpu.h.
+//
+// A handle holds one mesh and plays the roles of the reference's FEMContext
+// (mesh, idx_map, assembled matrices; src/FEM/FEMContext.cpp) and of a Solver
+// implementation (state fields u, v and advance_time; include/FEM/Solver.hpp).
+#include <cstdarg>
+#include <cstring>
+#include <new>
+
+#include "fea_internal.cuh"
+
+namespace fea {
+
+namespace {
+thread_local char g_err[512] = "";
+}
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+    }
+    return n;
+}
+
+namespace {
+
+// ---- node <-> unknown maps (CPUSolver.cpp:13-37) --------------------------------
+template <typename R>
+__global__ void k_gather_nodes(const float* __restrict__ vals, const int32_t* __restrict__ idx, int64_t V, R* out,
+                               int stride, int off) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = idx[i];
+        if (k >= 0) out[(int64_t)k * stride + off] = (R)vals[i];
+    }
+}
+
+template <typename R>
+__global__ void k_scatter_nodes(const R* __restrict__ in, const int32_t* __restrict__ idx, int64_t V, float* out,
+                                int stride, int off) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = idx[i];
+        out[i] = k >= 0 ? (float)in[(int64_t)k * stride + off] : 0.0f;
+    }
+}
+
+template <typename R>
+__global__ void k_interleave(const R* __restrict__ u, const R* __restrict__ v, int64_t N, R* uv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        uv[2 * i] = u[i];
+        uv[2 * i + 1] = v[i];
+    }
+}
+
+template <typename R>
+__global__ void k_deinterleave(const R* __restrict__ uv, int64_t N, R* u, R* v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        u[i] = uv[2 * i];
+        v[i] = uv[2 * i + 1];
+    }
+}
+
+template <typename R>
+__global__ void k_copy_strided(const R* __restrict__ in, int64_t N, int in_stride, int in_off, R* out,
+                               int out_stride, int out_off) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+        out[i * out_stride + out_off] = in[i * in_stride + in_off];
+}
+
+template <typename R>
+__global__ void k_float_to(const float* __restrict__ in, int64_t n, R* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (R)in[i];
+}
+
+}  // namespace
+
+// Everything that depends on the arithmetic type.
+struct Fields {
+    int64_t N = 0;
+    void* u = nullptr;   // R[N]
+    void* v = nullptr;   // R[N]
+    void* a = nullptr;   // R[N]  Newmark acceleration
+    void* ut = nullptr;  // R[N]  Newmark predictors
+    void* vt = nullptr;
+    void* uv = nullptr;  // R[2N] interleaved (Gray-Scott)
+    bool interleaved = false;  // (u, v) currently live in uv
+    // solver work, one field
+    void *A1 = nullptr, *d1 = nullptr, *b1 = nullptr, *r1 = nullptr, *p1 = nullptr, *q1 = nullptr;
+    void *A0 = nullptr, *d0 = nullptr;  // Newmark start-up operator (M)
+    // two fields
+    void *A2 = nullptr, *d2 = nullptr, *b2 = nullptr, *r2 = nullptr, *p2 = nullptr, *q2 = nullptr;
+};
+
+}  // namespace fea
+
+using namespace fea;
+
+struct fea_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = FEA_FP32;
+    int bc = FEA_DIRICHLET;
+    int64_t V = 0, T = 0, nb = 0, N = 0;
+    fea_params prm{};
+    // mesh
+    DeviceArena mesh_mem;
+    float* xyz = nullptr;
+    uint32_t* tri = nullptr;
+    uint8_t* ob = nullptr;
+    float* elem_D = nullptr;    // [T] per-element diffusivity (null: 1)
+    float* elem_vel = nullptr;  // [3T]
+    void* elem_Dr = nullptr;    // diffusivity in R
+    // FEMContext state (rebuilt on BC change)
+    DeviceArena mat_mem;
+    int32_t* idx = nullptr;
+    Pattern P;
+    void *Kloc = nullptr, *Mloc = nullptr, *Aloc = nullptr;
+    void *K = nullptr, *M = nullptr, *Adv = nullptr;
+    uint8_t* adv_present = nullptr;
+    Fields F;
+    // loop state
+    DeviceArena run_mem;
+    StepParams* d_prm = nullptr;
+    CgState* d_cg = nullptr;
+    RunState* d_run = nullptr;
+    double* d_part = nullptr;
+    unsigned int* d_tickets = nullptr;
+    RunState* h_run = nullptr;  // pinned
+    StepGraph graph, init_graph;
+    int lanes = 8;
+    bool op_dirty = true;
+    int op_kind = -1;
+    bool acc_valid = false;
+    float cur_vel[3] = {1.f, 0.f, 0.f};
+    int cur_vel_mode = 0;
+    float* d_nodes = nullptr;  // node-indexed staging buffer [V] for host field copies
+};
+
+namespace fea {
+namespace {
+
+size_t rsize(const fea_solver* s) { return s->precision == FEA_FP64 ? 8 : 4; }
+
+void* ralloc(DeviceArena& ar, const fea_solver* s, int64_t n) {
+    if (s->precision == FEA_FP64) return ar.alloc<double>(n);
+    return ar.alloc<float>(n);
+}
+
+int step_kind(const fea_params& p) {
+    switch (p.equation) {
+    case FEA_HEAT: return EQ_HEAT;
+    case FEA_ADVECTION_DIFFUSION: return p.advection_scheme == 1 ? EQ_ADV_EXPLICIT : EQ_HEAT;
+    case FEA_WAVE: return p.wave_scheme == 1 ? EQ_WAVE_NEWMARK : EQ_WAVE_REF;
+    case FEA_REACTION_DIFFUSION: return p.reaction_mode == 1 ? EQ_GS_CONSISTENT : EQ_GS_REF;
+    default: return -1;
+    }
+}
+
+bool two_fields(int kind) { return kind == EQ_GS_REF || kind == EQ_GS_CONSISTENT; }
+
+double time_step(const fea_params& p) {
+    switch (p.equation) {
+    case FEA_HEAT: return p.heat_time_step;
+    case FEA_ADVECTION_DIFFUSION: return p.advdiff_time_step;
+    case FEA_WAVE: return p.wave_time_step;
+    default: return p.rd_time_step;
+    }
+}
+
+template <typename R>
+void assemble_values(fea_solver* s) {
+    const bool vel_elem = s->prm.velocity_mode == 1 && s->elem_vel;
+    element_matrices<R>(s->xyz, s->tri, s->T, vel_elem ? 1 : 0, s->prm.advdiff_velocity, s->elem_vel,
+                        (R*)s->Kloc, (R*)s->Mloc, (R*)s->Aloc, s->stream);
+    ordered_sum<R>(s->P, (R*)s->Kloc, (const R*)s->elem_Dr, (R*)s->K, s->stream);
+    ordered_sum<R>(s->P, (R*)s->Mloc, nullptr, (R*)s->M, s->stream);
+    ordered_sum_adv<R>(s->P, (R*)s->Aloc, s->tri, s->ob, (R*)s->Adv, s->adv_present, s->stream);
+    memcpy(s->cur_vel, s->prm.advdiff_velocity, sizeof(s->cur_vel));
+    s->cur_vel_mode = s->prm.velocity_mode;
+    s->op_dirty = true;
+}
+
+void assemble(fea_solver* s) {
+    if (s->precision == FEA_FP64) assemble_values<double>(s);
+    else assemble_values<float>(s);
+}
+
+// FEMContext::update_boundary_conditions + assemble_matrices and the state.
+void build_context(fea_solver* s) {
+    s->graph.destroy();
+    s->init_graph.destroy();
+    s->mat_mem.release();
+    s->P = Pattern{};
+    s->F = Fields{};
+    cudaStream_t st = s->stream;
+    s->idx = s->mat_mem.alloc<int32_t>(s->V);
+    s->N = build_idx_map(s->ob, s->V, s->bc, s->idx, st);
+    build_pattern(s->P, s->mat_mem, s->tri, s->T, s->ob, s->idx, s->bc, s->N, st);
+    const int64_t N = s->N, nnz = s->P.nnz, T = s->T;
+    s->Kloc = ralloc(s->mat_mem, s, 9 * T);
+    s->Mloc = ralloc(s->mat_mem, s, 9 * T);
+    s->Aloc = ralloc(s->mat_mem, s, 9 * T);
+    s->K = ralloc(s->mat_mem, s, nnz);
+    s->M = ralloc(s->mat_mem, s, nnz);
+    s->Adv = ralloc(s->mat_mem, s, nnz);
+    s->adv_present = s->mat_mem.alloc<uint8_t>(nnz);
+    Fields& F = s->F;
+    F.N = N;
+    F.u = ralloc(s->mat_mem, s, N);
+    F.v = ralloc(s->mat_mem, s, N);
+    F.a = ralloc(s->mat_mem, s, N);
+    F.ut = ralloc(s->mat_mem, s, N);
+    F.vt = ralloc(s->mat_mem, s, N);
+    F.uv = ralloc(s->mat_mem, s, 2 * N);
+    F.A1 = ralloc(s->mat_mem, s, nnz);
+    F.d1 = ralloc(s->mat_mem, s, N);
+    F.b1 = ralloc(s->mat_mem, s, N);
+    F.r1 = ralloc(s->mat_mem, s, N);
+    F.p1 = ralloc(s->mat_mem, s, N);
+    F.q1 = ralloc(s->mat_mem, s, N);
+    F.A0 = ralloc(s->mat_mem, s, nnz);
+    F.d0 = ralloc(s->mat_mem, s, N);
+    F.A2 = ralloc(s->mat_mem, s, 2 * nnz);
+    F.d2 = ralloc(s->mat_mem, s, 2 * N);
+    F.b2 = ralloc(s->mat_mem, s, 2 * N);
+    F.r2 = ralloc(s->mat_mem, s, 2 * N);
+    F.p2 = ralloc(s->mat_mem, s, 2 * N);
+    F.q2 = ralloc(s->mat_mem, s, 2 * N);
+    for (void* p : {F.u, F.v, F.a, F.ut, F.vt, F.uv, F.b1, F.r1, F.p1, F.q1, F.b2, F.r2, F.p2, F.q2}) {
+        const int64_t n = (p == F.uv || p == F.b2 || p == F.r2 || p == F.p2 || p == F.q2) ? 2 * N : N;
+        FEA_CUDA_TRY(cudaMemsetAsync(p, 0, rsize(s) * (size_t)(n > 0 ? n : 1), st));
+    }
+    F.interleaved = false;
+    s->acc_valid = false;
+    assemble(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+template <typename R, int NF>
+StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
+    StepArgs<R, NF> a{};
+    Fields& F = s->F;
+    a.N = (int)s->N;
+    a.rp = s->P.row_ptr;
+    a.col = s->P.col;
+    a.M = (const R*)s->M;
+    a.K = (const R*)s->K;
+    a.Adv = (const R*)s->Adv;
+    if constexpr (NF == 1) {
+        a.A = (const FV<R, 1>*)(init_op ? F.A0 : F.A1);
+        a.dinv = (const FV<R, 1>*)(init_op ? F.d0 : F.d1);
+        a.b = (FV<R, 1>*)F.b1;
+        a.r = (FV<R, 1>*)F.r1;
+        a.p = (FV<R, 1>*)F.p1;
+        a.q = (FV<R, 1>*)F.q1;
+    } else {
+        a.A = (const FV<R, 2>*)F.A2;
+        a.dinv = (const FV<R, 2>*)F.d2;
+        a.b = (FV<R, 2>*)F.b2;
+        a.r = (FV<R, 2>*)F.r2;
+        a.p = (FV<R, 2>*)F.p2;
+        a.q = (FV<R, 2>*)F.q2;
+    }
+    a.u = (R*)F.u;
+    a.v = (R*)F.v;
+    a.a = (R*)F.a;
+    a.ut = (R*)F.ut;
+    a.vt = (R*)F.vt;
+    a.prm = s->d_prm;
+    a.cg = s->d_cg;
+    a.run = s->d_run;
+    a.part = s->d_part;
+    a.part_stride = max_grid_blocks();
+    a.tickets = s->d_tickets;
+    return a;
+}
+
+// Unknown vector of the solve for each kind.
+template <typename R, int NF>
+void set_x(fea_solver* s, StepArgs<R, NF>& a, int kind) {
+    Fields& F = s->F;
+    if constexpr (NF == 2) {
+        a.x = (FV<R, 2>*)F.uv;
+    } else {
+        if (kind == EQ_WAVE_REF) a.x = (FV<R, 1>*)F.v;
+        else if (kind == EQ_WAVE_NEWMARK || kind == EQ_NEWMARK_INIT) a.x = (FV<R, 1>*)F.a;
+        else a.x = (FV<R, 1>*)F.u;
+    }
+}
+
+template <typename R>
+void upload_params(fea_solver* s) {
+    const fea_params& p = s->prm;
+    StepParams h{};
+    h.dt = time_step(p);
+    h.F = p.rd_feed_rate;
+    h.k = p.rd_kill_rate;
+    const R c = (R)p.wave_c;
+    h.c2 = (double)(R)(c * c);
+    h.beta = p.newmark_beta;
+    h.gamma = p.newmark_gamma;
+    h.adv_sign = p.advection_sign;
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->d_prm, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream));
+    RunState r{};
+    FEA_CUDA_TRY(cudaMemcpyAsync(&r, s->d_run, sizeof(r), cudaMemcpyDeviceToHost, s->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double tol = p.cg_tolerance;
+    if (!(tol > 0.0)) tol = s->precision == FEA_FP64 ? 1e-10 : 1.1920928955078125e-07;
+    r.tol = tol;
+    r.max_iter = p.cg_max_iterations > 0 ? p.cg_max_iterations : (int)(2 * s->N > 0x7fffffff ? 0x7fffffff : 2 * s->N);
+    r.refine = p.cg_refine;
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, &r, sizeof(r), cudaMemcpyHostToDevice, s->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+}
+
+// Operator coefficients, computed in R like the reference's float expressions.
+template <typename R>
+void update_operator(fea_solver* s, int kind) {
+    const fea_params& p = s->prm;
+    const R dt = (R)time_step(p);
+    if (kind == EQ_GS_REF || kind == EQ_GS_CONSISTENT) {
+        OpCoef<R, 2> c{};
+        c.md[0] = c.md[1] = dt;
+        c.k1[0] = (R)p.rd_Du;
+        c.k1[1] = (R)p.rd_Dv;
+        c.k2[0] = c.k2[1] = (R)1;
+        c.a1[0] = c.a1[1] = (R)0;
+        combine_operator<R, 2>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
+                               s->stream);
+    } else {
+        OpCoef<R, 1> c{};
+        c.md[0] = dt;
+        c.k2[0] = (R)1;
+        c.a1[0] = (R)0;
+        if (kind == EQ_HEAT && p.equation == FEA_HEAT) {
+            c.k1[0] = (R)p.heat_conductivity;
+        } else if (kind == EQ_HEAT) {  // implicit advection-diffusion, CPUSolver.cpp:95
+            c.k1[0] = (R)p.advdiff_c;
+            c.a1[0] = (R)-1;
+        } else if (kind == EQ_ADV_EXPLICIT) {
+            c.k1[0] = (R)p.advdiff_c;
+        } else if (kind == EQ_WAVE_REF) {  // M/dt + (c^2 K) dt, CPUSolver.cpp:113
+            const R cc = (R)p.wave_c;
+            c.k1[0] = cc * cc;
+            c.k2[0] = dt;
+        } else {  // Newmark: M + (beta dt^2 c^2) K
+            const R cc = (R)p.wave_c, be = (R)p.newmark_beta;
+            const R bdt2 = be * dt * dt;
+            c.md[0] = (R)1;
+            c.k1[0] = bdt2 * (cc * cc);
+            OpCoef<R, 1> m{};
+            m.md[0] = (R)1;
+            m.k1[0] = (R)0;
+            m.k2[0] = (R)1;
+            combine_operator<R, 1>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, m, (FV<R, 1>*)s->F.A0,
+                                   (FV<R, 1>*)s->F.d0, s->stream);
+        }
+        combine_operator<R, 1>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
+                               s->stream);
+    }
+}
+
+template <typename R>
+void ensure_layout(fea_solver* s, bool interleaved) {
+    Fields& F = s->F;
+    if (F.interleaved == interleaved || F.N == 0) {
+        F.interleaved = interleaved;
+        return;
+    }
+    if (interleaved)
+        k_interleave<R><<<launch_grid(F.N), kBlock, 0, s->stream>>>((R*)F.u, (R*)F.v, F.N, (R*)F.uv);
+    else
+        k_deinterleave<R><<<launch_grid(F.N), kBlock, 0, s->stream>>>((R*)F.uv, F.N, (R*)F.u, (R*)F.v);
+    FEA_CHECK_LAUNCH();
+    F.interleaved = interleaved;
+}
+
+template <typename R, int NF>
+void run_graph(fea_solver* s, StepGraph& g, int kind, bool init_op, int64_t nsteps) {
+    if (!g.exec || g.kind != kind || g.lanes != s->lanes) {
+        StepArgs<R, NF> a = make_args<R, NF>(s, init_op);
+        set_x<R, NF>(s, a, kind);
+        build_step_graph<R, NF>(g, a, kind, s->lanes);
+    }
+    long long ctl[2] = {nsteps, 0};  // steps_left, steps_done
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
+    FEA_CUDA_TRY(cudaGraphLaunch(g.exec, s->stream));
+}
+
+template <typename R>
+void advance(fea_solver* s, int64_t nsteps) {
+    const int kind = step_kind(s->prm);
+    if (kind < 0) throw Error{FEA_ERR_INVALID_ARGUMENT};
+    const bool vel_changed = s->prm.velocity_mode != s->cur_vel_mode ||
+                             memcmp(s->cur_vel, s->prm.advdiff_velocity, sizeof(s->cur_vel)) != 0;
+    if (vel_changed) assemble(s);
+    if (s->op_dirty || s->op_kind != kind) {
+        update_operator<R>(s, kind);
+        s->op_dirty = false;
+        s->op_kind = kind;
+    }
+    ensure_layout<R>(s, two_fields(kind));
+    if (kind == EQ_WAVE_NEWMARK && !s->acc_valid) {
+        // a0 from M a0 = -c^2 K u0
+        FEA_CUDA_TRY(cudaMemsetAsync(s->F.a, 0, rsize(s) * (size_t)(s->N > 0 ? s->N : 1), s->stream));
+        run_graph<R, 1>(s, s->init_graph, EQ_NEWMARK_INIT, true, 1);
+        s->acc_valid = true;
+    }
+    if (two_fields(kind)) run_graph<R, 2>(s, s->graph, kind, false, nsteps);
+    else run_graph<R, 1>(s, s->graph, kind, false, nsteps);
+}
+
+void check_handle(const fea_solver* s) {
+    if (!s) {
+        set_error("null handle");
+        throw Error{FEA_ERR_INVALID_ARGUMENT};
+    }
+    FEA_CUDA_TRY(cudaSetDevice(s->device));
+}
+
+// Host fields travel through the handle's node-sized staging buffer; the
+// copy is a DMA transfer when the caller's buffer is page-locked.
+template <typename R>
+void set_node_field(fea_solver* s, const float* host, int which /*0 u, 1 v*/) {
+    float* d = s->d_nodes;
+    FEA_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(float) * s->V, cudaMemcpyHostToDevice, s->stream));
+    Fields& F = s->F;
+    if (F.interleaved)
+        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx, s->V, (R*)F.uv, 2, which);
+    else
+        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx, s->V,
+                                                                        (R*)(which ? F.v : F.u), 1, 0);
+    FEA_CHECK_LAUNCH();
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+}
+
+template <typename R>
+void get_node_field(fea_solver* s, float* host, int which) {
+    float* d = s->d_nodes;
+    Fields& F = s->F;
+    if (F.interleaved)
+        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)F.uv, s->idx, s->V, d, 2, which);
+    else
+        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)(which ? F.v : F.u), s->idx, s->V, d,
+                                                                         1, 0);
+    FEA_CHECK_LAUNCH();
+    FEA_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(float) * s->V, cudaMemcpyDeviceToHost, s->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+}
+
+template <typename R>
+void copy_field_device(fea_solver* s, const void* src, void* dst, int which, bool to_state) {
+    Fields& F = s->F;
+    const int64_t N = s->N;
+    if (N == 0) return;
+    R* state = F.interleaved ? (R*)F.uv : (R*)(which ? F.v : F.u);
+    const int st = F.interleaved ? 2 : 1, off = F.interleaved ? which : 0;
+    if (to_state)
+        k_copy_strided<R><<<launch_grid(N), kBlock, 0, s->stream>>>((const R*)src, N, 1, 0, state, st, off);
+    else
+        k_copy_strided<R><<<launch_grid(N), kBlock, 0, s->stream>>>(state, N, st, off, (R*)dst, 1, 0);
+    FEA_CHECK_LAUNCH();
+}
+
+int displayed_field(const fea_params& p) { return p.equation == FEA_REACTION_DIFFUSION ? 1 : 0; }
+
+}  // namespace
+
+// Device partial-reduction storage sized for the widest grid.
+void alloc_run_state(fea_solver* s) {
+    s->d_prm = s->run_mem.alloc<StepParams>(1);
+    s->d_cg = s->run_mem.alloc<CgState>(1);
+    s->d_run = s->run_mem.alloc<RunState>(1);
+    s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
+    s->d_tickets = s->run_mem.alloc<unsigned int>(8);
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_cg, 0, sizeof(CgState), s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_run, 0, sizeof(RunState), s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_tickets, 0, 8 * sizeof(unsigned int), s->stream));
+    FEA_CUDA_TRY(cudaMallocHost(&s->h_run, sizeof(RunState)));
+}
+
+}  // namespace fea
+
+#define API_BEGIN try {
+#define API_END                                                          \
+    }                                                                    \
+    catch (const fea::Error& e) {                                        \
+        return e.code;                                                   \
+    }                                                                    \
+    catch (const std::bad_alloc&) {                                      \
+        return fea::fail(FEA_ERR_OUT_OF_MEMORY, "host allocation failed"); \
+    }                                                                    \
+    catch (...) {                                                        \
+        return fea::fail(FEA_ERR_CUDA, "unexpected failure");            \
+    }                                                                    \
+    return FEA_OK;
+
+extern "C" {
+
+const char* fea_last_error(void) { return fea::g_err; }
+const char* fea_version(void) { return "fea_gb300 1.0 (sm_103a)"; }
+
+int fea_params_default(fea_params* o) {
+    if (!o) return fail(FEA_ERR_INVALID_ARGUMENT, "null params");
+    memset(o, 0, sizeof(*o));
+    o->equation = FEA_WAVE;  // FEMContext.hpp:31
+    o->heat_time_step = 0.01f;
+    o->heat_conductivity = 0.05f;
+    o->advdiff_time_step = 0.001f;
+    o->advdiff_c = 0.25f;
+    o->advdiff_velocity[0] = 1.0f;
+    o->wave_time_step = 0.05f;
+    o->wave_c = 0.05f;
+    o->rd_time_step = 0.001f;
+    o->rd_Du = 0.08f;
+    o->rd_Dv = 0.04f;
+    o->rd_feed_rate = 0.035f;
+    o->rd_kill_rate = 0.06f;
+    o->reaction_mode = 0;
+    o->wave_scheme = 0;
+    o->newmark_beta = 0.25;
+    o->newmark_gamma = 0.5;
+    o->advection_scheme = 0;
+    o->advection_sign = 1.0f;
+    o->velocity_mode = 0;
+    o->cg_tolerance = 0.0;
+    o->cg_max_iterations = 0;
+    o->cg_refine = 1;
+    return FEA_OK;
+}
+
+int fea_create(const float* vertices, int64_t V, const uint32_t* triangles, int64_t T, const uint8_t* on_boundary,
+               int bc, int precision, const fea_params* params, fea_solver** out) {
+    if (!out) return fail(FEA_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (!vertices || !triangles || V <= 0 || T <= 0)
+        return fail(FEA_ERR_BAD_MESH, "mesh must have vertices and triangles");
+    if (bc != FEA_DIRICHLET && bc != FEA_NEUMANN) return fail(FEA_ERR_INVALID_ARGUMENT, "bad boundary condition");
+    if (precision != FEA_FP32 && precision != FEA_FP64) return fail(FEA_ERR_INVALID_ARGUMENT, "bad precision");
+    if (V >= (int64_t)INT32_MAX || 9 * T >= (int64_t)INT32_MAX) return fail(FEA_ERR_TOO_LARGE, "mesh exceeds int32 indexing");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FEA_ERR_NO_DEVICE, "no CUDA device");
+    fea_solver* s = nullptr;
+    API_BEGIN
+    s = new fea_solver();
+    FEA_CUDA_TRY(cudaGetDevice(&s->device));
+    FEA_CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->precision = precision;
+    s->bc = bc;
+    s->V = V;
+    s->T = T;
+    if (params) s->prm = *params;
+    else fea_params_default(&s->prm);
+    s->xyz = s->mesh_mem.alloc<float>(3 * V);
+    s->tri = s->mesh_mem.alloc<uint32_t>(3 * T);
+    s->ob = s->mesh_mem.alloc<uint8_t>(V);
+    s->d_nodes = s->mesh_mem.alloc<float>(V);
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->xyz, vertices, sizeof(float) * 3 * V, cudaMemcpyHostToDevice, s->stream));
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->tri, triangles, sizeof(uint32_t) * 3 * T, cudaMemcpyHostToDevice, s->stream));
+    if (!check_triangles(s->tri, T, V, s->stream)) {
+        fea_destroy(s);
+        return fail(FEA_ERR_BAD_MESH, "triangle index out of range");
+    }
+    if (on_boundary) {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->ob, on_boundary, V, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        detect_boundary(s->tri, T, V, s->ob, s->stream);
+    }
+    {
+        std::vector<uint8_t> h(V);
+        FEA_CUDA_TRY(cudaMemcpyAsync(h.data(), s->ob, V, cudaMemcpyDeviceToHost, s->stream));
+        FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        int64_t nb = 0;
+        for (int64_t i = 0; i < V; i++) nb += h[i] ? 1 : 0;
+        s->nb = nb;
+    }
+    alloc_run_state(s);
+    build_context(s);
+    if (precision == FEA_FP64) upload_params<double>(s);
+    else upload_params<float>(s);
+    *out = s;
+    return FEA_OK;
+    }
+    catch (const fea::Error& e) {
+        if (s) fea_destroy(s);
+        return e.code;
+    }
+    catch (const std::bad_alloc&) {
+        if (s) fea_destroy(s);
+        return fail(FEA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    catch (...) {
+        if (s) fea_destroy(s);
+        return fail(FEA_ERR_CUDA, "unexpected failure");
+    }
+}
+
+int fea_destroy(fea_solver* s) {
+    if (!s) return FEA_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->graph.destroy();
+    s->init_graph.destroy();
+    s->mat_mem.release();
+    s->run_mem.release();
+    s->mesh_mem.release();
+    if (s->h_run) cudaFreeHost(s->h_run);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return FEA_OK;
+}
+
+int fea_set_boundary_condition(fea_solver* s, int bc) {
+    API_BEGIN
+    check_handle(s);
+    if (bc != FEA_DIRICHLET && bc != FEA_NEUMANN) return fail(FEA_ERR_INVALID_ARGUMENT, "bad boundary condition");
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->bc = bc;
+    build_context(s);
+    s->op_dirty = true;
+    if (s->precision == FEA_FP64) upload_params<double>(s);
+    else upload_params<float>(s);
+    API_END
+}
+
+int fea_set_params(fea_solver* s, const fea_params* p) {
+    API_BEGIN
+    check_handle(s);
+    if (!p) return fail(FEA_ERR_INVALID_ARGUMENT, "null params");
+    if (p->equation < FEA_HEAT || p->equation > FEA_REACTION_DIFFUSION)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "bad equation");
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const bool wave_changed = p->wave_c != s->prm.wave_c || p->wave_time_step != s->prm.wave_time_step ||
+                              p->newmark_beta != s->prm.newmark_beta;
+    if (wave_changed) s->acc_valid = false;
+    s->prm = *p;
+    s->op_dirty = true;
+    if (s->precision == FEA_FP64) upload_params<double>(s);
+    else upload_params<float>(s);
+    API_END
+}
+
+int fea_set_element_fields(fea_solver* s, const float* diffusivity, const float* velocity) {
+    API_BEGIN
+    check_handle(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (diffusivity) {
+        if (!s->elem_D) {
+            s->elem_D = s->mesh_mem.alloc<float>(s->T);
+            s->elem_Dr = ralloc(s->mesh_mem, s, s->T);
+        }
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->elem_D, diffusivity, sizeof(float) * s->T, cudaMemcpyHostToDevice, s->stream));
+        if (s->precision == FEA_FP64)
+            k_float_to<double><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, (double*)s->elem_Dr);
+        else
+            k_float_to<float><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, (float*)s->elem_Dr);
+        FEA_CHECK_LAUNCH();
+    }
+    if (velocity) {
+        if (!s->elem_vel) s->elem_vel = s->mesh_mem.alloc<float>(3 * s->T);
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->elem_vel, velocity, sizeof(float) * 3 * s->T, cudaMemcpyHostToDevice,
+                                     s->stream));
+    }
+    assemble(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_clear_values(fea_solver* s) {
+    API_BEGIN
+    check_handle(s);
+    Fields& F = s->F;
+    const size_t n = rsize(s) * (size_t)(s->N > 0 ? s->N : 1);
+    for (void* p : {F.u, F.v, F.a}) FEA_CUDA_TRY(cudaMemsetAsync(p, 0, n, s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(F.uv, 0, 2 * n, s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
+    s->acc_valid = false;
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_set_values(fea_solver* s, const float* values) {
+    API_BEGIN
+    check_handle(s);
+    if (!values) return fail(FEA_ERR_INVALID_ARGUMENT, "null values");
+    if (s->precision == FEA_FP64) set_node_field<double>(s, values, displayed_field(s->prm));
+    else set_node_field<float>(s, values, displayed_field(s->prm));
+    if (displayed_field(s->prm) == 0) s->acc_valid = false;
+    API_END
+}
+
+int fea_get_values(fea_solver* s, float* values) {
+    API_BEGIN
+    check_handle(s);
+    if (!values) return fail(FEA_ERR_INVALID_ARGUMENT, "null values");
+    if (s->precision == FEA_FP64) get_node_field<double>(s, values, displayed_field(s->prm));
+    else get_node_field<float>(s, values, displayed_field(s->prm));
+    API_END
+}
+
+int fea_set_fields(fea_solver* s, const float* u, const float* v) {
+    API_BEGIN
+    check_handle(s);
+    if (s->precision == FEA_FP64) {
+        if (u) set_node_field<double>(s, u, 0);
+        if (v) set_node_field<double>(s, v, 1);
+    } else {
+        if (u) set_node_field<float>(s, u, 0);
+        if (v) set_node_field<float>(s, v, 1);
+    }
+    s->acc_valid = false;
+    API_END
+}
+
+int fea_get_fields(fea_solver* s, float* u, float* v) {
+    API_BEGIN
+    check_handle(s);
+    if (s->precision == FEA_FP64) {
+        if (u) get_node_field<double>(s, u, 0);
+        if (v) get_node_field<double>(s, v, 1);
+    } else {
+        if (u) get_node_field<float>(s, u, 0);
+        if (v) get_node_field<float>(s, v, 1);
+    }
+    API_END
+}
+
+int fea_set_fields_device(fea_solver* s, const void* u, const void* v) {
+    API_BEGIN
+    check_handle(s);
+    if (s->precision == FEA_FP64) {
+        if (u) copy_field_device<double>(s, u, nullptr, 0, true);
+        if (v) copy_field_device<double>(s, v, nullptr, 1, true);
+    } else {
+        if (u) copy_field_device<float>(s, u, nullptr, 0, true);
+        if (v) copy_field_device<float>(s, v, nullptr, 1, true);
+    }
+    s->acc_valid = false;
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_get_fields_device(fea_solver* s, void* u, void* v) {
+    API_BEGIN
+    check_handle(s);
+    if (s->precision == FEA_FP64) {
+        if (u) copy_field_device<double>(s, nullptr, u, 0, false);
+        if (v) copy_field_device<double>(s, nullptr, v, 1, false);
+    } else {
+        if (u) copy_field_device<float>(s, nullptr, u, 0, false);
+        if (v) copy_field_device<float>(s, nullptr, v, 1, false);
+    }
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_advance_time(fea_solver* s, int64_t nsteps) {
+    API_BEGIN
+    check_handle(s);
+    if (nsteps < 0) return fail(FEA_ERR_INVALID_ARGUMENT, "negative step count");
+    if (nsteps == 0 || s->N == 0) return FEA_OK;
+    if (s->precision == FEA_FP64) advance<double>(s, nsteps);
+    else advance<float>(s, nsteps);
+    API_END
+}
+
+int fea_synchronize(fea_solver* s) {
+    API_BEGIN
+    check_handle(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_get_status(fea_solver* s, fea_status* out) {
+    API_BEGIN
+    check_handle(s);
+    if (!out) return fail(FEA_ERR_INVALID_ARGUMENT, "null status");
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->h_run, s->d_run, sizeof(RunState), cudaMemcpyDeviceToHost, s->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const RunState& r = *s->h_run;
+    out->flags = r.flags;
+    out->last_iterations[0] = r.last_iters[0];
+    out->last_iterations[1] = r.last_iters[1];
+    out->last_rel_residual[0] = r.last_rel[0];
+    out->last_rel_residual[1] = r.last_rel[1];
+    out->steps_done = r.steps_done;
+    out->total_iterations = r.total_iters;
+    API_END
+}
+
+int fea_has_numerical_instability(fea_solver* s, int* out) {
+    fea_status st;
+    int rc = fea_get_status(s, &st);
+    if (rc != FEA_OK) return rc;
+    if (out) *out = (st.flags & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) ? 1 : 0;
+    return FEA_OK;
+}
+
+int fea_get_info(fea_solver* s, fea_info* out) {
+    API_BEGIN
+    check_handle(s);
+    if (!out) return fail(FEA_ERR_INVALID_ARGUMENT, "null info");
+    out->num_vertices = s->V;
+    out->num_triangles = s->T;
+    out->num_boundary_points = s->nb;
+    out->num_unknowns = s->N;
+    out->nnz = s->P.nnz;
+    out->max_row_nonzeros = s->P.max_row;
+    out->precision = s->precision;
+    out->boundary_condition = s->bc;
+    out->rows_per_warp_lanes = s->lanes;
+    out->device_bytes = s->mesh_mem.bytes + s->mat_mem.bytes + s->run_mem.bytes;
+    API_END
+}
+
+int fea_get_matrix(fea_solver* s, int which, int32_t* row_ptr, int32_t* col, void* values, uint8_t* present) {
+    API_BEGIN
+    check_handle(s);
+    const void* src = which == FEA_MATRIX_STIFFNESS ? s->K : which == FEA_MATRIX_MASS ? s->M
+                    : which == FEA_MATRIX_ADVECTION ? s->Adv : nullptr;
+    if (!src) return fail(FEA_ERR_INVALID_ARGUMENT, "bad matrix selector");
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (row_ptr)
+        FEA_CUDA_TRY(cudaMemcpy(row_ptr, s->P.row_ptr, sizeof(int32_t) * (s->N + 1), cudaMemcpyDeviceToHost));
+    if (col && s->P.nnz) FEA_CUDA_TRY(cudaMemcpy(col, s->P.col, sizeof(int32_t) * s->P.nnz, cudaMemcpyDeviceToHost));
+    if (values && s->P.nnz) FEA_CUDA_TRY(cudaMemcpy(values, src, rsize(s) * s->P.nnz, cudaMemcpyDeviceToHost));
+    if (present && s->P.nnz) {
+        if (which == FEA_MATRIX_ADVECTION)
+            FEA_CUDA_TRY(cudaMemcpy(present, s->adv_present, s->P.nnz, cudaMemcpyDeviceToHost));
+        else
+            memset(present, 1, s->P.nnz);
+    }
+    API_END
+}
+
+int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary) {
+    API_BEGIN
+    check_handle(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (idx_map) FEA_CUDA_TRY(cudaMemcpy(idx_map, s->idx, sizeof(int32_t) * s->V, cudaMemcpyDeviceToHost));
+    if (on_boundary) FEA_CUDA_TRY(cudaMemcpy(on_boundary, s->ob, s->V, cudaMemcpyDeviceToHost));
+    API_END
+}
+
+int fea_autotune(fea_solver* s) {
+    API_BEGIN
+    check_handle(s);
+    if (s->N == 0) return FEA_OK;
+    const int kind = step_kind(s->prm);
+    const bool two = two_fields(kind);
+    cudaEvent_t e0, e1;
+    FEA_CUDA_TRY(cudaEventCreate(&e0));
+    FEA_CUDA_TRY(cudaEventCreate(&e1));
+    const int cand[4] = {2, 4, 8, 16};
+    float best = 1e30f;
+    int best_l = s->lanes;
+    for (int l : cand) {
+        for (int rep = 0; rep < 23; rep++) {
+            if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
+            if (s->precision == FEA_FP64) {
+                if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), l, s->stream);
+                else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), l, s->stream);
+            } else {
+                if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), l, s->stream);
+                else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), l, s->stream);
+            }
+        }
+        FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
+        FEA_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        FEA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            best_l = l;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->lanes = best_l;
+    API_END
+}
+
+int fea_get_stream(fea_solver* s, void** stream) {
+    API_BEGIN
+    check_handle(s);
+    if (!stream) return fail(FEA_ERR_INVALID_ARGUMENT, "null stream output");
+    *stream = (void*)s->stream;
+    API_END
+}
+
+int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch) {
+    API_BEGIN
+    check_handle(s);
+    if (reps <= 0 || !ms_per_launch) return fail(FEA_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (s->N == 0) {
+        *ms_per_launch = 0;
+        return FEA_OK;
+    }
+    const int kind = step_kind(s->prm);
+    const bool two = two_fields(kind);
+    if (s->op_dirty || s->op_kind != kind) {
+        if (s->precision == FEA_FP64) update_operator<double>(s, kind);
+        else update_operator<float>(s, kind);
+        s->op_dirty = false;
+        s->op_kind = kind;
+    }
+    DeviceArena tmp;
+    const size_t flush_bytes = (size_t)256 << 20;
+    void* junk = flush_l2 ? (void*)tmp.alloc<uint8_t>((int64_t)flush_bytes) : nullptr;
+    cudaEvent_t e0, e1;
+    FEA_CUDA_TRY(cudaEventCreate(&e0));
+    FEA_CUDA_TRY(cudaEventCreate(&e1));
+    double total = 0;
+    for (int rep = 0; rep < reps + 1; rep++) {  // the first launch is a warm-up
+        if (junk) FEA_CUDA_TRY(cudaMemsetAsync(junk, rep & 0xff, flush_bytes, s->stream));
+        FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
+        if (s->precision == FEA_FP64) {
+            if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), s->lanes, s->stream);
+            else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), s->lanes, s->stream);
+        } else {
+            if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), s->lanes, s->stream);
+            else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), s->lanes, s->stream);
+        }
+        FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
+        FEA_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        FEA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_launch = total / reps;
+    API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,297 @@
+"""ctypes binding of libfea_gb300.so (include/fea_gpu.h).
+
+`CUDASolver` mirrors the reference's solver interface (include/FEM/Solver.hpp:8-14:
+advance_time / clear_values / has_numerical_instability) over the C ABI, with
+the FEMContext inputs (mesh, boundary condition, equation parameters) passed
+at construction.  There is no CPU fallback: constructing a solver without the
+CUDA library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "lib", "libfea_gb300.so")
+
+HEAT, WAVE, ADVECTION_DIFFUSION, REACTION_DIFFUSION = 0, 1, 2, 3
+DIRICHLET, NEUMANN = 0, 1
+FP32, FP64 = 0, 1
+STIFFNESS, MASS, ADVECTION = 0, 1, 2
+
+STATUS_BLOWUP, STATUS_NONFINITE, STATUS_NOT_CONVERGED, STATUS_BREAKDOWN = 1, 2, 4, 8
+
+ERRORS = {
+    -1: "invalid argument", -2: "CUDA error", -3: "no CUDA device", -4: "bad mesh",
+    -5: "out of memory", -6: "bad call order", -7: "unsupported", -8: "too large",
+}
+
+
+class FeaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """fea_params (include/fea_gpu.h)."""
+    _fields_ = [
+        ("equation", C.c_int),
+        ("heat_time_step", C.c_float), ("heat_conductivity", C.c_float),
+        ("advdiff_time_step", C.c_float), ("advdiff_c", C.c_float), ("advdiff_velocity", C.c_float * 3),
+        ("wave_time_step", C.c_float), ("wave_c", C.c_float),
+        ("rd_time_step", C.c_float), ("rd_Du", C.c_float), ("rd_Dv", C.c_float),
+        ("rd_feed_rate", C.c_float), ("rd_kill_rate", C.c_float),
+        ("reaction_mode", C.c_int), ("wave_scheme", C.c_int),
+        ("newmark_beta", C.c_double), ("newmark_gamma", C.c_double),
+        ("advection_scheme", C.c_int), ("advection_sign", C.c_float), ("velocity_mode", C.c_int),
+        ("cg_tolerance", C.c_double), ("cg_max_iterations", C.c_int), ("cg_refine", C.c_int),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_int64), ("num_triangles", C.c_int64), ("num_boundary_points", C.c_int64),
+        ("num_unknowns", C.c_int64), ("nnz", C.c_int64), ("max_row_nonzeros", C.c_int64),
+        ("precision", C.c_int), ("boundary_condition", C.c_int), ("rows_per_warp_lanes", C.c_int),
+        ("device_bytes", C.c_int64),
+    ]
+
+
+class Status(C.Structure):
+    _fields_ = [
+        ("flags", C.c_uint32), ("last_iterations", C.c_int32 * 2),
+        ("last_rel_residual", C.c_double * 2), ("steps_done", C.c_int64), ("total_iterations", C.c_int64),
+    ]
+
+
+class InstanceDesc(C.Structure):
+    _fields_ = [
+        ("vertices", C.c_void_p), ("num_vertices", C.c_int64),
+        ("triangles", C.c_void_p), ("num_triangles", C.c_int64),
+        ("boundary_condition", C.c_int),
+        ("time_step", C.c_float), ("Du", C.c_float), ("Dv", C.c_float),
+        ("feed_rate", C.c_float), ("kill_rate", C.c_float),
+    ]
+
+
+# every function of include/fea_gpu.h with its argument types
+_P = C.c_void_p
+_I64 = C.c_int64
+SIGNATURES = {
+    "fea_params_default": [C.POINTER(Params)],
+    "fea_create": [_P, _I64, _P, _I64, _P, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(C.c_void_p)],
+    "fea_destroy": [_P],
+    "fea_set_boundary_condition": [_P, C.c_int],
+    "fea_set_params": [_P, C.POINTER(Params)],
+    "fea_set_element_fields": [_P, _P, _P],
+    "fea_clear_values": [_P],
+    "fea_set_values": [_P, _P],
+    "fea_get_values": [_P, _P],
+    "fea_set_fields": [_P, _P, _P],
+    "fea_get_fields": [_P, _P, _P],
+    "fea_set_fields_device": [_P, _P, _P],
+    "fea_get_fields_device": [_P, _P, _P],
+    "fea_advance_time": [_P, _I64],
+    "fea_synchronize": [_P],
+    "fea_has_numerical_instability": [_P, C.POINTER(C.c_int)],
+    "fea_get_status": [_P, C.POINTER(Status)],
+    "fea_get_info": [_P, C.POINTER(Info)],
+    "fea_get_matrix": [_P, C.c_int, _P, _P, _P, _P],
+    "fea_get_idx_map": [_P, _P, _P],
+    "fea_autotune": [_P],
+    "fea_get_stream": [_P, C.POINTER(C.c_void_p)],
+    "fea_time_spmv": [_P, C.c_int, C.c_int, C.POINTER(C.c_double)],
+    "fea_adjoint_advdiff": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
+    "fea_adjoint_advdiff_device": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
+    "fea_batch_create": [C.POINTER(InstanceDesc), C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)],
+    "fea_batch_destroy": [_P],
+    "fea_batch_set_fields": [_P, C.c_int, _P, _P],
+    "fea_batch_get_fields": [_P, C.c_int, _P, _P],
+    "fea_batch_advance_time": [_P, _I64],
+    "fea_batch_synchronize": [_P],
+    "fea_batch_get_status": [_P, _P, _P],
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise FeaError(-3, f"{path} is missing: build it with fea-visualizer_gb300/build.py")
+        L = C.CDLL(path)
+        for name, argt in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = argt
+            f.restype = C.c_int
+        L.fea_last_error.restype = C.c_char_p
+        L.fea_last_error.argtypes = []
+        L.fea_version.restype = C.c_char_p
+        L.fea_version.argtypes = []
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise FeaError(rc, load().fea_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def default_params(**kw) -> Params:
+    """EquationParameters.hpp defaults, then keyword overrides."""
+    p = Params()
+    check(load().fea_params_default(C.byref(p)))
+    for k, v in kw.items():
+        if k == "advdiff_velocity":
+            p.advdiff_velocity[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class CUDASolver:
+    """The reference's Solver interface over the C ABI (one mesh, one GPU)."""
+
+    def __init__(self, vertices, triangles, boundary_condition=DIRICHLET, precision=FP32, params=None,
+                 on_boundary=None):
+        L = load()
+        self.vertices = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        self.triangles = np.ascontiguousarray(triangles, dtype=np.uint32).reshape(-1, 3)
+        ob = None if on_boundary is None else np.ascontiguousarray(on_boundary, dtype=np.uint8)
+        self.params = params if params is not None else default_params()
+        self.precision = precision
+        self.real = np.float64 if precision == FP64 else np.float32
+        h = C.c_void_p()
+        check(L.fea_create(_ptr(self.vertices), self.vertices.shape[0], _ptr(self.triangles),
+                           self.triangles.shape[0], _ptr(ob), boundary_condition, precision,
+                           C.byref(self.params), C.byref(h)))
+        self._h = h
+
+    # -- Solver.hpp:8-14 ---------------------------------------------------------
+    def advance_time(self, nsteps: int = 1):
+        check(load().fea_advance_time(self._h, int(nsteps)))
+
+    def clear_values(self):
+        check(load().fea_clear_values(self._h))
+
+    def has_numerical_instability(self) -> bool:
+        out = C.c_int(0)
+        check(load().fea_has_numerical_instability(self._h, C.byref(out)))
+        return bool(out.value)
+
+    # -- FEMContext-side inputs ---------------------------------------------------
+    def set_params(self, params: Params):
+        self.params = params
+        check(load().fea_set_params(self._h, C.byref(params)))
+
+    def set_boundary_condition(self, bc: int):
+        check(load().fea_set_boundary_condition(self._h, bc))
+
+    def set_element_fields(self, diffusivity=None, velocity=None):
+        d = None if diffusivity is None else np.ascontiguousarray(diffusivity, dtype=np.float32)
+        v = None if velocity is None else np.ascontiguousarray(velocity, dtype=np.float32)
+        check(load().fea_set_element_fields(self._h, _ptr(d), _ptr(v)))
+
+    # -- fields -------------------------------------------------------------------
+    @property
+    def info(self) -> Info:
+        i = Info()
+        check(load().fea_get_info(self._h, C.byref(i)))
+        return i
+
+    def status(self) -> Status:
+        s = Status()
+        check(load().fea_get_status(self._h, C.byref(s)))
+        return s
+
+    def set_values(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        check(load().fea_set_values(self._h, _ptr(v)))
+
+    def get_values(self):
+        out = np.zeros(self.vertices.shape[0], dtype=np.float32)
+        check(load().fea_get_values(self._h, _ptr(out)))
+        return out
+
+    def set_fields(self, u=None, v=None):
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float32)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float32)
+        check(load().fea_set_fields(self._h, _ptr(uu), _ptr(vv)))
+
+    def get_fields(self):
+        u = np.zeros(self.vertices.shape[0], dtype=np.float32)
+        v = np.zeros(self.vertices.shape[0], dtype=np.float32)
+        check(load().fea_get_fields(self._h, _ptr(u), _ptr(v)))
+        return u, v
+
+    def set_fields_device(self, u_ptr, v_ptr):
+        check(load().fea_set_fields_device(self._h, u_ptr, v_ptr))
+
+    def get_fields_device(self, u_ptr, v_ptr):
+        check(load().fea_get_fields_device(self._h, u_ptr, v_ptr))
+
+    def synchronize(self):
+        check(load().fea_synchronize(self._h))
+
+    def autotune(self):
+        check(load().fea_autotune(self._h))
+        return self.info.rows_per_warp_lanes
+
+    def stream(self) -> int:
+        """cudaStream_t of the handle, as an integer."""
+        st = C.c_void_p()
+        check(load().fea_get_stream(self._h, C.byref(st)))
+        return st.value or 0
+
+    def time_spmv(self, reps=20, flush_l2=True) -> float:
+        ms = C.c_double(0)
+        check(load().fea_time_spmv(self._h, int(reps), 1 if flush_l2 else 0, C.byref(ms)))
+        return ms.value
+
+    def matrix(self, which):
+        """(row_ptr, col, values, present) of K / M / Adv."""
+        inf = self.info
+        rp = np.zeros(inf.num_unknowns + 1, dtype=np.int32)
+        col = np.zeros(inf.nnz, dtype=np.int32)
+        val = np.zeros(inf.nnz, dtype=self.real)
+        pres = np.zeros(inf.nnz, dtype=np.uint8)
+        check(load().fea_get_matrix(self._h, which, _ptr(rp), _ptr(col), _ptr(val), _ptr(pres)))
+        return rp, col, val, pres
+
+    def idx_map(self):
+        idx = np.zeros(self.vertices.shape[0], dtype=np.int32)
+        ob = np.zeros(self.vertices.shape[0], dtype=np.uint8)
+        check(load().fea_get_idx_map(self._h, _ptr(idx), _ptr(ob)))
+        return idx, ob
+
+    def adjoint_advdiff(self, u0, target, nsteps, checkpoint_every):
+        """(J, dJ/du0 node-indexed, dJ/dD per element) of the explicit advection-diffusion loss."""
+        u0 = np.ascontiguousarray(u0, dtype=np.float32)
+        tg = np.ascontiguousarray(target, dtype=np.float32)
+        gu = np.zeros(self.vertices.shape[0], dtype=np.float32)
+        gd = np.zeros(self.triangles.shape[0], dtype=np.float32)
+        J = C.c_double(0)
+        check(load().fea_adjoint_advdiff(self._h, _ptr(u0), _ptr(tg), int(nsteps), int(checkpoint_every),
+                                         C.byref(J), _ptr(gu), _ptr(gd)))
+        return J.value, gu, gd
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().fea_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,275 @@
+/*
+ * fea_gpu.h -- C ABI of the GB300 FEM time-stepping library (libfea_gb300.so).
+ *
+ * It replaces the reference's solver layer for triangle meshes: the Solver
+ * interface (include/FEM/Solver.hpp:8-14) with its CPU implementation
+ * (src/FEM/CPUSolver.cpp) and compute-shader implementation
+ * (src/FEM/GPUSolver.cpp, shaders/FEM/cgm.glsl, shaders/FEM/cgm_helper.glsl),
+ * and the matrix assembly of FEMContext (src/FEM/FEMContext.cpp:57-240).
+ * Paths are relative to the reference project.
+ *
+ * Conventions
+ *   - Plain C types only.  Host pointers unless a name ends in _device.
+ *   - Every function returns an int status: FEA_OK (0) or a negative FEA_ERR_*
+ *     code; fea_last_error() gives a one-line message for the calling thread.
+ *     No C++ exception crosses this boundary.
+ *   - A handle owns one CUDA stream on the device that was current when it
+ *     was created.  Calls on one handle must not run concurrently; distinct
+ *     handles are independent.  Calls that return host data synchronise.
+ *   - Fields are node-indexed float arrays of length num_vertices, like the
+ *     reference's Surface::values (include/Utils/Surface.hpp:38).
+ */
+#ifndef FEA_GPU_H
+#define FEA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define FEA_OK 0
+#define FEA_ERR_INVALID_ARGUMENT (-1)
+#define FEA_ERR_CUDA (-2)
+#define FEA_ERR_NO_DEVICE (-3)
+#define FEA_ERR_BAD_MESH (-4)    /* Surface.cpp:40-41, 59-74 throw runtime_error */
+#define FEA_ERR_OUT_OF_MEMORY (-5)
+#define FEA_ERR_STATE (-6)       /* call order violated (e.g. step before assemble) */
+#define FEA_ERR_UNSUPPORTED (-7)
+#define FEA_ERR_TOO_LARGE (-8)
+
+/* ---- step status flags (fea_get_status) ---------------------------------- */
+#define FEA_STATUS_BLOWUP 1u       /* some u_i or v_i > 1e4 (CPUSolver.cpp:41-48) */
+#define FEA_STATUS_NONFINITE 2u    /* NaN or Inf in a field */
+#define FEA_STATUS_NOT_CONVERGED 4u /* a CG solve hit max_iter before tol */
+#define FEA_STATUS_BREAKDOWN 8u    /* CG breakdown: p.Ap <= 0 or non-finite */
+
+/* ---- enums mirroring the reference --------------------------------------- */
+/* Equation, include/FEM/FEMContext.hpp:9-14 (same order and values) */
+#define FEA_HEAT 0
+#define FEA_WAVE 1
+#define FEA_ADVECTION_DIFFUSION 2
+#define FEA_REACTION_DIFFUSION 3
+/* BoundaryCondition, include/FEM/FEMContext.hpp:16-19 */
+#define FEA_DIRICHLET 0
+#define FEA_NEUMANN 1
+/* arithmetic type of matrix values and fields */
+#define FEA_FP32 0
+#define FEA_FP64 1
+/* matrices for fea_get_matrix */
+#define FEA_MATRIX_STIFFNESS 0
+#define FEA_MATRIX_MASS 1
+#define FEA_MATRIX_ADVECTION 2
+
+/* Parameters: the four structs of include/FEM/EquationParameters.hpp:8-49
+ * (same fields, same defaults from fea_params_default) plus the extensions
+ * this library adds.  Extensions default to the reference's behaviour. */
+typedef struct {
+    int equation;                 /* FEA_HEAT .. FEA_REACTION_DIFFUSION */
+    /* HeatParameters (EquationParameters.hpp:8-15) */
+    float heat_time_step;         /* 0.01 */
+    float heat_conductivity;      /* 0.05 */
+    /* AdvectionDiffusionParameters (:17-26) */
+    float advdiff_time_step;      /* 0.001 */
+    float advdiff_c;              /* 0.25 */
+    float advdiff_velocity[3];    /* (1, 0, 0) */
+    /* WaveParameters (:28-35) */
+    float wave_time_step;         /* 0.05 */
+    float wave_c;                 /* 0.05 */
+    /* ReactionDiffusionParameters (:37-49) */
+    float rd_time_step;           /* 0.001 */
+    float rd_Du;                  /* 0.08 */
+    float rd_Dv;                  /* 0.04 */
+    float rd_feed_rate;           /* 0.035 */
+    float rd_kill_rate;           /* 0.06 */
+    /* --- extensions --- */
+    int reaction_mode;   /* 0: reaction added nodally (CPUSolver.cpp:134,137);
+                            1: mass-weighted, b = M (u/dt + f(u, v)) */
+    int wave_scheme;     /* 0: semi-implicit velocity form (CPUSolver.cpp:113-118);
+                            1: Newmark-beta, solve (M + beta dt^2 c^2 K) a = -c^2 K u~ */
+    double newmark_beta;  /* 0.25 */
+    double newmark_gamma; /* 0.5 */
+    int advection_scheme; /* 0: implicit, A = M/dt + cK - Adv (CPUSolver.cpp:95);
+                             1: explicit, A = M/dt + K_D, b = (M/dt) u + s Adv u (SPD) */
+    float advection_sign; /* s for the explicit scheme (1 = the reference's sign) */
+    int velocity_mode;    /* 0: constant velocity, tangential part normalised
+                             (FEMContext.cpp:180); 1: per-element velocity from
+                             fea_set_element_fields, magnitude kept */
+    double cg_tolerance;  /* relative: stop when |r| < tol |b|.  0 -> FLT_EPSILON
+                             for FP32 handles, 1e-10 for FP64 (Eigen's default is
+                             the type's epsilon) */
+    int cg_max_iterations; /* 0 -> 2N (Eigen's default) */
+    int cg_refine;         /* 1: one FP64 true-residual refinement pass per solve */
+} fea_params;
+
+typedef struct {
+    int64_t num_vertices;        /* FEMContext::num_nodes (FEMContext.cpp:33-35) */
+    int64_t num_triangles;
+    int64_t num_boundary_points; /* Surface::num_boundary_points */
+    int64_t num_unknowns;        /* FEMContext::num_unknowns (:46-48) */
+    int64_t nnz;                 /* entries of the compressed stiffness/mass pattern */
+    int64_t max_row_nonzeros;    /* FEMContext::compute_max_row_nonzeros (:207-219) */
+    int precision;               /* FEA_FP32 / FEA_FP64 */
+    int boundary_condition;
+    int rows_per_warp_lanes;     /* lanes per CSR row chosen for the SpMV */
+    int64_t device_bytes;        /* device memory held by the handle */
+} fea_info;
+
+typedef struct {
+    uint32_t flags;              /* FEA_STATUS_* accumulated since the last clear */
+    int32_t last_iterations[2];  /* CG iterations of the last solve of field 0/1 */
+    double last_rel_residual[2]; /* |r| / |b| at exit of that solve */
+    int64_t steps_done;          /* steps completed by the last fea_advance_time */
+    int64_t total_iterations;    /* CG iterations summed over all solves */
+} fea_status;
+
+typedef struct fea_solver fea_solver;
+
+/* Defaults of EquationParameters.hpp:8-49 plus reference-behaviour extensions. */
+int fea_params_default(fea_params* out);
+
+/* Mesh in, assembly included: replaces FEMContext::init_from_surface
+ * (FEMContext.cpp:21-27) -> update_boundary_conditions (:224-240) ->
+ * assemble_matrices (:57-64).  vertices: xyz float[3V]; triangles: uint32[3T];
+ * on_boundary: uint8[V] or NULL to detect boundary points on the device as
+ * Surface::init_from_obj does (Surface.cpp:104-122).  params may be NULL
+ * (defaults).  Returns FEA_ERR_BAD_MESH for an empty mesh or an index >= V. */
+int fea_create(const float* vertices, int64_t num_vertices, const uint32_t* triangles,
+               int64_t num_triangles, const uint8_t* on_boundary, int boundary_condition,
+               int precision, const fea_params* params, fea_solver** out);
+int fea_destroy(fea_solver* s);
+
+/* FEMContext::update_boundary_conditions (FEMContext.cpp:224-240): rebuild
+ * idx_map, pattern and matrices for a new BC.  Fields are cleared. */
+int fea_set_boundary_condition(fea_solver* s, int boundary_condition);
+
+/* Equation and parameters (FEMContext::equation, FEMContext::parameters).
+ * A changed advection velocity re-assembles Adv, as the reference's velocity
+ * slider does (Application.cpp:393-394). */
+int fea_set_params(fea_solver* s, const fea_params* params);
+
+/* Per-element diffusivity D_e (K_D = sum_e D_e K_e; float[T], NULL = 1) and
+ * per-element velocity (float[3T], used when velocity_mode == 1). */
+int fea_set_element_fields(fea_solver* s, const float* diffusivity, const float* velocity);
+
+/* Solver::clear_values (CPUSolver.cpp:54-59): u = v = 0 (and Newmark a = 0). */
+int fea_clear_values(fea_solver* s);
+
+/* Surface::values in/out.  The displayed field is u for heat, wave and
+ * advection-diffusion and v for Gray-Scott, as in CPUSolver.cpp:75/130;
+ * set copies values[idx] of unknown points in (get_surface_value_vector,
+ * CPUSolver.cpp:13-21), get writes every point, Dirichlet points as 0
+ * (map_vector_to_surface, CPUSolver.cpp:28-37). */
+int fea_set_values(fea_solver* s, const float* values);
+int fea_get_values(fea_solver* s, float* values);
+
+/* Both state fields at once (node-indexed, float[V] each; NULL leaves a field
+ * unchanged).  u/v are the solver-private vectors of CPUSolver.hpp:17-18; for
+ * the wave equation v is the velocity.  Setting fields resets Newmark's
+ * acceleration, recomputed from M a = -c^2 K u at the next step. */
+int fea_set_fields(fea_solver* s, const float* u, const float* v);
+int fea_get_fields(fea_solver* s, float* u, float* v);
+
+/* Device-resident variants: pointers to device memory of the handle's
+ * device, unknown-indexed, in the handle's precision (float or double).
+ * Ordered on the handle's stream and synchronised before returning. */
+int fea_set_fields_device(fea_solver* s, const void* u, const void* v);
+int fea_get_fields_device(fea_solver* s, void* u, void* v);
+
+/* Solver::advance_time (CPUSolver.cpp:64-146) nsteps times.  The whole step
+ * loop runs as one CUDA graph launch; stepping stops early once
+ * FEA_STATUS_BLOWUP or FEA_STATUS_NONFINITE is raised (the application pauses
+ * there, Application.cpp:532-538).  Asynchronous: returns after the launch. */
+int fea_advance_time(fea_solver* s, int64_t nsteps);
+/* Wait for the handle's stream. */
+int fea_synchronize(fea_solver* s);
+
+/* Solver::has_numerical_instability (CPUSolver.cpp:41-48): *out = 1 when a
+ * field value exceeds 1e4 (or is not finite).  Synchronises. */
+int fea_has_numerical_instability(fea_solver* s, int* out);
+int fea_get_status(fea_solver* s, fea_status* out);
+int fea_get_info(fea_solver* s, fea_info* out);
+
+/* Assembled matrix in compressed-row form: row_ptr int32[N+1], col int32[nnz],
+ * values in the handle's precision (float or double) [nnz].  The index arrays
+ * equal Eigen's compressed column-major storage of the reference's matrices
+ * (FEMContext.cpp:110-112) because the pattern is symmetric.  For
+ * FEA_MATRIX_ADVECTION the values live on the stiffness pattern; `present`
+ * (uint8[nnz], may be NULL) marks the entries that exist in the reference's
+ * advection matrix, whose filter ignores the BC (FEMContext.cpp:188). */
+int fea_get_matrix(fea_solver* s, int which, int32_t* row_ptr, int32_t* col, void* values,
+                   uint8_t* present);
+
+/* Node -> unknown map (FEMContext::idx_map, int32[V]) and boundary flags. */
+int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
+
+/* Pick the lanes-per-row of the CSR SpMV by timing the candidates on this
+ * mesh (2, 4, 8, 16 lanes); the choice is kept in fea_info. */
+int fea_autotune(fea_solver* s);
+
+/* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
+ * their own work or events after it. */
+int fea_get_stream(fea_solver* s, void** stream);
+
+/* Diagnostics: mean device time in ms of the step loop's SpMV kernel (the
+ * dominant kernel of a step) over `reps` launches on the current operator of
+ * the current equation, each launch preceded by a 256 MiB write that evicts
+ * the L2 cache when flush_l2 != 0.  CUDA events on the handle's stream. */
+int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch);
+
+/* ---- adjoint (explicit advection-diffusion) ------------------------------
+ * Loss J = 1/2 (u_N - target)^T M (u_N - target) after nsteps explicit
+ * advection-diffusion steps from u0 with the current per-element diffusivity.
+ * Writes J, dJ/du0 (node-indexed float[V]) and dJ/dD (float[T]).  Forward
+ * states are recomputed from checkpoints every `checkpoint_every` steps.
+ * No reference counterpart: the reference has no differentiation. */
+int fea_adjoint_advdiff(fea_solver* s, const float* u0, const float* target, int64_t nsteps,
+                        int64_t checkpoint_every, double* loss, float* grad_u0, float* grad_D);
+/* Device-resident variant, unknown-indexed arrays in the handle's precision;
+ * grad_D is [T]. */
+int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target, int64_t nsteps,
+                               int64_t checkpoint_every, double* loss, void* grad_u0, void* grad_D);
+
+/* ---- batched Gray-Scott ---------------------------------------------------
+ * Many independent meshes with their own (F, k, Du, Dv, dt), stepped together
+ * by one persistent kernel per CG phase.  No reference counterpart (the
+ * reference steps one mesh); each instance follows the Gray-Scott step of
+ * CPUSolver.cpp:127-145 with reaction_mode 1. */
+typedef struct {
+    const float* vertices;      /* xyz float[3V] */
+    int64_t num_vertices;
+    const uint32_t* triangles;  /* uint32[3T] */
+    int64_t num_triangles;
+    int boundary_condition;
+    float time_step, Du, Dv, feed_rate, kill_rate;
+} fea_instance_desc;
+
+typedef struct fea_batch fea_batch;
+
+int fea_batch_create(const fea_instance_desc* instances, int num_instances, int precision,
+                     double cg_tolerance, int cg_max_iterations, fea_batch** out);
+int fea_batch_destroy(fea_batch* b);
+/* u, v: node-indexed float[V] of instance i */
+int fea_batch_set_fields(fea_batch* b, int instance, const float* u, const float* v);
+int fea_batch_get_fields(fea_batch* b, int instance, float* u, float* v);
+int fea_batch_advance_time(fea_batch* b, int64_t nsteps);
+int fea_batch_synchronize(fea_batch* b);
+/* flags: uint32[num_instances]; iterations: int32[2*num_instances] (last solve) */
+int fea_batch_get_status(fea_batch* b, uint32_t* flags, int32_t* iterations);
+
+/* ---- misc ----------------------------------------------------------------- */
+const char* fea_last_error(void);
+const char* fea_version(void);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEA_GPU_H */

@@ -1,0 +1,281 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle.
+
+Bars: the compressed pattern, boundary flags and idx_map are bit-exact; FP32
+matrix values agree with the FP64 oracle to 2e-6 of the row's largest entry,
+FP64 values to 1e-13; one time step agrees with the FP64 oracle (solved to
+1e-14) to rel-L2 1e-5 per field for FP32 handles and 1e-9 for FP64 handles.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from fea_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+
+MESHES = {
+    "ico3": (lambda: mg.icosphere(3)),
+    "grid33": (lambda: mg.jittered_grid(33, seed=2)),
+    "grid_right": (lambda: mg.jittered_grid(17, seed=0, jitter=0.0)),
+    "cyl": (lambda: mg.cylinder(40, 15)),
+}
+
+
+def _solver(fea, xyz, tri, bc, precision=None, **kw):
+    p = fea.default_params(**kw)
+    return fea.CUDASolver(xyz, tri, boundary_condition=bc, precision=fea.FP32 if precision is None else precision,
+                          params=p)
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("bc", [0, 1])
+def test_pattern_and_boundary_bit_exact(fea, oracle_mod, name, bc):
+    xyz, tri = MESHES[name]()
+    s = _solver(fea, xyz, tri, bc)
+    S = oracle_mod.System(xyz, tri, bc=bc)
+    idx, ob = s.idx_map()
+    np.testing.assert_array_equal(ob, S.on_boundary)
+    np.testing.assert_array_equal(idx, S.idx)
+    inf = s.info
+    assert (inf.num_unknowns, inf.nnz, inf.max_row_nonzeros) == (S.N, S.nnz, S.max_row_nonzeros)
+    assert inf.num_boundary_points == S.num_boundary
+    rp, col, _, _ = s.matrix(fea.STIFFNESS)
+    np.testing.assert_array_equal(rp, S.row_ptr)
+    np.testing.assert_array_equal(col, S.col)
+    _, _, _, pres = s.matrix(fea.ADVECTION)
+    np.testing.assert_array_equal(pres, S.adv_present)
+
+
+def _row_scale(S, val):
+    rows = np.repeat(np.arange(S.N), np.diff(S.row_ptr))
+    mx = np.zeros(S.N)
+    np.maximum.at(mx, rows, np.abs(val))
+    return mx[rows]
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("precision", [0, 1])
+def test_matrix_values(fea, oracle_mod, name, precision):
+    xyz, tri = MESHES[name]()
+    vel = (0.3, 1.0, -0.2)
+    s = _solver(fea, xyz, tri, 1, precision, advdiff_velocity=vel)
+    S = oracle_mod.System(xyz, tri, bc=1, velocity=vel)
+    tol = 2e-6 if precision == 0 else 1e-13
+    for which, ref in ((fea.STIFFNESS, S.K), (fea.MASS, S.M), (fea.ADVECTION, S.Adv)):
+        _, _, val, _ = s.matrix(which)
+        err = np.abs(val.astype(np.float64) - ref) / np.maximum(_row_scale(S, ref), 1e-30)
+        assert err.max() < tol, (which, err.max())
+
+
+def test_assembly_deterministic(fea):
+    xyz, tri = mg.jittered_grid(65, seed=4)
+    a = _solver(fea, xyz, tri, 1).matrix(fea.STIFFNESS)[2]
+    b = _solver(fea, xyz, tri, 1).matrix(fea.STIFFNESS)[2]
+    assert np.array_equal(a, b)
+
+
+def test_explicit_zeros_kept_on_device(fea, oracle_mod):
+    xyz, tri = mg.jittered_grid(9, seed=0, jitter=0.0)
+    s = _solver(fea, xyz, tri, 1)
+    _, _, val, _ = s.matrix(fea.STIFFNESS)
+    S = oracle_mod.System(xyz, tri, bc=1)
+    assert np.array_equal(val == 0, S.K == 0) and np.sum(val == 0) > 0
+
+
+def _oracle_step(oracle_mod, S, eq, dt, u, v, n, **kw):
+    p = oracle_mod.params(eq, dt, tol=1e-14, **kw)
+    a = None
+    if eq == oracle_mod.WAVE and kw.get("wave_scheme", 0) == 1:
+        a = S.newmark_init(p, u)
+    return S.step(p, u, v, a, nsteps=n)
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-5), (1, 1e-9)])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_heat_steps(fea, oracle_mod, precision, tol, bc):
+    xyz, tri = mg.cylinder(48, 20) if bc == 0 else mg.icosphere(4)
+    u0 = np.exp(-np.sum((xyz - xyz[7]) ** 2, axis=1) / 0.1).astype(np.float32)
+    s = _solver(fea, xyz, tri, bc, precision, equation=fea.HEAT, heat_time_step=1e-2, heat_conductivity=1.0,
+                cg_tolerance=1e-7 if precision == 0 else 1e-12)
+    s.set_values(u0)
+    S = oracle_mod.System(xyz, tri, bc=bc)
+    u = S.gather(u0.astype(np.float64))
+    for step in range(3):
+        s.advance_time(1)
+        u, *_ = _oracle_step(oracle_mod, S, oracle_mod.HEAT, 1e-2, u, np.zeros(S.N), 1, kappa=1.0)
+        g = s.get_values()
+        assert rel_l2(g, S.scatter(u)) < tol, step
+        if bc == 0:
+            assert np.all(g[S.on_boundary == 1] == 0)  # map_vector_to_surface
+    st = s.status()
+    assert st.flags == 0 and st.steps_done == 1 and st.last_iterations[0] > 0
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gray_scott_per_step(fea, oracle_mod, mode):
+    """Per-step error from the oracle's state, and 20-step drift."""
+    xyz, tri = mg.jittered_grid(65, seed=8)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=2, side=0.12)
+    if mode == 1:
+        kw = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+    else:  # the reference's own defaults (EquationParameters.hpp:37-49)
+        kw = dict()
+    s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=mode, cg_tolerance=1e-7, **kw)
+    p = s.params
+    S = oracle_mod.System(xyz, tri, bc=1)
+    okw = dict(Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate, reaction_mode=mode)
+    u, v = S.gather(u0), S.gather(v0)
+    s.set_fields(u0, v0)
+    for step in range(3):
+        s.set_fields(S.scatter(u).astype(np.float32), S.scatter(v).astype(np.float32))
+        uo, vo, *_ = _oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step,
+                                  S.gather(S.scatter(u).astype(np.float32)),
+                                  S.gather(S.scatter(v).astype(np.float32)), 1, **okw)
+        s.advance_time(1)
+        ug, vg = s.get_fields()
+        assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, step
+        np.testing.assert_array_equal(s.get_values(), vg)  # the surface shows v
+        u, v = uo, vo
+    # drift over 20 steps from the same start
+    s.set_fields(u0, v0)
+    s.advance_time(20)
+    ug, vg = s.get_fields()
+    uo, vo, *_ = _oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
+                              S.gather(v0), 20, **okw)
+    assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5
+    assert s.status().steps_done == 20
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_wave_steps(fea, oracle_mod, scheme):
+    xyz, tri = mg.icosphere(4)
+    u0 = mg.gaussian_bumps(xyz, seed=5, n_bumps=3, width2=0.05, amplitude=(-1, 1)).astype(np.float32)
+    dt, c = 2e-3, 1.0
+    s = _solver(fea, xyz, tri, 1, equation=fea.WAVE, wave_time_step=dt, wave_c=c, wave_scheme=scheme,
+                cg_tolerance=1e-7)
+    s.set_fields(u0, np.zeros_like(u0))
+    S = oracle_mod.System(xyz, tri, bc=1)
+    s.advance_time(10)
+    ug, vg = s.get_fields()
+    uo, vo, *_ = _oracle_step(oracle_mod, S, oracle_mod.WAVE, dt, S.gather(u0), np.zeros(S.N), 10, kappa=c,
+                              wave_scheme=scheme)
+    assert rel_l2(ug, S.scatter(uo)) < 1e-5
+    assert rel_l2(vg, S.scatter(vo)) < 1e-4
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_advection_diffusion_steps(fea, oracle_mod, scheme):
+    xyz, tri = mg.jittered_grid(41, seed=6)
+    vel = (1.0, 0.3, 0.0)
+    u0 = np.exp(-((xyz[:, 0] - 0.4) ** 2 + (xyz[:, 1] - 0.5) ** 2) / 0.01).astype(np.float32)
+    sign = -1.0 if scheme == 1 else 1.0
+    s = _solver(fea, xyz, tri, 1, equation=fea.ADVECTION_DIFFUSION, advdiff_time_step=1e-3, advdiff_c=0.05,
+                advdiff_velocity=vel, advection_scheme=scheme, advection_sign=sign, cg_tolerance=1e-7,
+                cg_max_iterations=2000)
+    s.set_values(u0)
+    S = oracle_mod.System(xyz, tri, bc=1, velocity=vel)
+    s.advance_time(5)
+    uo, *_ = _oracle_step(oracle_mod, S, oracle_mod.ADVECTION_DIFFUSION, 1e-3, S.gather(u0), np.zeros(S.N), 5,
+                          kappa=0.05, adv_scheme=scheme, adv_sign=sign)
+    assert rel_l2(s.get_values(), S.scatter(uo)) < 1e-5
+
+
+def test_per_element_diffusivity(fea, oracle_mod):
+    xyz, tri = mg.jittered_grid(33, seed=1)
+    D = (1e-2 * np.exp(0.5 * mg.fourier_field(xyz[tri].mean(axis=1), seed=2))).astype(np.float32)
+    s = _solver(fea, xyz, tri, 1, equation=fea.HEAT, heat_time_step=1e-2, heat_conductivity=1.0,
+                cg_tolerance=1e-7)
+    s.set_element_fields(diffusivity=D)
+    S = oracle_mod.System(xyz, tri, bc=1, diffusivity=D.astype(np.float64))
+    _, _, K, _ = s.matrix(fea.STIFFNESS)
+    assert np.abs(K - S.K).max() / np.abs(S.K).max() < 2e-6
+    u0 = np.sin(3 * xyz[:, 0]).astype(np.float32)
+    s.set_values(u0)
+    s.advance_time(4)
+    uo, *_ = _oracle_step(oracle_mod, S, oracle_mod.HEAT, 1e-2, S.gather(u0), np.zeros(S.N), 4, kappa=1.0)
+    assert rel_l2(s.get_values(), S.scatter(uo)) < 1e-5
+
+
+def test_instability_detection(fea):
+    """has_numerical_instability (CPUSolver.cpp:41-48): > 1e4 and non-finite values."""
+    xyz, tri = mg.icosphere(2)
+    s = _solver(fea, xyz, tri, 1, equation=fea.HEAT, heat_time_step=1e-2, heat_conductivity=1.0)
+    u = np.zeros(xyz.shape[0], np.float32)
+    s.set_values(u)
+    s.advance_time(2)
+    assert not s.has_numerical_instability()
+    u[3] = 5e4
+    s.set_values(u)
+    s.advance_time(5)
+    assert s.has_numerical_instability()
+    st = s.status()
+    assert st.flags & 1 and st.steps_done == 0  # stepping stopped before touching the state
+    np.testing.assert_array_equal(s.get_values(), u)
+    u[3] = np.nan
+    s.set_values(u)
+    s.advance_time(1)
+    assert s.status().flags & 2
+    s.clear_values()
+    assert not s.has_numerical_instability()
+    assert np.all(s.get_values() == 0)
+
+
+def test_max_iterations_flag(fea):
+    xyz, tri = mg.icosphere(3)
+    s = _solver(fea, xyz, tri, 1, equation=fea.HEAT, heat_time_step=1.0, heat_conductivity=1.0,
+                cg_max_iterations=2, cg_tolerance=1e-12)
+    s.set_values(np.random.default_rng(0).uniform(size=xyz.shape[0]).astype(np.float32))
+    s.advance_time(1)
+    st = s.status()
+    assert st.flags & 4 and st.last_iterations[0] == 2
+
+
+def test_device_field_roundtrip(fea):
+    import torch
+    xyz, tri = mg.jittered_grid(17, seed=3)
+    s = _solver(fea, xyz, tri, 0, equation=fea.REACTION_DIFFUSION)
+    N = s.info.num_unknowns
+    u = torch.rand(N, device="cuda", dtype=torch.float32)
+    v = torch.rand(N, device="cuda", dtype=torch.float32)
+    s.set_fields_device(u.data_ptr(), v.data_ptr())
+    u2 = torch.empty_like(u)
+    v2 = torch.empty_like(v)
+    s.get_fields_device(u2.data_ptr(), v2.data_ptr())
+    assert torch.equal(u, u2) and torch.equal(v, v2)
+    idx, _ = s.idx_map()
+    hu, hv = s.get_fields()
+    m = idx >= 0
+    assert np.array_equal(hu[m], u.cpu().numpy()[idx[m]])
+    assert np.all(hu[~m] == 0)
+
+
+def test_step_determinism(fea):
+    xyz, tri = mg.jittered_grid(65, seed=2)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=1, side=0.1)
+    outs = []
+    for _ in range(2):
+        s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=1.0,
+                    rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+        s.set_fields(u0, v0)
+        s.advance_time(5)
+        outs.append(s.get_fields())
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("lanes", [2, 4, 8, 16])
+def test_autotune_choice_is_valid(fea, lanes):
+    xyz, tri = mg.jittered_grid(129, seed=1)
+    s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
+    assert s.autotune() in (2, 4, 8, 16)
+
+
+def test_boundary_condition_switch(fea, oracle_mod):
+    """update_boundary_conditions (FEMContext.cpp:224-240) rebuilds everything."""
+    xyz, tri = mg.cylinder(24, 8)
+    s = _solver(fea, xyz, tri, 1)
+    assert s.info.num_unknowns == xyz.shape[0]
+    s.set_boundary_condition(0)
+    S = oracle_mod.System(xyz, tri, bc=0)
+    assert s.info.num_unknowns == S.N
+    rp, col, _, _ = s.matrix(fea.MASS)
+    np.testing.assert_array_equal(col, S.col)
