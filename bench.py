@@ -166,8 +166,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--grid", type=int, default=GRID_N,
+                    help="vertices per side (other sizes are for profiling captures, not bench lines)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    globals()["GRID_N"] = args.grid
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

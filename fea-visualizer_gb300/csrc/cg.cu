@@ -100,6 +100,15 @@ __device__ __forceinline__ bool grid_reduce(Acc<R> (&acc)[NV], double* part, int
     return last_block_commit<NV>(x, part, stride, ticket, sm, out);
 }
 
+// Loop condition: stored for host-driven loops, and set on the graph's
+// conditional node when the kernel runs inside the step graph.  Called by one
+// thread only (concurrent cudaGraphSetConditional calls are undefined).
+template <typename A>
+__device__ __forceinline__ void signal_loop(const A& a, bool cont) {
+    *a.cont = cont ? 1 : 0;
+    if (a.use_graph) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+}
+
 __device__ __forceinline__ void raise_flags(RunState* run, unsigned int f) {
     const unsigned int w = __reduce_or_sync(0xffffffffu, f);
     if (w && (threadIdx.x & 31) == 0) {
@@ -273,7 +282,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
                     cg->iters[f] = it;
                 }
         }
-        cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+        signal_loop(a, cont);
     }
 }
 
@@ -417,7 +426,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
             cg->active[f] = (!stop && bb > 0.0 && rr >= cg->thr[f]) ? 1 : 0;
             any |= cg->active[f];
         }
-        cudaGraphSetConditional(a.cond, any ? 1u : 0u);
+        signal_loop(a, any != 0);
     }
 }
 
@@ -496,7 +505,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                 }
             }
         }
-        cudaGraphSetConditional(a.cond, any ? 1u : 0u);
+        signal_loop(a, any != 0);
     }
 }
 
@@ -533,12 +542,12 @@ __global__ void k_stepctl(StepArgs<R, NF> a) {
     }
     const int cont = !cg->stop && run->steps_left > 0 &&
                      !(run->flags & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE));
-    cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+    signal_loop(a, cont != 0);
 }
 
 template <typename R, int NF>
 __global__ void k_start(StepArgs<R, NF> a) {
-    cudaGraphSetConditional(a.cond, a.run->steps_left > 0 ? 1u : 0u);
+    signal_loop(a, a.run->steps_left > 0);
 }
 
 // has_numerical_instability of the state after the last step.
@@ -610,46 +619,118 @@ void add_cg_body(cudaGraph_t body, const StepArgs<R, NF>& a) {
     add_kernel(body, n2, k_cg_dir<R, NF>, stream_grid(a.N), kBlock, a);
 }
 
+// The three argument sets of a step: the step loop (a), the first CG loop
+// (a1) and the refinement loop (a2); each names the condition it sets.
+template <typename R, int NF>
+struct LoopArgs {
+    StepArgs<R, NF> a, a1, a2;
+    LoopArgs(const StepArgs<R, NF>& base, LoopFlags* lf, int use_graph) : a(base), a1(base), a2(base) {
+        a.use_graph = a1.use_graph = a2.use_graph = use_graph;
+        a.cont = &lf->step;
+        a1.cont = &lf->cg1;
+        a2.cont = &lf->cg2;
+    }
+};
+
+// Step graph:  start -> WHILE(step) { rhs -> WHILE(cg1) {spmv, update, dir}
+//              -> refine -> WHILE(cg2) {spmv, update, dir} -> [post] -> stepctl }
+//              -> final_check
 template <typename R, int NF, int EQ, int LANES>
-void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base) {
+void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
+    LoopArgs<R, NF> L(base, lf, 1);
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
     G.graph = top;
-    cudaGraphConditionalHandle h_step;
-    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_step, top, 0, 0));
-    StepArgs<R, NF> a = base;
-    a.cond = h_step;
-    cudaGraphNode_t n = add_kernel(top, nullptr, k_start<R, NF>, 1, 1, a);
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a.cond, top, 0, 0));
+    cudaGraphNode_t n = add_kernel(top, nullptr, k_start<R, NF>, 1, 1, L.a);
     cudaGraph_t step_body;
-    n = add_while(top, n, h_step, &step_body);
-    add_kernel(top, n, k_final_check<R, NF, EQ>, stream_grid(a.N), kBlock, a);
-
-    cudaGraphConditionalHandle h_cg1, h_cg2;
-    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_cg1, step_body, 0, 0));
-    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h_cg2, step_body, 0, 0));
-    StepArgs<R, NF> a1 = base, a2 = base;
-    a1.cond = h_cg1;
-    a2.cond = h_cg2;
-    cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, LANES>, row_grid<LANES>(a.N), kBlock, a1);
+    n = add_while(top, n, L.a.cond, &step_body);
+    add_kernel(top, n, k_final_check<R, NF, EQ>, stream_grid(base.N), kBlock, L.a);
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
+    cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, LANES>, row_grid<LANES>(base.N), kBlock, L.a1);
     cudaGraph_t cg_body1, cg_body2;
-    s = add_while(step_body, s, h_cg1, &cg_body1);
-    add_cg_body<R, NF, LANES>(cg_body1, a1);
-    s = add_kernel(step_body, s, k_refine<R, NF, LANES>, row_grid<LANES>(a.N), kBlock, a2);
-    s = add_while(step_body, s, h_cg2, &cg_body2);
-    add_cg_body<R, NF, LANES>(cg_body2, a2);
+    s = add_while(step_body, s, L.a1.cond, &cg_body1);
+    add_cg_body<R, NF, LANES>(cg_body1, L.a1);
+    s = add_kernel(step_body, s, k_refine<R, NF, LANES>, row_grid<LANES>(base.N), kBlock, L.a2);
+    s = add_while(step_body, s, L.a2.cond, &cg_body2);
+    add_cg_body<R, NF, LANES>(cg_body2, L.a2);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
-        s = add_kernel(step_body, s, k_post<R, NF, EQ>, stream_grid(a.N), kBlock, a);
-    add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, a);
+        s = add_kernel(step_body, s, k_post<R, NF, EQ>, stream_grid(base.N), kBlock, L.a);
+    add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
 }
 
+int read_flag(const int* d, cudaStream_t st) {
+    int h = 0;
+    FEA_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    return h;
+}
+
+// The same kernels launched one by one with the loop conditions read back
+// on the host: every kernel is then visible to profilers (kernels inside
+// graphs with conditional nodes are not).  Each loop is bounded by the
+// kernels' own iteration and step limits.
+template <typename R, int NF, int EQ, int LANES>
+void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
+    LoopArgs<R, NF> L(base, lf, 0);
+    const int rg = row_grid<LANES>(base.N), sg = stream_grid(base.N);
+    k_start<R, NF><<<1, 1, 0, st>>>(L.a);
+    FEA_CHECK_LAUNCH();
+    while (read_flag(&lf->step, st)) {
+        k_rhs<R, NF, EQ, LANES><<<rg, kBlock, 0, st>>>(L.a1);
+        FEA_CHECK_LAUNCH();
+        for (const StepArgs<R, NF>* la : {&L.a1, &L.a2}) {
+            if (la == &L.a2) {
+                k_refine<R, NF, LANES><<<rg, kBlock, 0, st>>>(L.a2);
+                FEA_CHECK_LAUNCH();
+            }
+            while (read_flag(la->cont, st)) {
+                k_cg_spmv<R, NF, LANES><<<rg, kBlock, 0, st>>>(*la);
+                k_cg_update<R, NF><<<sg, kBlock, 0, st>>>(*la);
+                k_cg_dir<R, NF><<<sg, kBlock, 0, st>>>(*la);
+                FEA_CHECK_LAUNCH();
+            }
+        }
+        if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK) {
+            k_post<R, NF, EQ><<<sg, kBlock, 0, st>>>(L.a);
+            FEA_CHECK_LAUNCH();
+        }
+        k_stepctl<R, NF><<<1, 1, 0, st>>>(L.a);
+        FEA_CHECK_LAUNCH();
+    }
+    k_final_check<R, NF, EQ><<<sg, kBlock, 0, st>>>(L.a);
+    FEA_CHECK_LAUNCH();
+}
+
 template <typename R, int NF, int EQ>
-void build_graph_lanes(StepGraph& G, const StepArgs<R, NF>& a, int lanes) {
+void dispatch_lanes(StepGraph* G, const StepArgs<R, NF>& a, int lanes, LoopFlags* lf, cudaStream_t st) {
     switch (lanes) {
-    case 2: build_graph_t<R, NF, EQ, 2>(G, a); break;
-    case 4: build_graph_t<R, NF, EQ, 4>(G, a); break;
-    case 16: build_graph_t<R, NF, EQ, 16>(G, a); break;
-    default: build_graph_t<R, NF, EQ, 8>(G, a); break;
+    case 2: G ? build_graph_t<R, NF, EQ, 2>(*G, a, lf) : run_stream_t<R, NF, EQ, 2>(a, lf, st); break;
+    case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
+    case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
+    default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
+    }
+}
+
+template <typename R, int NF>
+void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf, cudaStream_t st) {
+    if constexpr (NF == 1) {
+        switch (kind) {
+        case EQ_HEAT: dispatch_lanes<R, 1, EQ_HEAT>(G, a, lanes, lf, st); break;
+        case EQ_ADV_EXPLICIT: dispatch_lanes<R, 1, EQ_ADV_EXPLICIT>(G, a, lanes, lf, st); break;
+        case EQ_WAVE_REF: dispatch_lanes<R, 1, EQ_WAVE_REF>(G, a, lanes, lf, st); break;
+        case EQ_WAVE_NEWMARK: dispatch_lanes<R, 1, EQ_WAVE_NEWMARK>(G, a, lanes, lf, st); break;
+        case EQ_NEWMARK_INIT: dispatch_lanes<R, 1, EQ_NEWMARK_INIT>(G, a, lanes, lf, st); break;
+        default: throw Error{FEA_ERR_UNSUPPORTED};
+        }
+    } else {
+        switch (kind) {
+        case EQ_GS_REF: dispatch_lanes<R, 2, EQ_GS_REF>(G, a, lanes, lf, st); break;
+        case EQ_GS_CONSISTENT: dispatch_lanes<R, 2, EQ_GS_CONSISTENT>(G, a, lanes, lf, st); break;
+        default: throw Error{FEA_ERR_UNSUPPORTED};
+        }
     }
 }
 
@@ -661,26 +742,16 @@ int max_grid_blocks() {
 }
 
 template <typename R, int NF>
-void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int lanes) {
+void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf) {
     G.destroy();
     G.kind = kind;
     G.lanes = lanes;
-    if constexpr (NF == 1) {
-        switch (kind) {
-        case EQ_HEAT: build_graph_lanes<R, 1, EQ_HEAT>(G, a, lanes); break;
-        case EQ_ADV_EXPLICIT: build_graph_lanes<R, 1, EQ_ADV_EXPLICIT>(G, a, lanes); break;
-        case EQ_WAVE_REF: build_graph_lanes<R, 1, EQ_WAVE_REF>(G, a, lanes); break;
-        case EQ_WAVE_NEWMARK: build_graph_lanes<R, 1, EQ_WAVE_NEWMARK>(G, a, lanes); break;
-        case EQ_NEWMARK_INIT: build_graph_lanes<R, 1, EQ_NEWMARK_INIT>(G, a, lanes); break;
-        default: throw Error{FEA_ERR_UNSUPPORTED};
-        }
-    } else {
-        switch (kind) {
-        case EQ_GS_REF: build_graph_lanes<R, 2, EQ_GS_REF>(G, a, lanes); break;
-        case EQ_GS_CONSISTENT: build_graph_lanes<R, 2, EQ_GS_CONSISTENT>(G, a, lanes); break;
-        default: throw Error{FEA_ERR_UNSUPPORTED};
-        }
-    }
+    dispatch_kind<R, NF>(&G, a, kind, lanes, lf, nullptr);
+}
+
+template <typename R, int NF>
+void run_steps_stream(const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf, cudaStream_t st) {
+    dispatch_kind<R, NF>(nullptr, a, kind, lanes, lf, st);
 }
 
 template <typename R, int NF>
@@ -694,13 +765,13 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st) {
     FEA_CHECK_LAUNCH();
 }
 
-template void build_step_graph<float, 1>(StepGraph&, const StepArgs<float, 1>&, int, int);
-template void build_step_graph<float, 2>(StepGraph&, const StepArgs<float, 2>&, int, int);
-template void build_step_graph<double, 1>(StepGraph&, const StepArgs<double, 1>&, int, int);
-template void build_step_graph<double, 2>(StepGraph&, const StepArgs<double, 2>&, int, int);
-template void launch_spmv_probe<float, 1>(const StepArgs<float, 1>&, int, cudaStream_t);
-template void launch_spmv_probe<float, 2>(const StepArgs<float, 2>&, int, cudaStream_t);
-template void launch_spmv_probe<double, 1>(const StepArgs<double, 1>&, int, cudaStream_t);
-template void launch_spmv_probe<double, 2>(const StepArgs<double, 2>&, int, cudaStream_t);
+#define FEA_INST_STEP(R, NF)                                                                              \
+    template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \
+    template void run_steps_stream<R, NF>(const StepArgs<R, NF>&, int, int, LoopFlags*, cudaStream_t);    \
+    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t);
+FEA_INST_STEP(float, 1)
+FEA_INST_STEP(float, 2)
+FEA_INST_STEP(double, 1)
+FEA_INST_STEP(double, 2)
 
 }  // namespace fea

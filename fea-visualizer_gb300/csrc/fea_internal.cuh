@@ -110,7 +110,14 @@ struct StepArgs {
     double* part;           // block partials [8 * part_stride]
     int part_stride;
     unsigned int* tickets;  // [8]
-    cudaGraphConditionalHandle cond;
+    cudaGraphConditionalHandle cond;  // loop condition set by this kernel (graph mode)
+    int* cont;              // the same condition, also stored here for host-driven loops
+    int use_graph;          // 1: kernels run as graph nodes and set `cond`
+};
+
+// Loop-condition slots in device memory for host-driven (stream) execution.
+struct LoopFlags {
+    int cg1, cg2, step;
 };
 
 // A built step-loop graph for one (precision, fields, equation, lanes) plan.
@@ -127,7 +134,12 @@ struct StepGraph {
 };
 
 template <typename R, int NF>
-void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int lanes);
+void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int lanes, LoopFlags* lf);
+
+// The same step loop launched kernel by kernel, conditions read on the host
+// (profiling mode: FEA_LAUNCH_MODE=stream).
+template <typename R, int NF>
+void run_steps_stream(const StepArgs<R, NF>& base, int kind, int lanes, LoopFlags* lf, cudaStream_t st);
 
 // One SpMV + dot launch with the given lanes per row (autotuning probe).
 template <typename R, int NF>

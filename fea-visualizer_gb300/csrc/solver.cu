@@ -135,6 +135,8 @@ struct fea_solver {
     RunState* d_run = nullptr;
     double* d_part = nullptr;
     unsigned int* d_tickets = nullptr;
+    LoopFlags* d_flags = nullptr;
+    bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
     int lanes = 8;
@@ -387,15 +389,22 @@ void ensure_layout(fea_solver* s, bool interleaved) {
 
 template <typename R, int NF>
 void run_graph(fea_solver* s, StepGraph& g, int kind, bool init_op, int64_t nsteps) {
-    if (!g.exec || g.kind != kind || g.lanes != s->lanes) {
+    const bool stream_mode = s->stream_mode;
+    if (!stream_mode && (!g.exec || g.kind != kind || g.lanes != s->lanes)) {
         StepArgs<R, NF> a = make_args<R, NF>(s, init_op);
         set_x<R, NF>(s, a, kind);
-        build_step_graph<R, NF>(g, a, kind, s->lanes);
+        build_step_graph<R, NF>(g, a, kind, s->lanes, s->d_flags);
     }
     long long ctl[2] = {nsteps, 0};  // steps_left, steps_done
     FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
-    FEA_CUDA_TRY(cudaGraphLaunch(g.exec, s->stream));
+    if (stream_mode) {
+        StepArgs<R, NF> a = make_args<R, NF>(s, init_op);
+        set_x<R, NF>(s, a, kind);
+        run_steps_stream<R, NF>(a, kind, s->lanes, s->d_flags, s->stream);
+    } else {
+        FEA_CUDA_TRY(cudaGraphLaunch(g.exec, s->stream));
+    }
 }
 
 template <typename R>
@@ -484,6 +493,10 @@ void alloc_run_state(fea_solver* s) {
     s->d_run = s->run_mem.alloc<RunState>(1);
     s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
     s->d_tickets = s->run_mem.alloc<unsigned int>(8);
+    s->d_flags = s->run_mem.alloc<LoopFlags>(1);
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, sizeof(LoopFlags), s->stream));
+    const char* mode = getenv("FEA_LAUNCH_MODE");
+    s->stream_mode = mode && strcmp(mode, "stream") == 0;
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_cg, 0, sizeof(CgState), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_run, 0, sizeof(RunState), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_tickets, 0, 8 * sizeof(unsigned int), s->stream));

@@ -82,8 +82,27 @@ def test_explicit_zeros_kept_on_device(fea, oracle_mod):
     assert np.array_equal(val == 0, S.K == 0) and np.sum(val == 0) > 0
 
 
+def _device_field(s, which):
+    """Unknown-indexed state field in the handle's precision (float64 for FP64)."""
+    import torch
+    dt = torch.float64 if s.precision == 1 else torch.float32
+    t = [torch.zeros(s.info.num_unknowns, dtype=dt, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    s.get_fields_device(t[0].data_ptr(), t[1].data_ptr())
+    return t[which].cpu().numpy().astype(np.float64)
+
+
+def _f32(x):
+    return float(np.float32(x))
+
+
 def _oracle_step(oracle_mod, S, eq, dt, u, v, n, **kw):
-    p = oracle_mod.params(eq, dt, tol=1e-14, **kw)
+    """FP64 oracle steps with the float32-rounded parameters the ABI carries
+    (the reference's parameter structs hold floats, EquationParameters.hpp)."""
+    for key in ("kappa", "Du", "Dv", "F", "k", "adv_sign"):
+        if key in kw:
+            kw[key] = _f32(kw[key])
+    p = oracle_mod.params(eq, _f32(dt), tol=1e-14, **kw)
     a = None
     if eq == oracle_mod.WAVE and kw.get("wave_scheme", 0) == 1:
         a = S.newmark_init(p, u)
@@ -104,9 +123,11 @@ def test_heat_steps(fea, oracle_mod, precision, tol, bc):
         s.advance_time(1)
         u, *_ = _oracle_step(oracle_mod, S, oracle_mod.HEAT, 1e-2, u, np.zeros(S.N), 1, kappa=1.0)
         g = s.get_values()
-        assert rel_l2(g, S.scatter(u)) < tol, step
+        assert rel_l2(g, S.scatter(u)) < max(tol, 1e-7), step  # float32 node values
         if bc == 0:
             assert np.all(g[S.on_boundary == 1] == 0)  # map_vector_to_surface
+        if precision == 1:  # full FP64 state through the device API
+            assert rel_l2(_device_field(s, 0), u) < tol, step
     st = s.status()
     assert st.flags == 0 and st.steps_done == 1 and st.last_iterations[0] > 0
 
@@ -237,6 +258,7 @@ def test_device_field_roundtrip(fea):
     N = s.info.num_unknowns
     u = torch.rand(N, device="cuda", dtype=torch.float32)
     v = torch.rand(N, device="cuda", dtype=torch.float32)
+    torch.cuda.synchronize()  # the handle runs on its own stream
     s.set_fields_device(u.data_ptr(), v.data_ptr())
     u2 = torch.empty_like(u)
     v2 = torch.empty_like(v)
