@@ -113,6 +113,8 @@ SIGNATURES = {
     "fea_batch_advance_time": [_P, _I64],
     "fea_batch_synchronize": [_P],
     "fea_batch_get_status": [_P, _P, _P],
+    "fea_pcg_solve_csr_noalloc": [_I64, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int, _P,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double)],
 }
 
 _lib = None

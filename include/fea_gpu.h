@@ -262,6 +262,28 @@ int fea_batch_synchronize(fea_batch* b);
 /* flags: uint32[num_instances]; iterations: int32[2*num_instances] (last solve) */
 int fea_batch_get_status(fea_batch* b, uint32_t* flags, int32_t* iterations);
 
+/* ---- solve without device allocation ---------------------------------------
+ * No counterpart in the reference.  Solves A x = b with Jacobi-preconditioned
+ * CG (the solver of the step loop) on a caller's compressed-row matrix, for
+ * callers that cannot allocate device memory mid-run: a render loop where a
+ * cudaMalloc/cudaFree would stall the frame (cudaFree synchronises the
+ * device), a host framework that has reserved the GPU's memory up front, or
+ * code that must not hit out-of-memory half way through a step.  All
+ * pointers are device pointers: row_ptr int32[n+1], col int32[nnz], values,
+ * b and x of the given precision; x holds the initial guess on entry and the
+ * solution on return.  tolerance <= 0 and max_iterations <= 0 select the
+ * defaults of fea_params (type epsilon or 1e-10, and 2n).  stream may be
+ * NULL (the default stream); the call returns after the solve finished.
+ * The work vectors live in one static device array of 16 MiB + 64 KiB that
+ * every GPU loading the library holds until exit, so n is limited to
+ * 1,048,576 (FP32) or 524,288 (FP64); larger n returns FEA_ERR_TOO_LARGE.
+ * The first call on a device looks up that array's device address; make it
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race, so serialise them per device. */
+int fea_pcg_solve_csr_noalloc(int64_t n, const int32_t* row_ptr, const int32_t* col, const void* values,
+                              const void* b, void* x, int precision, double tolerance, int max_iterations,
+                              void* stream, int* iterations, double* rel_residual);
+
 /* ---- misc ----------------------------------------------------------------- */
 const char* fea_last_error(void);
 const char* fea_version(void);
