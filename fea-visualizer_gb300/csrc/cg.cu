@@ -8,16 +8,17 @@
 // runs the same recurrences with a host round trip per stage; here the loop is
 // a CUDA graph WHILE node whose condition the update kernel sets on the device.
 //
-// Per CG iteration, three kernels:
-//   k_cg_spmv    q = A p (CSR, `LANES` lanes per row) and p.q
+// Per CG iteration, two kernels:
+//   k_cg_spmv    p = z + beta p (fused, two alternating p buffers),
+//                q = A p (warp-cooperative CSR) and p.q
 //   k_cg_update  x += alpha p, r -= alpha q, z = D^-1 r, r.z and r.r,
 //                convergence test and the loop condition
-//   k_cg_dir     p = z + beta p
 // Inner products: FP32 products are accumulated exactly as float-float pairs
 // per thread and per warp, then in FP64 across warps and blocks (the GB300's
 // FP64 pipe is narrow, so FP64 arithmetic is kept off the per-element path).
 // The block partials are combined by the last block to finish, in a fixed
 // order, so every reduction is deterministic.
+#include <algorithm>
 #include <cmath>
 
 #include "fea_internal.cuh"
@@ -167,45 +168,106 @@ struct RowMap {
 
 // ---- kernels --------------------------------------------------------------------
 
-template <typename R, int NF, int LANES>
+// q = A p_new with p_new = z + beta p_old computed for every gathered column
+// (the direction update of the previous iteration, fused; the two p buffers
+// alternate with the iteration parity), plus p_new.q.
+//
+// Warp-cooperative CSR: a warp owns 32 consecutive rows, whose stored entries
+// form one contiguous range.  The warp streams that range in windows of
+// 32*WCH entries: every lane issues WCH coalesced value/column loads, then WCH
+// independent gathers, so each round trip to memory carries a whole window
+// rather than one row.  Products go to shared memory and each lane sums its
+// own row in column order.
+template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(StepArgs<R, NF> a) {
+    constexpr int WIN = 32 * WCH;
+    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
     CgState* cg = a.cg;
+    const int par = cg->iter & 1;
+    const FV<R, NF>* __restrict__ pold = a.pp[par];
+    FV<R, NF>* __restrict__ pnew = a.pp[par ^ 1];
     int act[NF];
+    bool fresh[NF];
+    R beta[NF];
+    bool need_old = false;
 #pragma unroll
-    for (int f = 0; f < NF; f++) act[f] = cg->active[f];
-    Acc<R> acc[NF];
-    RowMap<LANES> m;
-    for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
-        const int64_t row = base + m.grp;
-        R s[NF];
+    for (int f = 0; f < NF; f++) {
+        act[f] = cg->active[f];
+        fresh[f] = cg->fresh[f] != 0;
+        beta[f] = fresh[f] ? (R)0 : (R)cg->beta[f];
+        need_old |= !fresh[f];
+    }
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t N = a.N;
+    Acc<R> dot[NF];
+    for (int64_t r0 = warp * 32; r0 < N; r0 += nwarps * 32) {
+        const int64_t row = r0 + lane;
+        const int32_t rs = ldg(a.rp + (row < N ? row : N));
+        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+        if (lane == 31) re = ldg(a.rp + (r0 + 32 < N ? r0 + 32 : N));
+        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
+        R acc[NF];
 #pragma unroll
-        for (int f = 0; f < NF; f++) s[f] = 0;
-        if (row < a.N) {
-            const int32_t e1 = ldg(a.rp + row + 1);
-            for (int32_t e = ldg(a.rp + row) + m.sub; e < e1; e += LANES) {
-                const FV<R, NF> av = ldfv(a.A + e);
-                const FV<R, NF> pv = ldfv(a.p + ldg(a.col + e));
+        for (int f = 0; f < NF; f++) acc[f] = 0;
+        for (int32_t wb = e0; wb < e1; wb += WIN) {
+            FV<R, NF> av[WCH];
+            int32_t cc[WCH];
 #pragma unroll
-                for (int f = 0; f < NF; f++) s[f] = fma(av.v[f], pv.v[f], s[f]);
+            for (int c = 0; c < WCH; c++) {
+                const int32_t idx = wb + c * 32 + lane;
+                cc[c] = -1;
+                if (idx < e1) {
+                    av[c] = ldfv(a.A + idx);
+                    cc[c] = ldg(a.col + idx);
+                }
             }
+#pragma unroll
+            for (int c = 0; c < WCH; c++) {
+                FV<R, NF> prod;
+#pragma unroll
+                for (int f = 0; f < NF; f++) prod.v[f] = 0;
+                if (cc[c] >= 0) {
+                    const FV<R, NF> zc = ldfv(a.z + cc[c]);
+                    FV<R, NF> pc = zc;
+                    if (need_old) pc = ldfv(pold + cc[c]);
+#pragma unroll
+                    for (int f = 0; f < NF; f++) {
+                        const R pn = fresh[f] ? zc.v[f] : fma(beta[f], pc.v[f], zc.v[f]);
+                        prod.v[f] = av[c].v[f] * pn;
+                    }
+                }
+                sm[wib][c * 32 + lane] = prod;
+            }
+            __syncwarp();
+            const int32_t lo = (rs > wb ? rs : wb) - wb;
+            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
+            for (int32_t k = lo; k < hi; k++) {
+                const FV<R, NF> t = sm[wib][k];
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
+            }
+            __syncwarp();
         }
-#pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1)
-#pragma unroll
-            for (int f = 0; f < NF; f++) s[f] += __shfl_xor_sync(0xffffffffu, s[f], o);
-        if (m.sub == 0 && row < a.N) {
-            FV<R, NF> qv;
-            const FV<R, NF> pr = a.p[row];
+        if (row < N) {
+            const FV<R, NF> zr = ldfv(a.z + row);
+            FV<R, NF> pr = zr, qv;
+            if (need_old) pr = ldfv(pold + row);
 #pragma unroll
             for (int f = 0; f < NF; f++) {
-                qv.v[f] = s[f];
-                acc[f].add_prod(pr.v[f], s[f]);
+                const R pn = fresh[f] ? zr.v[f] : fma(beta[f], pr.v[f], zr.v[f]);
+                pr.v[f] = pn;
+                qv.v[f] = acc[f];
+                dot[f].add_prod(pn, acc[f]);
             }
+            pnew[row] = pr;
             a.q[row] = qv;
         }
     }
     double tot[NF];
-    if (grid_reduce<R, NF>(acc, a.part, a.part_stride, a.tickets + 0, tot) && threadIdx.x == 0) {
+    if (grid_reduce<R, NF>(dot, a.part, a.part_stride, a.tickets + 0, tot) && threadIdx.x == 0) {
 #pragma unroll
         for (int f = 0; f < NF; f++) {
             if (!act[f]) continue;
@@ -222,9 +284,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(StepArgs<R, NF> a) {
     }
 }
 
+// x += alpha p_new, r -= alpha q, z = D^-1 r, r.z and r.r; the last block
+// tests convergence (|r|^2 < tol^2 |b|^2), forms beta and sets the loop
+// condition.  Two unknowns per thread and pass, loads issued up front.
 template <typename R, int NF>
 __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
     CgState* cg = a.cg;
+    const FV<R, NF>* __restrict__ pnew = a.pp[(cg->iter & 1) ^ 1];
     int act[NF];
     R alpha[NF];
 #pragma unroll
@@ -233,21 +299,43 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
         alpha[f] = act[f] ? (R)cg->alpha[f] : (R)0;
     }
     Acc<R> acc[2 * NF];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
-        FV<R, NF> x = a.x[i], r = a.r[i];
-        const FV<R, NF> p = a.p[i], q = a.q[i], d = ldfv(a.dinv + i);
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            if (act[f]) {
-                x.v[f] = fma(alpha[f], p.v[f], x.v[f]);
-                r.v[f] = fma(-alpha[f], q.v[f], r.v[f]);
-            }
-            const R z = d.v[f] * r.v[f];
-            acc[f].add_prod(r.v[f], z);
-            acc[NF + f].add_prod(r.v[f], r.v[f]);
+    const int64_t N = a.N;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < N; i0 += 2 * stride) {
+        const int64_t i1 = i0 + stride;
+        const bool has1 = i1 < N;
+        FV<R, NF> x[2], r[2], p[2], q[2], d[2];
+        x[0] = a.x[i0];
+        r[0] = a.r[i0];
+        p[0] = ldfv(pnew + i0);
+        q[0] = ldfv(a.q + i0);
+        d[0] = ldfv(a.dinv + i0);
+        if (has1) {
+            x[1] = a.x[i1];
+            r[1] = a.r[i1];
+            p[1] = ldfv(pnew + i1);
+            q[1] = ldfv(a.q + i1);
+            d[1] = ldfv(a.dinv + i1);
         }
-        a.x[i] = x;
-        a.r[i] = r;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            if (j == 1 && !has1) break;
+            FV<R, NF> z;
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (act[f]) {
+                    x[j].v[f] = fma(alpha[f], p[j].v[f], x[j].v[f]);
+                    r[j].v[f] = fma(-alpha[f], q[j].v[f], r[j].v[f]);
+                }
+                z.v[f] = d[j].v[f] * r[j].v[f];
+                acc[f].add_prod(r[j].v[f], z.v[f]);
+                acc[NF + f].add_prod(r[j].v[f], r[j].v[f]);
+            }
+            const int64_t i = j ? i1 : i0;
+            a.x[i] = x[j];
+            a.r[i] = r[j];
+            a.z[i] = z;
+        }
     }
     double tot[2 * NF];
     if (grid_reduce<R, 2 * NF>(acc, a.part, a.part_stride, a.tickets + 1, tot) && threadIdx.x == 0) {
@@ -256,6 +344,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
         int any = 0;
 #pragma unroll
         for (int f = 0; f < NF; f++) {
+            cg->fresh[f] = 0;
             if (!act[f]) continue;
             const double rz = tot[f], rr = tot[NF + f];
             cg->rr[f] = rr;
@@ -283,29 +372,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
                 }
         }
         signal_loop(a, cont);
-    }
-}
-
-template <typename R, int NF>
-__global__ void __launch_bounds__(kBlock) k_cg_dir(StepArgs<R, NF> a) {
-    const CgState* cg = a.cg;
-    int act[NF];
-    R beta[NF];
-    bool any = false;
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        act[f] = cg->active[f];
-        beta[f] = (R)cg->beta[f];
-        any = any || act[f];
-    }
-    if (!any) return;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
-        const FV<R, NF> r = a.r[i], d = ldfv(a.dinv + i);
-        FV<R, NF> p = a.p[i];
-#pragma unroll
-        for (int f = 0; f < NF; f++)
-            if (act[f]) p.v[f] = fma(beta[f], p.v[f], d.v[f] * r.v[f]);
-        a.p[i] = p;
     }
 }
 
@@ -400,7 +466,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
             }
             a.b[row] = bv;
             a.r[row] = rv;
-            a.p[row] = pv;
+            a.z[row] = pv;
         }
     }
     raise_flags(a.run, flags);
@@ -423,6 +489,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
             cg->rr[f] = rr;
             cg->rz[f] = rz;
             cg->iters[f] = 0;
+            cg->fresh[f] = 1;  // the first direction is p = z
             cg->active[f] = (!stop && bb > 0.0 && rr >= cg->thr[f]) ? 1 : 0;
             any |= cg->active[f];
         }
@@ -486,7 +553,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                     dots[NF + f].add_prod(rv.v[f], pv.v[f]);
                 }
                 a.r[row] = rv;
-                a.p[row] = pv;
+                a.z[row] = pv;
             }
         }
     }
@@ -496,6 +563,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
 #pragma unroll
         for (int f = 0; f < NF; f++) {
             cg->active[f] = 0;
+            cg->fresh[f] = 1;
             if (refine && !zero[f] && cg->bb[f] > 0.0) {
                 cg->rr[f] = tot[f];
                 if (tot[f] >= cg->thr[f]) {
@@ -598,25 +666,36 @@ cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphCondition
 
 int g_max_grid = 0;
 
-int stream_grid(int64_t n) {
-    int64_t g = ceil_div(n, kBlock);
+// Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
+// calculator), capped by the work and by the partial-sum stride.
+template <typename K>
+int wave_grid(K kernel, int64_t work_blocks) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t g = (int64_t)num_sms() * per_sm;
     if (g > max_grid_blocks()) g = max_grid_blocks();
+    if (g > work_blocks) g = work_blocks;
     return (int)(g < 1 ? 1 : g);
 }
 
-template <int LANES>
-int row_grid(int64_t n) {
-    const int64_t rpb = (kBlock / 32) * (32 / LANES);  // rows per block per pass
-    int64_t g = ceil_div(n, rpb);
-    if (g > max_grid_blocks()) g = max_grid_blocks();
-    return (int)(g < 1 ? 1 : g);
-}
+constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
-template <typename R, int NF, int LANES>
-void add_cg_body(cudaGraph_t body, const StepArgs<R, NF>& a) {
-    cudaGraphNode_t n1 = add_kernel(body, nullptr, k_cg_spmv<R, NF, LANES>, row_grid<LANES>(a.N), kBlock, a);
-    cudaGraphNode_t n2 = add_kernel(body, n1, k_cg_update<R, NF>, stream_grid(a.N), kBlock, a);
-    add_kernel(body, n2, k_cg_dir<R, NF>, stream_grid(a.N), kBlock, a);
+template <typename R, int NF, int WCH>
+struct Grids {
+    int spmv, update, rhs, stream;
+    explicit Grids(int64_t N) {
+        spmv = wave_grid(k_cg_spmv<R, NF, WCH>, ceil_div(N, kBlock));
+        update = wave_grid(k_cg_update<R, NF>, ceil_div(N, 2 * kBlock));
+        rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
+        stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
+    }
+};
+
+template <typename R, int NF, int WCH>
+void add_cg_body(cudaGraph_t body, const StepArgs<R, NF>& a, const Grids<R, NF, WCH>& g) {
+    cudaGraphNode_t n1 = add_kernel(body, nullptr, k_cg_spmv<R, NF, WCH>, g.spmv, kBlock, a);
+    add_kernel(body, n1, k_cg_update<R, NF>, g.update, kBlock, a);
 }
 
 // The three argument sets of a step: the step loop (a), the first CG loop
@@ -632,12 +711,13 @@ struct LoopArgs {
     }
 };
 
-// Step graph:  start -> WHILE(step) { rhs -> WHILE(cg1) {spmv, update, dir}
-//              -> refine -> WHILE(cg2) {spmv, update, dir} -> [post] -> stepctl }
+// Step graph:  start -> WHILE(step) { rhs -> WHILE(cg1) {spmv, update}
+//              -> refine -> WHILE(cg2) {spmv, update} -> [post] -> stepctl }
 //              -> final_check
-template <typename R, int NF, int EQ, int LANES>
+template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
+    const Grids<R, NF, WCH> g(base.N);
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
     G.graph = top;
@@ -645,18 +725,18 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     cudaGraphNode_t n = add_kernel(top, nullptr, k_start<R, NF>, 1, 1, L.a);
     cudaGraph_t step_body;
     n = add_while(top, n, L.a.cond, &step_body);
-    add_kernel(top, n, k_final_check<R, NF, EQ>, stream_grid(base.N), kBlock, L.a);
+    add_kernel(top, n, k_final_check<R, NF, EQ>, g.stream, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
-    cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, LANES>, row_grid<LANES>(base.N), kBlock, L.a1);
+    cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
     cudaGraph_t cg_body1, cg_body2;
     s = add_while(step_body, s, L.a1.cond, &cg_body1);
-    add_cg_body<R, NF, LANES>(cg_body1, L.a1);
-    s = add_kernel(step_body, s, k_refine<R, NF, LANES>, row_grid<LANES>(base.N), kBlock, L.a2);
+    add_cg_body<R, NF, WCH>(cg_body1, L.a1, g);
+    s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
     s = add_while(step_body, s, L.a2.cond, &cg_body2);
-    add_cg_body<R, NF, LANES>(cg_body2, L.a2);
+    add_cg_body<R, NF, WCH>(cg_body2, L.a2, g);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
-        s = add_kernel(step_body, s, k_post<R, NF, EQ>, stream_grid(base.N), kBlock, L.a);
+        s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
 }
@@ -672,42 +752,41 @@ int read_flag(const int* d, cudaStream_t st) {
 // on the host: every kernel is then visible to profilers (kernels inside
 // graphs with conditional nodes are not).  Each loop is bounded by the
 // kernels' own iteration and step limits.
-template <typename R, int NF, int EQ, int LANES>
+template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
-    const int rg = row_grid<LANES>(base.N), sg = stream_grid(base.N);
+    const Grids<R, NF, WCH> g(base.N);
     k_start<R, NF><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_flag(&lf->step, st)) {
-        k_rhs<R, NF, EQ, LANES><<<rg, kBlock, 0, st>>>(L.a1);
+        k_rhs<R, NF, EQ, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
         for (const StepArgs<R, NF>* la : {&L.a1, &L.a2}) {
             if (la == &L.a2) {
-                k_refine<R, NF, LANES><<<rg, kBlock, 0, st>>>(L.a2);
+                k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
             while (read_flag(la->cont, st)) {
-                k_cg_spmv<R, NF, LANES><<<rg, kBlock, 0, st>>>(*la);
-                k_cg_update<R, NF><<<sg, kBlock, 0, st>>>(*la);
-                k_cg_dir<R, NF><<<sg, kBlock, 0, st>>>(*la);
+                k_cg_spmv<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
+                k_cg_update<R, NF><<<g.update, kBlock, 0, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK) {
-            k_post<R, NF, EQ><<<sg, kBlock, 0, st>>>(L.a);
+            k_post<R, NF, EQ><<<g.stream, kBlock, 0, st>>>(L.a);
             FEA_CHECK_LAUNCH();
         }
         k_stepctl<R, NF><<<1, 1, 0, st>>>(L.a);
         FEA_CHECK_LAUNCH();
     }
-    k_final_check<R, NF, EQ><<<sg, kBlock, 0, st>>>(L.a);
+    k_final_check<R, NF, EQ><<<g.stream, kBlock, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
 }
 
+// SpMV variants: entries streamed per lane and window (the autotuned shape).
 template <typename R, int NF, int EQ>
-void dispatch_lanes(StepGraph* G, const StepArgs<R, NF>& a, int lanes, LoopFlags* lf, cudaStream_t st) {
-    switch (lanes) {
-    case 2: G ? build_graph_t<R, NF, EQ, 2>(*G, a, lf) : run_stream_t<R, NF, EQ, 2>(a, lf, st); break;
+void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags* lf, cudaStream_t st) {
+    switch (wch) {
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -715,20 +794,20 @@ void dispatch_lanes(StepGraph* G, const StepArgs<R, NF>& a, int lanes, LoopFlags
 }
 
 template <typename R, int NF>
-void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf, cudaStream_t st) {
+void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
     if constexpr (NF == 1) {
         switch (kind) {
-        case EQ_HEAT: dispatch_lanes<R, 1, EQ_HEAT>(G, a, lanes, lf, st); break;
-        case EQ_ADV_EXPLICIT: dispatch_lanes<R, 1, EQ_ADV_EXPLICIT>(G, a, lanes, lf, st); break;
-        case EQ_WAVE_REF: dispatch_lanes<R, 1, EQ_WAVE_REF>(G, a, lanes, lf, st); break;
-        case EQ_WAVE_NEWMARK: dispatch_lanes<R, 1, EQ_WAVE_NEWMARK>(G, a, lanes, lf, st); break;
-        case EQ_NEWMARK_INIT: dispatch_lanes<R, 1, EQ_NEWMARK_INIT>(G, a, lanes, lf, st); break;
+        case EQ_HEAT: dispatch_variant<R, 1, EQ_HEAT>(G, a, wch, lf, st); break;
+        case EQ_ADV_EXPLICIT: dispatch_variant<R, 1, EQ_ADV_EXPLICIT>(G, a, wch, lf, st); break;
+        case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, wch, lf, st); break;
+        case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, wch, lf, st); break;
+        case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     } else {
         switch (kind) {
-        case EQ_GS_REF: dispatch_lanes<R, 2, EQ_GS_REF>(G, a, lanes, lf, st); break;
-        case EQ_GS_CONSISTENT: dispatch_lanes<R, 2, EQ_GS_CONSISTENT>(G, a, lanes, lf, st); break;
+        case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, wch, lf, st); break;
+        case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     }
@@ -742,25 +821,24 @@ int max_grid_blocks() {
 }
 
 template <typename R, int NF>
-void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf) {
+void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf) {
     G.destroy();
     G.kind = kind;
-    G.lanes = lanes;
-    dispatch_kind<R, NF>(&G, a, kind, lanes, lf, nullptr);
+    G.lanes = wch;
+    dispatch_kind<R, NF>(&G, a, kind, wch, lf, nullptr);
 }
 
 template <typename R, int NF>
-void run_steps_stream(const StepArgs<R, NF>& a, int kind, int lanes, LoopFlags* lf, cudaStream_t st) {
-    dispatch_kind<R, NF>(nullptr, a, kind, lanes, lf, st);
+void run_steps_stream(const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
+    dispatch_kind<R, NF>(nullptr, a, kind, wch, lf, st);
 }
 
 template <typename R, int NF>
-void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st) {
-    switch (lanes) {
-    case 2: k_cg_spmv<R, NF, 2><<<row_grid<2>(a.N), kBlock, 0, st>>>(a); break;
-    case 4: k_cg_spmv<R, NF, 4><<<row_grid<4>(a.N), kBlock, 0, st>>>(a); break;
-    case 16: k_cg_spmv<R, NF, 16><<<row_grid<16>(a.N), kBlock, 0, st>>>(a); break;
-    default: k_cg_spmv<R, NF, 8><<<row_grid<8>(a.N), kBlock, 0, st>>>(a); break;
+void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
+    switch (wch) {
+    case 4: k_cg_spmv<R, NF, 4><<<Grids<R, NF, 4>(a.N).spmv, kBlock, 0, st>>>(a); break;
+    case 16: k_cg_spmv<R, NF, 16><<<Grids<R, NF, 16>(a.N).spmv, kBlock, 0, st>>>(a); break;
+    default: k_cg_spmv<R, NF, 8><<<Grids<R, NF, 8>(a.N).spmv, kBlock, 0, st>>>(a); break;
     }
     FEA_CHECK_LAUNCH();
 }

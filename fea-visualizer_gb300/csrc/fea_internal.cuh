@@ -67,6 +67,7 @@ struct StepParams {
 struct CgState {
     double rz[2], rr[2], pq[2], thr[2], bb[2], alpha[2], beta[2];
     int active[2];
+    int fresh[2];  // the next direction is p = z (first iteration of a loop)
     int iters[2];
     int iter;
     int max_iter;
@@ -97,7 +98,8 @@ struct StepArgs {
     FV<R, NF>* x;           // unknown of the solve (warm start and result)
     FV<R, NF>* b;
     FV<R, NF>* r;
-    FV<R, NF>* p;
+    FV<R, NF>* z;           // D^-1 r
+    FV<R, NF>* pp[2];       // search directions, alternating with the iteration parity
     FV<R, NF>* q;
     R* u;                   // NF == 1 equations: displacement / field
     R* v;                   // velocity (wave)

@@ -94,11 +94,11 @@ struct Fields {
     void* vt = nullptr;
     void* uv = nullptr;  // R[2N] interleaved (Gray-Scott)
     bool interleaved = false;  // (u, v) currently live in uv
-    // solver work, one field
-    void *A1 = nullptr, *d1 = nullptr, *b1 = nullptr, *r1 = nullptr, *p1 = nullptr, *q1 = nullptr;
+    // solver work, one field (p1 holds the two alternating direction buffers)
+    void *A1 = nullptr, *d1 = nullptr, *b1 = nullptr, *r1 = nullptr, *z1 = nullptr, *p1 = nullptr, *q1 = nullptr;
     void *A0 = nullptr, *d0 = nullptr;  // Newmark start-up operator (M)
     // two fields
-    void *A2 = nullptr, *d2 = nullptr, *b2 = nullptr, *r2 = nullptr, *p2 = nullptr, *q2 = nullptr;
+    void *A2 = nullptr, *d2 = nullptr, *b2 = nullptr, *r2 = nullptr, *z2 = nullptr, *p2 = nullptr, *q2 = nullptr;
 };
 
 }  // namespace fea
@@ -139,7 +139,7 @@ struct fea_solver {
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
-    int lanes = 8;
+    int lanes = 8;  // SpMV variant: entries per lane and window (4, 8, 16)
     bool op_dirty = true;
     int op_kind = -1;
     bool acc_valid = false;
@@ -228,7 +228,8 @@ void build_context(fea_solver* s) {
     F.d1 = ralloc(s->mat_mem, s, N);
     F.b1 = ralloc(s->mat_mem, s, N);
     F.r1 = ralloc(s->mat_mem, s, N);
-    F.p1 = ralloc(s->mat_mem, s, N);
+    F.z1 = ralloc(s->mat_mem, s, N);
+    F.p1 = ralloc(s->mat_mem, s, 2 * N);
     F.q1 = ralloc(s->mat_mem, s, N);
     F.A0 = ralloc(s->mat_mem, s, nnz);
     F.d0 = ralloc(s->mat_mem, s, N);
@@ -236,12 +237,16 @@ void build_context(fea_solver* s) {
     F.d2 = ralloc(s->mat_mem, s, 2 * N);
     F.b2 = ralloc(s->mat_mem, s, 2 * N);
     F.r2 = ralloc(s->mat_mem, s, 2 * N);
-    F.p2 = ralloc(s->mat_mem, s, 2 * N);
+    F.z2 = ralloc(s->mat_mem, s, 2 * N);
+    F.p2 = ralloc(s->mat_mem, s, 4 * N);
     F.q2 = ralloc(s->mat_mem, s, 2 * N);
-    for (void* p : {F.u, F.v, F.a, F.ut, F.vt, F.uv, F.b1, F.r1, F.p1, F.q1, F.b2, F.r2, F.p2, F.q2}) {
-        const int64_t n = (p == F.uv || p == F.b2 || p == F.r2 || p == F.p2 || p == F.q2) ? 2 * N : N;
-        FEA_CUDA_TRY(cudaMemsetAsync(p, 0, rsize(s) * (size_t)(n > 0 ? n : 1), st));
-    }
+    // every vector starts at zero (the direction buffers are read with weight
+    // beta = 0 only after a write, but a zero start keeps them finite)
+    const std::pair<void*, int64_t> zeroed[] = {
+        {F.u, N}, {F.v, N}, {F.a, N}, {F.ut, N}, {F.vt, N}, {F.uv, 2 * N}, {F.b1, N}, {F.r1, N}, {F.z1, N},
+        {F.p1, 2 * N}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 2 * N}, {F.z2, 2 * N}, {F.p2, 4 * N}, {F.q2, 2 * N}};
+    for (const auto& zv : zeroed)
+        FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
     F.interleaved = false;
     s->acc_valid = false;
     assemble(s);
@@ -263,14 +268,18 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.dinv = (const FV<R, 1>*)(init_op ? F.d0 : F.d1);
         a.b = (FV<R, 1>*)F.b1;
         a.r = (FV<R, 1>*)F.r1;
-        a.p = (FV<R, 1>*)F.p1;
+        a.z = (FV<R, 1>*)F.z1;
+        a.pp[0] = (FV<R, 1>*)F.p1;
+        a.pp[1] = a.pp[0] + s->N;
         a.q = (FV<R, 1>*)F.q1;
     } else {
         a.A = (const FV<R, 2>*)F.A2;
         a.dinv = (const FV<R, 2>*)F.d2;
         a.b = (FV<R, 2>*)F.b2;
         a.r = (FV<R, 2>*)F.r2;
-        a.p = (FV<R, 2>*)F.p2;
+        a.z = (FV<R, 2>*)F.z2;
+        a.pp[0] = (FV<R, 2>*)F.p2;
+        a.pp[1] = a.pp[0] + s->N;
         a.q = (FV<R, 2>*)F.q2;
     }
     a.u = (R*)F.u;
@@ -875,7 +884,7 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[4] = {2, 4, 8, 16};
+    const int cand[3] = {4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
