@@ -111,20 +111,27 @@ __global__ void k_ordered_sum_adv(const int32_t* __restrict__ seg_start, const i
 }
 
 template <typename R, int NF>
-__global__ void k_combine(int64_t nnz, const R* __restrict__ M, const R* __restrict__ K,
-                          const R* __restrict__ Adv, OpCoef<R, NF> c, FV<R, NF>* A) {
+__global__ void k_combine(int64_t nnz, const double* __restrict__ M, const double* __restrict__ K,
+                          const double* __restrict__ Adv, OpCoef<NF> c, FV<R, NF>* A) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
-        const R m = M[e], kk = K[e];
-        const R ad = Adv ? Adv[e] : (R)0;
+        const double m = M[e], kk = K[e];
+        const double ad = Adv ? Adv[e] : 0.0;
         FV<R, NF> out;
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-            R v = add_rn(div_rn(m, c.md[f]), mul_rn(mul_rn(c.k1[f], kk), c.k2[f]));
-            if (c.a1[f] != (R)0) v = add_rn(v, mul_rn(c.a1[f], ad));
-            out.v[f] = v;
+            const OpCoef1& cf = c.f[f];
+            double v = add_rn(div_rn(m, cf.md), mul_rn(mul_rn(cf.k1, kk), cf.k2));
+            if (cf.a1 != 0.0) v = add_rn(v, mul_rn(cf.a1, ad));
+            out.v[f] = (R)v;
         }
         A[e] = out;
     }
+}
+
+template <typename R>
+__global__ void k_round_copy(const double* __restrict__ in, int64_t n, R* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (R)in[i];
 }
 
 // Inverse diagonal (Eigen's DiagonalPreconditioner: 1 where the diagonal is 0).
@@ -171,7 +178,7 @@ void ordered_sum_adv(const Pattern& P, const R* loc, const uint32_t* tri, const 
 }
 
 template <typename R, int NF>
-void combine_operator(const Pattern& P, const R* M, const R* K, const R* Adv, const OpCoef<R, NF>& c,
+void combine_operator(const Pattern& P, const double* M, const double* K, const double* Adv, const OpCoef<NF>& c,
                       FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st) {
     if (P.nnz > 0) {
         k_combine<R, NF><<<launch_grid(P.nnz), kBlock, 0, st>>>(P.nnz, M, K, Adv, c, A);
@@ -183,16 +190,24 @@ void combine_operator(const Pattern& P, const R* M, const R* K, const R* Adv, co
     }
 }
 
+template <typename R>
+void round_copy(const double* in, int64_t n, R* out, cudaStream_t st) {
+    if (n <= 0) return;
+    k_round_copy<R><<<launch_grid(n), kBlock, 0, st>>>(in, n, out);
+    FEA_CHECK_LAUNCH();
+}
+
 #define FEA_INST_R(R)                                                                                       \
     template void element_matrices<R>(const float*, const uint32_t*, int64_t, int, const float*, const float*, \
                                       R*, R*, R*, cudaStream_t);                                           \
     template void ordered_sum<R>(const Pattern&, const R*, const R*, R*, cudaStream_t);                    \
     template void ordered_sum_adv<R>(const Pattern&, const R*, const uint32_t*, const uint8_t*, R*, uint8_t*, \
                                      cudaStream_t);                                                        \
-    template void combine_operator<R, 1>(const Pattern&, const R*, const R*, const R*, const OpCoef<R, 1>&,  \
-                                         FV<R, 1>*, FV<R, 1>*, cudaStream_t);                              \
-    template void combine_operator<R, 2>(const Pattern&, const R*, const R*, const R*, const OpCoef<R, 2>&,  \
-                                         FV<R, 2>*, FV<R, 2>*, cudaStream_t);
+    template void combine_operator<R, 1>(const Pattern&, const double*, const double*, const double*,      \
+                                         const OpCoef<1>&, FV<R, 1>*, FV<R, 1>*, cudaStream_t);             \
+    template void combine_operator<R, 2>(const Pattern&, const double*, const double*, const double*,      \
+                                         const OpCoef<2>&, FV<R, 2>*, FV<R, 2>*, cudaStream_t);             \
+    template void round_copy<R>(const double*, int64_t, R*, cudaStream_t);
 FEA_INST_R(float)
 FEA_INST_R(double)
 

@@ -179,7 +179,7 @@ struct RowMap {
 // rather than one row.  Products go to shared memory and each lane sums its
 // own row in column order.
 template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(StepArgs<R, NF> a) {
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
     constexpr int WIN = 32 * WCH;
     __shared__ FV<R, NF> sm[kBlock / 32][WIN];
     CgState* cg = a.cg;
@@ -284,11 +284,30 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(StepArgs<R, NF> a) {
     }
 }
 
+// Group of consecutive unknowns moved by one 16-byte access.
+template <typename R, int NF>
+struct alignas(16) Vec16 {
+    static constexpr int E = 16 / sizeof(FV<R, NF>);
+    FV<R, NF> e[E];
+};
+
+template <typename T>
+__device__ __forceinline__ T ld16(const T* p) {
+    static_assert(sizeof(T) == 16, "16-byte group");
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    T o;
+    memcpy(&o, &t, 16);
+    return o;
+}
+
 // x += alpha p_new, r -= alpha q, z = D^-1 r, r.z and r.r; the last block
 // tests convergence (|r|^2 < tol^2 |b|^2), forms beta and sets the loop
-// condition.  Two unknowns per thread and pass, loads issued up front.
+// condition.  Each thread moves 16-byte groups of unknowns (all vectors are
+// 16-byte aligned), so every load brings 16 bytes.
 template <typename R, int NF>
-__global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
+__global__ void __launch_bounds__(kBlock, 6) k_cg_update(StepArgs<R, NF> a) {
+    using G = Vec16<R, NF>;
+    constexpr int E = G::E;
     CgState* cg = a.cg;
     const FV<R, NF>* __restrict__ pnew = a.pp[(cg->iter & 1) ^ 1];
     int act[NF];
@@ -300,42 +319,41 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(StepArgs<R, NF> a) {
     }
     Acc<R> acc[2 * NF];
     const int64_t N = a.N;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < N; i0 += 2 * stride) {
-        const int64_t i1 = i0 + stride;
-        const bool has1 = i1 < N;
-        FV<R, NF> x[2], r[2], p[2], q[2], d[2];
-        x[0] = a.x[i0];
-        r[0] = a.r[i0];
-        p[0] = ldfv(pnew + i0);
-        q[0] = ldfv(a.q + i0);
-        d[0] = ldfv(a.dinv + i0);
-        if (has1) {
-            x[1] = a.x[i1];
-            r[1] = a.r[i1];
-            p[1] = ldfv(pnew + i1);
-            q[1] = ldfv(a.q + i1);
-            d[1] = ldfv(a.dinv + i1);
-        }
+    const int64_t ngroups = N / E;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    auto one = [&](FV<R, NF>& x, FV<R, NF>& r, const FV<R, NF>& p, const FV<R, NF>& q, const FV<R, NF>& d,
+                   FV<R, NF>& z) {
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-            if (j == 1 && !has1) break;
-            FV<R, NF> z;
-#pragma unroll
-            for (int f = 0; f < NF; f++) {
-                if (act[f]) {
-                    x[j].v[f] = fma(alpha[f], p[j].v[f], x[j].v[f]);
-                    r[j].v[f] = fma(-alpha[f], q[j].v[f], r[j].v[f]);
-                }
-                z.v[f] = d[j].v[f] * r[j].v[f];
-                acc[f].add_prod(r[j].v[f], z.v[f]);
-                acc[NF + f].add_prod(r[j].v[f], r[j].v[f]);
+        for (int f = 0; f < NF; f++) {
+            if (act[f]) {
+                x.v[f] = fma(alpha[f], p.v[f], x.v[f]);
+                r.v[f] = fma(-alpha[f], q.v[f], r.v[f]);
             }
-            const int64_t i = j ? i1 : i0;
-            a.x[i] = x[j];
-            a.r[i] = r[j];
-            a.z[i] = z;
+            z.v[f] = d.v[f] * r.v[f];
+            acc[f].add_prod(r.v[f], z.v[f]);
+            acc[NF + f].add_prod(r.v[f], r.v[f]);
         }
+    };
+    for (int64_t g = tid; g < ngroups; g += nthreads) {
+        G x = reinterpret_cast<const G*>(a.x)[g];
+        G r = reinterpret_cast<const G*>(a.r)[g];
+        const G p = ld16(reinterpret_cast<const G*>(pnew) + g);
+        const G q = ld16(reinterpret_cast<const G*>(a.q) + g);
+        const G d = ld16(reinterpret_cast<const G*>(a.dinv) + g);
+        G z;
+#pragma unroll
+        for (int j = 0; j < E; j++) one(x.e[j], r.e[j], p.e[j], q.e[j], d.e[j], z.e[j]);
+        reinterpret_cast<G*>(a.x)[g] = x;
+        reinterpret_cast<G*>(a.r)[g] = r;
+        reinterpret_cast<G*>(a.z)[g] = z;
+    }
+    for (int64_t i = ngroups * E + tid; i < N; i += nthreads) {  // tail
+        FV<R, NF> x = a.x[i], r = a.r[i], z;
+        one(x, r, pnew[i], a.q[i], a.dinv[i], z);
+        a.x[i] = x;
+        a.r[i] = r;
+        a.z[i] = z;
     }
     double tot[2 * NF];
     if (grid_reduce<R, 2 * NF>(acc, a.part, a.part_stride, a.tickets + 1, tot) && threadIdx.x == 0) {

@@ -39,14 +39,22 @@ void ordered_sum_adv(const Pattern& P, const R* loc, const uint32_t* tri, const 
                      uint8_t* present, cudaStream_t st);
 
 // Operator values for NF fields: A_f = M / md_f + (k1_f * K) * k2_f + a1_f * Adv,
-// evaluated per entry with round-to-nearest operations in that order.
-template <typename R, int NF>
+// evaluated per entry in FP64 from the FP64 matrices, then rounded once to R
+// (FP32 handles store FP32 operators assembled in FP64).  dinv is the inverse
+// of the stored (rounded) diagonal.
+struct OpCoef1 {
+    double md, k1, k2, a1;
+};
+template <int NF>
 struct OpCoef {
-    R md[NF], k1[NF], k2[NF], a1[NF];
+    OpCoef1 f[NF];
 };
 template <typename R, int NF>
-void combine_operator(const Pattern& P, const R* M, const R* K, const R* Adv, const OpCoef<R, NF>& c,
+void combine_operator(const Pattern& P, const double* M, const double* K, const double* Adv, const OpCoef<NF>& c,
                       FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st);
+// out[i] = (R)in[i]
+template <typename R>
+void round_copy(const double* in, int64_t n, R* out, cudaStream_t st);
 
 // ---- time stepping (cg.cu) ------------------------------------------------------
 enum StepKind : int {

@@ -119,13 +119,14 @@ struct fea_solver {
     uint8_t* ob = nullptr;
     float* elem_D = nullptr;    // [T] per-element diffusivity (null: 1)
     float* elem_vel = nullptr;  // [3T]
-    void* elem_Dr = nullptr;    // diffusivity in R
+    double* elem_Dr = nullptr;  // diffusivity widened to FP64 for assembly
     // FEMContext state (rebuilt on BC change)
     DeviceArena mat_mem;
     int32_t* idx = nullptr;
     Pattern P;
-    void *Kloc = nullptr, *Mloc = nullptr, *Aloc = nullptr;
-    void *K = nullptr, *M = nullptr, *Adv = nullptr;
+    double *Kloc = nullptr, *Mloc = nullptr, *Aloc = nullptr;  // element blocks [9T], FP64
+    double *K64 = nullptr, *M64 = nullptr, *Adv64 = nullptr;   // assembled in FP64
+    void *K = nullptr, *M = nullptr, *Adv = nullptr;           // in the handle's type
     uint8_t* adv_present = nullptr;
     Fields F;
     // loop state
@@ -153,6 +154,8 @@ namespace {
 
 size_t rsize(const fea_solver* s) { return s->precision == FEA_FP64 ? 8 : 4; }
 
+int64_t pad4(int64_t n) { return (n + 3) & ~(int64_t)3; }
+
 void* ralloc(DeviceArena& ar, const fea_solver* s, int64_t n) {
     if (s->precision == FEA_FP64) return ar.alloc<double>(n);
     return ar.alloc<float>(n);
@@ -179,22 +182,24 @@ double time_step(const fea_params& p) {
     }
 }
 
-template <typename R>
-void assemble_values(fea_solver* s) {
+// Assembly runs in FP64 for both precisions (once per mesh or parameter
+// change); FP32 handles then round the assembled values once, so their
+// matrices carry only the final FP32 rounding.
+void assemble(fea_solver* s) {
     const bool vel_elem = s->prm.velocity_mode == 1 && s->elem_vel;
-    element_matrices<R>(s->xyz, s->tri, s->T, vel_elem ? 1 : 0, s->prm.advdiff_velocity, s->elem_vel,
-                        (R*)s->Kloc, (R*)s->Mloc, (R*)s->Aloc, s->stream);
-    ordered_sum<R>(s->P, (R*)s->Kloc, (const R*)s->elem_Dr, (R*)s->K, s->stream);
-    ordered_sum<R>(s->P, (R*)s->Mloc, nullptr, (R*)s->M, s->stream);
-    ordered_sum_adv<R>(s->P, (R*)s->Aloc, s->tri, s->ob, (R*)s->Adv, s->adv_present, s->stream);
+    element_matrices<double>(s->xyz, s->tri, s->T, vel_elem ? 1 : 0, s->prm.advdiff_velocity, s->elem_vel,
+                             s->Kloc, s->Mloc, s->Aloc, s->stream);
+    ordered_sum<double>(s->P, s->Kloc, s->elem_Dr, s->K64, s->stream);
+    ordered_sum<double>(s->P, s->Mloc, nullptr, s->M64, s->stream);
+    ordered_sum_adv<double>(s->P, s->Aloc, s->tri, s->ob, s->Adv64, s->adv_present, s->stream);
+    if (s->precision == FEA_FP32) {
+        round_copy<float>(s->K64, s->P.nnz, (float*)s->K, s->stream);
+        round_copy<float>(s->M64, s->P.nnz, (float*)s->M, s->stream);
+        round_copy<float>(s->Adv64, s->P.nnz, (float*)s->Adv, s->stream);
+    }
     memcpy(s->cur_vel, s->prm.advdiff_velocity, sizeof(s->cur_vel));
     s->cur_vel_mode = s->prm.velocity_mode;
     s->op_dirty = true;
-}
-
-void assemble(fea_solver* s) {
-    if (s->precision == FEA_FP64) assemble_values<double>(s);
-    else assemble_values<float>(s);
 }
 
 // FEMContext::update_boundary_conditions + assemble_matrices and the state.
@@ -209,12 +214,21 @@ void build_context(fea_solver* s) {
     s->N = build_idx_map(s->ob, s->V, s->bc, s->idx, st);
     build_pattern(s->P, s->mat_mem, s->tri, s->T, s->ob, s->idx, s->bc, s->N, st);
     const int64_t N = s->N, nnz = s->P.nnz, T = s->T;
-    s->Kloc = ralloc(s->mat_mem, s, 9 * T);
-    s->Mloc = ralloc(s->mat_mem, s, 9 * T);
-    s->Aloc = ralloc(s->mat_mem, s, 9 * T);
-    s->K = ralloc(s->mat_mem, s, nnz);
-    s->M = ralloc(s->mat_mem, s, nnz);
-    s->Adv = ralloc(s->mat_mem, s, nnz);
+    s->Kloc = s->mat_mem.alloc<double>(9 * T);
+    s->Mloc = s->mat_mem.alloc<double>(9 * T);
+    s->Aloc = s->mat_mem.alloc<double>(9 * T);
+    s->K64 = s->mat_mem.alloc<double>(nnz);
+    s->M64 = s->mat_mem.alloc<double>(nnz);
+    s->Adv64 = s->mat_mem.alloc<double>(nnz);
+    if (s->precision == FEA_FP64) {
+        s->K = s->K64;
+        s->M = s->M64;
+        s->Adv = s->Adv64;
+    } else {
+        s->K = ralloc(s->mat_mem, s, nnz);
+        s->M = ralloc(s->mat_mem, s, nnz);
+        s->Adv = ralloc(s->mat_mem, s, nnz);
+    }
     s->adv_present = s->mat_mem.alloc<uint8_t>(nnz);
     Fields& F = s->F;
     F.N = N;
@@ -229,7 +243,8 @@ void build_context(fea_solver* s) {
     F.b1 = ralloc(s->mat_mem, s, N);
     F.r1 = ralloc(s->mat_mem, s, N);
     F.z1 = ralloc(s->mat_mem, s, N);
-    F.p1 = ralloc(s->mat_mem, s, 2 * N);
+    const int64_t Np = pad4(N);  // the second direction buffer starts 16-byte aligned
+    F.p1 = ralloc(s->mat_mem, s, 2 * Np);
     F.q1 = ralloc(s->mat_mem, s, N);
     F.A0 = ralloc(s->mat_mem, s, nnz);
     F.d0 = ralloc(s->mat_mem, s, N);
@@ -238,13 +253,13 @@ void build_context(fea_solver* s) {
     F.b2 = ralloc(s->mat_mem, s, 2 * N);
     F.r2 = ralloc(s->mat_mem, s, 2 * N);
     F.z2 = ralloc(s->mat_mem, s, 2 * N);
-    F.p2 = ralloc(s->mat_mem, s, 4 * N);
+    F.p2 = ralloc(s->mat_mem, s, 4 * Np);
     F.q2 = ralloc(s->mat_mem, s, 2 * N);
     // every vector starts at zero (the direction buffers are read with weight
     // beta = 0 only after a write, but a zero start keeps them finite)
     const std::pair<void*, int64_t> zeroed[] = {
         {F.u, N}, {F.v, N}, {F.a, N}, {F.ut, N}, {F.vt, N}, {F.uv, 2 * N}, {F.b1, N}, {F.r1, N}, {F.z1, N},
-        {F.p1, 2 * N}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 2 * N}, {F.z2, 2 * N}, {F.p2, 4 * N}, {F.q2, 2 * N}};
+        {F.p1, 2 * Np}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 2 * N}, {F.z2, 2 * N}, {F.p2, 4 * Np}, {F.q2, 2 * N}};
     for (const auto& zv : zeroed)
         FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
     F.interleaved = false;
@@ -270,7 +285,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.r = (FV<R, 1>*)F.r1;
         a.z = (FV<R, 1>*)F.z1;
         a.pp[0] = (FV<R, 1>*)F.p1;
-        a.pp[1] = a.pp[0] + s->N;
+        a.pp[1] = a.pp[0] + pad4(s->N);
         a.q = (FV<R, 1>*)F.q1;
     } else {
         a.A = (const FV<R, 2>*)F.A2;
@@ -279,7 +294,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.r = (FV<R, 2>*)F.r2;
         a.z = (FV<R, 2>*)F.z2;
         a.pp[0] = (FV<R, 2>*)F.p2;
-        a.pp[1] = a.pp[0] + s->N;
+        a.pp[1] = a.pp[0] + pad4(s->N);
         a.q = (FV<R, 2>*)F.q2;
     }
     a.u = (R*)F.u;
@@ -334,49 +349,42 @@ void upload_params(fea_solver* s) {
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
 }
 
-// Operator coefficients, computed in R like the reference's float expressions.
+// Operator coefficients (the float parameters widened to double; the
+// operator is evaluated in FP64 and rounded once to the handle's type).
 template <typename R>
 void update_operator(fea_solver* s, int kind) {
     const fea_params& p = s->prm;
-    const R dt = (R)time_step(p);
+    const double dt = time_step(p);
     if (kind == EQ_GS_REF || kind == EQ_GS_CONSISTENT) {
-        OpCoef<R, 2> c{};
-        c.md[0] = c.md[1] = dt;
-        c.k1[0] = (R)p.rd_Du;
-        c.k1[1] = (R)p.rd_Dv;
-        c.k2[0] = c.k2[1] = (R)1;
-        c.a1[0] = c.a1[1] = (R)0;
-        combine_operator<R, 2>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
+        OpCoef<2> c{};
+        c.f[0] = {dt, (double)p.rd_Du, 1.0, 0.0};
+        c.f[1] = {dt, (double)p.rd_Dv, 1.0, 0.0};
+        combine_operator<R, 2>(s->P, s->M64, s->K64, s->Adv64, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
                                s->stream);
     } else {
-        OpCoef<R, 1> c{};
-        c.md[0] = dt;
-        c.k2[0] = (R)1;
-        c.a1[0] = (R)0;
+        OpCoef<1> c{};
+        c.f[0] = {dt, 0.0, 1.0, 0.0};
         if (kind == EQ_HEAT && p.equation == FEA_HEAT) {
-            c.k1[0] = (R)p.heat_conductivity;
+            c.f[0].k1 = p.heat_conductivity;
         } else if (kind == EQ_HEAT) {  // implicit advection-diffusion, CPUSolver.cpp:95
-            c.k1[0] = (R)p.advdiff_c;
-            c.a1[0] = (R)-1;
+            c.f[0].k1 = p.advdiff_c;
+            c.f[0].a1 = -1.0;
         } else if (kind == EQ_ADV_EXPLICIT) {
-            c.k1[0] = (R)p.advdiff_c;
+            c.f[0].k1 = p.advdiff_c;
         } else if (kind == EQ_WAVE_REF) {  // M/dt + (c^2 K) dt, CPUSolver.cpp:113
-            const R cc = (R)p.wave_c;
-            c.k1[0] = cc * cc;
-            c.k2[0] = dt;
+            const double cc = p.wave_c;
+            c.f[0].k1 = cc * cc;
+            c.f[0].k2 = dt;
         } else {  // Newmark: M + (beta dt^2 c^2) K
-            const R cc = (R)p.wave_c, be = (R)p.newmark_beta;
-            const R bdt2 = be * dt * dt;
-            c.md[0] = (R)1;
-            c.k1[0] = bdt2 * (cc * cc);
-            OpCoef<R, 1> m{};
-            m.md[0] = (R)1;
-            m.k1[0] = (R)0;
-            m.k2[0] = (R)1;
-            combine_operator<R, 1>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, m, (FV<R, 1>*)s->F.A0,
-                                   (FV<R, 1>*)s->F.d0, s->stream);
+            const double cc = p.wave_c;
+            c.f[0].md = 1.0;
+            c.f[0].k1 = p.newmark_beta * dt * dt * (cc * cc);
+            OpCoef<1> m{};
+            m.f[0] = {1.0, 0.0, 1.0, 0.0};
+            combine_operator<R, 1>(s->P, s->M64, s->K64, s->Adv64, m, (FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->F.d0,
+                                   s->stream);
         }
-        combine_operator<R, 1>(s->P, (R*)s->M, (R*)s->K, (R*)s->Adv, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
+        combine_operator<R, 1>(s->P, s->M64, s->K64, s->Adv64, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
                                s->stream);
     }
 }
@@ -680,13 +688,10 @@ int fea_set_element_fields(fea_solver* s, const float* diffusivity, const float*
     if (diffusivity) {
         if (!s->elem_D) {
             s->elem_D = s->mesh_mem.alloc<float>(s->T);
-            s->elem_Dr = ralloc(s->mesh_mem, s, s->T);
+            s->elem_Dr = s->mesh_mem.alloc<double>(s->T);
         }
         FEA_CUDA_TRY(cudaMemcpyAsync(s->elem_D, diffusivity, sizeof(float) * s->T, cudaMemcpyHostToDevice, s->stream));
-        if (s->precision == FEA_FP64)
-            k_float_to<double><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, (double*)s->elem_Dr);
-        else
-            k_float_to<float><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, (float*)s->elem_Dr);
+        k_float_to<double><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, s->elem_Dr);
         FEA_CHECK_LAUNCH();
     }
     if (velocity) {
