@@ -6,13 +6,14 @@
 // preconditioner (:65): stop when |r|^2 < tol^2 |b|^2, at most max_iter
 // iterations.  The compute-shader path (cgm.glsl:104-149, GPUSolver.cpp:326-361)
 // runs the same recurrences with a host round trip per stage; here the loop is
-// a CUDA graph WHILE node whose condition the update kernel sets on the device.
+// a CUDA graph WHILE node over time steps; each linear solve is one
+// persistent cooperative kernel (k_cg_solve) that runs its whole CG loop.
 //
-// Per CG iteration, two kernels:
-//   k_cg_spmv    p = z + beta p (fused, two alternating p buffers),
-//                q = A p (warp-cooperative CSR) and p.q
-//   k_cg_update  x += alpha p, r -= alpha q, z = D^-1 r, r.z and r.r,
-//                convergence test and the loop condition
+// A CG iteration is two phases separated by grid-wide barriers:
+//   spmv    p = z + beta p (fused, two alternating p buffers),
+//           q = A p (warp-cooperative CSR) and p.q
+//   update  x += alpha p, r -= alpha q, z = D^-1 r, r.z and r.r,
+//           convergence test
 // Inner products: FP32 products are accumulated exactly as float-float pairs
 // per thread and per warp, then in FP64 across warps and blocks (the GB300's
 // FP64 pipe is narrow, so FP64 arithmetic is kept off the per-element path).
@@ -130,24 +131,31 @@ template <typename R>
 __device__ __forceinline__ R ldg(const R* p) {
     return __ldg(p);
 }
+// Load of a 4-, 8- or 16-byte value: through the read-only cache, or from L2
+// only (l2only) for data that other blocks of the running kernel wrote.
+template <typename T>
+__device__ __forceinline__ T ldv(const T* p, bool l2only) {
+    T o;
+    if constexpr (sizeof(T) == 4) {
+        const float* q = reinterpret_cast<const float*>(p);
+        const float t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        const float2* q = reinterpret_cast<const float2*>(p);
+        const float2 t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 8);
+    } else {
+        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
+        const float4* q = reinterpret_cast<const float4*>(p);
+        const float4 t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 16);
+    }
+    return o;
+}
+
 template <typename R, int NF>
 __device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
-    if constexpr (sizeof(FV<R, NF>) == 4) {
-        const float t = __ldg(reinterpret_cast<const float*>(p));
-        FV<R, NF> o;
-        memcpy(&o, &t, 4);
-        return o;
-    } else if constexpr (sizeof(FV<R, NF>) == 8) {
-        const float2 t = __ldg(reinterpret_cast<const float2*>(p));
-        FV<R, NF> o;
-        memcpy(&o, &t, 8);
-        return o;
-    } else {
-        const double2 t = __ldg(reinterpret_cast<const double2*>(p));
-        FV<R, NF> o;
-        memcpy(&o, &t, 16);
-        return o;
-    }
+    return ldv(p, false);
 }
 
 // Threads are grouped LANES per CSR row; a warp covers 32/LANES consecutive
@@ -166,11 +174,61 @@ struct RowMap {
     }
 };
 
-// ---- kernels --------------------------------------------------------------------
+// ---- the two phases of a CG iteration ----------------------------------------------
+//
+// Both phases exist as device bodies used by (a) standalone kernels, where
+// every vector was written by an earlier launch and is read through the
+// read-only path, and (b) the persistent solve kernel, where vectors written
+// by other blocks of the same launch must be read from L2 (LoadCG).
+
+struct LoadRO {
+    template <typename T>
+    static __device__ __forceinline__ T ld(const T* p) {
+        return ldv<T>(p, false);
+    }
+};
+struct LoadCG {
+    template <typename T>
+    static __device__ __forceinline__ T ld(const T* p) {
+        return ldv<T>(p, true);
+    }
+};
+
+template <typename R, int NF>
+struct alignas(16) Vec16 {
+    static constexpr int E = 16 / sizeof(FV<R, NF>);
+    FV<R, NF> e[E];
+};
+
+// Control values of one phase, read once per phase by every thread.
+template <typename R, int NF>
+struct PhaseCtl {
+    int par;          // iteration parity: p_old = pp[par], p_new = pp[par ^ 1]
+    int act[NF];
+    bool fresh[NF];
+    bool need_old;
+    bool any;
+    R beta[NF], alpha[NF];
+    __device__ __forceinline__ void load(const CgState* cg) {
+        const volatile CgState* v = cg;
+        par = v->iter & 1;
+        need_old = false;
+        any = false;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            act[f] = v->active[f];
+            fresh[f] = v->fresh[f] != 0;
+            beta[f] = fresh[f] ? (R)0 : (R)v->beta[f];
+            alpha[f] = act[f] ? (R)v->alpha[f] : (R)0;
+            need_old |= !fresh[f];
+            any |= act[f] != 0;
+        }
+    }
+};
 
 // q = A p_new with p_new = z + beta p_old computed for every gathered column
 // (the direction update of the previous iteration, fused; the two p buffers
-// alternate with the iteration parity), plus p_new.q.
+// alternate with the iteration parity), plus p_new.q into dot[].
 //
 // Warp-cooperative CSR: a warp owns 32 consecutive rows, whose stored entries
 // form one contiguous range.  The warp streams that range in windows of
@@ -178,30 +236,16 @@ struct RowMap {
 // independent gathers, so each round trip to memory carries a whole window
 // rather than one row.  Products go to shared memory and each lane sums its
 // own row in column order.
-template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
+template <typename R, int NF, int WCH, typename LP>
+__device__ __forceinline__ void spmv_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
+                                           FV<R, NF> (*sm)[32 * WCH], Acc<R> (&dot)[NF]) {
     constexpr int WIN = 32 * WCH;
-    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
-    CgState* cg = a.cg;
-    const int par = cg->iter & 1;
-    const FV<R, NF>* __restrict__ pold = a.pp[par];
-    FV<R, NF>* __restrict__ pnew = a.pp[par ^ 1];
-    int act[NF];
-    bool fresh[NF];
-    R beta[NF];
-    bool need_old = false;
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        act[f] = cg->active[f];
-        fresh[f] = cg->fresh[f] != 0;
-        beta[f] = fresh[f] ? (R)0 : (R)cg->beta[f];
-        need_old |= !fresh[f];
-    }
+    const FV<R, NF>* pold = a.pp[c.par];
+    FV<R, NF>* pnew = a.pp[c.par ^ 1];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t N = a.N;
-    Acc<R> dot[NF];
     for (int64_t r0 = warp * 32; r0 < N; r0 += nwarps * 32) {
         const int64_t row = r0 + lane;
         const int32_t rs = ldg(a.rp + (row < N ? row : N));
@@ -216,30 +260,30 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
             FV<R, NF> av[WCH];
             int32_t cc[WCH];
 #pragma unroll
-            for (int c = 0; c < WCH; c++) {
-                const int32_t idx = wb + c * 32 + lane;
-                cc[c] = -1;
+            for (int k = 0; k < WCH; k++) {
+                const int32_t idx = wb + k * 32 + lane;
+                cc[k] = -1;
                 if (idx < e1) {
-                    av[c] = ldfv(a.A + idx);
-                    cc[c] = ldg(a.col + idx);
+                    av[k] = ldv(a.A + idx, false);
+                    cc[k] = ldg(a.col + idx);
                 }
             }
 #pragma unroll
-            for (int c = 0; c < WCH; c++) {
+            for (int k = 0; k < WCH; k++) {
                 FV<R, NF> prod;
 #pragma unroll
                 for (int f = 0; f < NF; f++) prod.v[f] = 0;
-                if (cc[c] >= 0) {
-                    const FV<R, NF> zc = ldfv(a.z + cc[c]);
+                if (cc[k] >= 0) {
+                    const FV<R, NF> zc = LP::ld(a.z + cc[k]);
                     FV<R, NF> pc = zc;
-                    if (need_old) pc = ldfv(pold + cc[c]);
+                    if (c.need_old) pc = LP::ld(pold + cc[k]);
 #pragma unroll
                     for (int f = 0; f < NF; f++) {
-                        const R pn = fresh[f] ? zc.v[f] : fma(beta[f], pc.v[f], zc.v[f]);
-                        prod.v[f] = av[c].v[f] * pn;
+                        const R pn = c.fresh[f] ? zc.v[f] : fma(c.beta[f], pc.v[f], zc.v[f]);
+                        prod.v[f] = av[k].v[f] * pn;
                     }
                 }
-                sm[wib][c * 32 + lane] = prod;
+                sm[wib][k * 32 + lane] = prod;
             }
             __syncwarp();
             const int32_t lo = (rs > wb ? rs : wb) - wb;
@@ -252,12 +296,12 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
             __syncwarp();
         }
         if (row < N) {
-            const FV<R, NF> zr = ldfv(a.z + row);
+            const FV<R, NF> zr = LP::ld(a.z + row);
             FV<R, NF> pr = zr, qv;
-            if (need_old) pr = ldfv(pold + row);
+            if (c.need_old) pr = LP::ld(pold + row);
 #pragma unroll
             for (int f = 0; f < NF; f++) {
-                const R pn = fresh[f] ? zr.v[f] : fma(beta[f], pr.v[f], zr.v[f]);
+                const R pn = c.fresh[f] ? zr.v[f] : fma(c.beta[f], pr.v[f], zr.v[f]);
                 pr.v[f] = pn;
                 qv.v[f] = acc[f];
                 dot[f].add_prod(pn, acc[f]);
@@ -266,58 +310,17 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
             a.q[row] = qv;
         }
     }
-    double tot[NF];
-    if (grid_reduce<R, NF>(dot, a.part, a.part_stride, a.tickets + 0, tot) && threadIdx.x == 0) {
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            if (!act[f]) continue;
-            cg->pq[f] = tot[f];
-            const double al = cg->rz[f] / tot[f];
-            if (!(tot[f] > 0.0) || !isfinite(al)) {
-                cg->active[f] = 0;
-                cg->iters[f] = cg->iter;
-                atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
-            } else {
-                cg->alpha[f] = al;
-            }
-        }
-    }
 }
 
-// Group of consecutive unknowns moved by one 16-byte access.
-template <typename R, int NF>
-struct alignas(16) Vec16 {
-    static constexpr int E = 16 / sizeof(FV<R, NF>);
-    FV<R, NF> e[E];
-};
-
-template <typename T>
-__device__ __forceinline__ T ld16(const T* p) {
-    static_assert(sizeof(T) == 16, "16-byte group");
-    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
-    T o;
-    memcpy(&o, &t, 16);
-    return o;
-}
-
-// x += alpha p_new, r -= alpha q, z = D^-1 r, r.z and r.r; the last block
-// tests convergence (|r|^2 < tol^2 |b|^2), forms beta and sets the loop
-// condition.  Each thread moves 16-byte groups of unknowns (all vectors are
-// 16-byte aligned), so every load brings 16 bytes.
-template <typename R, int NF>
-__global__ void __launch_bounds__(kBlock, 6) k_cg_update(StepArgs<R, NF> a) {
+// x += alpha p_new, r -= alpha q, z = D^-1 r, with r.z and r.r into acc[].
+// Each thread moves 16-byte groups of unknowns (all vectors are 16-byte
+// aligned), so every load brings 16 bytes.
+template <typename R, int NF, typename LP>
+__device__ __forceinline__ void update_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
+                                             Acc<R> (&acc)[2 * NF]) {
     using G = Vec16<R, NF>;
     constexpr int E = G::E;
-    CgState* cg = a.cg;
-    const FV<R, NF>* __restrict__ pnew = a.pp[(cg->iter & 1) ^ 1];
-    int act[NF];
-    R alpha[NF];
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        act[f] = cg->active[f];
-        alpha[f] = act[f] ? (R)cg->alpha[f] : (R)0;
-    }
-    Acc<R> acc[2 * NF];
+    const FV<R, NF>* pnew = a.pp[c.par ^ 1];
     const int64_t N = a.N;
     const int64_t ngroups = N / E;
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -326,9 +329,9 @@ __global__ void __launch_bounds__(kBlock, 6) k_cg_update(StepArgs<R, NF> a) {
                    FV<R, NF>& z) {
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-            if (act[f]) {
-                x.v[f] = fma(alpha[f], p.v[f], x.v[f]);
-                r.v[f] = fma(-alpha[f], q.v[f], r.v[f]);
+            if (c.act[f]) {
+                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                r.v[f] = fma(-c.alpha[f], q.v[f], r.v[f]);
             }
             z.v[f] = d.v[f] * r.v[f];
             acc[f].add_prod(r.v[f], z.v[f]);
@@ -336,11 +339,11 @@ __global__ void __launch_bounds__(kBlock, 6) k_cg_update(StepArgs<R, NF> a) {
         }
     };
     for (int64_t g = tid; g < ngroups; g += nthreads) {
-        G x = reinterpret_cast<const G*>(a.x)[g];
-        G r = reinterpret_cast<const G*>(a.r)[g];
-        const G p = ld16(reinterpret_cast<const G*>(pnew) + g);
-        const G q = ld16(reinterpret_cast<const G*>(a.q) + g);
-        const G d = ld16(reinterpret_cast<const G*>(a.dinv) + g);
+        G x = LP::ld(reinterpret_cast<const G*>(a.x) + g);
+        G r = LP::ld(reinterpret_cast<const G*>(a.r) + g);
+        const G p = LP::ld(reinterpret_cast<const G*>(pnew) + g);
+        const G q = LP::ld(reinterpret_cast<const G*>(a.q) + g);
+        const G d = ldv(reinterpret_cast<const G*>(a.dinv) + g, false);
         G z;
 #pragma unroll
         for (int j = 0; j < E; j++) one(x.e[j], r.e[j], p.e[j], q.e[j], d.e[j], z.e[j]);
@@ -349,48 +352,200 @@ __global__ void __launch_bounds__(kBlock, 6) k_cg_update(StepArgs<R, NF> a) {
         reinterpret_cast<G*>(a.z)[g] = z;
     }
     for (int64_t i = ngroups * E + tid; i < N; i += nthreads) {  // tail
-        FV<R, NF> x = a.x[i], r = a.r[i], z;
-        one(x, r, pnew[i], a.q[i], a.dinv[i], z);
+        FV<R, NF> x = LP::ld(a.x + i), r = LP::ld(a.r + i), z;
+        one(x, r, LP::ld(pnew + i), LP::ld(a.q + i), ldv(a.dinv + i, false), z);
         a.x[i] = x;
         a.r[i] = r;
         a.z[i] = z;
     }
-    double tot[2 * NF];
-    if (grid_reduce<R, 2 * NF>(acc, a.part, a.part_stride, a.tickets + 1, tot) && threadIdx.x == 0) {
-        const int it = cg->iter + 1;
-        cg->iter = it;
-        int any = 0;
+}
+
+// After the SpMV phase: alpha = r.z / p.q, or breakdown.
+template <typename R, int NF>
+__device__ void finish_spmv(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
 #pragma unroll
-        for (int f = 0; f < NF; f++) {
-            cg->fresh[f] = 0;
-            if (!act[f]) continue;
-            const double rz = tot[f], rr = tot[NF + f];
-            cg->rr[f] = rr;
-            if (!isfinite(rr)) {
+    for (int f = 0; f < NF; f++) {
+        if (!act[f]) continue;
+        cg->pq[f] = tot[f];
+        const double al = cg->rz[f] / tot[f];
+        if (!(tot[f] > 0.0) || !isfinite(al)) {
+            cg->active[f] = 0;
+            cg->iters[f] = cg->iter;
+            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
+        } else {
+            cg->alpha[f] = al;
+        }
+    }
+}
+
+// After the update phase: convergence |r|^2 < tol^2 |b|^2, beta, iteration
+// count, the max_iter limit.  Returns whether another iteration runs.
+template <typename R, int NF>
+__device__ bool finish_update(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
+    const int it = cg->iter + 1;
+    cg->iter = it;
+    int any = 0;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        cg->fresh[f] = 0;
+        if (!act[f]) continue;
+        const double rz = tot[f], rr = tot[NF + f];
+        cg->rr[f] = rr;
+        if (!isfinite(rr)) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
+        } else if (rr < cg->thr[f]) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+        } else {
+            cg->beta[f] = rz / cg->rz[f];
+            cg->rz[f] = rz;
+            any = 1;
+        }
+    }
+    const bool cont = any && it < cg->max_iter;
+    if (any && !cont) {
+        atomicOr(&run->flags, FEA_STATUS_NOT_CONVERGED);
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            if (cg->active[f]) {
                 cg->active[f] = 0;
                 cg->iters[f] = it;
-                atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
-            } else if (rr < cg->thr[f]) {
-                cg->active[f] = 0;
-                cg->iters[f] = it;
-            } else {
-                cg->beta[f] = rz / cg->rz[f];
-                cg->rz[f] = rz;
-                any = 1;
+            }
+    }
+    return cont;
+}
+
+template <int NV, typename R>
+__device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, double (&blk)[NV]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
+        if (lane == 0) sm[wid * NV + k] = acc[k].value();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) blk[k] = 0.0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < nw; w++)
+#pragma unroll
+            for (int k = 0; k < NV; k++) blk[k] += sm[w * NV + k];
+    }
+    __syncthreads();
+}
+
+// ---- standalone kernels (autotuning and timing probes) -------------------------------
+
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    Acc<R> dot[NF];
+    spmv_phase<R, NF, WCH, LoadRO>(a, c, sm, dot);
+    double blk[NF], tot[NF];
+    block_totals<NF>(dot, red, blk);
+    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0)
+        finish_spmv<R, NF>(a.cg, a.run, c.act, tot);
+}
+
+// ---- the persistent solve ----------------------------------------------------------------
+//
+// One cooperative launch runs the whole CG loop of a solve: every block stays
+// resident, the two phases of an iteration are separated by grid-wide
+// barriers, and the block that arrives last at a barrier sums the block
+// partials (in block order) and writes alpha or the convergence decision
+// before releasing the others.  Waits are bounded: a block that waits longer
+// than kSpinLimit polls records an error in GridSync::err and every block
+// leaves at its next barrier, so a fault in the barrier cannot hang the GPU.
+
+constexpr long long kSpinLimit = 1ll << 25;  // ~3 s of 100 ns sleeps
+
+template <int NV, typename F>
+__device__ bool grid_barrier_reduce(const double (&blk)[NV], double* part, int stride, GridSync* gs,
+                                    double* sm, F on_last) {
+    __shared__ int s_last, s_ok;
+    __shared__ unsigned int s_gen;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[k * stride + blockIdx.x] = blk[k];
+        s_gen = *(volatile unsigned int*)&gs->gen;
+        __threadfence();
+        s_last = atomicAdd(&gs->count, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        double y[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double acc = 0.0;
+            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&part[k * stride + b]);
+            y[k] = acc;
+        }
+        block_sum<NV>(y, sm);
+        if (threadIdx.x == 0) {
+            gs->count = 0u;
+            on_last(y);
+            __threadfence();
+            atomicAdd(&gs->gen, 1u);
+            s_ok = 1;
+        }
+    } else if (threadIdx.x == 0) {
+        long long n = 0;
+        int ok = 1;
+        while (*(volatile unsigned int*)&gs->gen == s_gen) {
+            __nanosleep(100);
+            if (++n > kSpinLimit) {
+                atomicExch(&gs->err, 1);
+                ok = 0;
+                break;
             }
         }
-        const int cont = any && it < cg->max_iter;
-        if (any && !cont) {
-            atomicOr(&a.run->flags, FEA_STATUS_NOT_CONVERGED);
-#pragma unroll
-            for (int f = 0; f < NF; f++)
-                if (cg->active[f]) {
-                    cg->active[f] = 0;
-                    cg->iters[f] = it;
-                }
-        }
-        signal_loop(a, cont);
+        __threadfence();
+        s_ok = ok;
     }
+    __syncthreads();
+    return s_ok && *(volatile int*)&gs->err == 0;
+}
+
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_solve(StepArgs<R, NF> a) {
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * 2 * NF];
+    CgState* cg = a.cg;
+    RunState* run = a.run;
+    for (;;) {
+        PhaseCtl<R, NF> c;
+        c.load(cg);
+        if (!c.any) break;
+        {
+            Acc<R> dot[NF];
+            spmv_phase<R, NF, WCH, LoadCG>(a, c, sm, dot);
+            double blk[NF];
+            block_totals<NF>(dot, red, blk);
+            if (!grid_barrier_reduce<NF>(blk, a.part, a.part_stride, a.gs, red,
+                                         [&](const double* tot) { finish_spmv<R, NF>(cg, run, c.act, tot); }))
+                break;
+        }
+        c.load(cg);
+        {
+            Acc<R> acc[2 * NF];
+            update_phase<R, NF, LoadCG>(a, c, acc);
+            double blk[2 * NF];
+            block_totals<2 * NF>(acc, red, blk);
+            if (!grid_barrier_reduce<2 * NF>(blk, a.part, a.part_stride, a.gs, red,
+                                             [&](const double* tot) { finish_update<R, NF>(cg, run, c.act, tot); }))
+                break;
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0 && *(volatile int*)&a.gs->err)
+        atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
 }
 
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
@@ -494,6 +649,8 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
         RunState* run = a.run;
         const int stop = (atomicOr(&run->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
         cg->stop = stop;
+        a.gs->count = 0u;  // the solve that follows starts from a clean barrier
+        a.gs->err = 0;
         cg->iter = 0;
         cg->max_iter = run->max_iter;
         int any = 0;
@@ -579,6 +736,8 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
     if (grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot) && threadIdx.x == 0) {
         int any = 0;
 #pragma unroll
+        a.gs->count = 0u;
+        a.gs->err = 0;
         for (int f = 0; f < NF; f++) {
             cg->active[f] = 0;
             cg->fresh[f] = 1;
@@ -701,37 +860,51 @@ constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
 template <typename R, int NF, int WCH>
 struct Grids {
-    int spmv, update, rhs, stream;
+    int spmv, solve, rhs, stream;
     explicit Grids(int64_t N) {
         spmv = wave_grid(k_cg_spmv<R, NF, WCH>, ceil_div(N, kBlock));
-        update = wave_grid(k_cg_update<R, NF>, ceil_div(N, 2 * kBlock));
+        // the cooperative solve needs every block resident: exactly one wave
+        solve = wave_grid(k_cg_solve<R, NF, WCH>, max_grid_blocks());
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
 };
 
 template <typename R, int NF, int WCH>
-void add_cg_body(cudaGraph_t body, const StepArgs<R, NF>& a, const Grids<R, NF, WCH>& g) {
-    cudaGraphNode_t n1 = add_kernel(body, nullptr, k_cg_spmv<R, NF, WCH>, g.spmv, kBlock, a);
-    add_kernel(body, n1, k_cg_update<R, NF>, g.update, kBlock, a);
+cudaGraphNode_t add_solve(cudaGraph_t g, cudaGraphNode_t dep, const StepArgs<R, NF>& a, int grid) {
+    cudaGraphNode_t n = add_kernel(g, dep, k_cg_solve<R, NF, WCH>, grid, kBlock, a);
+    cudaKernelNodeAttrValue v = {};
+    v.cooperative = 1;
+    FEA_CUDA_TRY(cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v));
+    return n;
 }
 
-// The three argument sets of a step: the step loop (a), the first CG loop
-// (a1) and the refinement loop (a2); each names the condition it sets.
+template <typename R, int NF, int WCH>
+void launch_solve(const StepArgs<R, NF>& a, int grid, cudaStream_t st) {
+    StepArgs<R, NF> local = a;
+    void* argv[] = {(void*)&local};
+    FEA_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_solve<R, NF, WCH>, dim3((unsigned)grid),
+                                             dim3((unsigned)kBlock), argv, 0, st));
+}
+
+// Argument sets of a step: the step loop (a, sets the step condition) and the
+// set-up kernels of the two solves (a1: rhs, a2: refine), which only store
+// whether their solve has work; the solve kernel reads that from CgState.
 template <typename R, int NF>
 struct LoopArgs {
     StepArgs<R, NF> a, a1, a2;
     LoopArgs(const StepArgs<R, NF>& base, LoopFlags* lf, int use_graph) : a(base), a1(base), a2(base) {
-        a.use_graph = a1.use_graph = a2.use_graph = use_graph;
+        a.use_graph = use_graph;
+        a1.use_graph = a2.use_graph = 0;
         a.cont = &lf->step;
         a1.cont = &lf->cg1;
         a2.cont = &lf->cg2;
     }
 };
 
-// Step graph:  start -> WHILE(step) { rhs -> WHILE(cg1) {spmv, update}
-//              -> refine -> WHILE(cg2) {spmv, update} -> [post] -> stepctl }
-//              -> final_check
+// Step graph:  start -> WHILE(step) { rhs -> solve -> refine -> solve -> [post]
+//              -> stepctl } -> final_check, each solve one cooperative launch
+//              running its whole CG loop.
 template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
@@ -744,15 +917,10 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     cudaGraph_t step_body;
     n = add_while(top, n, L.a.cond, &step_body);
     add_kernel(top, n, k_final_check<R, NF, EQ>, g.stream, kBlock, L.a);
-    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
-    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    cudaGraph_t cg_body1, cg_body2;
-    s = add_while(step_body, s, L.a1.cond, &cg_body1);
-    add_cg_body<R, NF, WCH>(cg_body1, L.a1, g);
+    s = add_solve<R, NF, WCH>(step_body, s, L.a1, g.solve);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_while(step_body, s, L.a2.cond, &cg_body2);
-    add_cg_body<R, NF, WCH>(cg_body2, L.a2, g);
+    s = add_solve<R, NF, WCH>(step_body, s, L.a2, g.solve);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -766,10 +934,9 @@ int read_flag(const int* d, cudaStream_t st) {
     return h;
 }
 
-// The same kernels launched one by one with the loop conditions read back
-// on the host: every kernel is then visible to profilers (kernels inside
-// graphs with conditional nodes are not).  Each loop is bounded by the
-// kernels' own iteration and step limits.
+// The same kernels launched one by one with the step condition read back on
+// the host: every kernel is then visible to profilers (kernels inside graphs
+// with conditional nodes are not).  Bounded by the step count.
 template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
@@ -779,17 +946,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     while (read_flag(&lf->step, st)) {
         k_rhs<R, NF, EQ, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
-        for (const StepArgs<R, NF>* la : {&L.a1, &L.a2}) {
-            if (la == &L.a2) {
-                k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
-                FEA_CHECK_LAUNCH();
-            }
-            while (read_flag(la->cont, st)) {
-                k_cg_spmv<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
-                k_cg_update<R, NF><<<g.update, kBlock, 0, st>>>(*la);
-                FEA_CHECK_LAUNCH();
-            }
-        }
+        launch_solve<R, NF, WCH>(L.a1, g.solve, st);
+        k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
+        FEA_CHECK_LAUNCH();
+        launch_solve<R, NF, WCH>(L.a2, g.solve, st);
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK) {
             k_post<R, NF, EQ><<<g.stream, kBlock, 0, st>>>(L.a);
             FEA_CHECK_LAUNCH();

@@ -92,6 +92,14 @@ struct RunState {
     int refine;
 };
 
+// Grid-wide barrier state of the persistent solve kernel (zero at start).
+struct GridSync {
+    unsigned int count;  // blocks arrived at the current barrier
+    unsigned int gen;    // barrier generation, advanced by the last arriver
+    int err;             // a wait hit its iteration limit
+    int pad;
+};
+
 // Everything a step-loop kernel needs, passed by value.
 template <typename R, int NF>
 struct StepArgs {
@@ -123,6 +131,7 @@ struct StepArgs {
     cudaGraphConditionalHandle cond;  // loop condition set by this kernel (graph mode)
     int* cont;              // the same condition, also stored here for host-driven loops
     int use_graph;          // 1: kernels run as graph nodes and set `cond`
+    GridSync* gs;           // barrier state of the persistent solve
 };
 
 // Loop-condition slots in device memory for host-driven (stream) execution.

@@ -137,6 +137,7 @@ struct fea_solver {
     double* d_part = nullptr;
     unsigned int* d_tickets = nullptr;
     LoopFlags* d_flags = nullptr;
+    GridSync* d_gs = nullptr;  // barrier state of the persistent solve
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
@@ -308,6 +309,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
     a.part = s->d_part;
     a.part_stride = max_grid_blocks();
     a.tickets = s->d_tickets;
+    a.gs = s->d_gs;
     return a;
 }
 
@@ -511,6 +513,8 @@ void alloc_run_state(fea_solver* s) {
     s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
     s->d_tickets = s->run_mem.alloc<unsigned int>(8);
     s->d_flags = s->run_mem.alloc<LoopFlags>(1);
+    s->d_gs = s->run_mem.alloc<GridSync>(1);
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_gs, 0, sizeof(GridSync), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, sizeof(LoopFlags), s->stream));
     const char* mode = getenv("FEA_LAUNCH_MODE");
     s->stream_mode = mode && strcmp(mode, "stream") == 0;
