@@ -6,14 +6,10 @@
 // preconditioner (:65): stop when |r|^2 < tol^2 |b|^2, at most max_iter
 // iterations.  The compute-shader path (cgm.glsl:104-149, GPUSolver.cpp:326-361)
 // runs the same recurrences with a host round trip per stage; here the loop is
-// a CUDA graph WHILE node over time steps; each linear solve is one
-// persistent cooperative kernel (k_cg_solve) that runs its whole CG loop.
-//
-// A CG iteration is two phases separated by grid-wide barriers:
-//   spmv    p = z + beta p (fused, two alternating p buffers),
-//           q = A p (warp-cooperative CSR) and p.q
-//   update  x += alpha p, r -= alpha q, z = D^-1 r, r.z and r.r,
-//           convergence test
+// a CUDA graph WHILE node over time steps with a WHILE node per solve whose
+// body is ONE kernel per CG iteration (the Chronopoulos-Gear form below): the
+// vector updates are fused into the SpMV, and a single grid-wide reduction
+// gives every scalar of the next iteration.
 // Inner products: FP32 products are accumulated exactly as float-float pairs
 // per thread and per warp, then in FP64 across warps and blocks (the GB300's
 // FP64 pipe is narrow, so FP64 arithmetic is kept off the per-element path).
@@ -174,30 +170,16 @@ struct RowMap {
     }
 };
 
-// ---- the two phases of a CG iteration ----------------------------------------------
+// ---- CSR SpMV building blocks ------------------------------------------------------
 //
-// Both phases exist as device bodies used by (a) standalone kernels, where
-// every vector was written by an earlier launch and is read through the
-// read-only path, and (b) the persistent solve kernel, where vectors written
-// by other blocks of the same launch must be read from L2 (LoadCG).
+// Every kernel reads vectors that earlier launches wrote, so the read-only
+// path (LoadRO) is valid for all of them.
 
 struct LoadRO {
     template <typename T>
     static __device__ __forceinline__ T ld(const T* p) {
         return ldv<T>(p, false);
     }
-};
-struct LoadCG {
-    template <typename T>
-    static __device__ __forceinline__ T ld(const T* p) {
-        return ldv<T>(p, true);
-    }
-};
-
-template <typename R, int NF>
-struct alignas(16) Vec16 {
-    static constexpr int E = 16 / sizeof(FV<R, NF>);
-    FV<R, NF> e[E];
 };
 
 // Control values of one phase, read once per phase by every thread.
@@ -312,54 +294,6 @@ __device__ __forceinline__ void spmv_phase(const StepArgs<R, NF>& a, const Phase
     }
 }
 
-// x += alpha p_new, r -= alpha q, z = D^-1 r, with r.z and r.r into acc[].
-// Each thread moves 16-byte groups of unknowns (all vectors are 16-byte
-// aligned), so every load brings 16 bytes.
-template <typename R, int NF, typename LP>
-__device__ __forceinline__ void update_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
-                                             Acc<R> (&acc)[2 * NF]) {
-    using G = Vec16<R, NF>;
-    constexpr int E = G::E;
-    const FV<R, NF>* pnew = a.pp[c.par ^ 1];
-    const int64_t N = a.N;
-    const int64_t ngroups = N / E;
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    auto one = [&](FV<R, NF>& x, FV<R, NF>& r, const FV<R, NF>& p, const FV<R, NF>& q, const FV<R, NF>& d,
-                   FV<R, NF>& z) {
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            if (c.act[f]) {
-                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
-                r.v[f] = fma(-c.alpha[f], q.v[f], r.v[f]);
-            }
-            z.v[f] = d.v[f] * r.v[f];
-            acc[f].add_prod(r.v[f], z.v[f]);
-            acc[NF + f].add_prod(r.v[f], r.v[f]);
-        }
-    };
-    for (int64_t g = tid; g < ngroups; g += nthreads) {
-        G x = LP::ld(reinterpret_cast<const G*>(a.x) + g);
-        G r = LP::ld(reinterpret_cast<const G*>(a.r) + g);
-        const G p = LP::ld(reinterpret_cast<const G*>(pnew) + g);
-        const G q = LP::ld(reinterpret_cast<const G*>(a.q) + g);
-        const G d = ldv(reinterpret_cast<const G*>(a.dinv) + g, false);
-        G z;
-#pragma unroll
-        for (int j = 0; j < E; j++) one(x.e[j], r.e[j], p.e[j], q.e[j], d.e[j], z.e[j]);
-        reinterpret_cast<G*>(a.x)[g] = x;
-        reinterpret_cast<G*>(a.r)[g] = r;
-        reinterpret_cast<G*>(a.z)[g] = z;
-    }
-    for (int64_t i = ngroups * E + tid; i < N; i += nthreads) {  // tail
-        FV<R, NF> x = LP::ld(a.x + i), r = LP::ld(a.r + i), z;
-        one(x, r, LP::ld(pnew + i), LP::ld(a.q + i), ldv(a.dinv + i, false), z);
-        a.x[i] = x;
-        a.r[i] = r;
-        a.z[i] = z;
-    }
-}
-
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
 template <typename R, int NF>
 __device__ void finish_spmv(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
@@ -378,10 +312,13 @@ __device__ void finish_spmv(volatile CgState* cg, RunState* run, const int (&act
     }
 }
 
-// After the update phase: convergence |r|^2 < tol^2 |b|^2, beta, iteration
-// count, the max_iter limit.  Returns whether another iteration runs.
+// After a Chronopoulos-Gear iteration: convergence |r|^2 < tol^2 |b|^2, then
+// beta = gamma'/gamma and alpha = gamma' / (delta' - beta gamma'/alpha) for
+// the next iteration; iteration count and the max_iter limit.  tot holds
+// gamma' = r.u, delta' = w.u and r.r per field.  Returns whether another
+// iteration runs.
 template <typename R, int NF>
-__device__ bool finish_update(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
+__device__ bool finish_cgcg(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
     const int it = cg->iter + 1;
     cg->iter = it;
     int any = 0;
@@ -389,20 +326,32 @@ __device__ bool finish_update(volatile CgState* cg, RunState* run, const int (&a
     for (int f = 0; f < NF; f++) {
         cg->fresh[f] = 0;
         if (!act[f]) continue;
-        const double rz = tot[f], rr = tot[NF + f];
+        const double g = tot[f], d = tot[NF + f], rr = tot[2 * NF + f];
         cg->rr[f] = rr;
         if (!isfinite(rr)) {
             cg->active[f] = 0;
             cg->iters[f] = it;
             atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
-        } else if (rr < cg->thr[f]) {
+            continue;
+        }
+        if (rr < cg->thr[f]) {
             cg->active[f] = 0;
             cg->iters[f] = it;
-        } else {
-            cg->beta[f] = rz / cg->rz[f];
-            cg->rz[f] = rz;
-            any = 1;
+            continue;
         }
+        const double beta = g / cg->rz[f];
+        const double den = d - beta * g / cg->alpha[f];
+        const double alpha = g / den;
+        if (!(den > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
+            continue;
+        }
+        cg->beta[f] = beta;
+        cg->alpha[f] = alpha;
+        cg->rz[f] = g;
+        any = 1;
     }
     const bool cont = any && it < cg->max_iter;
     if (any && !cont) {
@@ -454,98 +403,160 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
         finish_spmv<R, NF>(a.cg, a.run, c.act, tot);
 }
 
-// ---- the persistent solve ----------------------------------------------------------------
+// ---- Chronopoulos-Gear iteration -----------------------------------------------------
 //
-// One cooperative launch runs the whole CG loop of a solve: every block stays
-// resident, the two phases of an iteration are separated by grid-wide
-// barriers, and the block that arrives last at a barrier sums the block
-// partials (in block order) and writes alpha or the convergence decision
-// before releasing the others.  Waits are bounded: a block that waits longer
-// than kSpinLimit polls records an error in GridSync::err and every block
-// leaves at its next barrier, so a fault in the barrier cannot hang the GPU.
+// Jacobi-preconditioned CG rearranged (Chronopoulos & Gear, 1989) so that one
+// iteration needs one global reduction: with u = D^-1 r, w = A u and s = A p,
+//   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,
+//   u' = D^-1 r,  w' = A u',  gamma' = r.u',  delta' = w'.u',
+//   beta' = gamma'/gamma,  alpha' = gamma' / (delta' - beta' gamma'/alpha).
+// It produces the same iterates as the textbook recurrence in exact
+// arithmetic.  One kernel per iteration: every row owner applies the vector
+// updates, and the SpMV recomputes u' at each gathered column from the old r,
+// w and s there (so r, w and s alternate between two buffers).
 
-constexpr long long kSpinLimit = 1ll << 25;  // ~3 s of 100 ns sleeps
-
-template <int NV, typename F>
-__device__ bool grid_barrier_reduce(const double (&blk)[NV], double* part, int stride, GridSync* gs,
-                                    double* sm, F on_last) {
-    __shared__ int s_last, s_ok;
-    __shared__ unsigned int s_gen;
-    if (threadIdx.x == 0) {
+// Set-up of a solve: w0 = A z (z = D^-1 r0 from k_rhs / k_refine), delta0 =
+// z.w0 and alpha0 = r0.z / delta0.  The SpMV of the probe kernel with p = z.
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    c.need_old = false;
 #pragma unroll
-        for (int k = 0; k < NV; k++) part[k * stride + blockIdx.x] = blk[k];
-        s_gen = *(volatile unsigned int*)&gs->gen;
-        __threadfence();
-        s_last = atomicAdd(&gs->count, 1u) == gridDim.x - 1;
+    for (int f = 0; f < NF; f++) {
+        c.fresh[f] = true;
+        c.beta[f] = 0;
     }
-    __syncthreads();
-    if (s_last) {
-        __threadfence();
-        double y[NV];
+    StepArgs<R, NF> v = a;
+    v.pp[c.par ^ 1] = a.pp[0];
+    v.q = a.wb[c.par];
+    Acc<R> dot[NF];
+    spmv_phase<R, NF, WCH, LoadRO>(v, c, sm, dot);
+    double blk[NF], tot[NF];
+    block_totals<NF>(dot, red, blk);
+    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
+        volatile CgState* cg = a.cg;
+        finish_spmv<R, NF>(cg, a.run, c.act, tot);
+        int any = 0;
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double acc = 0.0;
-            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&part[k * stride + b]);
-            y[k] = acc;
+        for (int f = 0; f < NF; f++) {
+            cg->fresh[f] = 1;  // the first iteration takes p = u, s = w
+            any |= cg->active[f];
         }
-        block_sum<NV>(y, sm);
-        if (threadIdx.x == 0) {
-            gs->count = 0u;
-            on_last(y);
-            __threadfence();
-            atomicAdd(&gs->gen, 1u);
-            s_ok = 1;
-        }
-    } else if (threadIdx.x == 0) {
-        long long n = 0;
-        int ok = 1;
-        while (*(volatile unsigned int*)&gs->gen == s_gen) {
-            __nanosleep(100);
-            if (++n > kSpinLimit) {
-                atomicExch(&gs->err, 1);
-                ok = 0;
-                break;
-            }
-        }
-        __threadfence();
-        s_ok = ok;
+        signal_loop(a, any != 0);
     }
-    __syncthreads();
-    return s_ok && *(volatile int*)&gs->err == 0;
 }
 
 template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_solve(StepArgs<R, NF> a) {
-    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
-    __shared__ double red[32 * 2 * NF];
-    CgState* cg = a.cg;
-    RunState* run = a.run;
-    for (;;) {
-        PhaseCtl<R, NF> c;
-        c.load(cg);
-        if (!c.any) break;
-        {
-            Acc<R> dot[NF];
-            spmv_phase<R, NF, WCH, LoadCG>(a, c, sm, dot);
-            double blk[NF];
-            block_totals<NF>(dot, red, blk);
-            if (!grid_barrier_reduce<NF>(blk, a.part, a.part_stride, a.gs, red,
-                                         [&](const double* tot) { finish_spmv<R, NF>(cg, run, c.act, tot); }))
-                break;
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
+    constexpr int WIN = 32 * WCH;
+    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
+    __shared__ double red[32 * 3 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    const FV<R, NF>* __restrict__ r0 = a.rb[c.par];
+    const FV<R, NF>* __restrict__ w0 = a.wb[c.par];
+    const FV<R, NF>* __restrict__ s0 = a.sb[c.par];
+    FV<R, NF>* __restrict__ r1 = a.rb[c.par ^ 1];
+    FV<R, NF>* __restrict__ w1 = a.wb[c.par ^ 1];
+    FV<R, NF>* __restrict__ s1 = a.sb[c.par ^ 1];
+    // new residual and preconditioned residual of one unknown from its old r, w, s
+    auto advance = [&](const FV<R, NF>& ro, const FV<R, NF>& wo, const FV<R, NF>& so, const FV<R, NF>& d,
+                       FV<R, NF>& sn, FV<R, NF>& rn, FV<R, NF>& un) {
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            sn.v[f] = c.fresh[f] ? wo.v[f] : fma(c.beta[f], so.v[f], wo.v[f]);
+            rn.v[f] = c.act[f] ? fma(-c.alpha[f], sn.v[f], ro.v[f]) : ro.v[f];
+            un.v[f] = d.v[f] * rn.v[f];
         }
-        c.load(cg);
-        {
-            Acc<R> acc[2 * NF];
-            update_phase<R, NF, LoadCG>(a, c, acc);
-            double blk[2 * NF];
-            block_totals<2 * NF>(acc, red, blk);
-            if (!grid_barrier_reduce<2 * NF>(blk, a.part, a.part_stride, a.gs, red,
-                                             [&](const double* tot) { finish_update<R, NF>(cg, run, c.act, tot); }))
-                break;
+    };
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t N = a.N;
+    Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
+    for (int64_t row0 = warp * 32; row0 < N; row0 += nwarps * 32) {
+        const int64_t row = row0 + lane;
+        const int32_t rs = ldg(a.rp + (row < N ? row : N));
+        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+        if (lane == 31) re = ldg(a.rp + (row0 + 32 < N ? row0 + 32 : N));
+        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
+        R acc[NF];
+#pragma unroll
+        for (int f = 0; f < NF; f++) acc[f] = 0;
+        for (int32_t wb = e0; wb < e1; wb += WIN) {
+            FV<R, NF> av[WCH];
+            int32_t cc[WCH];
+#pragma unroll
+            for (int k = 0; k < WCH; k++) {
+                const int32_t idx = wb + k * 32 + lane;
+                cc[k] = -1;
+                if (idx < e1) {
+                    av[k] = ldv(a.A + idx, false);
+                    cc[k] = ldg(a.col + idx);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < WCH; k++) {
+                FV<R, NF> prod;
+#pragma unroll
+                for (int f = 0; f < NF; f++) prod.v[f] = 0;
+                if (cc[k] >= 0) {
+                    const int32_t col = cc[k];
+                    const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false);
+                    const FV<R, NF> d = ldv(a.dinv + col, false);
+                    FV<R, NF> so = wo;
+                    if (c.need_old) so = ldv(s0 + col, false);
+                    FV<R, NF> sn, rn, un;
+                    advance(ro, wo, so, d, sn, rn, un);
+#pragma unroll
+                    for (int f = 0; f < NF; f++) prod.v[f] = av[k].v[f] * un.v[f];
+                }
+                sm[wib][k * 32 + lane] = prod;
+            }
+            __syncwarp();
+            const int32_t lo = (rs > wb ? rs : wb) - wb;
+            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
+            for (int32_t k = lo; k < hi; k++) {
+                const FV<R, NF> t = sm[wib][k];
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
+            }
+            __syncwarp();
+        }
+        if (row < N) {
+            const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
+            FV<R, NF> so = wo;
+            if (c.need_old) so = ldv(s0 + row, false);
+            FV<R, NF> x = a.x[row], p = a.pp[0][row];
+            FV<R, NF> sn, rn, un, wn;
+            advance(ro, wo, so, d, sn, rn, un);
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (c.act[f]) {
+                    const R ui = d.v[f] * ro.v[f];
+                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                }
+                wn.v[f] = acc[f];
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[NF + f].add_prod(wn.v[f], un.v[f]);
+                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            a.x[row] = x;
+            a.pp[0][row] = p;
+            r1[row] = rn;
+            s1[row] = sn;
+            w1[row] = wn;
         }
     }
-    if (threadIdx.x == 0 && blockIdx.x == 0 && *(volatile int*)&a.gs->err)
-        atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
+    double blk[3 * NF], tot[3 * NF];
+    block_totals<3 * NF>(dots, red, blk);
+    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+        signal_loop(a, finish_cgcg<R, NF>(a.cg, a.run, c.act, tot));
 }
 
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
@@ -638,7 +649,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                 dots[2 * NF + f].add_prod(rv.v[f], pv.v[f]);
             }
             a.b[row] = bv;
-            a.r[row] = rv;
+            a.rb[0][row] = rv;  // iteration 0 reads parity 0
             a.z[row] = pv;
         }
     }
@@ -649,8 +660,6 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
         RunState* run = a.run;
         const int stop = (atomicOr(&run->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
         cg->stop = stop;
-        a.gs->count = 0u;  // the solve that follows starts from a clean barrier
-        a.gs->err = 0;
         cg->iter = 0;
         cg->max_iter = run->max_iter;
         int any = 0;
@@ -727,7 +736,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                     dots[f].add_prod(rv.v[f], rv.v[f]);
                     dots[NF + f].add_prod(rv.v[f], pv.v[f]);
                 }
-                a.r[row] = rv;
+                a.rb[cg->iter & 1][row] = rv;  // the restart continues the iteration parity
                 a.z[row] = pv;
             }
         }
@@ -736,8 +745,6 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
     if (grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot) && threadIdx.x == 0) {
         int any = 0;
 #pragma unroll
-        a.gs->count = 0u;
-        a.gs->err = 0;
         for (int f = 0; f < NF; f++) {
             cg->active[f] = 0;
             cg->fresh[f] = 1;
@@ -860,51 +867,31 @@ constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
 template <typename R, int NF, int WCH>
 struct Grids {
-    int spmv, solve, rhs, stream;
+    int spmv, iter, rhs, stream;
     explicit Grids(int64_t N) {
-        spmv = wave_grid(k_cg_spmv<R, NF, WCH>, ceil_div(N, kBlock));
-        // the cooperative solve needs every block resident: exactly one wave
-        solve = wave_grid(k_cg_solve<R, NF, WCH>, max_grid_blocks());
+        spmv = wave_grid(k_cgcg_init<R, NF, WCH>, ceil_div(N, kBlock));
+        iter = wave_grid(k_cgcg_iter<R, NF, WCH>, ceil_div(N, kBlock));
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
 };
 
-template <typename R, int NF, int WCH>
-cudaGraphNode_t add_solve(cudaGraph_t g, cudaGraphNode_t dep, const StepArgs<R, NF>& a, int grid) {
-    cudaGraphNode_t n = add_kernel(g, dep, k_cg_solve<R, NF, WCH>, grid, kBlock, a);
-    cudaKernelNodeAttrValue v = {};
-    v.cooperative = 1;
-    FEA_CUDA_TRY(cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v));
-    return n;
-}
-
-template <typename R, int NF, int WCH>
-void launch_solve(const StepArgs<R, NF>& a, int grid, cudaStream_t st) {
-    StepArgs<R, NF> local = a;
-    void* argv[] = {(void*)&local};
-    FEA_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_solve<R, NF, WCH>, dim3((unsigned)grid),
-                                             dim3((unsigned)kBlock), argv, 0, st));
-}
-
-// Argument sets of a step: the step loop (a, sets the step condition) and the
-// set-up kernels of the two solves (a1: rhs, a2: refine), which only store
-// whether their solve has work; the solve kernel reads that from CgState.
+// Argument sets of a step: the step loop (a) and the two CG loops (a1: after
+// k_rhs, a2: after k_refine); each names the condition it sets.
 template <typename R, int NF>
 struct LoopArgs {
     StepArgs<R, NF> a, a1, a2;
     LoopArgs(const StepArgs<R, NF>& base, LoopFlags* lf, int use_graph) : a(base), a1(base), a2(base) {
-        a.use_graph = use_graph;
-        a1.use_graph = a2.use_graph = 0;
+        a.use_graph = a1.use_graph = a2.use_graph = use_graph;
         a.cont = &lf->step;
         a1.cont = &lf->cg1;
         a2.cont = &lf->cg2;
     }
 };
 
-// Step graph:  start -> WHILE(step) { rhs -> solve -> refine -> solve -> [post]
-//              -> stepctl } -> final_check, each solve one cooperative launch
-//              running its whole CG loop.
+// Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter }
+//              -> refine -> init -> WHILE(cg2) { iter } -> [post] -> stepctl }
+//              -> final_check
 template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
@@ -917,10 +904,17 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     cudaGraph_t step_body;
     n = add_while(top, n, L.a.cond, &step_body);
     add_kernel(top, n, k_final_check<R, NF, EQ>, g.stream, kBlock, L.a);
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_solve<R, NF, WCH>(step_body, s, L.a1, g.solve);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a1);
+    cudaGraph_t body1, body2;
+    s = add_while(step_body, s, L.a1.cond, &body1);
+    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a1);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_solve<R, NF, WCH>(step_body, s, L.a2, g.solve);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a2);
+    s = add_while(step_body, s, L.a2.cond, &body2);
+    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a2);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -934,9 +928,10 @@ int read_flag(const int* d, cudaStream_t st) {
     return h;
 }
 
-// The same kernels launched one by one with the step condition read back on
-// the host: every kernel is then visible to profilers (kernels inside graphs
-// with conditional nodes are not).  Bounded by the step count.
+// The same kernels launched one by one with the loop conditions read back
+// on the host: every kernel is then visible to profilers (kernels inside
+// graphs with conditional nodes are not).  Each loop is bounded by the
+// kernels' own iteration and step limits.
 template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
@@ -946,10 +941,18 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     while (read_flag(&lf->step, st)) {
         k_rhs<R, NF, EQ, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
-        launch_solve<R, NF, WCH>(L.a1, g.solve, st);
-        k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
-        FEA_CHECK_LAUNCH();
-        launch_solve<R, NF, WCH>(L.a2, g.solve, st);
+        for (const StepArgs<R, NF>* la : {&L.a1, &L.a2}) {
+            if (la == &L.a2) {
+                k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
+                FEA_CHECK_LAUNCH();
+            }
+            k_cgcg_init<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
+            FEA_CHECK_LAUNCH();
+            while (read_flag(la->cont, st)) {
+                k_cgcg_iter<R, NF, WCH><<<g.iter, kBlock, 0, st>>>(*la);
+                FEA_CHECK_LAUNCH();
+            }
+        }
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK) {
             k_post<R, NF, EQ><<<g.stream, kBlock, 0, st>>>(L.a);
             FEA_CHECK_LAUNCH();

@@ -92,14 +92,6 @@ struct RunState {
     int refine;
 };
 
-// Grid-wide barrier state of the persistent solve kernel (zero at start).
-struct GridSync {
-    unsigned int count;  // blocks arrived at the current barrier
-    unsigned int gen;    // barrier generation, advanced by the last arriver
-    int err;             // a wait hit its iteration limit
-    int pad;
-};
-
 // Everything a step-loop kernel needs, passed by value.
 template <typename R, int NF>
 struct StepArgs {
@@ -113,10 +105,12 @@ struct StepArgs {
     const R* Adv;           // advection values [nnz]
     FV<R, NF>* x;           // unknown of the solve (warm start and result)
     FV<R, NF>* b;
-    FV<R, NF>* r;
-    FV<R, NF>* z;           // D^-1 r
-    FV<R, NF>* pp[2];       // search directions, alternating with the iteration parity
-    FV<R, NF>* q;
+    FV<R, NF>* z;           // D^-1 r of the initial residual
+    FV<R, NF>* pp[2];       // search direction (pp[0]; pp[1] only for the SpMV probe)
+    FV<R, NF>* q;           // SpMV probe output
+    FV<R, NF>* rb[2];       // residual r, w = A D^-1 r and s = A p, each in two
+    FV<R, NF>* wb[2];       // buffers that alternate with the iteration parity
+    FV<R, NF>* sb[2];       // (an iteration gathers the old and writes the new)
     R* u;                   // NF == 1 equations: displacement / field
     R* v;                   // velocity (wave)
     R* a;                   // acceleration (Newmark)
@@ -131,7 +125,6 @@ struct StepArgs {
     cudaGraphConditionalHandle cond;  // loop condition set by this kernel (graph mode)
     int* cont;              // the same condition, also stored here for host-driven loops
     int use_graph;          // 1: kernels run as graph nodes and set `cond`
-    GridSync* gs;           // barrier state of the persistent solve
 };
 
 // Loop-condition slots in device memory for host-driven (stream) execution.

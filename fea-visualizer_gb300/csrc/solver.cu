@@ -95,6 +95,7 @@ struct Fields {
     void* uv = nullptr;  // R[2N] interleaved (Gray-Scott)
     bool interleaved = false;  // (u, v) currently live in uv
     // solver work, one field (p1 holds the two alternating direction buffers)
+    // r1/r2 hold the alternating r, w, s buffers of the Chronopoulos-Gear loop
     void *A1 = nullptr, *d1 = nullptr, *b1 = nullptr, *r1 = nullptr, *z1 = nullptr, *p1 = nullptr, *q1 = nullptr;
     void *A0 = nullptr, *d0 = nullptr;  // Newmark start-up operator (M)
     // two fields
@@ -137,7 +138,6 @@ struct fea_solver {
     double* d_part = nullptr;
     unsigned int* d_tickets = nullptr;
     LoopFlags* d_flags = nullptr;
-    GridSync* d_gs = nullptr;  // barrier state of the persistent solve
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
@@ -242,9 +242,9 @@ void build_context(fea_solver* s) {
     F.A1 = ralloc(s->mat_mem, s, nnz);
     F.d1 = ralloc(s->mat_mem, s, N);
     F.b1 = ralloc(s->mat_mem, s, N);
-    F.r1 = ralloc(s->mat_mem, s, N);
+    const int64_t Np = pad4(N);  // every buffer of a group starts 16-byte aligned
+    F.r1 = ralloc(s->mat_mem, s, 6 * Np);  // r, w, s: two buffers each
     F.z1 = ralloc(s->mat_mem, s, N);
-    const int64_t Np = pad4(N);  // the second direction buffer starts 16-byte aligned
     F.p1 = ralloc(s->mat_mem, s, 2 * Np);
     F.q1 = ralloc(s->mat_mem, s, N);
     F.A0 = ralloc(s->mat_mem, s, nnz);
@@ -252,21 +252,32 @@ void build_context(fea_solver* s) {
     F.A2 = ralloc(s->mat_mem, s, 2 * nnz);
     F.d2 = ralloc(s->mat_mem, s, 2 * N);
     F.b2 = ralloc(s->mat_mem, s, 2 * N);
-    F.r2 = ralloc(s->mat_mem, s, 2 * N);
+    F.r2 = ralloc(s->mat_mem, s, 12 * Np);
     F.z2 = ralloc(s->mat_mem, s, 2 * N);
     F.p2 = ralloc(s->mat_mem, s, 4 * Np);
     F.q2 = ralloc(s->mat_mem, s, 2 * N);
     // every vector starts at zero (the direction buffers are read with weight
     // beta = 0 only after a write, but a zero start keeps them finite)
     const std::pair<void*, int64_t> zeroed[] = {
-        {F.u, N}, {F.v, N}, {F.a, N}, {F.ut, N}, {F.vt, N}, {F.uv, 2 * N}, {F.b1, N}, {F.r1, N}, {F.z1, N},
-        {F.p1, 2 * Np}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 2 * N}, {F.z2, 2 * N}, {F.p2, 4 * Np}, {F.q2, 2 * N}};
+        {F.u, N}, {F.v, N}, {F.a, N}, {F.ut, N}, {F.vt, N}, {F.uv, 2 * N}, {F.b1, N}, {F.r1, 6 * Np}, {F.z1, N},
+        {F.p1, 2 * Np}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 12 * Np}, {F.z2, 2 * N}, {F.p2, 4 * Np}, {F.q2, 2 * N}};
     for (const auto& zv : zeroed)
         FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
     F.interleaved = false;
     s->acc_valid = false;
     assemble(s);
     FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// r, w and s of the Chronopoulos-Gear iteration, two buffers each, carved
+// from one allocation of 6 * Np unknowns.
+template <typename R, int NF>
+void set_rws(StepArgs<R, NF>& a, FV<R, NF>* base, int64_t Np) {
+    for (int k = 0; k < 2; k++) {
+        a.rb[k] = base + k * Np;
+        a.wb[k] = base + (2 + k) * Np;
+        a.sb[k] = base + (4 + k) * Np;
+    }
 }
 
 template <typename R, int NF>
@@ -283,7 +294,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.A = (const FV<R, 1>*)(init_op ? F.A0 : F.A1);
         a.dinv = (const FV<R, 1>*)(init_op ? F.d0 : F.d1);
         a.b = (FV<R, 1>*)F.b1;
-        a.r = (FV<R, 1>*)F.r1;
+        set_rws(a, (FV<R, 1>*)F.r1, pad4(s->N));
         a.z = (FV<R, 1>*)F.z1;
         a.pp[0] = (FV<R, 1>*)F.p1;
         a.pp[1] = a.pp[0] + pad4(s->N);
@@ -292,7 +303,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.A = (const FV<R, 2>*)F.A2;
         a.dinv = (const FV<R, 2>*)F.d2;
         a.b = (FV<R, 2>*)F.b2;
-        a.r = (FV<R, 2>*)F.r2;
+        set_rws(a, (FV<R, 2>*)F.r2, pad4(s->N));
         a.z = (FV<R, 2>*)F.z2;
         a.pp[0] = (FV<R, 2>*)F.p2;
         a.pp[1] = a.pp[0] + pad4(s->N);
@@ -309,7 +320,6 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
     a.part = s->d_part;
     a.part_stride = max_grid_blocks();
     a.tickets = s->d_tickets;
-    a.gs = s->d_gs;
     return a;
 }
 
@@ -513,8 +523,6 @@ void alloc_run_state(fea_solver* s) {
     s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
     s->d_tickets = s->run_mem.alloc<unsigned int>(8);
     s->d_flags = s->run_mem.alloc<LoopFlags>(1);
-    s->d_gs = s->run_mem.alloc<GridSync>(1);
-    FEA_CUDA_TRY(cudaMemsetAsync(s->d_gs, 0, sizeof(GridSync), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, sizeof(LoopFlags), s->stream));
     const char* mode = getenv("FEA_LAUNCH_MODE");
     s->stream_mode = mode && strcmp(mode, "stream") == 0;
