@@ -111,11 +111,12 @@ __global__ void k_ordered_sum_adv(const int32_t* __restrict__ seg_start, const i
 }
 
 template <typename R, int NF>
-__global__ void k_combine(int64_t nnz, const double* __restrict__ M, const double* __restrict__ K,
-                          const double* __restrict__ Adv, OpCoef<NF> c, FV<R, NF>* A) {
+__global__ void k_combine(int64_t nnz, const int32_t* __restrict__ emap, const double* __restrict__ M,
+                          const double* __restrict__ K, const double* __restrict__ Adv, OpCoef<NF> c, FV<R, NF>* A) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
-        const double m = M[e], kk = K[e];
-        const double ad = Adv ? Adv[e] : 0.0;
+        const int64_t src = emap ? emap[e] : e;
+        const double m = M[src], kk = K[src];
+        const double ad = Adv ? Adv[src] : 0.0;
         FV<R, NF> out;
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -129,9 +130,9 @@ __global__ void k_combine(int64_t nnz, const double* __restrict__ M, const doubl
 }
 
 template <typename R>
-__global__ void k_round_copy(const double* __restrict__ in, int64_t n, R* out) {
+__global__ void k_round_copy(const double* __restrict__ in, const int32_t* __restrict__ map, int64_t n, R* out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (R)in[i];
+        out[i] = (R)in[map ? map[i] : i];
 }
 
 // Inverse diagonal (Eigen's DiagonalPreconditioner: 1 where the diagonal is 0).
@@ -178,10 +179,10 @@ void ordered_sum_adv(const Pattern& P, const R* loc, const uint32_t* tri, const 
 }
 
 template <typename R, int NF>
-void combine_operator(const Pattern& P, const double* M, const double* K, const double* Adv, const OpCoef<NF>& c,
-                      FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st) {
+void combine_operator(const Pattern& P, const int32_t* emap, const double* M, const double* K, const double* Adv,
+                      const OpCoef<NF>& c, FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st) {
     if (P.nnz > 0) {
-        k_combine<R, NF><<<launch_grid(P.nnz), kBlock, 0, st>>>(P.nnz, M, K, Adv, c, A);
+        k_combine<R, NF><<<launch_grid(P.nnz), kBlock, 0, st>>>(P.nnz, emap, M, K, Adv, c, A);
         FEA_CHECK_LAUNCH();
     }
     if (P.N > 0) {
@@ -191,9 +192,9 @@ void combine_operator(const Pattern& P, const double* M, const double* K, const 
 }
 
 template <typename R>
-void round_copy(const double* in, int64_t n, R* out, cudaStream_t st) {
+void round_copy(const double* in, const int32_t* map, int64_t n, R* out, cudaStream_t st) {
     if (n <= 0) return;
-    k_round_copy<R><<<launch_grid(n), kBlock, 0, st>>>(in, n, out);
+    k_round_copy<R><<<launch_grid(n), kBlock, 0, st>>>(in, map, n, out);
     FEA_CHECK_LAUNCH();
 }
 
@@ -203,11 +204,11 @@ void round_copy(const double* in, int64_t n, R* out, cudaStream_t st) {
     template void ordered_sum<R>(const Pattern&, const R*, const R*, R*, cudaStream_t);                    \
     template void ordered_sum_adv<R>(const Pattern&, const R*, const uint32_t*, const uint8_t*, R*, uint8_t*, \
                                      cudaStream_t);                                                        \
-    template void combine_operator<R, 1>(const Pattern&, const double*, const double*, const double*,      \
-                                         const OpCoef<1>&, FV<R, 1>*, FV<R, 1>*, cudaStream_t);             \
-    template void combine_operator<R, 2>(const Pattern&, const double*, const double*, const double*,      \
-                                         const OpCoef<2>&, FV<R, 2>*, FV<R, 2>*, cudaStream_t);             \
-    template void round_copy<R>(const double*, int64_t, R*, cudaStream_t);
+    template void combine_operator<R, 1>(const Pattern&, const int32_t*, const double*, const double*,     \
+                                         const double*, const OpCoef<1>&, FV<R, 1>*, FV<R, 1>*, cudaStream_t); \
+    template void combine_operator<R, 2>(const Pattern&, const int32_t*, const double*, const double*,     \
+                                         const double*, const OpCoef<2>&, FV<R, 2>*, FV<R, 2>*, cudaStream_t); \
+    template void round_copy<R>(const double*, const int32_t*, int64_t, R*, cudaStream_t);
 FEA_INST_R(float)
 FEA_INST_R(double)
 

@@ -22,6 +22,10 @@ struct Pattern {
 };
 
 int launch_grid(int64_t n);
+// Copy of P with the unknowns renumbered (pos[u] = new index, inv = inverse);
+// emap[e'] receives the original slot of every new slot.
+void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pattern& Pc, int32_t* emap,
+                    DeviceArena& keep, cudaStream_t st);
 void detect_boundary(const uint32_t* tri, int64_t T, int64_t V, uint8_t* ob, cudaStream_t st);
 bool check_triangles(const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st);
 int64_t build_idx_map(const uint8_t* ob, int64_t V, int bc, int32_t* idx, cudaStream_t st);
@@ -49,12 +53,14 @@ template <int NF>
 struct OpCoef {
     OpCoef1 f[NF];
 };
+// P is the pattern the operator is stored on; with emap, its slot e' takes the
+// matrix values of slot emap[e'] (the matrices stay in the assembly order).
 template <typename R, int NF>
-void combine_operator(const Pattern& P, const double* M, const double* K, const double* Adv, const OpCoef<NF>& c,
-                      FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st);
-// out[i] = (R)in[i]
+void combine_operator(const Pattern& P, const int32_t* emap, const double* M, const double* K, const double* Adv,
+                      const OpCoef<NF>& c, FV<R, NF>* A, FV<R, NF>* dinv, cudaStream_t st);
+// out[i] = (R)in[map ? map[i] : i]
 template <typename R>
-void round_copy(const double* in, int64_t n, R* out, cudaStream_t st);
+void round_copy(const double* in, const int32_t* map, int64_t n, R* out, cudaStream_t st);
 
 // ---- time stepping (cg.cu) ------------------------------------------------------
 enum StepKind : int {

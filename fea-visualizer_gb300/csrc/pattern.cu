@@ -398,4 +398,68 @@ void build_pattern(Pattern& P, DeviceArena& keep, const uint32_t* tri, int64_t T
     P.max_row = mx;
 }
 
+// ---- computational ordering --------------------------------------------------------
+//
+// The solver iterates on a copy of the pattern whose unknowns are renumbered
+// along a Morton (Z-order) curve of their coordinates, so that the rows a
+// warp processes together have their columns in a few nearby ranges and the
+// gathered vector entries hit in L1.  pos[u] is the new index of unknown u,
+// inv its inverse; emap[e'] is the original slot of new slot e'.  Within a
+// row the columns are sorted again, so the copy is a valid CSR matrix.
+
+namespace {
+
+__global__ void k_perm_rowlen(const int32_t* rp, const int32_t* inv, int64_t N, int32_t* len) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = inv[c];
+        len[c] = rp[u + 1] - rp[u];
+    }
+}
+
+__global__ void k_perm_fill(const int32_t* rp, const int32_t* col, const int32_t* pos, const int32_t* inv,
+                            int64_t N, const int32_t* rpc, int32_t* colc, int32_t* emap) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < N; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = inv[c];
+        const int32_t s = rp[u], n = rp[u + 1] - s, o = rpc[c];
+        // insertion sort by new column, written straight to the output row
+        for (int32_t k = 0; k < n; k++) {
+            const int32_t nc = pos[col[s + k]];
+            int32_t j = k - 1;
+            while (j >= 0 && colc[o + j] > nc) {
+                colc[o + j + 1] = colc[o + j];
+                emap[o + j + 1] = emap[o + j];
+                j--;
+            }
+            colc[o + j + 1] = nc;
+            emap[o + j + 1] = s + k;
+        }
+    }
+}
+
+}  // namespace
+
+void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pattern& Pc, int32_t* emap,
+                    DeviceArena& keep, cudaStream_t st) {
+    DeviceArena tmp;
+    const int64_t N = P.N;
+    Pc.N = N;
+    Pc.nnz = P.nnz;
+    Pc.max_row = P.max_row;
+    int32_t* len = tmp.alloc<int32_t>(N + 1);
+    k_perm_rowlen<<<grid_for(N), kBlock, 0, st>>>(P.row_ptr, inv, N, len);
+    FEA_CHECK_LAUNCH();
+    Pc.row_ptr = keep.alloc<int32_t>(N + 1);
+    exclusive_scan_i32(len, Pc.row_ptr, N, st);
+    Pc.col = keep.alloc<int32_t>(P.nnz);
+    k_perm_fill<<<grid_for(N), kBlock, 0, st>>>(P.row_ptr, P.col, pos, inv, N, Pc.row_ptr, Pc.col, emap);
+    FEA_CHECK_LAUNCH();
+    Pc.diag = keep.alloc<int32_t>(N);
+    k_find_diag<<<grid_for(N), kBlock, 0, st>>>(Pc.row_ptr, Pc.col, N, Pc.diag);
+    FEA_CHECK_LAUNCH();
+    Pc.tpos = keep.alloc<int32_t>(P.nnz);
+    k_transpose_index<<<grid_for(N), kBlock, 0, st>>>(Pc.row_ptr, Pc.col, N, Pc.tpos);
+    FEA_CHECK_LAUNCH();
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
 }  // namespace fea

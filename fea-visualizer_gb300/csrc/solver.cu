@@ -3,9 +3,11 @@
 // A handle holds one mesh and plays the roles of the reference's FEMContext
 // (mesh, idx_map, assembled matrices; src/FEM/FEMContext.cpp) and of a Solver
 // implementation (state fields u, v and advance_time; include/FEM/Solver.hpp).
+#include <algorithm>
 #include <cstdarg>
 #include <cstring>
 #include <new>
+#include <utility>
 
 #include "fea_internal.cuh"
 
@@ -69,11 +71,25 @@ __global__ void k_deinterleave(const R* __restrict__ uv, int64_t N, R* u, R* v) 
     }
 }
 
+// Caller-order unknown u <-> solver-order index pos[u].
 template <typename R>
-__global__ void k_copy_strided(const R* __restrict__ in, int64_t N, int in_stride, int in_off, R* out,
-                               int out_stride, int out_off) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-        out[i * out_stride + out_off] = in[i * in_stride + in_off];
+__global__ void k_copy_to_state(const R* __restrict__ in, const int32_t* __restrict__ pos, int64_t N, R* out,
+                                int stride, int off) {
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < N; u += (int64_t)gridDim.x * blockDim.x)
+        out[(int64_t)pos[u] * stride + off] = in[u];
+}
+
+template <typename R>
+__global__ void k_copy_from_state(const R* __restrict__ in, const int32_t* __restrict__ pos, int64_t N, R* out,
+                                  int stride, int off) {
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < N; u += (int64_t)gridDim.x * blockDim.x)
+        out[u] = in[(int64_t)pos[u] * stride + off];
+}
+
+__global__ void k_compose_idx(const int32_t* __restrict__ idx, const int32_t* __restrict__ pos, int64_t V,
+                              int32_t* idx_c) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x)
+        idx_c[i] = idx[i] >= 0 ? pos[idx[i]] : -1;
 }
 
 template <typename R>
@@ -127,7 +143,15 @@ struct fea_solver {
     Pattern P;
     double *Kloc = nullptr, *Mloc = nullptr, *Aloc = nullptr;  // element blocks [9T], FP64
     double *K64 = nullptr, *M64 = nullptr, *Adv64 = nullptr;   // assembled in FP64
-    void *K = nullptr, *M = nullptr, *Adv = nullptr;           // in the handle's type
+    void *K = nullptr, *M = nullptr, *Adv = nullptr;           // in the handle's type (export)
+    // the solver's ordering of the unknowns (Morton order of their points)
+    Pattern Pc;                     // pattern in solver order
+    int32_t* pos = nullptr;         // [N] unknown -> solver index
+    int32_t* inv = nullptr;         // [N] solver index -> unknown
+    int32_t* emap = nullptr;        // [nnz] solver slot -> assembly slot
+    int32_t* idx_c = nullptr;       // [V] node -> solver index (-1 on Dirichlet points)
+    void *Kc = nullptr, *Mc = nullptr, *Advc = nullptr;        // values in solver order
+    std::vector<float> h_xyz;       // host copy of the points (ordering keys)
     uint8_t* adv_present = nullptr;
     Fields F;
     // loop state
@@ -194,13 +218,81 @@ void assemble(fea_solver* s) {
     ordered_sum<double>(s->P, s->Mloc, nullptr, s->M64, s->stream);
     ordered_sum_adv<double>(s->P, s->Aloc, s->tri, s->ob, s->Adv64, s->adv_present, s->stream);
     if (s->precision == FEA_FP32) {
-        round_copy<float>(s->K64, s->P.nnz, (float*)s->K, s->stream);
-        round_copy<float>(s->M64, s->P.nnz, (float*)s->M, s->stream);
-        round_copy<float>(s->Adv64, s->P.nnz, (float*)s->Adv, s->stream);
+        round_copy<float>(s->K64, nullptr, s->P.nnz, (float*)s->K, s->stream);
+        round_copy<float>(s->M64, nullptr, s->P.nnz, (float*)s->M, s->stream);
+        round_copy<float>(s->Adv64, nullptr, s->P.nnz, (float*)s->Adv, s->stream);
+        round_copy<float>(s->K64, s->emap, s->P.nnz, (float*)s->Kc, s->stream);
+        round_copy<float>(s->M64, s->emap, s->P.nnz, (float*)s->Mc, s->stream);
+        round_copy<float>(s->Adv64, s->emap, s->P.nnz, (float*)s->Advc, s->stream);
+    } else {
+        round_copy<double>(s->K64, s->emap, s->P.nnz, (double*)s->Kc, s->stream);
+        round_copy<double>(s->M64, s->emap, s->P.nnz, (double*)s->Mc, s->stream);
+        round_copy<double>(s->Adv64, s->emap, s->P.nnz, (double*)s->Advc, s->stream);
     }
     memcpy(s->cur_vel, s->prm.advdiff_velocity, sizeof(s->cur_vel));
     s->cur_vel_mode = s->prm.velocity_mode;
     s->op_dirty = true;
+}
+
+uint64_t spread3(uint32_t x) {  // 21 bits -> every third bit of 63
+    uint64_t v = x & 0x1fffffu;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// The solver's ordering of the unknowns: sorted by the 63-bit Morton key of
+// their points (coordinates quantised to 21 bits over the bounding box), ties
+// by unknown number.  Neighbouring points get nearby numbers, so the columns a
+// warp gathers sit in few cache lines.  Computed on the host once per mesh and
+// boundary condition.
+void build_ordering(fea_solver* s) {
+    cudaStream_t st = s->stream;
+    const int64_t V = s->V, N = s->N;
+    std::vector<int32_t> idx(V);
+    FEA_CUDA_TRY(cudaMemcpyAsync(idx.data(), s->idx, sizeof(int32_t) * V, cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < 3; d++) {
+        lo[d] = hi[d] = V ? s->h_xyz[d] : 0.f;
+        for (int64_t i = 0; i < V; i++) {
+            lo[d] = std::min(lo[d], s->h_xyz[3 * i + d]);
+            hi[d] = std::max(hi[d], s->h_xyz[3 * i + d]);
+        }
+    }
+    std::vector<std::pair<uint64_t, int32_t>> key;
+    key.reserve(N);
+    for (int64_t i = 0; i < V; i++) {
+        if (idx[i] < 0) continue;
+        uint64_t m = 0;
+        for (int d = 0; d < 3; d++) {
+            const double ext = (double)hi[d] - (double)lo[d];
+            double t = ext > 0 ? ((double)s->h_xyz[3 * i + d] - lo[d]) / ext : 0.0;
+            t = t < 0 ? 0 : (t > 1 ? 1 : t);
+            m |= spread3((uint32_t)(t * 2097151.0)) << d;
+        }
+        key.emplace_back(m, idx[i]);
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int32_t> pos(N), inv(N);
+    for (int64_t c = 0; c < N; c++) {
+        inv[c] = key[c].second;
+        pos[key[c].second] = (int32_t)c;
+    }
+    s->pos = s->mat_mem.alloc<int32_t>(N);
+    s->inv = s->mat_mem.alloc<int32_t>(N);
+    s->emap = s->mat_mem.alloc<int32_t>(s->P.nnz);
+    s->idx_c = s->mat_mem.alloc<int32_t>(V);
+    if (N > 0) {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->pos, pos.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st));
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->inv, inv.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st));
+    }
+    k_compose_idx<<<launch_grid(V), kBlock, 0, st>>>(s->idx, s->pos, V, s->idx_c);
+    FEA_CHECK_LAUNCH();
+    build_permuted(s->P, s->pos, s->inv, s->Pc, s->emap, s->mat_mem, st);
 }
 
 // FEMContext::update_boundary_conditions + assemble_matrices and the state.
@@ -209,12 +301,14 @@ void build_context(fea_solver* s) {
     s->init_graph.destroy();
     s->mat_mem.release();
     s->P = Pattern{};
+    s->Pc = Pattern{};
     s->F = Fields{};
     cudaStream_t st = s->stream;
     s->idx = s->mat_mem.alloc<int32_t>(s->V);
     s->N = build_idx_map(s->ob, s->V, s->bc, s->idx, st);
     build_pattern(s->P, s->mat_mem, s->tri, s->T, s->ob, s->idx, s->bc, s->N, st);
     const int64_t N = s->N, nnz = s->P.nnz, T = s->T;
+    build_ordering(s);
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
     s->Mloc = s->mat_mem.alloc<double>(9 * T);
     s->Aloc = s->mat_mem.alloc<double>(9 * T);
@@ -230,6 +324,9 @@ void build_context(fea_solver* s) {
         s->M = ralloc(s->mat_mem, s, nnz);
         s->Adv = ralloc(s->mat_mem, s, nnz);
     }
+    s->Kc = ralloc(s->mat_mem, s, nnz);
+    s->Mc = ralloc(s->mat_mem, s, nnz);
+    s->Advc = ralloc(s->mat_mem, s, nnz);
     s->adv_present = s->mat_mem.alloc<uint8_t>(nnz);
     Fields& F = s->F;
     F.N = N;
@@ -285,11 +382,11 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
     StepArgs<R, NF> a{};
     Fields& F = s->F;
     a.N = (int)s->N;
-    a.rp = s->P.row_ptr;
-    a.col = s->P.col;
-    a.M = (const R*)s->M;
-    a.K = (const R*)s->K;
-    a.Adv = (const R*)s->Adv;
+    a.rp = s->Pc.row_ptr;
+    a.col = s->Pc.col;
+    a.M = (const R*)s->Mc;
+    a.K = (const R*)s->Kc;
+    a.Adv = (const R*)s->Advc;
     if constexpr (NF == 1) {
         a.A = (const FV<R, 1>*)(init_op ? F.A0 : F.A1);
         a.dinv = (const FV<R, 1>*)(init_op ? F.d0 : F.d1);
@@ -371,7 +468,7 @@ void update_operator(fea_solver* s, int kind) {
         OpCoef<2> c{};
         c.f[0] = {dt, (double)p.rd_Du, 1.0, 0.0};
         c.f[1] = {dt, (double)p.rd_Dv, 1.0, 0.0};
-        combine_operator<R, 2>(s->P, s->M64, s->K64, s->Adv64, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
+        combine_operator<R, 2>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
                                s->stream);
     } else {
         OpCoef<1> c{};
@@ -393,10 +490,10 @@ void update_operator(fea_solver* s, int kind) {
             c.f[0].k1 = p.newmark_beta * dt * dt * (cc * cc);
             OpCoef<1> m{};
             m.f[0] = {1.0, 0.0, 1.0, 0.0};
-            combine_operator<R, 1>(s->P, s->M64, s->K64, s->Adv64, m, (FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->F.d0,
+            combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, m, (FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->F.d0,
                                    s->stream);
         }
-        combine_operator<R, 1>(s->P, s->M64, s->K64, s->Adv64, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
+        combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
                                s->stream);
     }
 }
@@ -475,9 +572,9 @@ void set_node_field(fea_solver* s, const float* host, int which /*0 u, 1 v*/) {
     FEA_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(float) * s->V, cudaMemcpyHostToDevice, s->stream));
     Fields& F = s->F;
     if (F.interleaved)
-        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx, s->V, (R*)F.uv, 2, which);
+        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx_c, s->V, (R*)F.uv, 2, which);
     else
-        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx, s->V,
+        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx_c, s->V,
                                                                         (R*)(which ? F.v : F.u), 1, 0);
     FEA_CHECK_LAUNCH();
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -488,9 +585,9 @@ void get_node_field(fea_solver* s, float* host, int which) {
     float* d = s->d_nodes;
     Fields& F = s->F;
     if (F.interleaved)
-        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)F.uv, s->idx, s->V, d, 2, which);
+        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)F.uv, s->idx_c, s->V, d, 2, which);
     else
-        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)(which ? F.v : F.u), s->idx, s->V, d,
+        k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)(which ? F.v : F.u), s->idx_c, s->V, d,
                                                                          1, 0);
     FEA_CHECK_LAUNCH();
     FEA_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(float) * s->V, cudaMemcpyDeviceToHost, s->stream));
@@ -505,9 +602,9 @@ void copy_field_device(fea_solver* s, const void* src, void* dst, int which, boo
     R* state = F.interleaved ? (R*)F.uv : (R*)(which ? F.v : F.u);
     const int st = F.interleaved ? 2 : 1, off = F.interleaved ? which : 0;
     if (to_state)
-        k_copy_strided<R><<<launch_grid(N), kBlock, 0, s->stream>>>((const R*)src, N, 1, 0, state, st, off);
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, s->stream>>>((const R*)src, s->pos, N, state, st, off);
     else
-        k_copy_strided<R><<<launch_grid(N), kBlock, 0, s->stream>>>(state, N, st, off, (R*)dst, 1, 0);
+        k_copy_from_state<R><<<launch_grid(N), kBlock, 0, s->stream>>>(state, s->pos, N, (R*)dst, st, off);
     FEA_CHECK_LAUNCH();
 }
 
@@ -604,6 +701,7 @@ int fea_create(const float* vertices, int64_t V, const uint32_t* triangles, int6
     s->T = T;
     if (params) s->prm = *params;
     else fea_params_default(&s->prm);
+    s->h_xyz.assign(vertices, vertices + 3 * V);
     s->xyz = s->mesh_mem.alloc<float>(3 * V);
     s->tri = s->mesh_mem.alloc<uint32_t>(3 * T);
     s->ob = s->mesh_mem.alloc<uint8_t>(V);
