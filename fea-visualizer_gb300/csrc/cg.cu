@@ -19,6 +19,7 @@
 #include <cmath>
 
 #include "fea_internal.cuh"
+#include "tma.cuh"
 
 namespace fea {
 
@@ -170,17 +171,10 @@ struct RowMap {
     }
 };
 
-// ---- CSR SpMV building blocks ------------------------------------------------------
+// ---- CG building blocks -----------------------------------------------------------
 //
 // Every kernel reads vectors that earlier launches wrote, so the read-only
-// path (LoadRO) is valid for all of them.
-
-struct LoadRO {
-    template <typename T>
-    static __device__ __forceinline__ T ld(const T* p) {
-        return ldv<T>(p, false);
-    }
-};
+// cache path is valid for all of them.
 
 // Control values of one phase, read once per phase by every thread.
 template <typename R, int NF>
@@ -208,90 +202,113 @@ struct PhaseCtl {
     }
 };
 
-// q = A p_new with p_new = z + beta p_old computed for every gathered column
-// (the direction update of the previous iteration, fused; the two p buffers
-// alternate with the iteration parity), plus p_new.q into dot[].
+// ---- TMA-staged row tiles --------------------------------------------------------------
 //
-// Warp-cooperative CSR: a warp owns 32 consecutive rows, whose stored entries
-// form one contiguous range.  The warp streams that range in windows of
-// 32*WCH entries: every lane issues WCH coalesced value/column loads, then WCH
-// independent gathers, so each round trip to memory carries a whole window
-// rather than one row.  Products go to shared memory and each lane sums its
-// own row in column order.
-template <typename R, int NF, int WCH, typename LP>
-__device__ __forceinline__ void spmv_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
-                                           FV<R, NF> (*sm)[32 * WCH], Acc<R> (&dot)[NF]) {
-    constexpr int WIN = 32 * WCH;
-    const FV<R, NF>* pold = a.pp[c.par];
-    FV<R, NF>* pnew = a.pp[c.par ^ 1];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t N = a.N;
-    for (int64_t r0 = warp * 32; r0 < N; r0 += nwarps * 32) {
-        const int64_t row = r0 + lane;
-        const int32_t rs = ldg(a.rp + (row < N ? row : N));
-        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
-        if (lane == 31) re = ldg(a.rp + (r0 + 32 < N ? r0 + 32 : N));
-        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
-        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
-        R acc[NF];
-#pragma unroll
-        for (int f = 0; f < NF; f++) acc[f] = 0;
-        for (int32_t wb = e0; wb < e1; wb += WIN) {
-            FV<R, NF> av[WCH];
-            int32_t cc[WCH];
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                const int32_t idx = wb + k * 32 + lane;
-                cc[k] = -1;
-                if (idx < e1) {
-                    av[k] = ldv(a.A + idx, false);
-                    cc[k] = ldg(a.col + idx);
-                }
+// A block owns TR consecutive rows (32 per warp, one per lane).  Thread 0
+// stages the tile's row pointers, matrix values and column indices into
+// shared memory with three bulk copies (TMA) completing on one mbarrier; the
+// lanes then sum their own rows in column order from shared memory, so the
+// only global accesses left per entry are the gathers of vector values.  The
+// staged range is rounded out to multiples of 4 entries (16 bytes); the
+// arrays carry 4 entries of padding for that.  A tile with more than CAP
+// entries (a vertex of very high valence) is read from global memory instead.
+
+constexpr int kTileCap = 2560;  // staged entries per tile (10 per row for 256 rows)
+
+template <typename R, int NF, int TR>
+struct TileStage {
+    static_assert(TR + 4 <= kRowPtrPad, "row pointer padding covers a whole tile");
+    alignas(16) int32_t rp[TR + 4];
+    alignas(16) FV<R, NF> A[kTileCap];
+    alignas(16) int32_t col[kTileCap];
+    alignas(8) uint64_t bar;
+    int32_t e0;   // first staged entry
+    int use;      // 1: staged in shared memory
+};
+
+// Stage the tile that starts at row t0.  Returns false (with nothing to
+// compute) when a wait ran out; the caller then raises an error flag.
+template <typename R, int NF, int TR>
+__device__ bool stage_tile(TileStage<R, NF, TR>& ts, const StepArgs<R, NF>& a, int64_t t0) {
+    if (threadIdx.x == 0) {
+        const int64_t N = a.N;
+        const int32_t E0 = a.rp[t0], E1 = a.rp[t0 + TR < N ? t0 + TR : N];
+        const int32_t e0 = E0 & ~3, e1 = (E1 + 3) & ~3;
+        ts.e0 = e0;
+        ts.use = 0;
+        if (e1 - e0 <= kTileCap) {
+            ts.use = 1;
+            mbar_init(&ts.bar, 1);
+            mbar_fence_init();
+            const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
+            const uint32_t nC = (uint32_t)(e1 - e0) * 4u;
+            const uint32_t nR = (uint32_t)sizeof(ts.rp);
+            mbar_arrive_expect_tx(&ts.bar, nR + nA + nC);
+            bulk_g2s(ts.rp, a.rp + t0, nR, &ts.bar);
+            if (nA) {
+                bulk_g2s(ts.A, a.A + e0, nA, &ts.bar);
+                bulk_g2s(ts.col, a.col + e0, nC, &ts.bar);
             }
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                FV<R, NF> prod;
-#pragma unroll
-                for (int f = 0; f < NF; f++) prod.v[f] = 0;
-                if (cc[k] >= 0) {
-                    const FV<R, NF> zc = LP::ld(a.z + cc[k]);
-                    FV<R, NF> pc = zc;
-                    if (c.need_old) pc = LP::ld(pold + cc[k]);
-#pragma unroll
-                    for (int f = 0; f < NF; f++) {
-                        const R pn = c.fresh[f] ? zc.v[f] : fma(c.beta[f], pc.v[f], zc.v[f]);
-                        prod.v[f] = av[k].v[f] * pn;
-                    }
-                }
-                sm[wib][k * 32 + lane] = prod;
-            }
-            __syncwarp();
-            const int32_t lo = (rs > wb ? rs : wb) - wb;
-            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
-            for (int32_t k = lo; k < hi; k++) {
-                const FV<R, NF> t = sm[wib][k];
-#pragma unroll
-                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
-            }
-            __syncwarp();
-        }
-        if (row < N) {
-            const FV<R, NF> zr = LP::ld(a.z + row);
-            FV<R, NF> pr = zr, qv;
-            if (c.need_old) pr = LP::ld(pold + row);
-#pragma unroll
-            for (int f = 0; f < NF; f++) {
-                const R pn = c.fresh[f] ? zr.v[f] : fma(c.beta[f], pr.v[f], zr.v[f]);
-                pr.v[f] = pn;
-                qv.v[f] = acc[f];
-                dot[f].add_prod(pn, acc[f]);
-            }
-            pnew[row] = pr;
-            a.q[row] = qv;
         }
     }
+    __syncthreads();
+    bool ok = true;
+    if (ts.use) ok = mbar_wait(&ts.bar, 0);
+    if (__syncthreads_and(ok)) return true;
+    // a copy did not complete in time: wait (bounded) once more so that no copy
+    // into this block's shared memory is left in flight when it exits
+    if (ts.use) mbar_wait(&ts.bar, 0);
+    return false;
+}
+
+// Row extent and staged-entry accessors for lane row `row` of the tile.
+template <typename R, int NF, int TR>
+struct TileRow {
+    const TileStage<R, NF, TR>& ts;
+    const StepArgs<R, NF>& a;
+    int64_t t0;
+    __device__ __forceinline__ int32_t start(int64_t row) const {
+        return ts.use ? ts.rp[row - t0] : ldg(a.rp + row);
+    }
+    __device__ __forceinline__ int32_t end(int64_t row) const {
+        return ts.use ? ts.rp[row - t0 + 1] : ldg(a.rp + row + 1);
+    }
+    __device__ __forceinline__ FV<R, NF> val(int32_t e) const {
+        return ts.use ? ts.A[e - ts.e0] : ldv(a.A + e, false);
+    }
+    __device__ __forceinline__ int32_t col(int32_t e) const {
+        return ts.use ? ts.col[e - ts.e0] : ldg(a.col + e);
+    }
+};
+
+// Sum over the entries of one row of A_e * g(col_e), U entries in flight.
+template <int U, typename R, int NF, int TR, typename G>
+__device__ __forceinline__ FV<R, NF> row_product(const TileRow<R, NF, TR>& tr, int32_t rs, int32_t re, G g) {
+    FV<R, NF> acc;
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc.v[f] = 0;
+    for (int32_t e = rs; e < re; e += U) {
+        FV<R, NF> av[U];
+        int32_t cc[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            cc[k] = -1;
+            if (e + k < re) {
+                av[k] = tr.val(e + k);
+                cc[k] = tr.col(e + k);
+            }
+        }
+        FV<R, NF> gv[U];
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (cc[k] >= 0) gv[k] = g(cc[k]);
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (cc[k] >= 0)
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc.v[f] = fma(av[k].v[f], gv[k].v[f], acc.v[f]);
+    }
+    return acc;
 }
 
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
@@ -387,22 +404,6 @@ __device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, doub
     __syncthreads();
 }
 
-// ---- standalone kernels (autotuning and timing probes) -------------------------------
-
-template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
-    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
-    __shared__ double red[32 * NF];
-    PhaseCtl<R, NF> c;
-    c.load(a.cg);
-    Acc<R> dot[NF];
-    spmv_phase<R, NF, WCH, LoadRO>(a, c, sm, dot);
-    double blk[NF], tot[NF];
-    block_totals<NF>(dot, red, blk);
-    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0)
-        finish_spmv<R, NF>(a.cg, a.run, c.act, tot);
-}
-
 // ---- Chronopoulos-Gear iteration -----------------------------------------------------
 //
 // Jacobi-preconditioned CG rearranged (Chronopoulos & Gear, 1989) so that one
@@ -416,24 +417,28 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
 // w and s there (so r, w and s alternate between two buffers).
 
 // Set-up of a solve: w0 = A z (z = D^-1 r0 from k_rhs / k_refine), delta0 =
-// z.w0 and alpha0 = r0.z / delta0.  The SpMV of the probe kernel with p = z.
-template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
-    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+// z.w0 and alpha0 = r0.z / delta0.  Also the SpMV timing probe.
+template <typename R, int NF, int TR, int U>
+__global__ void __launch_bounds__(TR) k_cgcg_init(StepArgs<R, NF> a) {
+    __shared__ TileStage<R, NF, TR> ts;
     __shared__ double red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
-    c.need_old = false;
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        c.fresh[f] = true;
-        c.beta[f] = 0;
-    }
-    StepArgs<R, NF> v = a;
-    v.pp[c.par ^ 1] = a.pp[0];
-    v.q = a.wb[c.par];
+    const int64_t t0 = (int64_t)blockIdx.x * TR;
+    const bool ok = stage_tile<R, NF, TR>(ts, a, t0);
+    FV<R, NF>* w = a.wb[c.par];
     Acc<R> dot[NF];
-    spmv_phase<R, NF, WCH, LoadRO>(v, c, sm, dot);
+    const int64_t row = t0 + threadIdx.x;
+    if (ok && row < a.N) {
+        const TileRow<R, NF, TR> tr{ts, a, t0};
+        const FV<R, NF> wr = row_product<U>(tr, tr.start(row), tr.end(row),
+                                            [&](int32_t col) { return ldv(a.z + col, false); });
+        const FV<R, NF> zr = ldv(a.z + row, false);
+        w[row] = wr;
+#pragma unroll
+        for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
     double blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
     if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
@@ -449,20 +454,16 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
     }
 }
 
-template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
-    constexpr int WIN = 32 * WCH;
-    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
+template <typename R, int NF, int TR, int U>
+__global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
+    __shared__ TileStage<R, NF, TR> ts;
     __shared__ double red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     const FV<R, NF>* __restrict__ r0 = a.rb[c.par];
     const FV<R, NF>* __restrict__ w0 = a.wb[c.par];
     const FV<R, NF>* __restrict__ s0 = a.sb[c.par];
-    FV<R, NF>* __restrict__ r1 = a.rb[c.par ^ 1];
-    FV<R, NF>* __restrict__ w1 = a.wb[c.par ^ 1];
-    FV<R, NF>* __restrict__ s1 = a.sb[c.par ^ 1];
-    // new residual and preconditioned residual of one unknown from its old r, w, s
+    // new s, r and u = D^-1 r of one unknown from its old r, w, s
     auto advance = [&](const FV<R, NF>& ro, const FV<R, NF>& wo, const FV<R, NF>& so, const FV<R, NF>& d,
                        FV<R, NF>& sn, FV<R, NF>& rn, FV<R, NF>& un) {
 #pragma unroll
@@ -472,87 +473,44 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
             un.v[f] = d.v[f] * rn.v[f];
         }
     };
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t N = a.N;
+    const int64_t t0 = (int64_t)blockIdx.x * TR;
+    const bool ok = stage_tile<R, NF, TR>(ts, a, t0);
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
-    for (int64_t row0 = warp * 32; row0 < N; row0 += nwarps * 32) {
-        const int64_t row = row0 + lane;
-        const int32_t rs = ldg(a.rp + (row < N ? row : N));
-        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
-        if (lane == 31) re = ldg(a.rp + (row0 + 32 < N ? row0 + 32 : N));
-        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
-        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
-        R acc[NF];
-#pragma unroll
-        for (int f = 0; f < NF; f++) acc[f] = 0;
-        for (int32_t wb = e0; wb < e1; wb += WIN) {
-            FV<R, NF> av[WCH];
-            int32_t cc[WCH];
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                const int32_t idx = wb + k * 32 + lane;
-                cc[k] = -1;
-                if (idx < e1) {
-                    av[k] = ldv(a.A + idx, false);
-                    cc[k] = ldg(a.col + idx);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                FV<R, NF> prod;
-#pragma unroll
-                for (int f = 0; f < NF; f++) prod.v[f] = 0;
-                if (cc[k] >= 0) {
-                    const int32_t col = cc[k];
-                    const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false);
-                    const FV<R, NF> d = ldv(a.dinv + col, false);
-                    FV<R, NF> so = wo;
-                    if (c.need_old) so = ldv(s0 + col, false);
-                    FV<R, NF> sn, rn, un;
-                    advance(ro, wo, so, d, sn, rn, un);
-#pragma unroll
-                    for (int f = 0; f < NF; f++) prod.v[f] = av[k].v[f] * un.v[f];
-                }
-                sm[wib][k * 32 + lane] = prod;
-            }
-            __syncwarp();
-            const int32_t lo = (rs > wb ? rs : wb) - wb;
-            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
-            for (int32_t k = lo; k < hi; k++) {
-                const FV<R, NF> t = sm[wib][k];
-#pragma unroll
-                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
-            }
-            __syncwarp();
-        }
-        if (row < N) {
-            const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
+    const int64_t row = t0 + threadIdx.x;
+    if (ok && row < a.N) {
+        const TileRow<R, NF, TR> tr{ts, a, t0};
+        const FV<R, NF> wn = row_product<U>(tr, tr.start(row), tr.end(row), [&](int32_t col) {
+            const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false), d = ldv(a.dinv + col, false);
             FV<R, NF> so = wo;
-            if (c.need_old) so = ldv(s0 + row, false);
-            FV<R, NF> x = a.x[row], p = a.pp[0][row];
-            FV<R, NF> sn, rn, un, wn;
+            if (c.need_old) so = ldv(s0 + col, false);
+            FV<R, NF> sn, rn, un;
             advance(ro, wo, so, d, sn, rn, un);
+            return un;
+        });
+        const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
+        FV<R, NF> so = wo;
+        if (c.need_old) so = ldv(s0 + row, false);
+        FV<R, NF> x = a.x[row], p = a.pp[0][row];
+        FV<R, NF> sn, rn, un;
+        advance(ro, wo, so, d, sn, rn, un);
 #pragma unroll
-            for (int f = 0; f < NF; f++) {
-                if (c.act[f]) {
-                    const R ui = d.v[f] * ro.v[f];
-                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
-                }
-                wn.v[f] = acc[f];
-                dots[f].add_prod(rn.v[f], un.v[f]);
-                dots[NF + f].add_prod(wn.v[f], un.v[f]);
-                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+        for (int f = 0; f < NF; f++) {
+            if (c.act[f]) {
+                const R ui = d.v[f] * ro.v[f];
+                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
             }
-            a.x[row] = x;
-            a.pp[0][row] = p;
-            r1[row] = rn;
-            s1[row] = sn;
-            w1[row] = wn;
+            dots[f].add_prod(rn.v[f], un.v[f]);
+            dots[NF + f].add_prod(wn.v[f], un.v[f]);
+            dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
         }
+        a.x[row] = x;
+        a.pp[0][row] = p;
+        a.rb[c.par ^ 1][row] = rn;
+        a.sb[c.par ^ 1][row] = sn;
+        a.wb[c.par ^ 1][row] = wn;
     }
+    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -850,27 +808,20 @@ cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphCondition
 
 int g_max_grid = 0;
 
-// Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
-// calculator), capped by the work and by the partial-sum stride.
-template <typename K>
-int wave_grid(K kernel, int64_t work_blocks) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    int64_t g = (int64_t)num_sms() * per_sm;
-    if (g > max_grid_blocks()) g = max_grid_blocks();
-    if (g > work_blocks) g = work_blocks;
-    return (int)(g < 1 ? 1 : g);
-}
-
 constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
-template <typename R, int NF, int WCH>
+// The tile kernels run one block per TR-row tile (no grid-stride), so their
+// grid is the tile count; the partial-sum stride covers it.
+template <int TR>
+int tile_grid(int64_t N) {
+    return (int)std::max<int64_t>(1, ceil_div(N, TR));
+}
+
+template <typename R, int NF, int TR, int U>
 struct Grids {
-    int spmv, iter, rhs, stream;
+    int tiles, rhs, stream;
     explicit Grids(int64_t N) {
-        spmv = wave_grid(k_cgcg_init<R, NF, WCH>, ceil_div(N, kBlock));
-        iter = wave_grid(k_cgcg_iter<R, NF, WCH>, ceil_div(N, kBlock));
+        tiles = tile_grid<TR>(N);
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -892,10 +843,10 @@ struct LoopArgs {
 // Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter }
 //              -> refine -> init -> WHILE(cg2) { iter } -> [post] -> stepctl }
 //              -> final_check
-template <typename R, int NF, int EQ, int WCH>
+template <typename R, int NF, int EQ, int TR, int U>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
-    const Grids<R, NF, WCH> g(base.N);
+    const Grids<R, NF, TR, U> g(base.N);
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
     G.graph = top;
@@ -907,14 +858,14 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a1);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a1);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a1);
+    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a1);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a2);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a2);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a2);
+    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a2);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -932,10 +883,10 @@ int read_flag(const int* d, cudaStream_t st) {
 // on the host: every kernel is then visible to profilers (kernels inside
 // graphs with conditional nodes are not).  Each loop is bounded by the
 // kernels' own iteration and step limits.
-template <typename R, int NF, int EQ, int WCH>
+template <typename R, int NF, int EQ, int TR, int U>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
-    const Grids<R, NF, WCH> g(base.N);
+    const Grids<R, NF, TR, U> g(base.N);
     k_start<R, NF><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_flag(&lf->step, st)) {
@@ -946,10 +897,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                 k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            k_cgcg_init<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
+            k_cgcg_init<R, NF, TR, U><<<g.tiles, TR, 0, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                k_cgcg_iter<R, NF, WCH><<<g.iter, kBlock, 0, st>>>(*la);
+                k_cgcg_iter<R, NF, TR, U><<<g.tiles, TR, 0, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -964,31 +915,32 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     FEA_CHECK_LAUNCH();
 }
 
-// SpMV variants: entries streamed per lane and window (the autotuned shape).
+// Tile shapes picked by the autotuner: variant 4 = 256-row tiles with 4
+// gathers in flight per lane, 8 = 256 rows / 8 gathers, 16 = 128 rows / 8.
 template <typename R, int NF, int EQ>
-void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags* lf, cudaStream_t st) {
-    switch (wch) {
-    case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
-    case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
-    default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
+void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int var, LoopFlags* lf, cudaStream_t st) {
+    switch (var) {
+    case 4: G ? build_graph_t<R, NF, EQ, 256, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 256, 4>(a, lf, st); break;
+    case 16: G ? build_graph_t<R, NF, EQ, 128, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 128, 8>(a, lf, st); break;
+    default: G ? build_graph_t<R, NF, EQ, 256, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 256, 8>(a, lf, st); break;
     }
 }
 
 template <typename R, int NF>
-void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
+void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf, cudaStream_t st) {
     if constexpr (NF == 1) {
         switch (kind) {
-        case EQ_HEAT: dispatch_variant<R, 1, EQ_HEAT>(G, a, wch, lf, st); break;
-        case EQ_ADV_EXPLICIT: dispatch_variant<R, 1, EQ_ADV_EXPLICIT>(G, a, wch, lf, st); break;
-        case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, wch, lf, st); break;
-        case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, wch, lf, st); break;
-        case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, wch, lf, st); break;
+        case EQ_HEAT: dispatch_variant<R, 1, EQ_HEAT>(G, a, var, lf, st); break;
+        case EQ_ADV_EXPLICIT: dispatch_variant<R, 1, EQ_ADV_EXPLICIT>(G, a, var, lf, st); break;
+        case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, var, lf, st); break;
+        case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, var, lf, st); break;
+        case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, var, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     } else {
         switch (kind) {
-        case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, wch, lf, st); break;
-        case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, wch, lf, st); break;
+        case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, var, lf, st); break;
+        case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, var, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     }
@@ -1001,25 +953,33 @@ int max_grid_blocks() {
     return g_max_grid;
 }
 
+int partial_stride(int64_t N) { return (int)std::max<int64_t>(max_grid_blocks(), tile_grid<128>(N) + 1); }
+
 template <typename R, int NF>
-void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf) {
+void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf) {
     G.destroy();
     G.kind = kind;
-    G.lanes = wch;
-    dispatch_kind<R, NF>(&G, a, kind, wch, lf, nullptr);
+    G.lanes = var;
+    dispatch_kind<R, NF>(&G, a, kind, var, lf, nullptr);
 }
 
 template <typename R, int NF>
-void run_steps_stream(const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
-    dispatch_kind<R, NF>(nullptr, a, kind, wch, lf, st);
+void run_steps_stream(const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf, cudaStream_t st) {
+    dispatch_kind<R, NF>(nullptr, a, kind, var, lf, st);
 }
 
+// One solve set-up SpMV (w = A z) on the current operator: the probe used by
+// the autotuner and by fea_time_spmv.  It only writes w, CG scratch that the
+// next solve recomputes; `scratch_flag` receives its loop condition.
 template <typename R, int NF>
-void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
-    switch (wch) {
-    case 4: k_cg_spmv<R, NF, 4><<<Grids<R, NF, 4>(a.N).spmv, kBlock, 0, st>>>(a); break;
-    case 16: k_cg_spmv<R, NF, 16><<<Grids<R, NF, 16>(a.N).spmv, kBlock, 0, st>>>(a); break;
-    default: k_cg_spmv<R, NF, 8><<<Grids<R, NF, 8>(a.N).spmv, kBlock, 0, st>>>(a); break;
+void launch_spmv_probe(const StepArgs<R, NF>& base, int var, cudaStream_t st, int* scratch_flag) {
+    StepArgs<R, NF> a = base;
+    a.use_graph = 0;
+    a.cont = scratch_flag;
+    switch (var) {
+    case 4: k_cgcg_init<R, NF, 256, 4><<<tile_grid<256>(a.N), 256, 0, st>>>(a); break;
+    case 16: k_cgcg_init<R, NF, 128, 8><<<tile_grid<128>(a.N), 128, 0, st>>>(a); break;
+    default: k_cgcg_init<R, NF, 256, 8><<<tile_grid<256>(a.N), 256, 0, st>>>(a); break;
     }
     FEA_CHECK_LAUNCH();
 }
@@ -1027,7 +987,7 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
 #define FEA_INST_STEP(R, NF)                                                                              \
     template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \
     template void run_steps_stream<R, NF>(const StepArgs<R, NF>&, int, int, LoopFlags*, cudaStream_t);    \
-    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t);
+    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t, int*);
 FEA_INST_STEP(float, 1)
 FEA_INST_STEP(float, 2)
 FEA_INST_STEP(double, 1)

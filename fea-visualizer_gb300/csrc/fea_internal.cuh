@@ -22,6 +22,9 @@ struct Pattern {
 };
 
 int launch_grid(int64_t n);
+// Row-pointer padding of the solver-order pattern: the tile staging copies
+// (largest tile: 256 rows) read up to 260 entries from a tile's first row.
+constexpr int kRowPtrPad = 512;
 // Copy of P with the unknowns renumbered (pos[u] = new index, inv = inverse);
 // emap[e'] receives the original slot of every new slot.
 void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pattern& Pc, int32_t* emap,
@@ -159,11 +162,13 @@ void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int l
 template <typename R, int NF>
 void run_steps_stream(const StepArgs<R, NF>& base, int kind, int lanes, LoopFlags* lf, cudaStream_t st);
 
-// One SpMV + dot launch with the given lanes per row (autotuning probe).
+// One solve set-up SpMV (w = A z) with the given tile variant: the
+// autotuning and timing probe.  scratch_flag receives its loop condition.
 template <typename R, int NF>
-void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
+void launch_spmv_probe(const StepArgs<R, NF>& a, int var, cudaStream_t st, int* scratch_flag);
 
-// FP64-accurate true residual |b - A x| / |b| of the current solve (status).
 int max_grid_blocks();
+// Stride of the per-block partial sums for N unknowns (covers every grid).
+int partial_stride(int64_t N);
 
 }  // namespace fea
