@@ -204,74 +204,78 @@ struct PhaseCtl {
 
 // ---- TMA-staged row tiles --------------------------------------------------------------
 //
-// A block owns TR consecutive rows (32 per warp, one per lane).  Thread 0
-// stages the tile's row pointers, matrix values and column indices into
-// shared memory with three bulk copies (TMA) completing on one mbarrier; the
-// lanes then sum their own rows in column order from shared memory, so the
-// only global accesses left per entry are the gathers of vector values.  The
-// staged range is rounded out to multiples of 4 entries (16 bytes); the
-// arrays carry 4 entries of padding for that.  A tile with more than CAP
-// entries (a vertex of very high valence) is read from global memory instead.
-
-constexpr int kTileCap = 2560;  // staged entries per tile (10 per row for 256 rows)
+// The matrix is processed in tiles of TR consecutive rows (one row per
+// thread).  Blocks are persistent: block b takes tiles b, b + G, b + 2G, ...
+// (G = grid size) and double-buffers them in shared memory.  Thread 0 arms a
+// stage with three bulk copies (TMA: the tile's row pointers, values and
+// column indices) completing on the stage's mbarrier, two tiles ahead of the
+// tile being computed, so the copies overlap the gathers of the current tile.
+// Lanes sum their own rows in column order from shared memory; the only
+// per-entry global accesses left are the gathers of vector values.  Staged
+// ranges are rounded out to multiples of 4 entries (16 bytes) and the arrays
+// carry that padding; a tile with more than CAP entries (very high valence)
+// is read from global memory instead.  Every wait is bounded.
 
 template <typename R, int NF, int TR>
 struct TileStage {
+    static constexpr int CAP = TR * 9;  // 9 stored entries per row on average
     static_assert(TR + 4 <= kRowPtrPad, "row pointer padding covers a whole tile");
     alignas(16) int32_t rp[TR + 4];
-    alignas(16) FV<R, NF> A[kTileCap];
-    alignas(16) int32_t col[kTileCap];
+    alignas(16) FV<R, NF> A[CAP];
+    alignas(16) int32_t col[CAP];
     alignas(8) uint64_t bar;
-    int32_t e0;   // first staged entry
-    int use;      // 1: staged in shared memory
+    int64_t t0;       // first row of the staged tile
+    int32_t e0;       // first staged entry
+    int use;          // 1: staged in shared memory, 0: read from global memory
+    uint32_t parity;  // parity of the armed phase
+    uint32_t arms;    // phases armed so far
+    int pending;      // armed and not yet consumed
 };
 
-// Stage the tile that starts at row t0.  Returns false (with nothing to
-// compute) when a wait ran out; the caller then raises an error flag.
+constexpr int kStages = 2;
+
 template <typename R, int NF, int TR>
-__device__ bool stage_tile(TileStage<R, NF, TR>& ts, const StepArgs<R, NF>& a, int64_t t0) {
-    if (threadIdx.x == 0) {
-        const int64_t N = a.N;
-        const int32_t E0 = a.rp[t0], E1 = a.rp[t0 + TR < N ? t0 + TR : N];
-        const int32_t e0 = E0 & ~3, e1 = (E1 + 3) & ~3;
-        ts.e0 = e0;
-        ts.use = 0;
-        if (e1 - e0 <= kTileCap) {
-            ts.use = 1;
-            mbar_init(&ts.bar, 1);
-            mbar_fence_init();
-            const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
-            const uint32_t nC = (uint32_t)(e1 - e0) * 4u;
-            const uint32_t nR = (uint32_t)sizeof(ts.rp);
-            mbar_arrive_expect_tx(&ts.bar, nR + nA + nC);
-            bulk_g2s(ts.rp, a.rp + t0, nR, &ts.bar);
-            if (nA) {
-                bulk_g2s(ts.A, a.A + e0, nA, &ts.bar);
-                bulk_g2s(ts.col, a.col + e0, nC, &ts.bar);
-            }
-        }
+struct TilePipe {
+    TileStage<R, NF, TR> st[kStages];
+};
+
+// Thread 0: stage tile `tile` into ts (or mark it for global reads).
+template <typename R, int NF, int TR>
+__device__ void arm_tile(TileStage<R, NF, TR>& ts, const StepArgs<R, NF>& a, int64_t tile) {
+    const int64_t N = a.N, t0 = tile * TR;
+    const int32_t E0 = a.rp[t0], E1 = a.rp[t0 + TR < N ? t0 + TR : N];
+    const int32_t e0 = E0 & ~3, e1 = (E1 + 3) & ~3;
+    ts.t0 = t0;
+    ts.e0 = e0;
+    ts.use = 0;
+    if (e1 - e0 > TileStage<R, NF, TR>::CAP) return;
+    ts.use = 1;
+    ts.parity = ts.arms & 1u;
+    ts.arms += 1;
+    ts.pending = 1;
+    // order the block's earlier reads of this buffer before the copy engine's writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
+    const uint32_t nC = (uint32_t)(e1 - e0) * 4u;
+    const uint32_t nR = (uint32_t)sizeof(ts.rp);
+    mbar_arrive_expect_tx(&ts.bar, nR + nA + nC);
+    bulk_g2s(ts.rp, a.rp + t0, nR, &ts.bar);
+    if (nA) {
+        bulk_g2s(ts.A, a.A + e0, nA, &ts.bar);
+        bulk_g2s(ts.col, a.col + e0, nC, &ts.bar);
     }
-    __syncthreads();
-    bool ok = true;
-    if (ts.use) ok = mbar_wait(&ts.bar, 0);
-    if (__syncthreads_and(ok)) return true;
-    // a copy did not complete in time: wait (bounded) once more so that no copy
-    // into this block's shared memory is left in flight when it exits
-    if (ts.use) mbar_wait(&ts.bar, 0);
-    return false;
 }
 
-// Row extent and staged-entry accessors for lane row `row` of the tile.
+// Row extent and staged-entry accessors for the tile in ts.
 template <typename R, int NF, int TR>
 struct TileRow {
     const TileStage<R, NF, TR>& ts;
     const StepArgs<R, NF>& a;
-    int64_t t0;
     __device__ __forceinline__ int32_t start(int64_t row) const {
-        return ts.use ? ts.rp[row - t0] : ldg(a.rp + row);
+        return ts.use ? ts.rp[row - ts.t0] : ldg(a.rp + row);
     }
     __device__ __forceinline__ int32_t end(int64_t row) const {
-        return ts.use ? ts.rp[row - t0 + 1] : ldg(a.rp + row + 1);
+        return ts.use ? ts.rp[row - ts.t0 + 1] : ldg(a.rp + row + 1);
     }
     __device__ __forceinline__ FV<R, NF> val(int32_t e) const {
         return ts.use ? ts.A[e - ts.e0] : ldv(a.A + e, false);
@@ -280,6 +284,53 @@ struct TileRow {
         return ts.use ? ts.col[e - ts.e0] : ldg(a.col + e);
     }
 };
+
+// Runs row_fn(TileRow, row) for every row of the block's tiles.  Returns false
+// when a wait ran out (the caller raises an error flag); no copy into the
+// block's shared memory is left in flight when it returns.
+template <typename R, int NF, int TR, typename RowFn>
+__device__ bool tile_loop(TilePipe<R, NF, TR>& tp, const StepArgs<R, NF>& a, RowFn row_fn) {
+    const int64_t N = a.N, ntiles = ceil_div(N, TR), G = gridDim.x;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&tp.st[s].bar, 1);
+            tp.st[s].arms = 0;
+            tp.st[s].pending = 0;
+            tp.st[s].use = 0;
+        }
+        mbar_fence_init();
+        for (int s = 0; s < kStages; s++) {
+            const int64_t tile = blockIdx.x + (int64_t)s * G;
+            if (tile < ntiles) arm_tile(tp.st[s], a, tile);
+        }
+    }
+    __syncthreads();
+    bool ok_all = true;
+    for (int64_t k = 0;; k++) {
+        const int64_t tile = blockIdx.x + k * G;
+        if (tile >= ntiles) break;
+        TileStage<R, NF, TR>& ts = tp.st[k % kStages];
+        bool ok = true;
+        if (ts.use) ok = mbar_wait(&ts.bar, ts.parity);
+        if (!__syncthreads_and(ok)) {
+            ok_all = false;
+            break;
+        }
+        const int64_t row = tile * TR + threadIdx.x;
+        if (row < N) row_fn(TileRow<R, NF, TR>{ts, a}, row);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            ts.pending = 0;
+            const int64_t next = tile + (int64_t)kStages * G;
+            if (next < ntiles) arm_tile(ts, a, next);
+        }
+    }
+    if (!ok_all && threadIdx.x == 0)
+        for (int s = 0; s < kStages; s++)
+            if (tp.st[s].pending && tp.st[s].use) mbar_wait(&tp.st[s].bar, tp.st[s].parity);
+    __syncthreads();
+    return ok_all;
+}
 
 // Sum over the entries of one row of A_e * g(col_e), U entries in flight.
 template <int U, typename R, int NF, int TR, typename G>
@@ -420,24 +471,21 @@ __device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, doub
 // z.w0 and alpha0 = r0.z / delta0.  Also the SpMV timing probe.
 template <typename R, int NF, int TR, int U>
 __global__ void __launch_bounds__(TR) k_cgcg_init(StepArgs<R, NF> a) {
-    __shared__ TileStage<R, NF, TR> ts;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    TilePipe<R, NF, TR>& tp = *reinterpret_cast<TilePipe<R, NF, TR>*>(dyn_smem);
     __shared__ double red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
-    const int64_t t0 = (int64_t)blockIdx.x * TR;
-    const bool ok = stage_tile<R, NF, TR>(ts, a, t0);
     FV<R, NF>* w = a.wb[c.par];
     Acc<R> dot[NF];
-    const int64_t row = t0 + threadIdx.x;
-    if (ok && row < a.N) {
-        const TileRow<R, NF, TR> tr{ts, a, t0};
+    const bool ok = tile_loop<R, NF, TR>(tp, a, [&](const TileRow<R, NF, TR>& tr, int64_t row) {
         const FV<R, NF> wr = row_product<U>(tr, tr.start(row), tr.end(row),
                                             [&](int32_t col) { return ldv(a.z + col, false); });
         const FV<R, NF> zr = ldv(a.z + row, false);
         w[row] = wr;
 #pragma unroll
         for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
-    }
+    });
     if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
     double blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
@@ -456,7 +504,8 @@ __global__ void __launch_bounds__(TR) k_cgcg_init(StepArgs<R, NF> a) {
 
 template <typename R, int NF, int TR, int U>
 __global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
-    __shared__ TileStage<R, NF, TR> ts;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    TilePipe<R, NF, TR>& tp = *reinterpret_cast<TilePipe<R, NF, TR>*>(dyn_smem);
     __shared__ double red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
@@ -473,12 +522,8 @@ __global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
             un.v[f] = d.v[f] * rn.v[f];
         }
     };
-    const int64_t t0 = (int64_t)blockIdx.x * TR;
-    const bool ok = stage_tile<R, NF, TR>(ts, a, t0);
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
-    const int64_t row = t0 + threadIdx.x;
-    if (ok && row < a.N) {
-        const TileRow<R, NF, TR> tr{ts, a, t0};
+    const bool ok = tile_loop<R, NF, TR>(tp, a, [&](const TileRow<R, NF, TR>& tr, int64_t row) {
         const FV<R, NF> wn = row_product<U>(tr, tr.start(row), tr.end(row), [&](int32_t col) {
             const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false), d = ldv(a.dinv + col, false);
             FV<R, NF> so = wo;
@@ -509,7 +554,7 @@ __global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
         a.rb[c.par ^ 1][row] = rn;
         a.sb[c.par ^ 1][row] = sn;
         a.wb[c.par ^ 1][row] = wn;
-    }
+    });
     if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
@@ -780,14 +825,14 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
 
 template <typename... P>
 cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
-                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
+                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg, size_t smem = 0) {
     auto local = arg;
     void* argv[] = {(void*)&local};
     cudaKernelNodeParams kp = {};
     kp.func = (void*)fn;
     kp.gridDim = dim3((unsigned)grid);
     kp.blockDim = dim3((unsigned)block);
-    kp.sharedMemBytes = 0;
+    kp.sharedMemBytes = (unsigned)smem;
     kp.kernelParams = argv;
     cudaGraphNode_t n;
     FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
@@ -810,18 +855,34 @@ int g_max_grid = 0;
 
 constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
-// The tile kernels run one block per TR-row tile (no grid-stride), so their
-// grid is the tile count; the partial-sum stride covers it.
+// The tile kernels are persistent: one wave of resident blocks (SMs x blocks
+// per SM from the occupancy calculator), at most one block per tile.
 template <int TR>
-int tile_grid(int64_t N) {
+int tile_count(int64_t N) {
     return (int)std::max<int64_t>(1, ceil_div(N, TR));
+}
+
+// The staging buffers are dynamic shared memory (above the 48 KB default, so
+// each kernel opts in once).
+template <int TR, typename K>
+int tile_grid(K kernel, size_t smem, int64_t N) {
+    FEA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    FEA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TR, smem));
+    if (per_sm < 1) {
+        set_error("tile kernel (%d threads, %zu bytes of shared memory) does not fit on an SM", TR, smem);
+        throw Error{FEA_ERR_CUDA};
+    }
+    return (int)std::min<int64_t>((int64_t)num_sms() * per_sm, tile_count<TR>(N));
 }
 
 template <typename R, int NF, int TR, int U>
 struct Grids {
+    static constexpr size_t smem = sizeof(TilePipe<R, NF, TR>);
     int tiles, rhs, stream;
     explicit Grids(int64_t N) {
-        tiles = tile_grid<TR>(N);
+        tiles = std::min(tile_grid<TR>(k_cgcg_iter<R, NF, TR, U>, smem, N),
+                         tile_grid<TR>(k_cgcg_init<R, NF, TR, U>, smem, N));
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -858,14 +919,14 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a1);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a1, g.smem);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a1);
+    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a1, g.smem);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a2);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a2, g.smem);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a2);
+    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a2, g.smem);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -897,10 +958,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                 k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            k_cgcg_init<R, NF, TR, U><<<g.tiles, TR, 0, st>>>(*la);
+            k_cgcg_init<R, NF, TR, U><<<g.tiles, TR, g.smem, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                k_cgcg_iter<R, NF, TR, U><<<g.tiles, TR, 0, st>>>(*la);
+                k_cgcg_iter<R, NF, TR, U><<<g.tiles, TR, g.smem, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -953,7 +1014,7 @@ int max_grid_blocks() {
     return g_max_grid;
 }
 
-int partial_stride(int64_t N) { return (int)std::max<int64_t>(max_grid_blocks(), tile_grid<128>(N) + 1); }
+int partial_stride(int64_t N) { return (int)std::max<int64_t>(max_grid_blocks(), tile_count<128>(N) + 1); }
 
 template <typename R, int NF>
 void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf) {
@@ -977,9 +1038,18 @@ void launch_spmv_probe(const StepArgs<R, NF>& base, int var, cudaStream_t st, in
     a.use_graph = 0;
     a.cont = scratch_flag;
     switch (var) {
-    case 4: k_cgcg_init<R, NF, 256, 4><<<tile_grid<256>(a.N), 256, 0, st>>>(a); break;
-    case 16: k_cgcg_init<R, NF, 128, 8><<<tile_grid<128>(a.N), 128, 0, st>>>(a); break;
-    default: k_cgcg_init<R, NF, 256, 8><<<tile_grid<256>(a.N), 256, 0, st>>>(a); break;
+    case 4: {
+        const Grids<R, NF, 256, 4> g(a.N);
+        k_cgcg_init<R, NF, 256, 4><<<g.tiles, 256, g.smem, st>>>(a);
+    } break;
+    case 16: {
+        const Grids<R, NF, 128, 8> g(a.N);
+        k_cgcg_init<R, NF, 128, 8><<<g.tiles, 128, g.smem, st>>>(a);
+    } break;
+    default: {
+        const Grids<R, NF, 256, 8> g(a.N);
+        k_cgcg_init<R, NF, 256, 8><<<g.tiles, 256, g.smem, st>>>(a);
+    } break;
     }
     FEA_CHECK_LAUNCH();
 }

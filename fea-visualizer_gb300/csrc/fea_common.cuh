@@ -41,7 +41,7 @@ inline int fail(int code, const char* msg) {
 constexpr int kBlock = 256;        // threads per block of the streaming kernels
 constexpr int kMaxFields = 2;      // Gray-Scott solves u and v together
 
-inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 int num_sms();
 
