@@ -19,7 +19,6 @@
 #include <cmath>
 
 #include "fea_internal.cuh"
-#include "tma.cuh"
 
 namespace fea {
 
@@ -171,10 +170,17 @@ struct RowMap {
     }
 };
 
-// ---- CG building blocks -----------------------------------------------------------
+// ---- CSR SpMV building blocks ------------------------------------------------------
 //
 // Every kernel reads vectors that earlier launches wrote, so the read-only
-// cache path is valid for all of them.
+// path (LoadRO) is valid for all of them.
+
+struct LoadRO {
+    template <typename T>
+    static __device__ __forceinline__ T ld(const T* p) {
+        return ldv<T>(p, false);
+    }
+};
 
 // Control values of one phase, read once per phase by every thread.
 template <typename R, int NF>
@@ -202,164 +208,90 @@ struct PhaseCtl {
     }
 };
 
-// ---- TMA-staged row tiles --------------------------------------------------------------
+// q = A p_new with p_new = z + beta p_old computed for every gathered column
+// (the direction update of the previous iteration, fused; the two p buffers
+// alternate with the iteration parity), plus p_new.q into dot[].
 //
-// The matrix is processed in tiles of TR consecutive rows (one row per
-// thread).  Blocks are persistent: block b takes tiles b, b + G, b + 2G, ...
-// (G = grid size) and double-buffers them in shared memory.  Thread 0 arms a
-// stage with three bulk copies (TMA: the tile's row pointers, values and
-// column indices) completing on the stage's mbarrier, two tiles ahead of the
-// tile being computed, so the copies overlap the gathers of the current tile.
-// Lanes sum their own rows in column order from shared memory; the only
-// per-entry global accesses left are the gathers of vector values.  Staged
-// ranges are rounded out to multiples of 4 entries (16 bytes) and the arrays
-// carry that padding; a tile with more than CAP entries (very high valence)
-// is read from global memory instead.  Every wait is bounded.
-
-template <typename R, int NF, int TR>
-struct TileStage {
-    static constexpr int CAP = TR * 9;  // 9 stored entries per row on average
-    static_assert(TR + 4 <= kRowPtrPad, "row pointer padding covers a whole tile");
-    alignas(16) int32_t rp[TR + 4];
-    alignas(16) FV<R, NF> A[CAP];
-    alignas(16) int32_t col[CAP];
-    alignas(8) uint64_t bar;
-    int64_t t0;       // first row of the staged tile
-    int32_t e0;       // first staged entry
-    int use;          // 1: staged in shared memory, 0: read from global memory
-    uint32_t parity;  // parity of the armed phase
-    uint32_t arms;    // phases armed so far
-    int pending;      // armed and not yet consumed
-};
-
-constexpr int kStages = 2;
-
-template <typename R, int NF, int TR>
-struct TilePipe {
-    TileStage<R, NF, TR> st[kStages];
-};
-
-// Thread 0: stage tile `tile` into ts (or mark it for global reads).
-template <typename R, int NF, int TR>
-__device__ void arm_tile(TileStage<R, NF, TR>& ts, const StepArgs<R, NF>& a, int64_t tile) {
-    const int64_t N = a.N, t0 = tile * TR;
-    const int32_t E0 = a.rp[t0], E1 = a.rp[t0 + TR < N ? t0 + TR : N];
-    const int32_t e0 = E0 & ~3, e1 = (E1 + 3) & ~3;
-    ts.t0 = t0;
-    ts.e0 = e0;
-    ts.use = 0;
-    if (e1 - e0 > TileStage<R, NF, TR>::CAP) return;
-    ts.use = 1;
-    ts.parity = ts.arms & 1u;
-    ts.arms += 1;
-    ts.pending = 1;
-    // order the block's earlier reads of this buffer before the copy engine's writes
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
-    const uint32_t nC = (uint32_t)(e1 - e0) * 4u;
-    const uint32_t nR = (uint32_t)sizeof(ts.rp);
-    mbar_arrive_expect_tx(&ts.bar, nR + nA + nC);
-    bulk_g2s(ts.rp, a.rp + t0, nR, &ts.bar);
-    if (nA) {
-        bulk_g2s(ts.A, a.A + e0, nA, &ts.bar);
-        bulk_g2s(ts.col, a.col + e0, nC, &ts.bar);
-    }
-}
-
-// Row extent and staged-entry accessors for the tile in ts.
-template <typename R, int NF, int TR>
-struct TileRow {
-    const TileStage<R, NF, TR>& ts;
-    const StepArgs<R, NF>& a;
-    __device__ __forceinline__ int32_t start(int64_t row) const {
-        return ts.use ? ts.rp[row - ts.t0] : ldg(a.rp + row);
-    }
-    __device__ __forceinline__ int32_t end(int64_t row) const {
-        return ts.use ? ts.rp[row - ts.t0 + 1] : ldg(a.rp + row + 1);
-    }
-    __device__ __forceinline__ FV<R, NF> val(int32_t e) const {
-        return ts.use ? ts.A[e - ts.e0] : ldv(a.A + e, false);
-    }
-    __device__ __forceinline__ int32_t col(int32_t e) const {
-        return ts.use ? ts.col[e - ts.e0] : ldg(a.col + e);
-    }
-};
-
-// Runs row_fn(TileRow, row) for every row of the block's tiles.  Returns false
-// when a wait ran out (the caller raises an error flag); no copy into the
-// block's shared memory is left in flight when it returns.
-template <typename R, int NF, int TR, typename RowFn>
-__device__ bool tile_loop(TilePipe<R, NF, TR>& tp, const StepArgs<R, NF>& a, RowFn row_fn) {
-    const int64_t N = a.N, ntiles = ceil_div(N, TR), G = gridDim.x;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
-            mbar_init(&tp.st[s].bar, 1);
-            tp.st[s].arms = 0;
-            tp.st[s].pending = 0;
-            tp.st[s].use = 0;
-        }
-        mbar_fence_init();
-        for (int s = 0; s < kStages; s++) {
-            const int64_t tile = blockIdx.x + (int64_t)s * G;
-            if (tile < ntiles) arm_tile(tp.st[s], a, tile);
-        }
-    }
-    __syncthreads();
-    bool ok_all = true;
-    for (int64_t k = 0;; k++) {
-        const int64_t tile = blockIdx.x + k * G;
-        if (tile >= ntiles) break;
-        TileStage<R, NF, TR>& ts = tp.st[k % kStages];
-        bool ok = true;
-        if (ts.use) ok = mbar_wait(&ts.bar, ts.parity);
-        if (!__syncthreads_and(ok)) {
-            ok_all = false;
-            break;
-        }
-        const int64_t row = tile * TR + threadIdx.x;
-        if (row < N) row_fn(TileRow<R, NF, TR>{ts, a}, row);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            ts.pending = 0;
-            const int64_t next = tile + (int64_t)kStages * G;
-            if (next < ntiles) arm_tile(ts, a, next);
-        }
-    }
-    if (!ok_all && threadIdx.x == 0)
-        for (int s = 0; s < kStages; s++)
-            if (tp.st[s].pending && tp.st[s].use) mbar_wait(&tp.st[s].bar, tp.st[s].parity);
-    __syncthreads();
-    return ok_all;
-}
-
-// Sum over the entries of one row of A_e * g(col_e), U entries in flight.
-template <int U, typename R, int NF, int TR, typename G>
-__device__ __forceinline__ FV<R, NF> row_product(const TileRow<R, NF, TR>& tr, int32_t rs, int32_t re, G g) {
-    FV<R, NF> acc;
+// Warp-cooperative CSR: a warp owns 32 consecutive rows, whose stored entries
+// form one contiguous range.  The warp streams that range in windows of
+// 32*WCH entries: every lane issues WCH coalesced value/column loads, then WCH
+// independent gathers, so each round trip to memory carries a whole window
+// rather than one row.  Products go to shared memory and each lane sums its
+// own row in column order.
+template <typename R, int NF, int WCH, typename LP>
+__device__ __forceinline__ void spmv_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
+                                           FV<R, NF> (*sm)[32 * WCH], Acc<R> (&dot)[NF]) {
+    constexpr int WIN = 32 * WCH;
+    const FV<R, NF>* pold = a.pp[c.par];
+    FV<R, NF>* pnew = a.pp[c.par ^ 1];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t N = a.N;
+    for (int64_t r0 = warp * 32; r0 < N; r0 += nwarps * 32) {
+        const int64_t row = r0 + lane;
+        const int32_t rs = ldg(a.rp + (row < N ? row : N));
+        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+        if (lane == 31) re = ldg(a.rp + (r0 + 32 < N ? r0 + 32 : N));
+        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
+        R acc[NF];
 #pragma unroll
-    for (int f = 0; f < NF; f++) acc.v[f] = 0;
-    for (int32_t e = rs; e < re; e += U) {
-        FV<R, NF> av[U];
-        int32_t cc[U];
+        for (int f = 0; f < NF; f++) acc[f] = 0;
+        for (int32_t wb = e0; wb < e1; wb += WIN) {
+            FV<R, NF> av[WCH];
+            int32_t cc[WCH];
 #pragma unroll
-        for (int k = 0; k < U; k++) {
-            cc[k] = -1;
-            if (e + k < re) {
-                av[k] = tr.val(e + k);
-                cc[k] = tr.col(e + k);
+            for (int k = 0; k < WCH; k++) {
+                const int32_t idx = wb + k * 32 + lane;
+                cc[k] = -1;
+                if (idx < e1) {
+                    av[k] = ldv(a.A + idx, false);
+                    cc[k] = ldg(a.col + idx);
+                }
             }
+#pragma unroll
+            for (int k = 0; k < WCH; k++) {
+                FV<R, NF> prod;
+#pragma unroll
+                for (int f = 0; f < NF; f++) prod.v[f] = 0;
+                if (cc[k] >= 0) {
+                    const FV<R, NF> zc = LP::ld(a.z + cc[k]);
+                    FV<R, NF> pc = zc;
+                    if (c.need_old) pc = LP::ld(pold + cc[k]);
+#pragma unroll
+                    for (int f = 0; f < NF; f++) {
+                        const R pn = c.fresh[f] ? zc.v[f] : fma(c.beta[f], pc.v[f], zc.v[f]);
+                        prod.v[f] = av[k].v[f] * pn;
+                    }
+                }
+                sm[wib][k * 32 + lane] = prod;
+            }
+            __syncwarp();
+            const int32_t lo = (rs > wb ? rs : wb) - wb;
+            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
+            for (int32_t k = lo; k < hi; k++) {
+                const FV<R, NF> t = sm[wib][k];
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
+            }
+            __syncwarp();
         }
-        FV<R, NF> gv[U];
+        if (row < N) {
+            const FV<R, NF> zr = LP::ld(a.z + row);
+            FV<R, NF> pr = zr, qv;
+            if (c.need_old) pr = LP::ld(pold + row);
 #pragma unroll
-        for (int k = 0; k < U; k++)
-            if (cc[k] >= 0) gv[k] = g(cc[k]);
-#pragma unroll
-        for (int k = 0; k < U; k++)
-            if (cc[k] >= 0)
-#pragma unroll
-                for (int f = 0; f < NF; f++) acc.v[f] = fma(av[k].v[f], gv[k].v[f], acc.v[f]);
+            for (int f = 0; f < NF; f++) {
+                const R pn = c.fresh[f] ? zr.v[f] : fma(c.beta[f], pr.v[f], zr.v[f]);
+                pr.v[f] = pn;
+                qv.v[f] = acc[f];
+                dot[f].add_prod(pn, acc[f]);
+            }
+            pnew[row] = pr;
+            a.q[row] = qv;
+        }
     }
-    return acc;
 }
 
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
@@ -455,6 +387,22 @@ __device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, doub
     __syncthreads();
 }
 
+// ---- standalone kernels (autotuning and timing probes) -------------------------------
+
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    Acc<R> dot[NF];
+    spmv_phase<R, NF, WCH, LoadRO>(a, c, sm, dot);
+    double blk[NF], tot[NF];
+    block_totals<NF>(dot, red, blk);
+    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0)
+        finish_spmv<R, NF>(a.cg, a.run, c.act, tot);
+}
+
 // ---- Chronopoulos-Gear iteration -----------------------------------------------------
 //
 // Jacobi-preconditioned CG rearranged (Chronopoulos & Gear, 1989) so that one
@@ -468,25 +416,24 @@ __device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, doub
 // w and s there (so r, w and s alternate between two buffers).
 
 // Set-up of a solve: w0 = A z (z = D^-1 r0 from k_rhs / k_refine), delta0 =
-// z.w0 and alpha0 = r0.z / delta0.  Also the SpMV timing probe.
-template <typename R, int NF, int TR, int U>
-__global__ void __launch_bounds__(TR) k_cgcg_init(StepArgs<R, NF> a) {
-    extern __shared__ __align__(16) unsigned char dyn_smem[];
-    TilePipe<R, NF, TR>& tp = *reinterpret_cast<TilePipe<R, NF, TR>*>(dyn_smem);
+// z.w0 and alpha0 = r0.z / delta0.  The SpMV of the probe kernel with p = z.
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ double red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
-    FV<R, NF>* w = a.wb[c.par];
-    Acc<R> dot[NF];
-    const bool ok = tile_loop<R, NF, TR>(tp, a, [&](const TileRow<R, NF, TR>& tr, int64_t row) {
-        const FV<R, NF> wr = row_product<U>(tr, tr.start(row), tr.end(row),
-                                            [&](int32_t col) { return ldv(a.z + col, false); });
-        const FV<R, NF> zr = ldv(a.z + row, false);
-        w[row] = wr;
+    c.need_old = false;
 #pragma unroll
-        for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
-    });
-    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+    for (int f = 0; f < NF; f++) {
+        c.fresh[f] = true;
+        c.beta[f] = 0;
+    }
+    StepArgs<R, NF> v = a;
+    v.pp[c.par ^ 1] = a.pp[0];
+    v.q = a.wb[c.par];
+    Acc<R> dot[NF];
+    spmv_phase<R, NF, WCH, LoadRO>(v, c, sm, dot);
     double blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
     if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
@@ -502,17 +449,20 @@ __global__ void __launch_bounds__(TR) k_cgcg_init(StepArgs<R, NF> a) {
     }
 }
 
-template <typename R, int NF, int TR, int U>
-__global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
-    extern __shared__ __align__(16) unsigned char dyn_smem[];
-    TilePipe<R, NF, TR>& tp = *reinterpret_cast<TilePipe<R, NF, TR>*>(dyn_smem);
+template <typename R, int NF, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
+    constexpr int WIN = 32 * WCH;
+    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
     __shared__ double red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     const FV<R, NF>* __restrict__ r0 = a.rb[c.par];
     const FV<R, NF>* __restrict__ w0 = a.wb[c.par];
     const FV<R, NF>* __restrict__ s0 = a.sb[c.par];
-    // new s, r and u = D^-1 r of one unknown from its old r, w, s
+    FV<R, NF>* __restrict__ r1 = a.rb[c.par ^ 1];
+    FV<R, NF>* __restrict__ w1 = a.wb[c.par ^ 1];
+    FV<R, NF>* __restrict__ s1 = a.sb[c.par ^ 1];
+    // new residual and preconditioned residual of one unknown from its old r, w, s
     auto advance = [&](const FV<R, NF>& ro, const FV<R, NF>& wo, const FV<R, NF>& so, const FV<R, NF>& d,
                        FV<R, NF>& sn, FV<R, NF>& rn, FV<R, NF>& un) {
 #pragma unroll
@@ -522,40 +472,87 @@ __global__ void __launch_bounds__(TR) k_cgcg_iter(StepArgs<R, NF> a) {
             un.v[f] = d.v[f] * rn.v[f];
         }
     };
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t N = a.N;
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
-    const bool ok = tile_loop<R, NF, TR>(tp, a, [&](const TileRow<R, NF, TR>& tr, int64_t row) {
-        const FV<R, NF> wn = row_product<U>(tr, tr.start(row), tr.end(row), [&](int32_t col) {
-            const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false), d = ldv(a.dinv + col, false);
-            FV<R, NF> so = wo;
-            if (c.need_old) so = ldv(s0 + col, false);
-            FV<R, NF> sn, rn, un;
-            advance(ro, wo, so, d, sn, rn, un);
-            return un;
-        });
-        const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
-        FV<R, NF> so = wo;
-        if (c.need_old) so = ldv(s0 + row, false);
-        FV<R, NF> x = a.x[row], p = a.pp[0][row];
-        FV<R, NF> sn, rn, un;
-        advance(ro, wo, so, d, sn, rn, un);
+    for (int64_t row0 = warp * 32; row0 < N; row0 += nwarps * 32) {
+        const int64_t row = row0 + lane;
+        const int32_t rs = ldg(a.rp + (row < N ? row : N));
+        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+        if (lane == 31) re = ldg(a.rp + (row0 + 32 < N ? row0 + 32 : N));
+        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
+        R acc[NF];
 #pragma unroll
-        for (int f = 0; f < NF; f++) {
-            if (c.act[f]) {
-                const R ui = d.v[f] * ro.v[f];
-                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+        for (int f = 0; f < NF; f++) acc[f] = 0;
+        for (int32_t wb = e0; wb < e1; wb += WIN) {
+            FV<R, NF> av[WCH];
+            int32_t cc[WCH];
+#pragma unroll
+            for (int k = 0; k < WCH; k++) {
+                const int32_t idx = wb + k * 32 + lane;
+                cc[k] = -1;
+                if (idx < e1) {
+                    av[k] = ldv(a.A + idx, false);
+                    cc[k] = ldg(a.col + idx);
+                }
             }
-            dots[f].add_prod(rn.v[f], un.v[f]);
-            dots[NF + f].add_prod(wn.v[f], un.v[f]);
-            dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+#pragma unroll
+            for (int k = 0; k < WCH; k++) {
+                FV<R, NF> prod;
+#pragma unroll
+                for (int f = 0; f < NF; f++) prod.v[f] = 0;
+                if (cc[k] >= 0) {
+                    const int32_t col = cc[k];
+                    const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false);
+                    const FV<R, NF> d = ldv(a.dinv + col, false);
+                    FV<R, NF> so = wo;
+                    if (c.need_old) so = ldv(s0 + col, false);
+                    FV<R, NF> sn, rn, un;
+                    advance(ro, wo, so, d, sn, rn, un);
+#pragma unroll
+                    for (int f = 0; f < NF; f++) prod.v[f] = av[k].v[f] * un.v[f];
+                }
+                sm[wib][k * 32 + lane] = prod;
+            }
+            __syncwarp();
+            const int32_t lo = (rs > wb ? rs : wb) - wb;
+            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
+            for (int32_t k = lo; k < hi; k++) {
+                const FV<R, NF> t = sm[wib][k];
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
+            }
+            __syncwarp();
         }
-        a.x[row] = x;
-        a.pp[0][row] = p;
-        a.rb[c.par ^ 1][row] = rn;
-        a.sb[c.par ^ 1][row] = sn;
-        a.wb[c.par ^ 1][row] = wn;
-    });
-    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+        if (row < N) {
+            const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
+            FV<R, NF> so = wo;
+            if (c.need_old) so = ldv(s0 + row, false);
+            FV<R, NF> x = a.x[row], p = a.pp[0][row];
+            FV<R, NF> sn, rn, un, wn;
+            advance(ro, wo, so, d, sn, rn, un);
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (c.act[f]) {
+                    const R ui = d.v[f] * ro.v[f];
+                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                }
+                wn.v[f] = acc[f];
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[NF + f].add_prod(wn.v[f], un.v[f]);
+                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            a.x[row] = x;
+            a.pp[0][row] = p;
+            r1[row] = rn;
+            s1[row] = sn;
+            w1[row] = wn;
+        }
+    }
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -825,14 +822,14 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
 
 template <typename... P>
 cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
-                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg, size_t smem = 0) {
+                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
     auto local = arg;
     void* argv[] = {(void*)&local};
     cudaKernelNodeParams kp = {};
     kp.func = (void*)fn;
     kp.gridDim = dim3((unsigned)grid);
     kp.blockDim = dim3((unsigned)block);
-    kp.sharedMemBytes = (unsigned)smem;
+    kp.sharedMemBytes = 0;
     kp.kernelParams = argv;
     cudaGraphNode_t n;
     FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
@@ -853,36 +850,27 @@ cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphCondition
 
 int g_max_grid = 0;
 
+// Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
+// calculator), capped by the work and by the partial-sum stride.
+template <typename K>
+int wave_grid(K kernel, int64_t work_blocks) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t g = (int64_t)num_sms() * per_sm;
+    if (g > max_grid_blocks()) g = max_grid_blocks();
+    if (g > work_blocks) g = work_blocks;
+    return (int)(g < 1 ? 1 : g);
+}
+
 constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
-// The tile kernels are persistent: one wave of resident blocks (SMs x blocks
-// per SM from the occupancy calculator), at most one block per tile.
-template <int TR>
-int tile_count(int64_t N) {
-    return (int)std::max<int64_t>(1, ceil_div(N, TR));
-}
-
-// The staging buffers are dynamic shared memory (above the 48 KB default, so
-// each kernel opts in once).
-template <int TR, typename K>
-int tile_grid(K kernel, size_t smem, int64_t N) {
-    FEA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    FEA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TR, smem));
-    if (per_sm < 1) {
-        set_error("tile kernel (%d threads, %zu bytes of shared memory) does not fit on an SM", TR, smem);
-        throw Error{FEA_ERR_CUDA};
-    }
-    return (int)std::min<int64_t>((int64_t)num_sms() * per_sm, tile_count<TR>(N));
-}
-
-template <typename R, int NF, int TR, int U>
+template <typename R, int NF, int WCH>
 struct Grids {
-    static constexpr size_t smem = sizeof(TilePipe<R, NF, TR>);
-    int tiles, rhs, stream;
+    int spmv, iter, rhs, stream;
     explicit Grids(int64_t N) {
-        tiles = std::min(tile_grid<TR>(k_cgcg_iter<R, NF, TR, U>, smem, N),
-                         tile_grid<TR>(k_cgcg_init<R, NF, TR, U>, smem, N));
+        spmv = wave_grid(k_cgcg_init<R, NF, WCH>, ceil_div(N, kBlock));
+        iter = wave_grid(k_cgcg_iter<R, NF, WCH>, ceil_div(N, kBlock));
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -904,10 +892,10 @@ struct LoopArgs {
 // Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter }
 //              -> refine -> init -> WHILE(cg2) { iter } -> [post] -> stepctl }
 //              -> final_check
-template <typename R, int NF, int EQ, int TR, int U>
+template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
-    const Grids<R, NF, TR, U> g(base.N);
+    const Grids<R, NF, WCH> g(base.N);
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
     G.graph = top;
@@ -919,14 +907,14 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a1, g.smem);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a1);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a1, g.smem);
+    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a1);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, TR, U>, g.tiles, TR, L.a2, g.smem);
+    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a2);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, TR, U>, g.tiles, TR, L.a2, g.smem);
+    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a2);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -944,10 +932,10 @@ int read_flag(const int* d, cudaStream_t st) {
 // on the host: every kernel is then visible to profilers (kernels inside
 // graphs with conditional nodes are not).  Each loop is bounded by the
 // kernels' own iteration and step limits.
-template <typename R, int NF, int EQ, int TR, int U>
+template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
-    const Grids<R, NF, TR, U> g(base.N);
+    const Grids<R, NF, WCH> g(base.N);
     k_start<R, NF><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_flag(&lf->step, st)) {
@@ -958,10 +946,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                 k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            k_cgcg_init<R, NF, TR, U><<<g.tiles, TR, g.smem, st>>>(*la);
+            k_cgcg_init<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                k_cgcg_iter<R, NF, TR, U><<<g.tiles, TR, g.smem, st>>>(*la);
+                k_cgcg_iter<R, NF, WCH><<<g.iter, kBlock, 0, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -976,32 +964,31 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     FEA_CHECK_LAUNCH();
 }
 
-// Tile shapes picked by the autotuner: variant 4 = 256-row tiles with 4
-// gathers in flight per lane, 8 = 256 rows / 8 gathers, 16 = 128 rows / 8.
+// SpMV variants: entries streamed per lane and window (the autotuned shape).
 template <typename R, int NF, int EQ>
-void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int var, LoopFlags* lf, cudaStream_t st) {
-    switch (var) {
-    case 4: G ? build_graph_t<R, NF, EQ, 256, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 256, 4>(a, lf, st); break;
-    case 16: G ? build_graph_t<R, NF, EQ, 128, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 128, 8>(a, lf, st); break;
-    default: G ? build_graph_t<R, NF, EQ, 256, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 256, 8>(a, lf, st); break;
+void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags* lf, cudaStream_t st) {
+    switch (wch) {
+    case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
+    case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
+    default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
     }
 }
 
 template <typename R, int NF>
-void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf, cudaStream_t st) {
+void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
     if constexpr (NF == 1) {
         switch (kind) {
-        case EQ_HEAT: dispatch_variant<R, 1, EQ_HEAT>(G, a, var, lf, st); break;
-        case EQ_ADV_EXPLICIT: dispatch_variant<R, 1, EQ_ADV_EXPLICIT>(G, a, var, lf, st); break;
-        case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, var, lf, st); break;
-        case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, var, lf, st); break;
-        case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, var, lf, st); break;
+        case EQ_HEAT: dispatch_variant<R, 1, EQ_HEAT>(G, a, wch, lf, st); break;
+        case EQ_ADV_EXPLICIT: dispatch_variant<R, 1, EQ_ADV_EXPLICIT>(G, a, wch, lf, st); break;
+        case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, wch, lf, st); break;
+        case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, wch, lf, st); break;
+        case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     } else {
         switch (kind) {
-        case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, var, lf, st); break;
-        case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, var, lf, st); break;
+        case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, wch, lf, st); break;
+        case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     }
@@ -1014,42 +1001,25 @@ int max_grid_blocks() {
     return g_max_grid;
 }
 
-int partial_stride(int64_t N) { return (int)std::max<int64_t>(max_grid_blocks(), tile_count<128>(N) + 1); }
-
 template <typename R, int NF>
-void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf) {
+void build_step_graph(StepGraph& G, const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf) {
     G.destroy();
     G.kind = kind;
-    G.lanes = var;
-    dispatch_kind<R, NF>(&G, a, kind, var, lf, nullptr);
+    G.lanes = wch;
+    dispatch_kind<R, NF>(&G, a, kind, wch, lf, nullptr);
 }
 
 template <typename R, int NF>
-void run_steps_stream(const StepArgs<R, NF>& a, int kind, int var, LoopFlags* lf, cudaStream_t st) {
-    dispatch_kind<R, NF>(nullptr, a, kind, var, lf, st);
+void run_steps_stream(const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf, cudaStream_t st) {
+    dispatch_kind<R, NF>(nullptr, a, kind, wch, lf, st);
 }
 
-// One solve set-up SpMV (w = A z) on the current operator: the probe used by
-// the autotuner and by fea_time_spmv.  It only writes w, CG scratch that the
-// next solve recomputes; `scratch_flag` receives its loop condition.
 template <typename R, int NF>
-void launch_spmv_probe(const StepArgs<R, NF>& base, int var, cudaStream_t st, int* scratch_flag) {
-    StepArgs<R, NF> a = base;
-    a.use_graph = 0;
-    a.cont = scratch_flag;
-    switch (var) {
-    case 4: {
-        const Grids<R, NF, 256, 4> g(a.N);
-        k_cgcg_init<R, NF, 256, 4><<<g.tiles, 256, g.smem, st>>>(a);
-    } break;
-    case 16: {
-        const Grids<R, NF, 128, 8> g(a.N);
-        k_cgcg_init<R, NF, 128, 8><<<g.tiles, 128, g.smem, st>>>(a);
-    } break;
-    default: {
-        const Grids<R, NF, 256, 8> g(a.N);
-        k_cgcg_init<R, NF, 256, 8><<<g.tiles, 256, g.smem, st>>>(a);
-    } break;
+void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
+    switch (wch) {
+    case 4: k_cg_spmv<R, NF, 4><<<Grids<R, NF, 4>(a.N).spmv, kBlock, 0, st>>>(a); break;
+    case 16: k_cg_spmv<R, NF, 16><<<Grids<R, NF, 16>(a.N).spmv, kBlock, 0, st>>>(a); break;
+    default: k_cg_spmv<R, NF, 8><<<Grids<R, NF, 8>(a.N).spmv, kBlock, 0, st>>>(a); break;
     }
     FEA_CHECK_LAUNCH();
 }
@@ -1057,7 +1027,7 @@ void launch_spmv_probe(const StepArgs<R, NF>& base, int var, cudaStream_t st, in
 #define FEA_INST_STEP(R, NF)                                                                              \
     template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \
     template void run_steps_stream<R, NF>(const StepArgs<R, NF>&, int, int, LoopFlags*, cudaStream_t);    \
-    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t, int*);
+    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t);
 FEA_INST_STEP(float, 1)
 FEA_INST_STEP(float, 2)
 FEA_INST_STEP(double, 1)

@@ -22,9 +22,6 @@ struct Pattern {
 };
 
 int launch_grid(int64_t n);
-// Row-pointer padding of the solver-order pattern: the tile staging copies
-// (largest tile: 256 rows) read up to 260 entries from a tile's first row.
-constexpr int kRowPtrPad = 512;
 // Copy of P with the unknowns renumbered (pos[u] = new index, inv = inverse);
 // emap[e'] receives the original slot of every new slot.
 void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pattern& Pc, int32_t* emap,
@@ -162,13 +159,11 @@ void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int l
 template <typename R, int NF>
 void run_steps_stream(const StepArgs<R, NF>& base, int kind, int lanes, LoopFlags* lf, cudaStream_t st);
 
-// One solve set-up SpMV (w = A z) with the given tile variant: the
-// autotuning and timing probe.  scratch_flag receives its loop condition.
+// One SpMV + dot launch with the given lanes per row (autotuning probe).
 template <typename R, int NF>
-void launch_spmv_probe(const StepArgs<R, NF>& a, int var, cudaStream_t st, int* scratch_flag);
+void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
 
+// FP64-accurate true residual |b - A x| / |b| of the current solve (status).
 int max_grid_blocks();
-// Stride of the per-block partial sums for N unknowns (covers every grid).
-int partial_stride(int64_t N);
 
 }  // namespace fea

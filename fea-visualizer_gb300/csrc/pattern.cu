@@ -448,13 +448,9 @@ void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pa
     int32_t* len = tmp.alloc<int32_t>(N + 1);
     k_perm_rowlen<<<grid_for(N), kBlock, 0, st>>>(P.row_ptr, inv, N, len);
     FEA_CHECK_LAUNCH();
-    // padding: tile staging copies the row pointers of a whole tile (up to 256
-    // rows + 4) from its first row, also for the last, partial tile
-    Pc.row_ptr = keep.alloc<int32_t>(N + 1 + kRowPtrPad);
-    FEA_CUDA_TRY(cudaMemsetAsync(Pc.row_ptr, 0, sizeof(int32_t) * (N + 1 + kRowPtrPad), st));
+    Pc.row_ptr = keep.alloc<int32_t>(N + 1);
     exclusive_scan_i32(len, Pc.row_ptr, N, st);
-    Pc.col = keep.alloc<int32_t>(P.nnz + 4);
-    FEA_CUDA_TRY(cudaMemsetAsync(Pc.col, 0, sizeof(int32_t) * (P.nnz + 4), st));
+    Pc.col = keep.alloc<int32_t>(P.nnz);
     k_perm_fill<<<grid_for(N), kBlock, 0, st>>>(P.row_ptr, P.col, pos, inv, N, Pc.row_ptr, Pc.col, emap);
     FEA_CHECK_LAUNCH();
     Pc.diag = keep.alloc<int32_t>(N);

@@ -159,8 +159,7 @@ struct fea_solver {
     StepParams* d_prm = nullptr;
     CgState* d_cg = nullptr;
     RunState* d_run = nullptr;
-    double* d_part = nullptr;  // per-block partial sums [8 * part_stride]
-    int part_stride = 0;
+    double* d_part = nullptr;
     unsigned int* d_tickets = nullptr;
     LoopFlags* d_flags = nullptr;
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
@@ -337,8 +336,7 @@ void build_context(fea_solver* s) {
     F.ut = ralloc(s->mat_mem, s, N);
     F.vt = ralloc(s->mat_mem, s, N);
     F.uv = ralloc(s->mat_mem, s, 2 * N);
-    // operator arrays carry 4 entries of padding for the tile staging copies
-    F.A1 = ralloc(s->mat_mem, s, nnz + 4);
+    F.A1 = ralloc(s->mat_mem, s, nnz);
     F.d1 = ralloc(s->mat_mem, s, N);
     F.b1 = ralloc(s->mat_mem, s, N);
     const int64_t Np = pad4(N);  // every buffer of a group starts 16-byte aligned
@@ -346,9 +344,9 @@ void build_context(fea_solver* s) {
     F.z1 = ralloc(s->mat_mem, s, N);
     F.p1 = ralloc(s->mat_mem, s, 2 * Np);
     F.q1 = ralloc(s->mat_mem, s, N);
-    F.A0 = ralloc(s->mat_mem, s, nnz + 4);
+    F.A0 = ralloc(s->mat_mem, s, nnz);
     F.d0 = ralloc(s->mat_mem, s, N);
-    F.A2 = ralloc(s->mat_mem, s, 2 * (nnz + 4));
+    F.A2 = ralloc(s->mat_mem, s, 2 * nnz);
     F.d2 = ralloc(s->mat_mem, s, 2 * N);
     F.b2 = ralloc(s->mat_mem, s, 2 * N);
     F.r2 = ralloc(s->mat_mem, s, 12 * Np);
@@ -362,10 +360,6 @@ void build_context(fea_solver* s) {
         {F.p1, 2 * Np}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 12 * Np}, {F.z2, 2 * N}, {F.p2, 4 * Np}, {F.q2, 2 * N}};
     for (const auto& zv : zeroed)
         FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
-    for (const auto& zv : {std::make_pair(F.A1, nnz + 4), std::make_pair(F.A0, nnz + 4), std::make_pair(F.A2, 2 * (nnz + 4))})
-        FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)zv.second, st));
-    s->part_stride = partial_stride(N);
-    s->d_part = s->mat_mem.alloc<double>(8 * (int64_t)s->part_stride);
     F.interleaved = false;
     s->acc_valid = false;
     assemble(s);
@@ -421,7 +415,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
     a.cg = s->d_cg;
     a.run = s->d_run;
     a.part = s->d_part;
-    a.part_stride = s->part_stride;
+    a.part_stride = max_grid_blocks();
     a.tickets = s->d_tickets;
     return a;
 }
@@ -623,6 +617,7 @@ void alloc_run_state(fea_solver* s) {
     s->d_prm = s->run_mem.alloc<StepParams>(1);
     s->d_cg = s->run_mem.alloc<CgState>(1);
     s->d_run = s->run_mem.alloc<RunState>(1);
+    s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
     s->d_tickets = s->run_mem.alloc<unsigned int>(8);
     s->d_flags = s->run_mem.alloc<LoopFlags>(1);
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, sizeof(LoopFlags), s->stream));
@@ -1011,11 +1006,11 @@ int fea_autotune(fea_solver* s) {
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
             if (s->precision == FEA_FP64) {
-                if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), l, s->stream, &s->d_flags->cg1);
-                else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), l, s->stream, &s->d_flags->cg1);
+                if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), l, s->stream);
+                else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), l, s->stream);
             } else {
-                if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), l, s->stream, &s->d_flags->cg1);
-                else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), l, s->stream, &s->d_flags->cg1);
+                if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), l, s->stream);
+                else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), l, s->stream);
             }
         }
         FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
@@ -1068,11 +1063,11 @@ int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch) 
         if (junk) FEA_CUDA_TRY(cudaMemsetAsync(junk, rep & 0xff, flush_bytes, s->stream));
         FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
         if (s->precision == FEA_FP64) {
-            if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), s->lanes, s->stream, &s->d_flags->cg1);
-            else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), s->lanes, s->stream, &s->d_flags->cg1);
+            if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), s->lanes, s->stream);
+            else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), s->lanes, s->stream);
         } else {
-            if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), s->lanes, s->stream, &s->d_flags->cg1);
-            else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), s->lanes, s->stream, &s->d_flags->cg1);
+            if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), s->lanes, s->stream);
+            else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), s->lanes, s->stream);
         }
         FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
         FEA_CUDA_TRY(cudaEventSynchronize(e1));
