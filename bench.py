@@ -117,11 +117,93 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def spmv_bytes(N, nnz, nfields=2):
-    """Algorithmic bytes of one paired CSR SpMV launch: values (4 B per field)
-    and a 4 B column index per stored entry, row pointers, the gathered vector
-    read once and the product written once (4 B per field per row)."""
-    return nnz * (4 * nfields + 4) + 4 * (N + 1) + 2 * 4 * nfields * N
+def iter_bytes(N, nnz, nfields=2):
+    """Algorithmic bytes of one CG iteration launch (the step's dominant
+    kernel: paired CSR SpMV with the vector updates fused): values (4 B per
+    field) and a 4 B column index per stored entry, row pointers, and per row
+    and field the reads of r, w, s, D^-1, x, p and the writes of x, p, r, s, w
+    (11 x 4 B; the gathered vectors counted once)."""
+    return nnz * (4 * nfields + 4) + 4 * (N + 1) + 11 * 4 * nfields * N
+
+
+# Batched sweep: 256 Gray-Scott instances on icospheres of uneven size
+BATCH_N = 256
+BATCH_LEVELS = (3, 4, 5, 6)
+BATCH_PARAMS = dict(time_step=0.5, Du=2e-4, Dv=1e-4)
+
+
+def batch_workload(n=BATCH_N, seed=0):
+    import numpy as np
+    from fea_gb300 import meshgen as mg
+    rng = np.random.default_rng(seed)
+    meshes = {L: mg.icosphere(L) for L in BATCH_LEVELS}
+    insts, starts = [], []
+    for i in range(n):
+        xyz, tri = meshes[int(rng.choice(BATCH_LEVELS))]
+        insts.append(dict(vertices=xyz, triangles=tri, boundary_condition=1,
+                          feed_rate=float(rng.uniform(0.01, 0.06)), kill_rate=float(rng.uniform(0.045, 0.07)),
+                          **BATCH_PARAMS))
+        starts.append(mg.sphere_patches(xyz, seed=1000 + i))
+    return insts, starts
+
+
+def bench_batched(F, steps, warmup, plain_steps):
+    """The 256-instance sweep in one batch vs the plain loop of single-mesh
+    handles (one after another, each advancing its own graph)."""
+    import numpy as np
+    insts, starts = batch_workload()
+    t0 = time.perf_counter()
+    B = F.BatchSolver(insts, cg_tolerance=CG_TOL)
+    setup_s = time.perf_counter() - t0
+    for i, (u, v) in enumerate(starts):
+        B.set_fields(i, u, v)
+    B.advance_time(warmup)
+    B.synchronize()
+    t0 = time.perf_counter()
+    B.advance_time(steps)
+    B.synchronize()
+    batch_s = time.perf_counter() - t0
+    flags, iters = B.status()
+    handles = []
+    for d in insts:
+        p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=d["time_step"],
+                             rd_Du=d["Du"], rd_Dv=d["Dv"], rd_feed_rate=d["feed_rate"],
+                             rd_kill_rate=d["kill_rate"], cg_tolerance=CG_TOL)
+        handles.append(F.CUDASolver(d["vertices"], d["triangles"], boundary_condition=F.NEUMANN, params=p))
+    for h, (u, v) in zip(handles, starts):
+        h.set_fields(u, v)
+        h.advance_time(1)
+        h.synchronize()
+    t0 = time.perf_counter()
+    for h in handles:
+        h.advance_time(plain_steps)
+        h.synchronize()
+    plain_s = time.perf_counter() - t0
+    # accuracy of the batch against the plain handles: the same 5 steps from the start state
+    for i, (h, (u, v)) in enumerate(zip(handles, starts)):
+        h.set_fields(u, v)
+        B.set_fields(i, u, v)
+        h.advance_time(5)
+    B.advance_time(5)
+    err = 0.0
+    for i, h in enumerate(handles):
+        for a, b in zip(B.get_fields(i), h.get_fields()):
+            err = max(err, float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b), 1e-30)))
+        h.close()
+    nverts = sum(d["vertices"].shape[0] for d in insts)
+    batch_rate = BATCH_N * steps / batch_s
+    plain_rate = BATCH_N * plain_steps / plain_s
+    B.close()
+    return {"workload": f"{BATCH_N} gray-scott instances, icospheres of levels {list(BATCH_LEVELS)} drawn "
+                        f"uniformly, F ~ U(0.01,0.06), k ~ U(0.045,0.07), Du 2e-4, Dv 1e-4, dt 0.5",
+            "vertices": nverts, "steps": steps, "instance_steps_per_s": batch_rate,
+            "sweep_steps_per_s": steps / batch_s, "plain_instance_steps_per_s": plain_rate,
+            "plain_steps_timed": plain_steps, "speedup_vs_plain": batch_rate / plain_rate,
+            "max_rel_l2_vs_plain_after_5_steps": err, "setup_s": setup_s,
+            "status_flags_or": int(np.bitwise_or.reduce(flags)),
+            "max_iterations_last_solve": int(iters.max()), "min_iterations_last_solve": int(iters.min()),
+            "timing": "wall clock around one advance_time(K) graph launch + synchronize; "
+                      "every CG iteration touches more than the L2 size (~0.6 GB)"}
 
 
 def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads):
@@ -170,6 +252,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched sweep")
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="vertices per side (other sizes are for profiling captures, not bench lines)")
     args = ap.parse_args()
@@ -229,8 +314,8 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     iters = st1.total_iterations - st0.total_iterations
-    # per step: rhs, refine, stepctl; per CG iteration: spmv, update; per call: start, final check
-    launches = args.steps * 3 + 2 * iters + 2 * args.steps
+    # per step: rhs, 2 x init, refine, stepctl; one kernel per CG iteration; per call: start, final check
+    launches = args.steps * 5 + iters + 2 * args.steps
     value = world * args.steps / (total_ms / 1000.0)
 
     # one K-step graph launch (no flush between steps) for reference
@@ -243,11 +328,11 @@ def main():
     s.synchronize()
     one_launch_ms = e0.elapsed_time(e1)
 
-    # dominant kernel: the paired SpMV, timed alone on the same operator
+    # dominant kernel: one CG iteration, timed alone on the same operator
     spmv_ms = s.time_spmv(reps=20, flush_l2=True)
     spmv_warm_ms = s.time_spmv(reps=20, flush_l2=False)
     peak, peak_kind = measured_peak_hbm()
-    bytes_spmv = spmv_bytes(N, nnz)
+    bytes_spmv = iter_bytes(N, nnz)
     achieved = bytes_spmv / (spmv_ms * 1e-3) / 1e9
 
     # end to end through the C ABI with host buffers (values = v, CPUSolver.cpp:130,144)
@@ -272,6 +357,9 @@ def main():
     e2e = world * args.steps / e2e_s
 
     flags = s.status().flags
+    batched = None
+    if not args.no_batch:
+        batched = bench_batched(F, args.batch_steps, 3, args.plain_steps)
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -291,10 +379,12 @@ def main():
                               "one_launch_ms_per_step": one_launch_ms / args.steps}),
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": 4 * V},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "k_cg_spmv (paired u,v SpMV + p.q)",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_cgcg_iter (one CG iteration: paired u,v SpMV with fused vector updates)",
                          "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": spmv_ms,
                          "ms_per_launch_l2_warm": spmv_warm_ms, "peak_source": peak_kind},
             "cpu_baseline": cpu,
+            "batched": batched,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "status_flags": int(flags),

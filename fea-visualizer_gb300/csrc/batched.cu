@@ -1,15 +1,1031 @@
 // batched.cu -- many Gray-Scott instances stepped together.
-#include "fea_internal.cuh"
+//
+// No reference counterpart: the reference steps one mesh.  Each instance is
+// one mesh with its own (F, k, Du, Dv, dt) and follows the Gray-Scott step of
+// CPUSolver.cpp:127-145 with the mass-weighted reaction, b = M (x/dt + f(x))
+// for x = (u, v), solved with the single-mesh solver's CG: the Jacobi-
+// preconditioned Chronopoulos-Gear iteration with FP64-accurate inner products
+// and one true-residual refinement pass per solve.
+//
+// Layout.  The instances' systems are stacked block-diagonally into one CSR
+// matrix, each in its own solver order (a single-mesh handle built per
+// instance supplies pattern, Morton ordering and FP64 matrices, then is
+// released).  Every instance starts on a tile boundary (a tile is kTile rows:
+// one pass of a kBlock-thread block, 32 rows per warp); the rows between
+// instances are empty.  So a tile belongs to exactly one instance.
+//
+// Kernels walk the tiles with a grid-stride loop.  Each tile reduces its rows'
+// inner products and stores them as the tile's partials; the tile that
+// completes an instance last sums that instance's partials in tile order (the
+// result does not depend on the schedule) and advances the instance's CG
+// scalars.  An instance whose solves have converged, or that is frozen after a
+// blow-up, is masked: its tiles are skipped.  A solve loop runs while any
+// instance iterates; the step loop is one CUDA graph with conditional WHILE
+// nodes, as in the single-mesh solver.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cg_device.cuh"
+
+namespace fea {
+namespace {
+
+constexpr int kTile = kBlock;  // rows per tile
+constexpr int kNV = 6;         // partials per tile: 3 inner products x 2 fields
+constexpr int kLanes = 8;      // lanes per row of the once-per-step kernels
+
+struct BPrm {
+    double dt, F, k;
+};
+
+// CG and step state of one instance.
+struct BInst {
+    double rz[2], rr[2], pq[2], thr[2], bb[2], alpha[2], beta[2];
+    int active[2], fresh[2], iters[2];
+    int iter;  // iterations of the current solve
+    int max_iter;
+    int stop;            // frozen: its state was unstable at the start of a step
+    unsigned int flags;  // FEA_STATUS_* since the last advance
+    int last_iters[2];
+    double last_rel[2];
+    long long steps_done, total_iters;
+};
+
+// Loop state shared by the instances.
+struct BCtl {
+    long long steps_left, steps_done;
+    int iter;             // CG iteration of the running solve loop: buffer parity
+    int n_next;           // (instance, field) solves left active by this phase
+    unsigned int ticket;  // blocks finished in this phase
+    int refine;
+    double tol;
+};
+
+struct BFlags {
+    int step, cg1, cg2, probe;
+};
+
+template <typename R>
+struct BArgs {
+    int64_t N;  // rows, padding included (= ntiles * kTile)
+    int ntiles, ninst;
+    const int32_t* rp;
+    const int32_t* col;
+    const FV<R, 2>* A;
+    const FV<R, 2>* dinv;
+    const R* M;
+    FV<R, 2>* x;
+    FV<R, 2>* b;
+    FV<R, 2>* z;
+    FV<R, 2>* p;
+    FV<R, 2>* rb[2];
+    FV<R, 2>* wb[2];
+    FV<R, 2>* sb[2];
+    const int32_t* tile_inst;  // [ntiles] instance of each tile
+    const int32_t* inst_tile;  // [ninst + 1] first tile of each instance
+    const BPrm* prm;           // [ninst]
+    BInst* inst;               // [ninst]
+    BCtl* ctl;
+    double* part;           // [ntiles * kNV] tile partials
+    unsigned int* iticket;  // [ninst] tiles finished per instance in this phase
+    int probe;              // timing probe: every tile, no state update
+    cudaGraphConditionalHandle cond;
+    int* cont;
+    int use_graph;
+};
+
+// Thread 0 holds the tile's NV totals in blk.  They become the tile's
+// partials; the tile that completes its instance last sums the instance's
+// partials in tile order and returns true in all its threads, with the totals
+// in out[] (valid in thread 0).  The instance's ticket is reset for the next
+// phase.
+template <int NV>
+__device__ bool inst_commit(const double (&blk)[NV], double* part, int tile, int t0, int nt, unsigned int* ticket,
+                            double* smem, double (&out)[NV]) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[(int64_t)tile * kNV + k] = blk[k];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == (unsigned int)(nt - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double y[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double acc = 0.0;
+        for (int t = t0 + threadIdx.x; t < t0 + nt; t += blockDim.x) acc += __ldcg(&part[(int64_t)t * kNV + k]);
+        y[k] = acc;
+    }
+    block_sum<NV>(y, smem);
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = y[k];
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+enum { kIterKeep = 0, kIterNext = 1, kIterReset = 2 };
+
+// End of a phase: the block that finishes last publishes whether any
+// (instance, field) solve is still active, resets the phase counter, moves the
+// iteration counter and sets the loop condition.
+template <typename R>
+__device__ void phase_end(const BArgs<R>& a, int iter_mode) {
+    __shared__ bool lastb;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        lastb = atomicAdd(&a.ctl->ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && lastb) {
+        __threadfence();
+        BCtl* c = a.ctl;
+        const int n = atomicExch(&c->n_next, 0);
+        c->ticket = 0u;
+        if (iter_mode == kIterNext) c->iter = c->iter + 1;
+        if (iter_mode == kIterReset) c->iter = 0;
+        signal_loop(a, n > 0);
+    }
+}
+
+__device__ __forceinline__ void raise_inst(BInst* s, unsigned int f) {
+    const unsigned int w = __reduce_or_sync(0xffffffffu, f);
+    if (w && (threadIdx.x & 31) == 0) {
+        atomicOr(&s->flags, w);
+        __threadfence();
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ int iter_of(const BArgs<R>& a) {
+    return ((const volatile BCtl*)a.ctl)->iter;
+}
+
+// Right-hand side b = M (x/dt + f(x)) of every unfrozen instance, initial
+// residual r = b - A x (warm start), z = D^-1 r, and the set-up scalars;
+// instances whose state entering the step is unstable are frozen.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_rhs(BArgs<R> a) {
+    __shared__ double red[32 * kNV];
+    constexpr int RPW = 32 / kLanes;      // rows per warp pass
+    constexpr int RPB = kBlock / kLanes;  // rows per block pass
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int sub = lane & (kLanes - 1), grp = lane / kLanes;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        BInst* s = a.inst + i;
+        if (((const volatile BInst*)s)->stop) continue;
+        const BPrm P = a.prm[i];
+        const R dt = (R)P.dt, Fr = (R)P.F, Kr = (R)P.k;
+        Acc<R> dots[kNV];  // |b|^2, |r|^2, r.z per field
+        unsigned int flags = 0;
+        for (int pass = 0; pass < kTile / RPB; pass++) {
+            const int64_t row = (int64_t)tile * kTile + pass * RPB + wib * RPW + grp;
+            Acc<R> bs[2], ax[2];
+            const int32_t e1 = ldg(a.rp + row + 1);
+            for (int32_t e = ldg(a.rp + row) + sub; e < e1; e += kLanes) {
+                const int32_t c = ldg(a.col + e);
+                const FV<R, 2> av = ldv(a.A + e, false);
+                const FV<R, 2> xc = a.x[c];
+                const R me = ldg(a.M + e);
+                const R u = xc.v[0], v = xc.v[1];
+                const R uvv = u * (v * v);
+                const R wu = u / dt - uvv + Fr * ((R)1 - u);
+                const R wv = v / dt + uvv - (Fr + Kr) * v;
+                bs[0].add_prod(me, wu);
+                bs[1].add_prod(me, wv);
+                ax[0].add_prod(av.v[0], u);
+                ax[1].add_prod(av.v[1], v);
+            }
+#pragma unroll
+            for (int o = kLanes / 2; o > 0; o >>= 1)
+#pragma unroll
+                for (int f = 0; f < 2; f++) {
+                    bs[f].shfl_add(o);
+                    ax[f].shfl_add(o);
+                }
+            if (sub == 0) {
+                const FV<R, 2> xr = a.x[row];
+                flags |= check_value(xr.v[0]) | check_value(xr.v[1]);
+                const FV<R, 2> d = ldv(a.dinv + row, false);
+                FV<R, 2> bv, rv, zv;
+#pragma unroll
+                for (int f = 0; f < 2; f++) {
+                    bv.v[f] = (R)bs[f].value();
+                    bs[f].sub(ax[f]);
+                    rv.v[f] = (R)bs[f].value();
+                    zv.v[f] = d.v[f] * rv.v[f];
+                    dots[f].add_prod(bv.v[f], bv.v[f]);
+                    dots[2 + f].add_prod(rv.v[f], rv.v[f]);
+                    dots[4 + f].add_prod(rv.v[f], zv.v[f]);
+                }
+                a.b[row] = bv;
+                a.rb[0][row] = rv;  // the solve starts at iteration 0 (parity 0)
+                a.z[row] = zv;
+            }
+        }
+        raise_inst(s, flags);
+        double blk[kNV], tot[kNV];
+        block_totals<kNV>(dots, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+            volatile BInst* vs = s;
+            const int stop = (atomicOr(&s->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
+            const double tol = a.ctl->tol;
+            const double tiny = sizeof(R) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+            vs->stop = stop;
+            vs->iter = 0;
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                const double bb = tot[f], rr = tot[2 + f], rz = tot[4 + f];
+                const double thr = tol * tol * bb;
+                vs->bb[f] = bb;
+                vs->thr[f] = thr < tiny ? tiny : thr;
+                vs->rr[f] = rr;
+                vs->rz[f] = rz;
+                vs->iters[f] = 0;
+                vs->fresh[f] = 1;
+                vs->active[f] = (!stop && bb > 0.0 && rr >= vs->thr[f]) ? 1 : 0;
+                nact += vs->active[f];
+            }
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterReset);
+}
+
+// Set-up of a solve for every instance with an active field: w0 = A z,
+// delta0 = z.w0, alpha0 = r0.z / delta0.  Also the SpMV timing probe.
+template <typename R, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a) {
+    __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * kNV];
+    const int wib = threadIdx.x >> 5;
+    const int iter = iter_of(a);
+    FV<R, 2>* w = a.wb[iter & 1];
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        PhaseCtl<R, 2> c;
+        c.set(iter, (const volatile BInst*)(a.inst + i));
+        if (!c.any && !a.probe) continue;
+        Acc<R> dot[2];
+        init_rows<R, 2, WCH>(a.rp, a.col, a.A, a.z, w, (int64_t)tile * kTile + wib * 32, a.N, sm[wib], dot);
+        double blk[2], tot[2];
+        block_totals<2>(dot, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<2>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
+            volatile BInst* s = a.inst + i;
+            finish_spmv<R, 2>(s, &a.inst[i].flags, c.act, tot);
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                s->fresh[f] = 1;  // the first iteration takes p = u, s = w
+                nact += s->active[f];
+            }
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterKeep);
+}
+
+// One Chronopoulos-Gear iteration of every instance that still iterates.
+template <typename R, int WCH>
+__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a) {
+    __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
+    __shared__ double red[32 * kNV];
+    const int wib = threadIdx.x >> 5;
+    const int iter = iter_of(a), par = iter & 1;
+    CgVecs<R, 2> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.p;
+    v.r0 = a.rb[par];
+    v.w0 = a.wb[par];
+    v.s0 = a.sb[par];
+    v.r1 = a.rb[par ^ 1];
+    v.w1 = a.wb[par ^ 1];
+    v.s1 = a.sb[par ^ 1];
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        PhaseCtl<R, 2> c;
+        c.set(iter, (const volatile BInst*)(a.inst + i));
+        if (!c.any) continue;
+        Acc<R> dots[kNV];  // gamma', delta', |r'|^2
+        cgcg_rows<R, 2, WCH>(v, c, (int64_t)tile * kTile + wib * 32, a.N, sm[wib], dots);
+        double blk[kNV], tot[kNV];
+        block_totals<kNV>(dots, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+            volatile BInst* s = a.inst + i;
+            if (finish_cgcg<R, 2>(s, &a.inst[i].flags, c.act, tot))
+                atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
+        }
+    }
+    phase_end(a, kIterNext);
+}
+
+// After the first solve loop: zero right-hand sides give x = 0, then one
+// FP64-accurate true-residual pass r = b - A x; fields still above their
+// threshold restart CG from there.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_refine(BArgs<R> a) {
+    __shared__ double red[32 * kNV];
+    constexpr int RPW = 32 / kLanes;
+    constexpr int RPB = kBlock / kLanes;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int sub = lane & (kLanes - 1), grp = lane / kLanes;
+    const int par = iter_of(a) & 1;
+    const int refine_on = a.ctl->refine;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        const volatile BInst* s = a.inst + i;
+        const int stop = s->stop;
+        const int refine = refine_on && s->iter < s->max_iter && !stop;
+        int zero[2];
+#pragma unroll
+        for (int f = 0; f < 2; f++) zero[f] = !stop && !(s->bb[f] > 0.0);
+        if (!refine && !zero[0] && !zero[1]) continue;
+        Acc<R> dots[4];  // |r|^2, r.z per field
+        for (int pass = 0; pass < kTile / RPB; pass++) {
+            const int64_t row = (int64_t)tile * kTile + pass * RPB + wib * RPW + grp;
+            Acc<R> ax[2];
+            if (refine) {
+                const int32_t e1 = ldg(a.rp + row + 1);
+                for (int32_t e = ldg(a.rp + row) + sub; e < e1; e += kLanes) {
+                    const FV<R, 2> av = ldv(a.A + e, false);
+                    const FV<R, 2> xc = a.x[ldg(a.col + e)];
+#pragma unroll
+                    for (int f = 0; f < 2; f++) ax[f].add_prod(av.v[f], xc.v[f]);
+                }
+#pragma unroll
+                for (int o = kLanes / 2; o > 0; o >>= 1)
+#pragma unroll
+                    for (int f = 0; f < 2; f++) ax[f].shfl_add(o);
+            }
+            if (sub == 0) {
+                if (zero[0] || zero[1]) {
+                    FV<R, 2> xr = a.x[row];
+#pragma unroll
+                    for (int f = 0; f < 2; f++)
+                        if (zero[f]) xr.v[f] = 0;
+                    a.x[row] = xr;
+                }
+                if (refine) {
+                    const FV<R, 2> bv = a.b[row], d = ldv(a.dinv + row, false);
+                    FV<R, 2> rv, zv;
+#pragma unroll
+                    for (int f = 0; f < 2; f++) {
+                        Acc<R> t;
+                        t.add(bv.v[f]);
+                        t.sub(ax[f]);
+                        rv.v[f] = (R)t.value();
+                        zv.v[f] = d.v[f] * rv.v[f];
+                        dots[f].add_prod(rv.v[f], rv.v[f]);
+                        dots[2 + f].add_prod(rv.v[f], zv.v[f]);
+                    }
+                    a.rb[par][row] = rv;  // the restart continues the iteration parity
+                    a.z[row] = zv;
+                }
+            }
+        }
+        double blk[4], tot[4];
+        block_totals<4>(dots, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<4>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+            volatile BInst* w = a.inst + i;
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                w->active[f] = 0;
+                w->fresh[f] = 1;
+                if (refine && !zero[f] && w->bb[f] > 0.0) {
+                    w->rr[f] = tot[f];
+                    if (tot[f] >= w->thr[f]) {
+                        w->rz[f] = tot[2 + f];
+                        w->active[f] = 1;
+                        nact++;
+                    }
+                }
+            }
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterKeep);
+}
+
+// Step bookkeeping of every instance and the outer loop condition (one block).
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_stepctl(BArgs<R> a) {
+    __shared__ int alive;
+    if (threadIdx.x == 0) alive = 0;
+    __syncthreads();
+    int mine = 0;
+    for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
+        BInst* s = a.inst + i;
+        if (!s->stop) {
+            s->steps_done += 1;
+            s->total_iters += s->iter;
+            for (int f = 0; f < 2; f++) {
+                s->last_iters[f] = s->iters[f];
+                s->last_rel[f] = s->bb[f] > 0.0 ? sqrt(s->rr[f] / s->bb[f]) : 0.0;
+            }
+            mine++;
+        }
+    }
+    if (mine) atomicAdd(&alive, mine);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        BCtl* c = a.ctl;
+        c->steps_left -= 1;
+        c->steps_done += 1;
+        signal_loop(a, c->steps_left > 0 && alive > 0);
+    }
+}
+
+template <typename R>
+__global__ void kb_start(BArgs<R> a) {
+    signal_loop(a, a.ctl->steps_left > 0);
+}
+
+// Instability test of the state after the last step.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_final_check(BArgs<R> a) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.N; r += (int64_t)gridDim.x * blockDim.x) {
+        const FV<R, 2> x = a.x[r];
+        const unsigned int f = check_value(x.v[0]) | check_value(x.v[1]);
+        if (f) atomicOr(&a.inst[a.tile_inst[r / kTile]].flags, f);
+    }
+}
+
+// Start of an advance: every instance unfrozen with clear flags (a state
+// that is still unstable is frozen again by the first step's check).
+__global__ void kb_clear(BInst* inst, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        inst[i].stop = 0;
+        inst[i].flags = 0u;
+    }
+}
+
+// ---- set-up kernels ------------------------------------------------------------------
+
+// Instance pattern -> stacked pattern: rows shifted by row0, slots by e0;
+// the padding rows up to the next tile boundary are empty.
+__global__ void kb_copy_pattern(const int32_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t n,
+                                int64_t nrows, int64_t nnz, int64_t row0, int64_t e0, int32_t* rp_out,
+                                int32_t* col_out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += stride)
+        rp_out[row0 + r] = (int32_t)(e0 + (r <= n ? rp[r] : nnz));
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += stride)
+        col_out[e0 + e] = (int32_t)(row0 + col[e]);
+}
+
+__global__ void kb_node_map(const int32_t* __restrict__ idx_c, int64_t V, int64_t row0, int32_t* out) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x)
+        out[v] = idx_c[v] >= 0 ? (int32_t)(row0 + idx_c[v]) : -1;
+}
+
+// node-indexed float field -> field f of the stacked state
+template <typename R>
+__global__ void kb_gather(const float* __restrict__ vals, const int32_t* __restrict__ map, int64_t V,
+                          FV<R, 2>* x, int f) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = map[v];
+        if (r >= 0) x[r].v[f] = (R)vals[v];
+    }
+}
+
+// field f of the stacked state -> node-indexed floats (Dirichlet points 0)
+template <typename R>
+__global__ void kb_scatter(const FV<R, 2>* __restrict__ x, const int32_t* __restrict__ map, int64_t V, float* out,
+                           int f) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = map[v];
+        out[v] = r >= 0 ? (float)x[r].v[f] : 0.f;
+    }
+}
+
+}  // namespace
+}  // namespace fea
+
+using namespace fea;
+
+struct fea_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = FEA_FP32;
+    int ninst = 0, ntiles = 0;
+    int64_t N = 0, nnz = 0;
+    int wch = 8;  // entries per lane and window of the CG kernels (autotuned)
+    std::vector<int64_t> V, node_off;
+    DeviceArena mem;
+    int32_t *rp = nullptr, *col = nullptr, *tile_inst = nullptr, *inst_tile = nullptr, *node_map = nullptr;
+    void *A = nullptr, *dinv = nullptr, *M = nullptr;
+    void *x = nullptr, *b = nullptr, *z = nullptr, *p = nullptr, *rws = nullptr;
+    BPrm* prm = nullptr;
+    BInst* inst = nullptr;
+    BCtl* ctl = nullptr;
+    double* part = nullptr;
+    unsigned int* iticket = nullptr;
+    BFlags* flags = nullptr;
+    float* staging = nullptr;  // node-sized staging buffer (largest instance)
+    double tol = 0.0;
+    int max_iter_cfg = 0;
+    bool stream_mode = false;
+    StepGraph graph;
+};
+
+namespace fea {
+namespace {
+
+template <typename R>
+BArgs<R> make_bargs(fea_batch* B) {
+    BArgs<R> a{};
+    a.N = B->N;
+    a.ntiles = B->ntiles;
+    a.ninst = B->ninst;
+    a.rp = B->rp;
+    a.col = B->col;
+    a.A = (const FV<R, 2>*)B->A;
+    a.dinv = (const FV<R, 2>*)B->dinv;
+    a.M = (const R*)B->M;
+    a.x = (FV<R, 2>*)B->x;
+    a.b = (FV<R, 2>*)B->b;
+    a.z = (FV<R, 2>*)B->z;
+    a.p = (FV<R, 2>*)B->p;
+    FV<R, 2>* w = (FV<R, 2>*)B->rws;
+    for (int k = 0; k < 2; k++) {
+        a.rb[k] = w + k * B->N;
+        a.wb[k] = w + (2 + k) * B->N;
+        a.sb[k] = w + (4 + k) * B->N;
+    }
+    a.tile_inst = B->tile_inst;
+    a.inst_tile = B->inst_tile;
+    a.prm = B->prm;
+    a.inst = B->inst;
+    a.ctl = B->ctl;
+    a.part = B->part;
+    a.iticket = B->iticket;
+    return a;
+}
+
+template <typename R>
+struct BLoop {
+    BArgs<R> a, a1, a2;
+    BLoop(const BArgs<R>& base, BFlags* fl, int use_graph) : a(base), a1(base), a2(base) {
+        a.use_graph = a1.use_graph = a2.use_graph = use_graph;
+        a.cont = &fl->step;
+        a1.cont = &fl->cg1;
+        a2.cont = &fl->cg2;
+    }
+};
+
+template <typename R, int WCH>
+struct BGrids {
+    int rhs, init, iter, stream;
+    explicit BGrids(const fea_batch* B) {
+        rhs = wave_grid(kb_rhs<R>, B->ntiles);
+        init = wave_grid(kb_init<R, WCH>, B->ntiles);
+        iter = wave_grid(kb_iter<R, WCH>, B->ntiles);
+        stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(B->N, kBlock)));
+    }
+};
+
+// start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter } -> refine -> init
+//          -> WHILE(cg2) { iter } -> stepctl } -> final_check
+template <typename R, int WCH>
+void build_batch_graph_t(fea_batch* B) {
+    BLoop<R> L(make_bargs<R>(B), B->flags, 1);
+    const BGrids<R, WCH> g(B);
+    StepGraph& G = B->graph;
+    cudaGraph_t top;
+    FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
+    G.graph = top;
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a.cond, top, 0, 0));
+    cudaGraphNode_t n = add_kernel(top, nullptr, kb_start<R>, 1, 1, L.a);
+    cudaGraph_t step_body;
+    n = add_while(top, n, L.a.cond, &step_body);
+    add_kernel(top, n, kb_final_check<R>, g.stream, kBlock, L.a);
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
+    FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
+    cudaGraphNode_t s = add_kernel(step_body, nullptr, kb_rhs<R>, g.rhs, kBlock, L.a1);
+    s = add_kernel(step_body, s, kb_init<R, WCH>, g.init, kBlock, L.a1);
+    cudaGraph_t body1, body2;
+    s = add_while(step_body, s, L.a1.cond, &body1);
+    add_kernel(body1, nullptr, kb_iter<R, WCH>, g.iter, kBlock, L.a1);
+    s = add_kernel(step_body, s, kb_refine<R>, g.rhs, kBlock, L.a2);
+    s = add_kernel(step_body, s, kb_init<R, WCH>, g.init, kBlock, L.a2);
+    s = add_while(step_body, s, L.a2.cond, &body2);
+    add_kernel(body2, nullptr, kb_iter<R, WCH>, g.iter, kBlock, L.a2);
+    add_kernel(step_body, s, kb_stepctl<R>, 1, kBlock, L.a);
+    FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
+    G.lanes = WCH;
+}
+
+int read_int(const int* d, cudaStream_t st) {
+    int h = 0;
+    FEA_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    return h;
+}
+
+// The same step loop launched kernel by kernel (profiling mode,
+// FEA_LAUNCH_MODE=stream); each loop is bounded by the kernels' own limits.
+template <typename R, int WCH>
+void run_batch_stream_t(fea_batch* B) {
+    BLoop<R> L(make_bargs<R>(B), B->flags, 0);
+    const BGrids<R, WCH> g(B);
+    cudaStream_t st = B->stream;
+    kb_start<R><<<1, 1, 0, st>>>(L.a);
+    FEA_CHECK_LAUNCH();
+    while (read_int(&B->flags->step, st)) {
+        kb_rhs<R><<<g.rhs, kBlock, 0, st>>>(L.a1);
+        for (int loop = 0; loop < 2; loop++) {
+            const BArgs<R>& la = loop ? L.a2 : L.a1;
+            if (loop) kb_refine<R><<<g.rhs, kBlock, 0, st>>>(L.a2);
+            kb_init<R, WCH><<<g.init, kBlock, 0, st>>>(la);
+            FEA_CHECK_LAUNCH();
+            while (read_int(la.cont, st)) {
+                kb_iter<R, WCH><<<g.iter, kBlock, 0, st>>>(la);
+                FEA_CHECK_LAUNCH();
+            }
+        }
+        kb_stepctl<R><<<1, kBlock, 0, st>>>(L.a);
+        FEA_CHECK_LAUNCH();
+    }
+    kb_final_check<R><<<g.stream, kBlock, 0, st>>>(L.a);
+    FEA_CHECK_LAUNCH();
+}
+
+template <typename R>
+void run_batch(fea_batch* B) {
+    if (B->stream_mode) {
+        if (B->wch == 4) run_batch_stream_t<R, 4>(B);
+        else run_batch_stream_t<R, 8>(B);
+        return;
+    }
+    if (!B->graph.exec || B->graph.lanes != B->wch) {
+        B->graph.destroy();
+        if (B->wch == 4) build_batch_graph_t<R, 4>(B);
+        else build_batch_graph_t<R, 8>(B);
+    }
+    FEA_CUDA_TRY(cudaGraphLaunch(B->graph.exec, B->stream));
+}
+
+// One set-up SpMV (w = A z over every tile) with the given window size: the
+// autotuning probe.  It writes only CG scratch that every solve recomputes.
+template <typename R>
+void batch_probe(fea_batch* B, int wch) {
+    BArgs<R> a = make_bargs<R>(B);
+    a.probe = 1;
+    a.use_graph = 0;
+    a.cont = &B->flags->probe;
+    if (wch == 4) kb_init<R, 4><<<BGrids<R, 4>(B).init, kBlock, 0, B->stream>>>(a);
+    else kb_init<R, 8><<<BGrids<R, 8>(B).init, kBlock, 0, B->stream>>>(a);
+    FEA_CHECK_LAUNCH();
+}
+
+// Pick the window size of the CG kernels by timing the set-up SpMV.
+template <typename R>
+void autotune_batch(fea_batch* B) {
+    cudaEvent_t e0, e1;
+    FEA_CUDA_TRY(cudaEventCreate(&e0));
+    FEA_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int pick = 8;
+    for (int w : {4, 8}) {
+        for (int rep = 0; rep < 13; rep++) {
+            if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, B->stream));
+            batch_probe<R>(B, w);
+        }
+        FEA_CUDA_TRY(cudaEventRecord(e1, B->stream));
+        FEA_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FEA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            pick = w;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->wch = pick;
+}
+
+void check_batch(const fea_batch* B) {
+    if (!B) {
+        set_error("null batch handle");
+        throw Error{FEA_ERR_INVALID_ARGUMENT};
+    }
+    FEA_CUDA_TRY(cudaSetDevice(B->device));
+}
+
+void check_instance(const fea_batch* B, int i) {
+    if (i < 0 || i >= B->ninst) {
+        set_error("instance %d out of range [0, %d)", i, B->ninst);
+        throw Error{FEA_ERR_INVALID_ARGUMENT};
+    }
+}
+
+// A single-mesh handle per instance builds its boundary, pattern, solver
+// order and FP64 matrices; they are copied into the stacked arrays and the
+// handles released.
+struct InstanceHandles {
+    std::vector<fea_solver*> h;
+    ~InstanceHandles() {
+        for (fea_solver* p : h) fea_destroy(p);
+    }
+};
+
+template <typename R>
+void copy_instance(fea_batch* B, int i, fea_solver* h, const fea_instance_desc& d, int64_t row0, int64_t e0,
+                   int64_t nrows) {
+    const MeshView m = mesh_view(h);
+    cudaStream_t st = m.stream;
+    const int64_t n = m.N, nnz = m.Pc->nnz;
+    kb_copy_pattern<<<launch_grid(std::max(nrows, nnz)), kBlock, 0, st>>>(m.Pc->row_ptr, m.Pc->col, n, nrows, nnz,
+                                                                          row0, e0, B->rp, B->col);
+    FEA_CHECK_LAUNCH();
+    OpCoef<2> c{};
+    c.f[0] = {(double)d.time_step, (double)d.Du, 1.0, 0.0};
+    c.f[1] = {(double)d.time_step, (double)d.Dv, 1.0, 0.0};
+    combine_operator<R, 2>(*m.Pc, m.emap, m.M64, m.K64, m.Adv64, c, (FV<R, 2>*)B->A + e0, (FV<R, 2>*)B->dinv + row0,
+                           st);
+    round_copy<R>(m.M64, m.emap, nnz, (R*)B->M + e0, st);
+    kb_node_map<<<launch_grid(m.V), kBlock, 0, st>>>(m.idx_c, m.V, row0, B->node_map + B->node_off[i]);
+    FEA_CHECK_LAUNCH();
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+template <typename R>
+void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
+    InstanceHandles H;
+    H.h.assign(n, nullptr);
+    std::vector<int64_t> N(n), NNZ(n);
+    for (int i = 0; i < n; i++) {
+        const fea_instance_desc& d = inst[i];
+        fea_params prm;
+        fea_params_default(&prm);
+        prm.equation = FEA_REACTION_DIFFUSION;
+        prm.reaction_mode = 1;
+        prm.rd_time_step = d.time_step;
+        prm.rd_Du = d.Du;
+        prm.rd_Dv = d.Dv;
+        prm.rd_feed_rate = d.feed_rate;
+        prm.rd_kill_rate = d.kill_rate;
+        const int rc = fea_create(d.vertices, d.num_vertices, d.triangles, d.num_triangles, nullptr,
+                                  d.boundary_condition, B->precision, &prm, &H.h[i]);
+        if (rc != FEA_OK) throw Error{rc};
+        const MeshView m = mesh_view(H.h[i]);
+        N[i] = m.N;
+        NNZ[i] = m.Pc->nnz;
+    }
+    std::vector<int32_t> tile0(n + 1), tinst;
+    std::vector<int64_t> e0(n + 1);
+    B->V.resize(n);
+    B->node_off.resize(n + 1);
+    int64_t tiles = 0, nnz = 0, nodes = 0, vmax = 1;
+    for (int i = 0; i < n; i++) {
+        const int64_t nt = std::max<int64_t>(1, ceil_div(N[i], kTile));
+        tile0[i] = (int32_t)tiles;
+        e0[i] = nnz;
+        B->V[i] = inst[i].num_vertices;
+        B->node_off[i] = nodes;
+        for (int64_t t = 0; t < nt; t++) tinst.push_back(i);
+        tiles += nt;
+        nnz += NNZ[i];
+        nodes += inst[i].num_vertices;
+        vmax = std::max<int64_t>(vmax, inst[i].num_vertices);
+    }
+    tile0[n] = (int32_t)tiles;
+    e0[n] = nnz;
+    B->node_off[n] = nodes;
+    if (tiles * kTile >= (int64_t)INT32_MAX || nnz >= (int64_t)INT32_MAX) {
+        set_error("batch exceeds int32 indexing (%lld rows, %lld entries)", (long long)(tiles * kTile),
+                  (long long)nnz);
+        throw Error{FEA_ERR_TOO_LARGE};
+    }
+    B->ntiles = (int)tiles;
+    B->N = tiles * kTile;
+    B->nnz = nnz;
+    const int64_t Nr = B->N;
+    cudaStream_t st = B->stream;
+    B->rp = B->mem.alloc<int32_t>(Nr + 1);
+    B->col = B->mem.alloc<int32_t>(nnz);
+    B->tile_inst = B->mem.alloc<int32_t>(tiles);
+    B->inst_tile = B->mem.alloc<int32_t>(n + 1);
+    B->node_map = B->mem.alloc<int32_t>(nodes);
+    B->A = B->mem.alloc<FV<R, 2>>(nnz);
+    B->M = B->mem.alloc<R>(nnz);
+    B->dinv = B->mem.alloc<FV<R, 2>>(Nr);
+    B->x = B->mem.alloc<FV<R, 2>>(Nr);
+    B->b = B->mem.alloc<FV<R, 2>>(Nr);
+    B->z = B->mem.alloc<FV<R, 2>>(Nr);
+    B->p = B->mem.alloc<FV<R, 2>>(Nr);
+    B->rws = B->mem.alloc<FV<R, 2>>(6 * Nr);
+    B->prm = B->mem.alloc<BPrm>(n);
+    B->inst = B->mem.alloc<BInst>(n);
+    B->ctl = B->mem.alloc<BCtl>(1);
+    B->part = B->mem.alloc<double>(tiles * kNV);
+    B->iticket = B->mem.alloc<unsigned int>(n);
+    B->flags = B->mem.alloc<BFlags>(1);
+    B->staging = B->mem.alloc<float>(vmax);
+    const size_t fv = sizeof(FV<R, 2>);
+    for (auto zv : {std::make_pair(B->dinv, Nr), std::make_pair(B->x, Nr), std::make_pair(B->b, Nr),
+                    std::make_pair(B->z, Nr), std::make_pair(B->p, Nr), std::make_pair(B->rws, 6 * Nr)})
+        FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, fv * (size_t)zv.second, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->ctl, 0, sizeof(BCtl), st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->iticket, 0, sizeof(unsigned int) * n, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->flags, 0, sizeof(BFlags), st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->part, 0, sizeof(double) * tiles * kNV, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->tile_inst, tinst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->inst_tile, tile0.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    std::vector<BPrm> hp(n);
+    std::vector<BInst> hi(n);
+    for (int i = 0; i < n; i++) {
+        hp[i] = {(double)inst[i].time_step, (double)inst[i].feed_rate, (double)inst[i].kill_rate};
+        memset(&hi[i], 0, sizeof(BInst));
+        const int64_t lim = B->max_iter_cfg > 0 ? B->max_iter_cfg : 2 * N[i];
+        hi[i].max_iter = (int)std::min<int64_t>(std::max<int64_t>(lim, 1), 0x7fffffff);
+    }
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->prm, hp.data(), sizeof(BPrm) * n, cudaMemcpyHostToDevice, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->inst, hi.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice, st));
+    BCtl hc{};
+    hc.tol = B->tol;
+    hc.refine = 1;
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    // closing row pointer of the stacked matrix
+    const int32_t last = (int32_t)nnz;
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->rp + Nr, &last, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; i++) {
+        copy_instance<R>(B, i, H.h[i], inst[i], (int64_t)tile0[i] * kTile, e0[i],
+                         (int64_t)(tile0[i + 1] - tile0[i]) * kTile);
+        fea_destroy(H.h[i]);
+        H.h[i] = nullptr;
+    }
+    autotune_batch<R>(B);
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+}  // namespace
+}  // namespace fea
+
+#define BATCH_API_BEGIN try {
+#define BATCH_API_END                                                    \
+    }                                                                    \
+    catch (const fea::Error& e) {                                        \
+        return e.code;                                                   \
+    }                                                                    \
+    catch (const std::bad_alloc&) {                                      \
+        return fea::fail(FEA_ERR_OUT_OF_MEMORY, "host allocation failed"); \
+    }                                                                    \
+    catch (...) {                                                        \
+        return fea::fail(FEA_ERR_CUDA, "unexpected failure");            \
+    }                                                                    \
+    return FEA_OK;
 
 extern "C" {
-int fea_batch_create(const fea_instance_desc*, int, int, double, int, fea_batch** out) {
-    if (out) *out = nullptr;
-    return fea::fail(FEA_ERR_UNSUPPORTED, "batched solver not built yet");
+
+int fea_batch_create(const fea_instance_desc* instances, int num_instances, int precision, double cg_tolerance,
+                     int cg_max_iterations, fea_batch** out) {
+    if (!out) return fail(FEA_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (!instances || num_instances <= 0) return fail(FEA_ERR_INVALID_ARGUMENT, "no instances");
+    if (precision != FEA_FP32 && precision != FEA_FP64) return fail(FEA_ERR_INVALID_ARGUMENT, "bad precision");
+    for (int i = 0; i < num_instances; i++) {
+        const fea_instance_desc& d = instances[i];
+        if (!d.vertices || !d.triangles || d.num_vertices <= 0 || d.num_triangles <= 0)
+            return fail(FEA_ERR_BAD_MESH, "instance mesh must have vertices and triangles");
+        if (!(d.time_step > 0.f)) return fail(FEA_ERR_INVALID_ARGUMENT, "instance time step must be positive");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FEA_ERR_NO_DEVICE, "no CUDA device");
+    fea_batch* B = nullptr;
+    try {
+        B = new fea_batch();
+        FEA_CUDA_TRY(cudaGetDevice(&B->device));
+        FEA_CUDA_TRY(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+        B->precision = precision;
+        B->ninst = num_instances;
+        B->tol = cg_tolerance > 0.0 ? cg_tolerance : (precision == FEA_FP64 ? 1e-10 : 1.1920928955078125e-07);
+        B->max_iter_cfg = cg_max_iterations;
+        const char* mode = getenv("FEA_LAUNCH_MODE");
+        B->stream_mode = mode && strcmp(mode, "stream") == 0;
+        if (precision == FEA_FP64) create_batch<double>(B, instances, num_instances);
+        else create_batch<float>(B, instances, num_instances);
+        *out = B;
+        return FEA_OK;
+    } catch (const fea::Error& e) {
+        if (B) fea_batch_destroy(B);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        if (B) fea_batch_destroy(B);
+        return fail(FEA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        if (B) fea_batch_destroy(B);
+        return fail(FEA_ERR_CUDA, "unexpected failure");
+    }
 }
-int fea_batch_destroy(fea_batch*) { return FEA_OK; }
-int fea_batch_set_fields(fea_batch*, int, const float*, const float*) { return FEA_ERR_UNSUPPORTED; }
-int fea_batch_get_fields(fea_batch*, int, float*, float*) { return FEA_ERR_UNSUPPORTED; }
-int fea_batch_advance_time(fea_batch*, int64_t) { return FEA_ERR_UNSUPPORTED; }
-int fea_batch_synchronize(fea_batch*) { return FEA_ERR_UNSUPPORTED; }
-int fea_batch_get_status(fea_batch*, uint32_t*, int32_t*) { return FEA_ERR_UNSUPPORTED; }
+
+int fea_batch_destroy(fea_batch* B) {
+    if (!B) return FEA_OK;
+    cudaSetDevice(B->device);
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    B->graph.destroy();
+    B->mem.release();
+    if (B->stream) cudaStreamDestroy(B->stream);
+    delete B;
+    return FEA_OK;
 }
+
+int fea_batch_set_fields(fea_batch* B, int instance, const float* u, const float* v) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    check_instance(B, instance);
+    const int64_t V = B->V[instance];
+    const int32_t* map = B->node_map + B->node_off[instance];
+    const float* src[2] = {u, v};
+    for (int f = 0; f < 2; f++) {
+        if (!src[f]) continue;
+        FEA_CUDA_TRY(cudaMemcpyAsync(B->staging, src[f], sizeof(float) * V, cudaMemcpyHostToDevice, B->stream));
+        if (B->precision == FEA_FP64)
+            kb_gather<double><<<launch_grid(V), kBlock, 0, B->stream>>>(B->staging, map, V, (FV<double, 2>*)B->x, f);
+        else
+            kb_gather<float><<<launch_grid(V), kBlock, 0, B->stream>>>(B->staging, map, V, (FV<float, 2>*)B->x, f);
+        FEA_CHECK_LAUNCH();
+    }
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    BATCH_API_END
+}
+
+int fea_batch_get_fields(fea_batch* B, int instance, float* u, float* v) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    check_instance(B, instance);
+    const int64_t V = B->V[instance];
+    const int32_t* map = B->node_map + B->node_off[instance];
+    float* dst[2] = {u, v};
+    for (int f = 0; f < 2; f++) {
+        if (!dst[f]) continue;
+        if (B->precision == FEA_FP64)
+            kb_scatter<double><<<launch_grid(V), kBlock, 0, B->stream>>>((const FV<double, 2>*)B->x, map, V,
+                                                                          B->staging, f);
+        else
+            kb_scatter<float><<<launch_grid(V), kBlock, 0, B->stream>>>((const FV<float, 2>*)B->x, map, V,
+                                                                         B->staging, f);
+        FEA_CHECK_LAUNCH();
+        FEA_CUDA_TRY(cudaMemcpyAsync(dst[f], B->staging, sizeof(float) * V, cudaMemcpyDeviceToHost, B->stream));
+        FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    }
+    BATCH_API_END
+}
+
+int fea_batch_advance_time(fea_batch* B, int64_t nsteps) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    if (nsteps < 0) return fail(FEA_ERR_INVALID_ARGUMENT, "negative step count");
+    if (nsteps == 0) return FEA_OK;
+    long long ctl[2] = {nsteps, 0};  // steps_left, steps_done
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->ctl, ctl, sizeof(ctl), cudaMemcpyHostToDevice, B->stream));
+    kb_clear<<<launch_grid(B->ninst), kBlock, 0, B->stream>>>(B->inst, B->ninst);
+    FEA_CHECK_LAUNCH();
+    if (B->precision == FEA_FP64) run_batch<double>(B);
+    else run_batch<float>(B);
+    BATCH_API_END
+}
+
+int fea_batch_synchronize(fea_batch* B) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    BATCH_API_END
+}
+
+int fea_batch_get_status(fea_batch* B, uint32_t* flags, int32_t* iterations) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    const int n = B->ninst;
+    std::vector<BInst> h(n);
+    FEA_CUDA_TRY(cudaMemcpyAsync(h.data(), B->inst, sizeof(BInst) * n, cudaMemcpyDeviceToHost, B->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    for (int i = 0; i < n; i++) {
+        if (flags) flags[i] = h[i].flags;
+        if (iterations) {
+            iterations[2 * i] = h[i].last_iters[0];
+            iterations[2 * i + 1] = h[i].last_iters[1];
+        }
+    }
+    BATCH_API_END
+}
+
+}  // extern "C"

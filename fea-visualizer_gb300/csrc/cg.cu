@@ -18,57 +18,11 @@
 #include <algorithm>
 #include <cmath>
 
-#include "fea_internal.cuh"
+#include "cg_device.cuh"
 
 namespace fea {
 
 namespace {
-
-// ---- accumulators -------------------------------------------------------------
-template <typename R>
-struct Acc;
-
-template <>
-struct Acc<double> {
-    double s = 0.0;
-    __device__ __forceinline__ void add(double x) { s += x; }
-    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
-    __device__ __forceinline__ void sub(const Acc& o) { s -= o.s; }
-    __device__ __forceinline__ double value() const { return s; }
-    __device__ __forceinline__ void shfl_add(int off) { s += __shfl_xor_sync(0xffffffffu, s, off); }
-};
-
-// float-float: value = hi + lo with |lo| <= ulp(hi)/2 (Knuth two-sum plus the
-// exact product error from fma); intrinsics keep the compiler from fusing.
-template <>
-struct Acc<float> {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        const float s = __fadd_rn(hi, x);
-        const float bb = __fsub_rn(s, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
-        const float l = __fadd_rn(lo, err);
-        hi = __fadd_rn(s, l);
-        lo = __fsub_rn(l, __fsub_rn(hi, s));
-    }
-    __device__ __forceinline__ void add_prod(float a, float b) {
-        const float p = __fmul_rn(a, b);
-        const float e = __fmaf_rn(a, b, -p);
-        add(p);
-        lo = __fadd_rn(lo, e);
-    }
-    __device__ __forceinline__ void sub(const Acc& o) {
-        add(-o.hi);
-        lo = __fsub_rn(lo, o.lo);
-    }
-    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-    __device__ __forceinline__ void shfl_add(int off) {
-        const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
-        const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
-        add(oh);
-        lo = __fadd_rn(lo, ol);
-    }
-};
 
 // Block reduction of NV accumulators, then the grid-wide last-block step.
 // Returns true in the last block, with totals in out[] valid in thread 0.
@@ -98,62 +52,6 @@ __device__ __forceinline__ bool grid_reduce(Acc<R> (&acc)[NV], double* part, int
     return last_block_commit<NV>(x, part, stride, ticket, sm, out);
 }
 
-// Loop condition: stored for host-driven loops, and set on the graph's
-// conditional node when the kernel runs inside the step graph.  Called by one
-// thread only (concurrent cudaGraphSetConditional calls are undefined).
-template <typename A>
-__device__ __forceinline__ void signal_loop(const A& a, bool cont) {
-    *a.cont = cont ? 1 : 0;
-    if (a.use_graph) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
-}
-
-__device__ __forceinline__ void raise_flags(RunState* run, unsigned int f) {
-    const unsigned int w = __reduce_or_sync(0xffffffffu, f);
-    if (w && (threadIdx.x & 31) == 0) {
-        atomicOr(&run->flags, w);
-        __threadfence();
-    }
-}
-
-template <typename R>
-__device__ __forceinline__ unsigned int check_value(R x) {
-    unsigned int f = 0;
-    if (x > (R)1e4f) f |= FEA_STATUS_BLOWUP;  // CPUSolver.cpp:43
-    if (!isfinite(x)) f |= FEA_STATUS_NONFINITE;
-    return f;
-}
-
-template <typename R>
-__device__ __forceinline__ R ldg(const R* p) {
-    return __ldg(p);
-}
-// Load of a 4-, 8- or 16-byte value: through the read-only cache, or from L2
-// only (l2only) for data that other blocks of the running kernel wrote.
-template <typename T>
-__device__ __forceinline__ T ldv(const T* p, bool l2only) {
-    T o;
-    if constexpr (sizeof(T) == 4) {
-        const float* q = reinterpret_cast<const float*>(p);
-        const float t = l2only ? __ldcg(q) : __ldg(q);
-        memcpy(&o, &t, 4);
-    } else if constexpr (sizeof(T) == 8) {
-        const float2* q = reinterpret_cast<const float2*>(p);
-        const float2 t = l2only ? __ldcg(q) : __ldg(q);
-        memcpy(&o, &t, 8);
-    } else {
-        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
-        const float4* q = reinterpret_cast<const float4*>(p);
-        const float4 t = l2only ? __ldcg(q) : __ldg(q);
-        memcpy(&o, &t, 16);
-    }
-    return o;
-}
-
-template <typename R, int NF>
-__device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
-    return ldv(p, false);
-}
-
 // Threads are grouped LANES per CSR row; a warp covers 32/LANES consecutive
 // rows per pass, so its loads of values and column indices are contiguous.
 template <int LANES>
@@ -170,239 +68,6 @@ struct RowMap {
     }
 };
 
-// ---- CSR SpMV building blocks ------------------------------------------------------
-//
-// Every kernel reads vectors that earlier launches wrote, so the read-only
-// path (LoadRO) is valid for all of them.
-
-struct LoadRO {
-    template <typename T>
-    static __device__ __forceinline__ T ld(const T* p) {
-        return ldv<T>(p, false);
-    }
-};
-
-// Control values of one phase, read once per phase by every thread.
-template <typename R, int NF>
-struct PhaseCtl {
-    int par;          // iteration parity: p_old = pp[par], p_new = pp[par ^ 1]
-    int act[NF];
-    bool fresh[NF];
-    bool need_old;
-    bool any;
-    R beta[NF], alpha[NF];
-    __device__ __forceinline__ void load(const CgState* cg) {
-        const volatile CgState* v = cg;
-        par = v->iter & 1;
-        need_old = false;
-        any = false;
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            act[f] = v->active[f];
-            fresh[f] = v->fresh[f] != 0;
-            beta[f] = fresh[f] ? (R)0 : (R)v->beta[f];
-            alpha[f] = act[f] ? (R)v->alpha[f] : (R)0;
-            need_old |= !fresh[f];
-            any |= act[f] != 0;
-        }
-    }
-};
-
-// q = A p_new with p_new = z + beta p_old computed for every gathered column
-// (the direction update of the previous iteration, fused; the two p buffers
-// alternate with the iteration parity), plus p_new.q into dot[].
-//
-// Warp-cooperative CSR: a warp owns 32 consecutive rows, whose stored entries
-// form one contiguous range.  The warp streams that range in windows of
-// 32*WCH entries: every lane issues WCH coalesced value/column loads, then WCH
-// independent gathers, so each round trip to memory carries a whole window
-// rather than one row.  Products go to shared memory and each lane sums its
-// own row in column order.
-template <typename R, int NF, int WCH, typename LP>
-__device__ __forceinline__ void spmv_phase(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c,
-                                           FV<R, NF> (*sm)[32 * WCH], Acc<R> (&dot)[NF]) {
-    constexpr int WIN = 32 * WCH;
-    const FV<R, NF>* pold = a.pp[c.par];
-    FV<R, NF>* pnew = a.pp[c.par ^ 1];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t N = a.N;
-    for (int64_t r0 = warp * 32; r0 < N; r0 += nwarps * 32) {
-        const int64_t row = r0 + lane;
-        const int32_t rs = ldg(a.rp + (row < N ? row : N));
-        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
-        if (lane == 31) re = ldg(a.rp + (r0 + 32 < N ? r0 + 32 : N));
-        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
-        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
-        R acc[NF];
-#pragma unroll
-        for (int f = 0; f < NF; f++) acc[f] = 0;
-        for (int32_t wb = e0; wb < e1; wb += WIN) {
-            FV<R, NF> av[WCH];
-            int32_t cc[WCH];
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                const int32_t idx = wb + k * 32 + lane;
-                cc[k] = -1;
-                if (idx < e1) {
-                    av[k] = ldv(a.A + idx, false);
-                    cc[k] = ldg(a.col + idx);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                FV<R, NF> prod;
-#pragma unroll
-                for (int f = 0; f < NF; f++) prod.v[f] = 0;
-                if (cc[k] >= 0) {
-                    const FV<R, NF> zc = LP::ld(a.z + cc[k]);
-                    FV<R, NF> pc = zc;
-                    if (c.need_old) pc = LP::ld(pold + cc[k]);
-#pragma unroll
-                    for (int f = 0; f < NF; f++) {
-                        const R pn = c.fresh[f] ? zc.v[f] : fma(c.beta[f], pc.v[f], zc.v[f]);
-                        prod.v[f] = av[k].v[f] * pn;
-                    }
-                }
-                sm[wib][k * 32 + lane] = prod;
-            }
-            __syncwarp();
-            const int32_t lo = (rs > wb ? rs : wb) - wb;
-            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
-            for (int32_t k = lo; k < hi; k++) {
-                const FV<R, NF> t = sm[wib][k];
-#pragma unroll
-                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
-            }
-            __syncwarp();
-        }
-        if (row < N) {
-            const FV<R, NF> zr = LP::ld(a.z + row);
-            FV<R, NF> pr = zr, qv;
-            if (c.need_old) pr = LP::ld(pold + row);
-#pragma unroll
-            for (int f = 0; f < NF; f++) {
-                const R pn = c.fresh[f] ? zr.v[f] : fma(c.beta[f], pr.v[f], zr.v[f]);
-                pr.v[f] = pn;
-                qv.v[f] = acc[f];
-                dot[f].add_prod(pn, acc[f]);
-            }
-            pnew[row] = pr;
-            a.q[row] = qv;
-        }
-    }
-}
-
-// After the SpMV phase: alpha = r.z / p.q, or breakdown.
-template <typename R, int NF>
-__device__ void finish_spmv(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        if (!act[f]) continue;
-        cg->pq[f] = tot[f];
-        const double al = cg->rz[f] / tot[f];
-        if (!(tot[f] > 0.0) || !isfinite(al)) {
-            cg->active[f] = 0;
-            cg->iters[f] = cg->iter;
-            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
-        } else {
-            cg->alpha[f] = al;
-        }
-    }
-}
-
-// After a Chronopoulos-Gear iteration: convergence |r|^2 < tol^2 |b|^2, then
-// beta = gamma'/gamma and alpha = gamma' / (delta' - beta gamma'/alpha) for
-// the next iteration; iteration count and the max_iter limit.  tot holds
-// gamma' = r.u, delta' = w.u and r.r per field.  Returns whether another
-// iteration runs.
-template <typename R, int NF>
-__device__ bool finish_cgcg(volatile CgState* cg, RunState* run, const int (&act)[NF], const double* tot) {
-    const int it = cg->iter + 1;
-    cg->iter = it;
-    int any = 0;
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        cg->fresh[f] = 0;
-        if (!act[f]) continue;
-        const double g = tot[f], d = tot[NF + f], rr = tot[2 * NF + f];
-        cg->rr[f] = rr;
-        if (!isfinite(rr)) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
-            continue;
-        }
-        if (rr < cg->thr[f]) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            continue;
-        }
-        const double beta = g / cg->rz[f];
-        const double den = d - beta * g / cg->alpha[f];
-        const double alpha = g / den;
-        if (!(den > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            atomicOr(&run->flags, FEA_STATUS_BREAKDOWN);
-            continue;
-        }
-        cg->beta[f] = beta;
-        cg->alpha[f] = alpha;
-        cg->rz[f] = g;
-        any = 1;
-    }
-    const bool cont = any && it < cg->max_iter;
-    if (any && !cont) {
-        atomicOr(&run->flags, FEA_STATUS_NOT_CONVERGED);
-#pragma unroll
-        for (int f = 0; f < NF; f++)
-            if (cg->active[f]) {
-                cg->active[f] = 0;
-                cg->iters[f] = it;
-            }
-    }
-    return cont;
-}
-
-template <int NV, typename R>
-__device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, double (&blk)[NV]) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
-        if (lane == 0) sm[wid * NV + k] = acc[k].value();
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < NV; k++) blk[k] = 0.0;
-    if (threadIdx.x == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        for (int w = 0; w < nw; w++)
-#pragma unroll
-            for (int k = 0; k < NV; k++) blk[k] += sm[w * NV + k];
-    }
-    __syncthreads();
-}
-
-// ---- standalone kernels (autotuning and timing probes) -------------------------------
-
-template <typename R, int NF, int WCH>
-__global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs<R, NF> a) {
-    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
-    __shared__ double red[32 * NF];
-    PhaseCtl<R, NF> c;
-    c.load(a.cg);
-    Acc<R> dot[NF];
-    spmv_phase<R, NF, WCH, LoadRO>(a, c, sm, dot);
-    double blk[NF], tot[NF];
-    block_totals<NF>(dot, red, blk);
-    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0)
-        finish_spmv<R, NF>(a.cg, a.run, c.act, tot);
-}
-
 // ---- Chronopoulos-Gear iteration -----------------------------------------------------
 //
 // Jacobi-preconditioned CG rearranged (Chronopoulos & Gear, 1989) so that one
@@ -416,29 +81,25 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cg_spmv(StepArgs
 // w and s there (so r, w and s alternate between two buffers).
 
 // Set-up of a solve: w0 = A z (z = D^-1 r0 from k_rhs / k_refine), delta0 =
-// z.w0 and alpha0 = r0.z / delta0.  The SpMV of the probe kernel with p = z.
+// z.w0 and alpha0 = r0.z / delta0.
 template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ double red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
-    c.need_old = false;
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-        c.fresh[f] = true;
-        c.beta[f] = 0;
-    }
-    StepArgs<R, NF> v = a;
-    v.pp[c.par ^ 1] = a.pp[0];
-    v.q = a.wb[c.par];
+    FV<R, NF>* w = a.wb[c.par];
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     Acc<R> dot[NF];
-    spmv_phase<R, NF, WCH, LoadRO>(v, c, sm, dot);
+    for (int64_t row0 = warp * 32; row0 < a.N; row0 += nwarps * 32)
+        init_rows<R, NF, WCH>(a.rp, a.col, a.A, a.z, w, row0, a.N, sm[wib], dot);
     double blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
     if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
         volatile CgState* cg = a.cg;
-        finish_spmv<R, NF>(cg, a.run, c.act, tot);
+        finish_spmv<R, NF>(cg, &a.run->flags, c.act, tot);
         int any = 0;
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -451,112 +112,33 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
 
 template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
-    constexpr int WIN = 32 * WCH;
-    __shared__ FV<R, NF> sm[kBlock / 32][WIN];
+    __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ double red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
-    const FV<R, NF>* __restrict__ r0 = a.rb[c.par];
-    const FV<R, NF>* __restrict__ w0 = a.wb[c.par];
-    const FV<R, NF>* __restrict__ s0 = a.sb[c.par];
-    FV<R, NF>* __restrict__ r1 = a.rb[c.par ^ 1];
-    FV<R, NF>* __restrict__ w1 = a.wb[c.par ^ 1];
-    FV<R, NF>* __restrict__ s1 = a.sb[c.par ^ 1];
-    // new residual and preconditioned residual of one unknown from its old r, w, s
-    auto advance = [&](const FV<R, NF>& ro, const FV<R, NF>& wo, const FV<R, NF>& so, const FV<R, NF>& d,
-                       FV<R, NF>& sn, FV<R, NF>& rn, FV<R, NF>& un) {
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            sn.v[f] = c.fresh[f] ? wo.v[f] : fma(c.beta[f], so.v[f], wo.v[f]);
-            rn.v[f] = c.act[f] ? fma(-c.alpha[f], sn.v[f], ro.v[f]) : ro.v[f];
-            un.v[f] = d.v[f] * rn.v[f];
-        }
-    };
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[c.par];
+    v.w0 = a.wb[c.par];
+    v.s0 = a.sb[c.par];
+    v.r1 = a.rb[c.par ^ 1];
+    v.w1 = a.wb[c.par ^ 1];
+    v.s1 = a.sb[c.par ^ 1];
+    const int wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t N = a.N;
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
-    for (int64_t row0 = warp * 32; row0 < N; row0 += nwarps * 32) {
-        const int64_t row = row0 + lane;
-        const int32_t rs = ldg(a.rp + (row < N ? row : N));
-        int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
-        if (lane == 31) re = ldg(a.rp + (row0 + 32 < N ? row0 + 32 : N));
-        const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
-        const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
-        R acc[NF];
-#pragma unroll
-        for (int f = 0; f < NF; f++) acc[f] = 0;
-        for (int32_t wb = e0; wb < e1; wb += WIN) {
-            FV<R, NF> av[WCH];
-            int32_t cc[WCH];
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                const int32_t idx = wb + k * 32 + lane;
-                cc[k] = -1;
-                if (idx < e1) {
-                    av[k] = ldv(a.A + idx, false);
-                    cc[k] = ldg(a.col + idx);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < WCH; k++) {
-                FV<R, NF> prod;
-#pragma unroll
-                for (int f = 0; f < NF; f++) prod.v[f] = 0;
-                if (cc[k] >= 0) {
-                    const int32_t col = cc[k];
-                    const FV<R, NF> ro = ldv(r0 + col, false), wo = ldv(w0 + col, false);
-                    const FV<R, NF> d = ldv(a.dinv + col, false);
-                    FV<R, NF> so = wo;
-                    if (c.need_old) so = ldv(s0 + col, false);
-                    FV<R, NF> sn, rn, un;
-                    advance(ro, wo, so, d, sn, rn, un);
-#pragma unroll
-                    for (int f = 0; f < NF; f++) prod.v[f] = av[k].v[f] * un.v[f];
-                }
-                sm[wib][k * 32 + lane] = prod;
-            }
-            __syncwarp();
-            const int32_t lo = (rs > wb ? rs : wb) - wb;
-            const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
-            for (int32_t k = lo; k < hi; k++) {
-                const FV<R, NF> t = sm[wib][k];
-#pragma unroll
-                for (int f = 0; f < NF; f++) acc[f] += t.v[f];
-            }
-            __syncwarp();
-        }
-        if (row < N) {
-            const FV<R, NF> ro = ldv(r0 + row, false), wo = ldv(w0 + row, false), d = ldv(a.dinv + row, false);
-            FV<R, NF> so = wo;
-            if (c.need_old) so = ldv(s0 + row, false);
-            FV<R, NF> x = a.x[row], p = a.pp[0][row];
-            FV<R, NF> sn, rn, un, wn;
-            advance(ro, wo, so, d, sn, rn, un);
-#pragma unroll
-            for (int f = 0; f < NF; f++) {
-                if (c.act[f]) {
-                    const R ui = d.v[f] * ro.v[f];
-                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
-                }
-                wn.v[f] = acc[f];
-                dots[f].add_prod(rn.v[f], un.v[f]);
-                dots[NF + f].add_prod(wn.v[f], un.v[f]);
-                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
-            }
-            a.x[row] = x;
-            a.pp[0][row] = p;
-            r1[row] = rn;
-            s1[row] = sn;
-            w1[row] = wn;
-        }
-    }
+    for (int64_t row0 = warp * 32; row0 < a.N; row0 += nwarps * 32)
+        cgcg_rows<R, NF, WCH>(v, c, row0, a.N, sm[wib], dots);
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
-        signal_loop(a, finish_cgcg<R, NF>(a.cg, a.run, c.act, tot));
+        signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
@@ -820,48 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
 
 // ---- graph construction ----------------------------------------------------------
 
-template <typename... P>
-cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
-                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
-    auto local = arg;
-    void* argv[] = {(void*)&local};
-    cudaKernelNodeParams kp = {};
-    kp.func = (void*)fn;
-    kp.gridDim = dim3((unsigned)grid);
-    kp.blockDim = dim3((unsigned)block);
-    kp.sharedMemBytes = 0;
-    kp.kernelParams = argv;
-    cudaGraphNode_t n;
-    FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
-    return n;
-}
-
-cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraph_t* body) {
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t n;
-    FEA_CUDA_TRY(cudaGraphAddNode(&n, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, &np));
-    *body = np.conditional.phGraph_out[0];
-    return n;
-}
-
 int g_max_grid = 0;
-
-// Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
-// calculator), capped by the work and by the partial-sum stride.
-template <typename K>
-int wave_grid(K kernel, int64_t work_blocks) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    int64_t g = (int64_t)num_sms() * per_sm;
-    if (g > max_grid_blocks()) g = max_grid_blocks();
-    if (g > work_blocks) g = work_blocks;
-    return (int)(g < 1 ? 1 : g);
-}
 
 constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
@@ -1014,12 +555,31 @@ void run_steps_stream(const StepArgs<R, NF>& a, int kind, int wch, LoopFlags* lf
     dispatch_kind<R, NF>(nullptr, a, kind, wch, lf, st);
 }
 
+// Probe state: every field masked, so an iteration writes x and p back
+// unchanged and leaves only CG scratch behind, while keeping the loads and
+// stores of a steady-state iteration (fresh = 0: the old s is gathered too).
+template <typename R, int NF>
+__global__ void k_probe_state(CgState* cg) {
+    for (int f = 0; f < NF; f++) {
+        cg->active[f] = 0;
+        cg->fresh[f] = 0;
+        cg->alpha[f] = 0.0;
+        cg->beta[f] = 0.0;
+    }
+}
+
+template <typename R, int NF>
+void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st) {
+    k_probe_state<R, NF><<<1, 1, 0, st>>>(a.cg);
+    FEA_CHECK_LAUNCH();
+}
+
 template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     switch (wch) {
-    case 4: k_cg_spmv<R, NF, 4><<<Grids<R, NF, 4>(a.N).spmv, kBlock, 0, st>>>(a); break;
-    case 16: k_cg_spmv<R, NF, 16><<<Grids<R, NF, 16>(a.N).spmv, kBlock, 0, st>>>(a); break;
-    default: k_cg_spmv<R, NF, 8><<<Grids<R, NF, 8>(a.N).spmv, kBlock, 0, st>>>(a); break;
+    case 4: k_cgcg_iter<R, NF, 4><<<Grids<R, NF, 4>(a.N).iter, kBlock, 0, st>>>(a); break;
+    case 16: k_cgcg_iter<R, NF, 16><<<Grids<R, NF, 16>(a.N).iter, kBlock, 0, st>>>(a); break;
+    default: k_cgcg_iter<R, NF, 8><<<Grids<R, NF, 8>(a.N).iter, kBlock, 0, st>>>(a); break;
     }
     FEA_CHECK_LAUNCH();
 }
@@ -1027,7 +587,8 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
 #define FEA_INST_STEP(R, NF)                                                                              \
     template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \
     template void run_steps_stream<R, NF>(const StepArgs<R, NF>&, int, int, LoopFlags*, cudaStream_t);    \
-    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t);
+    template void launch_spmv_probe<R, NF>(const StepArgs<R, NF>&, int, cudaStream_t);                 \
+    template void prepare_probe<R, NF>(const StepArgs<R, NF>&, cudaStream_t);
 FEA_INST_STEP(float, 1)
 FEA_INST_STEP(float, 2)
 FEA_INST_STEP(double, 1)

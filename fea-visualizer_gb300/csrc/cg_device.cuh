@@ -1,0 +1,443 @@
+// cg_device.cuh -- device building blocks shared by the single-mesh and the
+// batched step loops: exact accumulators for FP32 inner products, cached and
+// L2-only vector loads, block totals, loop signalling, and graph-node helpers.
+#pragma once
+
+#include <tuple>
+
+#include "fea_internal.cuh"
+
+namespace fea {
+namespace {
+
+// ---- accumulators -------------------------------------------------------------
+template <typename R>
+struct Acc;
+
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ void sub(const Acc& o) { s -= o.s; }
+    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ void shfl_add(int off) { s += __shfl_xor_sync(0xffffffffu, s, off); }
+};
+
+// float-float: value = hi + lo with |lo| <= ulp(hi)/2 (Knuth two-sum plus the
+// exact product error from fma); intrinsics keep the compiler from fusing.
+template <>
+struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        const float l = __fadd_rn(lo, err);
+        hi = __fadd_rn(s, l);
+        lo = __fsub_rn(l, __fsub_rn(hi, s));
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        const float e = __fmaf_rn(a, b, -p);
+        add(p);
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ void sub(const Acc& o) {
+        add(-o.hi);
+        lo = __fsub_rn(lo, o.lo);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ void shfl_add(int off) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+        add(oh);
+        lo = __fadd_rn(lo, ol);
+    }
+};
+
+// Loop condition: stored for host-driven loops, and set on the graph's
+// conditional node when the kernel runs inside the step graph.  Called by one
+// thread only (concurrent cudaGraphSetConditional calls are undefined).
+template <typename A>
+__device__ __forceinline__ void signal_loop(const A& a, bool cont) {
+    *a.cont = cont ? 1 : 0;
+    if (a.use_graph) cudaGraphSetConditional(a.cond, cont ? 1u : 0u);
+}
+
+__device__ __forceinline__ void raise_flags(RunState* run, unsigned int f) {
+    const unsigned int w = __reduce_or_sync(0xffffffffu, f);
+    if (w && (threadIdx.x & 31) == 0) {
+        atomicOr(&run->flags, w);
+        __threadfence();
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ unsigned int check_value(R x) {
+    unsigned int f = 0;
+    if (x > (R)1e4f) f |= FEA_STATUS_BLOWUP;  // CPUSolver.cpp:43
+    if (!isfinite(x)) f |= FEA_STATUS_NONFINITE;
+    return f;
+}
+
+template <typename R>
+__device__ __forceinline__ R ldg(const R* p) {
+    return __ldg(p);
+}
+// Load of a 4-, 8- or 16-byte value: through the read-only cache, or from L2
+// only (l2only) for data that other blocks of the running kernel wrote.
+template <typename T>
+__device__ __forceinline__ T ldv(const T* p, bool l2only) {
+    T o;
+    if constexpr (sizeof(T) == 4) {
+        const float* q = reinterpret_cast<const float*>(p);
+        const float t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        const float2* q = reinterpret_cast<const float2*>(p);
+        const float2 t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 8);
+    } else {
+        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
+        const float4* q = reinterpret_cast<const float4*>(p);
+        const float4 t = l2only ? __ldcg(q) : __ldg(q);
+        memcpy(&o, &t, 16);
+    }
+    return o;
+}
+
+template <typename R, int NF>
+__device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
+    return ldv(p, false);
+}
+
+template <int NV, typename R>
+__device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, double (&blk)[NV]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
+        if (lane == 0) sm[wid * NV + k] = acc[k].value();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) blk[k] = 0.0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < nw; w++)
+#pragma unroll
+            for (int k = 0; k < NV; k++) blk[k] += sm[w * NV + k];
+    }
+    __syncthreads();
+}
+
+// ---- CG building blocks ----------------------------------------------------------
+
+// Control values of one CG phase, read once per phase by every thread.
+template <typename R, int NF>
+struct PhaseCtl {
+    int par;  // iteration parity: which of the alternating buffers holds the old values
+    int act[NF];
+    bool fresh[NF];  // first iteration of a loop: p = u, s = w
+    bool need_old;
+    bool any;
+    R beta[NF], alpha[NF];
+    template <typename S>
+    __device__ __forceinline__ void set(int iter, const volatile S* st) {
+        par = iter & 1;
+        need_old = false;
+        any = false;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            act[f] = st->active[f];
+            fresh[f] = st->fresh[f] != 0;
+            beta[f] = fresh[f] ? (R)0 : (R)st->beta[f];
+            alpha[f] = act[f] ? (R)st->alpha[f] : (R)0;
+            need_old |= !fresh[f];
+            any |= act[f] != 0;
+        }
+    }
+    __device__ __forceinline__ void load(const CgState* cg) {
+        const volatile CgState* v = cg;
+        set(v->iter, v);
+    }
+};
+
+// Warp-cooperative CSR product over the warp's 32 consecutive rows row0 ..
+// row0+31 (rows >= N are empty): lane l returns sum_e A_e * g(col_e) of row
+// row0 + l, per field.  The rows' stored entries form one contiguous range,
+// streamed in windows of 32*WCH entries: every lane issues WCH coalesced
+// value/column loads, then WCH independent gathers g(col), so each round trip
+// to memory carries a whole window rather than one row.  Products go to the
+// warp's shared-memory window smw[32*WCH] and each lane sums its own row in
+// column order.
+template <typename R, int NF, int WCH, typename G>
+__device__ __forceinline__ FV<R, NF> warp_rows(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                               const FV<R, NF>* __restrict__ A, int64_t row0, int64_t N,
+                                               FV<R, NF>* smw, G g) {
+    constexpr int WIN = 32 * WCH;
+    const int lane = threadIdx.x & 31;
+    const int64_t row = row0 + lane;
+    const int32_t rs = ldg(rp + (row < N ? row : N));
+    int32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+    if (lane == 31) re = ldg(rp + (row0 + 32 < N ? row0 + 32 : N));
+    const int32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+    const int32_t e1 = __shfl_sync(0xffffffffu, re, 31);
+    FV<R, NF> acc;
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc.v[f] = 0;
+    for (int32_t wb = e0; wb < e1; wb += WIN) {
+        FV<R, NF> av[WCH];
+        int32_t cc[WCH];
+#pragma unroll
+        for (int k = 0; k < WCH; k++) {
+            const int32_t idx = wb + k * 32 + lane;
+            cc[k] = -1;
+            if (idx < e1) {
+                av[k] = ldv(A + idx, false);
+                cc[k] = ldg(col + idx);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < WCH; k++) {
+            FV<R, NF> prod;
+#pragma unroll
+            for (int f = 0; f < NF; f++) prod.v[f] = 0;
+            if (cc[k] >= 0) {
+                const FV<R, NF> gv = g(cc[k]);
+#pragma unroll
+                for (int f = 0; f < NF; f++) prod.v[f] = av[k].v[f] * gv.v[f];
+            }
+            smw[k * 32 + lane] = prod;
+        }
+        __syncwarp();
+        const int32_t lo = (rs > wb ? rs : wb) - wb;
+        const int32_t hi = (re < wb + WIN ? re : wb + WIN) - wb;
+        for (int32_t k = lo; k < hi; k++) {
+            const FV<R, NF> t = smw[k];
+#pragma unroll
+            for (int f = 0; f < NF; f++) acc.v[f] += t.v[f];
+        }
+        __syncwarp();
+    }
+    return acc;
+}
+
+// Set-up product of a Chronopoulos-Gear solve on one warp's rows: w = A z and
+// z.w into dot[] (delta0).
+template <typename R, int NF, int WCH>
+__device__ __forceinline__ void init_rows(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                          const FV<R, NF>* __restrict__ A, const FV<R, NF>* __restrict__ z,
+                                          FV<R, NF>* __restrict__ w, int64_t row0, int64_t N, FV<R, NF>* smw,
+                                          Acc<R> (&dot)[NF]) {
+    const FV<R, NF> wr =
+        warp_rows<R, NF, WCH>(rp, col, A, row0, N, smw, [&](int32_t c) { return ldv(z + c, false); });
+    const int64_t row = row0 + (threadIdx.x & 31);
+    if (row < N) {
+        const FV<R, NF> zr = ldv(z + row, false);
+#pragma unroll
+        for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
+        w[row] = wr;
+    }
+}
+
+// The vectors of one Chronopoulos-Gear iteration: r, w and s alternate
+// between two buffers with the iteration parity (old: 0 suffix, new: 1).
+template <typename R, int NF>
+struct CgVecs {
+    const int32_t* rp;
+    const int32_t* col;
+    const FV<R, NF>* A;
+    const FV<R, NF>* dinv;
+    FV<R, NF>* x;
+    FV<R, NF>* p;
+    const FV<R, NF>* r0;
+    const FV<R, NF>* w0;
+    const FV<R, NF>* s0;
+    FV<R, NF>* r1;
+    FV<R, NF>* w1;
+    FV<R, NF>* s1;
+};
+
+// New s, r and u = D^-1 r of one unknown from its old r, w, s (and D^-1).
+template <typename R, int NF>
+__device__ __forceinline__ void cg_advance(const PhaseCtl<R, NF>& c, const FV<R, NF>& ro, const FV<R, NF>& wo,
+                                           const FV<R, NF>& so, const FV<R, NF>& d, FV<R, NF>& sn,
+                                           FV<R, NF>& rn, FV<R, NF>& un) {
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        sn.v[f] = c.fresh[f] ? wo.v[f] : fma(c.beta[f], so.v[f], wo.v[f]);
+        rn.v[f] = c.act[f] ? fma(-c.alpha[f], sn.v[f], ro.v[f]) : ro.v[f];
+        un.v[f] = d.v[f] * rn.v[f];
+    }
+}
+
+// One Chronopoulos-Gear iteration on one warp's rows (Jacobi-preconditioned
+// CG rearranged, Chronopoulos & Gear 1989, so that an iteration needs one
+// global reduction): with u = D^-1 r, w = A u and s = A p,
+//   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,
+//   u' = D^-1 r,  w' = A u',  gamma' = r.u',  delta' = w'.u'.
+// The SpMV recomputes u' at each gathered column from the old r, w and s
+// there; every row owner applies the vector updates.  dots[] receives gamma',
+// delta' and |r'|^2 per field.
+template <typename R, int NF, int WCH>
+__device__ __forceinline__ void cgcg_rows(const CgVecs<R, NF>& v, const PhaseCtl<R, NF>& c, int64_t row0, int64_t N,
+                                          FV<R, NF>* smw, Acc<R> (&dots)[3 * NF]) {
+    const FV<R, NF> wn = warp_rows<R, NF, WCH>(v.rp, v.col, v.A, row0, N, smw, [&](int32_t col) {
+        const FV<R, NF> ro = ldv(v.r0 + col, false), wo = ldv(v.w0 + col, false);
+        const FV<R, NF> d = ldv(v.dinv + col, false);
+        FV<R, NF> so = wo;
+        if (c.need_old) so = ldv(v.s0 + col, false);
+        FV<R, NF> sn, rn, un;
+        cg_advance(c, ro, wo, so, d, sn, rn, un);
+        return un;
+    });
+    const int64_t row = row0 + (threadIdx.x & 31);
+    if (row < N) {
+        const FV<R, NF> ro = ldv(v.r0 + row, false), wo = ldv(v.w0 + row, false), d = ldv(v.dinv + row, false);
+        FV<R, NF> so = wo;
+        if (c.need_old) so = ldv(v.s0 + row, false);
+        FV<R, NF> x = v.x[row], p = v.p[row];
+        FV<R, NF> sn, rn, un;
+        cg_advance(c, ro, wo, so, d, sn, rn, un);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            if (c.act[f]) {
+                const R ui = d.v[f] * ro.v[f];
+                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+            }
+            dots[f].add_prod(rn.v[f], un.v[f]);
+            dots[NF + f].add_prod(wn.v[f], un.v[f]);
+            dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+        }
+        v.x[row] = x;
+        v.p[row] = p;
+        v.r1[row] = rn;
+        v.s1[row] = sn;
+        v.w1[row] = wn;
+    }
+}
+
+// After the SpMV phase: alpha = r.z / p.q, or breakdown.
+// (S: CgState or a batched instance's state; flags receives FEA_STATUS_*.)
+template <typename R, int NF, typename S>
+__device__ void finish_spmv(volatile S* cg, unsigned int* flags, const int (&act)[NF], const double* tot) {
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        if (!act[f]) continue;
+        cg->pq[f] = tot[f];
+        const double al = cg->rz[f] / tot[f];
+        if (!(tot[f] > 0.0) || !isfinite(al)) {
+            cg->active[f] = 0;
+            cg->iters[f] = cg->iter;
+            atomicOr(flags, FEA_STATUS_BREAKDOWN);
+        } else {
+            cg->alpha[f] = al;
+        }
+    }
+}
+
+// After a Chronopoulos-Gear iteration: convergence |r|^2 < tol^2 |b|^2, then
+// beta = gamma'/gamma and alpha = gamma' / (delta' - beta gamma'/alpha) for
+// the next iteration; iteration count and the max_iter limit.  tot holds
+// gamma' = r.u, delta' = w.u and r.r per field.  Returns whether another
+// iteration runs.
+template <typename R, int NF, typename S>
+__device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act)[NF], const double* tot) {
+    const int it = cg->iter + 1;
+    cg->iter = it;
+    int any = 0;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        cg->fresh[f] = 0;
+        if (!act[f]) continue;
+        const double g = tot[f], d = tot[NF + f], rr = tot[2 * NF + f];
+        cg->rr[f] = rr;
+        if (!isfinite(rr)) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+            atomicOr(flags, FEA_STATUS_BREAKDOWN);
+            continue;
+        }
+        if (rr < cg->thr[f]) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+            continue;
+        }
+        const double beta = g / cg->rz[f];
+        const double den = d - beta * g / cg->alpha[f];
+        const double alpha = g / den;
+        if (!(den > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+            cg->active[f] = 0;
+            cg->iters[f] = it;
+            atomicOr(flags, FEA_STATUS_BREAKDOWN);
+            continue;
+        }
+        cg->beta[f] = beta;
+        cg->alpha[f] = alpha;
+        cg->rz[f] = g;
+        any = 1;
+    }
+    const bool cont = any && it < cg->max_iter;
+    if (any && !cont) {
+        atomicOr(flags, FEA_STATUS_NOT_CONVERGED);
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            if (cg->active[f]) {
+                cg->active[f] = 0;
+                cg->iters[f] = it;
+            }
+    }
+    return cont;
+}
+
+// ---- standalone kernels (autotuning and timing probes) -------------------------------
+
+// ---- graph construction helpers ---------------------------------------------------
+
+template <typename... P>
+cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
+                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
+    auto local = arg;
+    void* argv[] = {(void*)&local};
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)fn;
+    kp.gridDim = dim3((unsigned)grid);
+    kp.blockDim = dim3((unsigned)block);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = argv;
+    cudaGraphNode_t n;
+    FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
+    return n;
+}
+
+cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t n;
+    FEA_CUDA_TRY(cudaGraphAddNode(&n, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, &np));
+    *body = np.conditional.phGraph_out[0];
+    return n;
+}
+
+// Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
+// calculator), capped by the work and by the partial-sum stride.
+template <typename K>
+int wave_grid(K kernel, int64_t work_blocks) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t g = (int64_t)num_sms() * per_sm;
+    if (g > max_grid_blocks()) g = max_grid_blocks();
+    if (g > work_blocks) g = work_blocks;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+}  // namespace fea

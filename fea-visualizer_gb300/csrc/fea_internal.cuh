@@ -135,7 +135,7 @@ struct StepArgs {
 
 // Loop-condition slots in device memory for host-driven (stream) execution.
 struct LoopFlags {
-    int cg1, cg2, step;
+    int cg1, cg2, step, probe;
 };
 
 // A built step-loop graph for one (precision, fields, equation, lanes) plan.
@@ -159,11 +159,29 @@ void build_step_graph(StepGraph& g, const StepArgs<R, NF>& base, int kind, int l
 template <typename R, int NF>
 void run_steps_stream(const StepArgs<R, NF>& base, int kind, int lanes, LoopFlags* lf, cudaStream_t st);
 
-// One SpMV + dot launch with the given lanes per row (autotuning probe).
+// Timing and autotuning probe: one CG iteration kernel with the given window
+// size, after prepare_probe has masked every field (x and p are written back
+// unchanged; only CG scratch changes, which the next step recomputes).
+// a.x and a.cont must be set.
+template <typename R, int NF>
+void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st);
 template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
 
-// FP64-accurate true residual |b - A x| / |b| of the current solve (status).
 int max_grid_blocks();
+
+// Solver-order view of a handle's assembled mesh: what the batched solver
+// copies out of a single-mesh handle built for each of its instances.
+struct MeshView {
+    int64_t V = 0, T = 0, N = 0;
+    const Pattern* Pc = nullptr;    // pattern in solver order (diag filled)
+    const int32_t* emap = nullptr;  // solver slot -> assembly slot
+    const double* M64 = nullptr;    // FP64 matrices in assembly order
+    const double* K64 = nullptr;
+    const double* Adv64 = nullptr;
+    const int32_t* idx_c = nullptr;  // node -> solver index, -1 on Dirichlet points
+    cudaStream_t stream = nullptr;
+};
+MeshView mesh_view(const fea_solver* s);
 
 }  // namespace fea

@@ -610,7 +610,61 @@ void copy_field_device(fea_solver* s, const void* src, void* dst, int which, boo
 
 int displayed_field(const fea_params& p) { return p.equation == FEA_REACTION_DIFFUSION ? 1 : 0; }
 
+// Arguments of the timing probe on the current equation's operator.
+template <typename R, int NF>
+StepArgs<R, NF> probe_args(fea_solver* s, int kind) {
+    StepArgs<R, NF> a = make_args<R, NF>(s, false);
+    set_x<R, NF>(s, a, kind);
+    a.cont = &s->d_flags->probe;
+    a.use_graph = 0;
+    return a;
+}
+
+// One probe launch (prepare: mask the fields first, outside any timing).
+template <typename R>
+void probe(fea_solver* s, int kind, int lanes, bool prepare) {
+    if (two_fields(kind)) {
+        const StepArgs<R, 2> a = probe_args<R, 2>(s, kind);
+        if (prepare) prepare_probe<R, 2>(a, s->stream);
+        else launch_spmv_probe<R, 2>(a, lanes, s->stream);
+    } else {
+        const StepArgs<R, 1> a = probe_args<R, 1>(s, kind);
+        if (prepare) prepare_probe<R, 1>(a, s->stream);
+        else launch_spmv_probe<R, 1>(a, lanes, s->stream);
+    }
+}
+
+void probe_any(fea_solver* s, int kind, int lanes, bool prepare) {
+    if (s->precision == FEA_FP64) probe<double>(s, kind, lanes, prepare);
+    else probe<float>(s, kind, lanes, prepare);
+}
+
+// The operator of `kind` up to date (the probe times the current equation).
+void ensure_operator(fea_solver* s, int kind) {
+    if (s->op_dirty || s->op_kind != kind) {
+        if (s->precision == FEA_FP64) update_operator<double>(s, kind);
+        else update_operator<float>(s, kind);
+        s->op_dirty = false;
+        s->op_kind = kind;
+    }
+}
+
 }  // namespace
+
+MeshView mesh_view(const fea_solver* s) {
+    MeshView m;
+    m.V = s->V;
+    m.T = s->T;
+    m.N = s->N;
+    m.Pc = &s->Pc;
+    m.emap = s->emap;
+    m.M64 = s->M64;
+    m.K64 = s->K64;
+    m.Adv64 = s->Adv64;
+    m.idx_c = s->idx_c;
+    m.stream = s->stream;
+    return m;
+}
 
 // Device partial-reduction storage sized for the widest grid.
 void alloc_run_state(fea_solver* s) {
@@ -995,7 +1049,8 @@ int fea_autotune(fea_solver* s) {
     check_handle(s);
     if (s->N == 0) return FEA_OK;
     const int kind = step_kind(s->prm);
-    const bool two = two_fields(kind);
+    if (kind < 0) return fail(FEA_ERR_INVALID_ARGUMENT, "bad equation");
+    ensure_operator(s, kind);
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
@@ -1003,15 +1058,10 @@ int fea_autotune(fea_solver* s) {
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
+        probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
-            if (s->precision == FEA_FP64) {
-                if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), l, s->stream);
-                else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), l, s->stream);
-            } else {
-                if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), l, s->stream);
-                else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), l, s->stream);
-            }
+            probe_any(s, kind, l, false);
         }
         FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
         FEA_CUDA_TRY(cudaEventSynchronize(e1));
@@ -1045,30 +1095,20 @@ int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch) 
         return FEA_OK;
     }
     const int kind = step_kind(s->prm);
-    const bool two = two_fields(kind);
-    if (s->op_dirty || s->op_kind != kind) {
-        if (s->precision == FEA_FP64) update_operator<double>(s, kind);
-        else update_operator<float>(s, kind);
-        s->op_dirty = false;
-        s->op_kind = kind;
-    }
+    if (kind < 0) return fail(FEA_ERR_INVALID_ARGUMENT, "bad equation");
+    ensure_operator(s, kind);
     DeviceArena tmp;
     const size_t flush_bytes = (size_t)256 << 20;
     void* junk = flush_l2 ? (void*)tmp.alloc<uint8_t>((int64_t)flush_bytes) : nullptr;
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
+    probe_any(s, kind, s->lanes, true);
     double total = 0;
     for (int rep = 0; rep < reps + 1; rep++) {  // the first launch is a warm-up
         if (junk) FEA_CUDA_TRY(cudaMemsetAsync(junk, rep & 0xff, flush_bytes, s->stream));
         FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
-        if (s->precision == FEA_FP64) {
-            if (two) launch_spmv_probe<double, 2>(make_args<double, 2>(s, false), s->lanes, s->stream);
-            else launch_spmv_probe<double, 1>(make_args<double, 1>(s, false), s->lanes, s->stream);
-        } else {
-            if (two) launch_spmv_probe<float, 2>(make_args<float, 2>(s, false), s->lanes, s->stream);
-            else launch_spmv_probe<float, 1>(make_args<float, 1>(s, false), s->lanes, s->stream);
-        }
+        probe_any(s, kind, s->lanes, false);
         FEA_CUDA_TRY(cudaEventRecord(e1, s->stream));
         FEA_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;

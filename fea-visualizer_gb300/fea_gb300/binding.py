@@ -297,3 +297,72 @@ class CUDASolver:
             self.close()
         except Exception:
             pass
+
+
+class BatchSolver:
+    """Many Gray-Scott instances stepped together (fea_batch_* of include/fea_gpu.h).
+
+    instances: sequence of dicts with keys vertices, triangles, and optionally
+    boundary_condition (NEUMANN), time_step, Du, Dv, feed_rate, kill_rate.
+    Each instance follows the mass-weighted Gray-Scott step of one mesh."""
+
+    def __init__(self, instances, precision=FP32, cg_tolerance=0.0, cg_max_iterations=0):
+        L = load()
+        self._keep = []
+        descs = (InstanceDesc * len(instances))()
+        self.num_vertices = []
+        for d, spec in zip(descs, instances):
+            v = np.ascontiguousarray(spec["vertices"], dtype=np.float32).reshape(-1, 3)
+            t = np.ascontiguousarray(spec["triangles"], dtype=np.uint32).reshape(-1, 3)
+            self._keep += [v, t]
+            d.vertices, d.num_vertices = v.ctypes.data, v.shape[0]
+            d.triangles, d.num_triangles = t.ctypes.data, t.shape[0]
+            d.boundary_condition = spec.get("boundary_condition", NEUMANN)
+            d.time_step = spec.get("time_step", 0.001)
+            d.Du = spec.get("Du", 0.08)
+            d.Dv = spec.get("Dv", 0.04)
+            d.feed_rate = spec.get("feed_rate", 0.035)
+            d.kill_rate = spec.get("kill_rate", 0.06)
+            self.num_vertices.append(v.shape[0])
+        h = C.c_void_p()
+        check(L.fea_batch_create(descs, len(instances), precision, float(cg_tolerance), int(cg_max_iterations),
+                                 C.byref(h)))
+        self._keep = []
+        self._h = h
+        self.num_instances = len(instances)
+
+    def set_fields(self, i, u=None, v=None):
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float32)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float32)
+        check(load().fea_batch_set_fields(self._h, int(i), _ptr(uu), _ptr(vv)))
+
+    def get_fields(self, i):
+        n = self.num_vertices[i]
+        u = np.zeros(n, dtype=np.float32)
+        v = np.zeros(n, dtype=np.float32)
+        check(load().fea_batch_get_fields(self._h, int(i), _ptr(u), _ptr(v)))
+        return u, v
+
+    def advance_time(self, nsteps: int = 1):
+        check(load().fea_batch_advance_time(self._h, int(nsteps)))
+
+    def synchronize(self):
+        check(load().fea_batch_synchronize(self._h))
+
+    def status(self):
+        """(flags uint32[n], iterations int32[n, 2] of the last solve)."""
+        f = np.zeros(self.num_instances, dtype=np.uint32)
+        it = np.zeros((self.num_instances, 2), dtype=np.int32)
+        check(load().fea_batch_get_status(self._h, _ptr(f), _ptr(it)))
+        return f, it
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().fea_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -208,18 +208,23 @@ int fea_get_matrix(fea_solver* s, int which, int32_t* row_ptr, int32_t* col, voi
 /* Node -> unknown map (FEMContext::idx_map, int32[V]) and boundary flags. */
 int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
 
-/* Pick the lanes-per-row of the CSR SpMV by timing the candidates on this
- * mesh (2, 4, 8, 16 lanes); the choice is kept in fea_info. */
+/* Pick the window size of the warp-cooperative CSR kernels (4, 8 or 16
+ * entries per lane and window) by timing one CG iteration of each candidate
+ * on this mesh; the choice is kept in fea_info.rows_per_warp_lanes.  Leaves
+ * the fields unchanged. */
 int fea_autotune(fea_solver* s);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
  * their own work or events after it. */
 int fea_get_stream(fea_solver* s, void** stream);
 
-/* Diagnostics: mean device time in ms of the step loop's SpMV kernel (the
- * dominant kernel of a step) over `reps` launches on the current operator of
- * the current equation, each launch preceded by a 256 MiB write that evicts
- * the L2 cache when flush_l2 != 0.  CUDA events on the handle's stream. */
+/* Diagnostics: mean device time in ms of one CG iteration kernel (the step
+ * loop's dominant kernel: the CSR SpMV with the vector updates fused) over
+ * `reps` launches on the current operator of the current equation, each
+ * launch preceded by a 256 MiB write that evicts the L2 cache when
+ * flush_l2 != 0.  CUDA events on the handle's stream.  The probe masks every
+ * field, so the fields are written back unchanged; only CG scratch, which the
+ * next step recomputes, changes. */
 int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch);
 
 /* ---- adjoint (explicit advection-diffusion) ------------------------------
@@ -236,10 +241,15 @@ int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target
                                int64_t checkpoint_every, double* loss, void* grad_u0, void* grad_D);
 
 /* ---- batched Gray-Scott ---------------------------------------------------
- * Many independent meshes with their own (F, k, Du, Dv, dt), stepped together
- * by one persistent kernel per CG phase.  No reference counterpart (the
- * reference steps one mesh); each instance follows the Gray-Scott step of
- * CPUSolver.cpp:127-145 with reaction_mode 1. */
+ * Many independent meshes with their own (F, k, Du, Dv, dt), stepped together:
+ * the instances' systems are stacked into one block-diagonal matrix and every
+ * CG phase is one persistent kernel over all instances, with per-instance
+ * scalars and convergence masks; the whole step loop is one CUDA graph.  No
+ * reference counterpart (the reference steps one mesh); each instance follows
+ * the Gray-Scott step of CPUSolver.cpp:127-145 with reaction_mode 1 and the
+ * single-mesh solver's CG (cg_tolerance 0 -> FLT_EPSILON / 1e-10, max
+ * iterations 0 -> 2N of the instance).  A state that exceeds 1e4 freezes only
+ * its own instance (FEA_STATUS_BLOWUP in its flags). */
 typedef struct {
     const float* vertices;      /* xyz float[3V] */
     int64_t num_vertices;

@@ -43,3 +43,20 @@ def rel_l2(a, b):
     b = np.asarray(b, dtype=np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def f32(x):
+    return float(np.float32(x))
+
+
+def oracle_step(oracle_mod, S, eq, dt, u, v, n, **kw):
+    """FP64 oracle steps with the float32-rounded parameters the ABI carries
+    (the reference's parameter structs hold floats, EquationParameters.hpp)."""
+    for key in ("kappa", "Du", "Dv", "F", "k", "adv_sign"):
+        if key in kw:
+            kw[key] = f32(kw[key])
+    p = oracle_mod.params(eq, f32(dt), tol=1e-14, **kw)
+    a = None
+    if eq == oracle_mod.WAVE and kw.get("wave_scheme", 0) == 1:
+        a = S.newmark_init(p, u)
+    return S.step(p, u, v, a, nsteps=n)

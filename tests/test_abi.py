@@ -90,6 +90,18 @@ def test_argument_errors_without_gpu(lib):
     assert rc == -1  # bad boundary condition
     assert lib.fea_params_default(None) == -1
     assert lib.fea_advance_time(None, 1) == -1
+    # batched: no instances, an empty instance mesh, a null handle
+    assert lib.fea_batch_create(None, 0, 0, 0.0, 0, C.byref(h)) == -1
+    d = (binding.InstanceDesc * 1)()
+    d[0].vertices, d[0].num_vertices = xyz.ctypes.data, 3
+    d[0].triangles, d[0].num_triangles = tri.ctypes.data, 0
+    d[0].time_step = 0.5
+    assert lib.fea_batch_create(d, 1, 0, 0.0, 0, C.byref(h)) == -4
+    d[0].num_triangles = 1
+    d[0].time_step = 0.0
+    assert lib.fea_batch_create(d, 1, 0, 0.0, 0, C.byref(h)) == -1
+    assert lib.fea_batch_advance_time(None, 1) == -1
+    assert lib.fea_batch_destroy(None) == 0
 
 
 def test_no_cpu_fallback_without_gpu(lib):
@@ -99,4 +111,8 @@ def test_no_cpu_fallback_without_gpu(lib):
     from fea_gb300 import binding, meshgen
     with pytest.raises(binding.FeaError) as ei:
         binding.CUDASolver(*meshgen.icosphere(1))
+    assert ei.value.code == -3
+    xyz, tri = meshgen.icosphere(1)
+    with pytest.raises(binding.FeaError) as ei:
+        binding.BatchSolver([dict(vertices=xyz, triangles=tri, time_step=0.5)])
     assert ei.value.code == -3

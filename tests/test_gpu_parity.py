@@ -8,7 +8,7 @@ FP64 values to 1e-13; one time step agrees with the FP64 oracle (solved to
 import numpy as np
 import pytest
 
-from conftest import rel_l2
+from conftest import oracle_step, rel_l2
 from fea_gb300 import meshgen as mg
 
 pytestmark = pytest.mark.gpu
@@ -92,21 +92,7 @@ def _device_field(s, which):
     return t[which].cpu().numpy().astype(np.float64)
 
 
-def _f32(x):
-    return float(np.float32(x))
-
-
-def _oracle_step(oracle_mod, S, eq, dt, u, v, n, **kw):
-    """FP64 oracle steps with the float32-rounded parameters the ABI carries
-    (the reference's parameter structs hold floats, EquationParameters.hpp)."""
-    for key in ("kappa", "Du", "Dv", "F", "k", "adv_sign"):
-        if key in kw:
-            kw[key] = _f32(kw[key])
-    p = oracle_mod.params(eq, _f32(dt), tol=1e-14, **kw)
-    a = None
-    if eq == oracle_mod.WAVE and kw.get("wave_scheme", 0) == 1:
-        a = S.newmark_init(p, u)
-    return S.step(p, u, v, a, nsteps=n)
+_oracle_step = oracle_step
 
 
 @pytest.mark.parametrize("precision,tol", [(0, 1e-5), (1, 1e-9)])
