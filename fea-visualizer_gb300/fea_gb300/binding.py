@@ -337,6 +337,8 @@ class BatchSolver:
         check(load().fea_batch_set_fields(self._h, int(i), _ptr(uu), _ptr(vv)))
 
     def get_fields(self, i):
+        if not 0 <= int(i) < self.num_instances:  # the library reports the bad index
+            check(load().fea_batch_get_fields(self._h, int(i), None, None))
         n = self.num_vertices[i]
         u = np.zeros(n, dtype=np.float32)
         v = np.zeros(n, dtype=np.float32)
