@@ -175,6 +175,8 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                     bs[0].add_prod(-(R)P.c2 * ldg(a.K + e), ut);
                 } else if constexpr (EQ == EQ_NEWMARK_INIT) {
                     bs[0].add_prod(-(R)P.c2 * ldg(a.K + e), a.u[c]);
+                } else if constexpr (EQ == EQ_GIVEN) {
+                    (void)me;  // b is given; only A x0 is gathered
                 } else if constexpr (EQ == EQ_GS_REF) {
 #pragma unroll
                     for (int f = 0; f < NF; f++) bs[f].add_prod(div_rn(me, dt), xc.v[f]);
@@ -207,7 +209,10 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                 bs[NF - 1].add(uvv);
                 bs[NF - 1].add(-((R)P.F + (R)P.k) * v);
             }
-            if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_NEWMARK_INIT) {
+            if constexpr (EQ == EQ_GIVEN) {  // adjoint values may be large: only non-finite stops
+                bs[0].add(a.rhs[row]);
+                if (!isfinite(xr.v[0])) flags |= FEA_STATUS_NONFINITE;
+            } else if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_NEWMARK_INIT) {
                 flags |= check_value(a.u[row]) | check_value(a.v[row]);
             } else if constexpr (EQ == EQ_WAVE_NEWMARK) {
                 const R ur = a.u[row], vr = a.v[row], ar = xr.v[0];
@@ -391,6 +396,8 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK || EQ == EQ_NEWMARK_INIT) {
             flags |= check_value(a.u[i]) | check_value(a.v[i]);
+        } else if constexpr (EQ == EQ_GIVEN) {
+            if (!isfinite(a.x[i].v[0])) flags |= FEA_STATUS_NONFINITE;
         } else {
             const FV<R, NF> x = a.x[i];
 #pragma unroll
@@ -524,6 +531,7 @@ void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int wch, Lo
         case EQ_WAVE_REF: dispatch_variant<R, 1, EQ_WAVE_REF>(G, a, wch, lf, st); break;
         case EQ_WAVE_NEWMARK: dispatch_variant<R, 1, EQ_WAVE_NEWMARK>(G, a, wch, lf, st); break;
         case EQ_NEWMARK_INIT: dispatch_variant<R, 1, EQ_NEWMARK_INIT>(G, a, wch, lf, st); break;
+        case EQ_GIVEN: dispatch_variant<R, 1, EQ_GIVEN>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     } else {

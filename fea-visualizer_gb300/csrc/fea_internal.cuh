@@ -70,7 +70,8 @@ enum StepKind : int {
     EQ_WAVE_NEWMARK = 3, // solve for a: b = -c^2 K u~; then u, v updates
     EQ_GS_REF = 4,       // (u, v): b = (M/dt) x + f(x) nodal
     EQ_GS_CONSISTENT = 5, // (u, v): b = M (x/dt + f(x))
-    EQ_NEWMARK_INIT = 6   // solve M a0 = -c^2 K u0 for Newmark's starting acceleration
+    EQ_NEWMARK_INIT = 6,  // solve M a0 = -c^2 K u0 for Newmark's starting acceleration
+    EQ_GIVEN = 7          // solve A x = rhs for a given right-hand side (the adjoint solve)
 };
 
 // Scalars of the step loop, device resident.
@@ -122,6 +123,7 @@ struct StepArgs {
     R* a;                   // acceleration (Newmark)
     R* ut;                  // Newmark predictors
     R* vt;
+    const R* rhs;           // EQ_GIVEN: right-hand side [N]
     const StepParams* prm;
     CgState* cg;
     RunState* run;
@@ -169,6 +171,22 @@ template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
 
 int max_grid_blocks();
+
+// ---- adjoint of the explicit advection-diffusion step (adjoint.cu) ----------------
+// lam = M (u - t), *J = 1/2 (u - t).lam  (FP64-accurate; one block-partial
+// reduction through part/ticket).
+template <typename R>
+void adjoint_loss(const Pattern& P, const R* M, const R* u, const R* t, R* lam, double* part, int stride,
+                  unsigned int* ticket, double* J, cudaStream_t st);
+// lam = (M/dt) mu + s Adv^T mu
+template <typename R>
+void adjoint_lambda(const Pattern& P, const R* M, const R* Adv, double dt, double adv_sign, const R* mu, R* lam,
+                    cudaStream_t st);
+// gD[e] -= c * mu_e^T K_e u_e for every element (K_e: unscaled element
+// stiffness, FP64; idx_c maps nodes to solver rows, -1 on Dirichlet points)
+template <typename R>
+void adjoint_grad_D(const double* Kloc, const uint32_t* tri, const int32_t* idx_c, int64_t T, double c, const R* mu,
+                    const R* u, double* gD, cudaStream_t st);
 
 // Solver-order view of a handle's assembled mesh: what the batched solver
 // copies out of a single-mesh handle built for each of its instances.

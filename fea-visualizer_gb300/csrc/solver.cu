@@ -98,6 +98,12 @@ __global__ void k_float_to(const float* __restrict__ in, int64_t n, R* out) {
         out[i] = (R)in[i];
 }
 
+template <typename A, typename B>
+__global__ void k_convert(const A* __restrict__ in, int64_t n, B* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (B)in[i];
+}
+
 }  // namespace
 
 // Everything that depends on the arithmetic type.
@@ -649,6 +655,158 @@ void ensure_operator(fea_solver* s, int kind) {
     }
 }
 
+// ---- adjoint of the explicit advection-diffusion step -------------------------------
+// (recurrences in adjoint.cu).  The transposed solves mu = A^-1 lam run the
+// forward operator (A is symmetric) through the step graph with a given
+// right-hand side; forward states are recomputed from checkpoints taken every
+// `ckpt` steps.
+
+// One solve A mu = lam with the graph g (built on first use).
+template <typename R>
+void run_given(fea_solver* s, StepGraph& g, const StepArgs<R, 1>& a) {
+    long long ctl[2] = {1, 0};  // steps_left, steps_done
+    FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
+    if (s->stream_mode) {
+        run_steps_stream<R, 1>(a, EQ_GIVEN, s->lanes, s->d_flags, s->stream);
+        return;
+    }
+    if (!g.exec) build_step_graph<R, 1>(g, a, EQ_GIVEN, s->lanes, s->d_flags);
+    FEA_CUDA_TRY(cudaGraphLaunch(g.exec, s->stream));
+}
+
+// u0, t: solver-order device arrays.  Leaves lam = dJ/du0 (solver order) and
+// gD = dJ/dD (FP64, per element) when `grads`, and the handle's field at u_N.
+template <typename R>
+double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int64_t ckpt, bool grads, R* lam,
+                    double* gD) {
+    if (step_kind(s->prm) != EQ_ADV_EXPLICIT) {
+        set_error("the adjoint needs equation FEA_ADVECTION_DIFFUSION with advection_scheme 1");
+        throw Error{FEA_ERR_STATE};
+    }
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N;
+    const size_t rb = sizeof(R) * (size_t)N;
+    const auto d2d = cudaMemcpyDeviceToDevice;
+    ckpt = std::min(ckpt, nsteps);
+    const int64_t nck = ceil_div(nsteps, ckpt);
+    ensure_layout<R>(s, false);
+    DeviceArena tmp;
+    R* ck = tmp.alloc<R>(nck * N);
+    R* seg = tmp.alloc<R>((ckpt + 1) * N);
+    R* mu = tmp.alloc<R>(N);
+    R* uN = tmp.alloc<R>(N);
+    R* lam_f = lam ? lam : tmp.alloc<R>(N);
+    double* J = tmp.alloc<double>(1);
+    R* u = (R*)s->F.u;
+    FEA_CUDA_TRY(cudaMemcpyAsync(u, u0, rb, d2d, st));
+    for (int64_t sg = 0; sg < nck; sg++) {  // forward sweep, a checkpoint per segment
+        FEA_CUDA_TRY(cudaMemcpyAsync(ck + sg * N, u, rb, d2d, st));
+        advance<R>(s, std::min(ckpt, nsteps - sg * ckpt));
+    }
+    FEA_CUDA_TRY(cudaMemcpyAsync(uN, u, rb, d2d, st));
+    adjoint_loss<R>(s->Pc, (const R*)s->Mc, u, t, lam_f, s->d_part, max_grid_blocks(), s->d_tickets + 5, J, st);
+    if (grads) {
+        FEA_CUDA_TRY(cudaMemsetAsync(gD, 0, sizeof(double) * (size_t)s->T, st));
+        FEA_CUDA_TRY(cudaMemsetAsync(mu, 0, rb, st));
+        StepArgs<R, 1> a = make_args<R, 1>(s, false);
+        a.x = (FV<R, 1>*)mu;
+        a.rhs = lam_f;
+        StepGraph g;
+        const double dt = time_step(s->prm), c = s->prm.advdiff_c, sign = s->prm.advection_sign;
+        try {
+            for (int64_t sg = nck - 1; sg >= 0; sg--) {
+                const int64_t n0 = sg * ckpt, n1 = std::min(n0 + ckpt, nsteps);
+                FEA_CUDA_TRY(cudaMemcpyAsync(u, ck + sg * N, rb, d2d, st));
+                for (int64_t n = n0; n < n1; n++) {  // u^{n0+1} .. u^{n1}
+                    advance<R>(s, 1);
+                    FEA_CUDA_TRY(cudaMemcpyAsync(seg + (n - n0 + 1) * N, u, rb, d2d, st));
+                }
+                for (int64_t n = n1 - 1; n >= n0; n--) {
+                    run_given<R>(s, g, a);  // mu = A^-1 lam, warm-started from the previous mu
+                    adjoint_grad_D<R>(s->Kloc, s->tri, s->idx_c, s->T, c, mu, seg + (n - n0 + 1) * N, gD, st);
+                    adjoint_lambda<R>(s->Pc, (const R*)s->Mc, (const R*)s->Advc, dt, sign, mu, lam_f, st);
+                }
+            }
+        } catch (...) {
+            cudaStreamSynchronize(st);
+            g.destroy();
+            throw;
+        }
+        FEA_CUDA_TRY(cudaStreamSynchronize(st));
+        g.destroy();
+    }
+    FEA_CUDA_TRY(cudaMemcpyAsync(u, uN, rb, d2d, st));
+    double h = 0;
+    FEA_CUDA_TRY(cudaMemcpyAsync(&h, J, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    return h;
+}
+
+// Node-indexed float inputs and outputs (the host entry point).
+template <typename R>
+void adjoint_host(fea_solver* s, const float* u0, const float* target, int64_t nsteps, int64_t ckpt, double* loss,
+                  float* grad_u0, float* grad_D) {
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N, V = s->V, T = s->T;
+    DeviceArena tmp;
+    R* u0s = tmp.alloc<R>(N);
+    R* ts = tmp.alloc<R>(N);
+    R* lam = tmp.alloc<R>(N);
+    double* gD = tmp.alloc<double>(T);
+    float* gDf = tmp.alloc<float>(T);
+    const std::pair<const float*, R*> ins[2] = {{u0, u0s}, {target, ts}};
+    for (const auto& in : ins) {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->d_nodes, in.first, sizeof(float) * V, cudaMemcpyHostToDevice, st));
+        k_gather_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(s->d_nodes, s->idx_c, V, in.second, 1, 0);
+        FEA_CHECK_LAUNCH();
+    }
+    const bool grads = grad_u0 || grad_D;
+    const double J = adjoint_core<R>(s, u0s, ts, nsteps, ckpt, grads, lam, gD);
+    if (loss) *loss = J;
+    if (grad_u0) {
+        k_scatter_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(lam, s->idx_c, V, s->d_nodes, 1, 0);
+        FEA_CHECK_LAUNCH();
+        FEA_CUDA_TRY(cudaMemcpyAsync(grad_u0, s->d_nodes, sizeof(float) * V, cudaMemcpyDeviceToHost, st));
+    }
+    if (grad_D) {
+        k_convert<double, float><<<launch_grid(T), kBlock, 0, st>>>(gD, T, gDf);
+        FEA_CHECK_LAUNCH();
+        FEA_CUDA_TRY(cudaMemcpyAsync(grad_D, gDf, sizeof(float) * T, cudaMemcpyDeviceToHost, st));
+    }
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// Unknown-indexed device arrays in the handle's precision.
+template <typename R>
+void adjoint_device(fea_solver* s, const void* u0, const void* target, int64_t nsteps, int64_t ckpt, double* loss,
+                    void* grad_u0, void* grad_D) {
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N, T = s->T;
+    DeviceArena tmp;
+    R* u0s = tmp.alloc<R>(N);
+    R* ts = tmp.alloc<R>(N);
+    R* lam = tmp.alloc<R>(N);
+    double* gD = tmp.alloc<double>(T);
+    if (N > 0) {
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)u0, s->pos, N, u0s, 1, 0);
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)target, s->pos, N, ts, 1, 0);
+        FEA_CHECK_LAUNCH();
+    }
+    const bool grads = grad_u0 || grad_D;
+    const double J = adjoint_core<R>(s, u0s, ts, nsteps, ckpt, grads, lam, gD);
+    if (loss) *loss = J;
+    if (grad_u0 && N > 0) {
+        k_copy_from_state<R><<<launch_grid(N), kBlock, 0, st>>>(lam, s->pos, N, (R*)grad_u0, 1, 0);
+        FEA_CHECK_LAUNCH();
+    }
+    if (grad_D) {
+        k_convert<double, R><<<launch_grid(T), kBlock, 0, st>>>(gD, T, (R*)grad_D);
+        FEA_CHECK_LAUNCH();
+    }
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
 }  // namespace
 
 MeshView mesh_view(const fea_solver* s) {
@@ -865,6 +1023,53 @@ int fea_set_element_fields(fea_solver* s, const float* diffusivity, const float*
     }
     assemble(s);
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_set_element_diffusivity_device(fea_solver* s, const void* diffusivity) {
+    API_BEGIN
+    check_handle(s);
+    if (!diffusivity) return fail(FEA_ERR_INVALID_ARGUMENT, "null diffusivity");
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (!s->elem_D) {
+        s->elem_D = s->mesh_mem.alloc<float>(s->T);
+        s->elem_Dr = s->mesh_mem.alloc<double>(s->T);
+    }
+    if (s->precision == FEA_FP64) {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->elem_Dr, diffusivity, sizeof(double) * s->T, cudaMemcpyDeviceToDevice,
+                                     s->stream));
+        k_convert<double, float><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_Dr, s->T, s->elem_D);
+    } else {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->elem_D, diffusivity, sizeof(float) * s->T, cudaMemcpyDeviceToDevice,
+                                     s->stream));
+        k_float_to<double><<<launch_grid(s->T), kBlock, 0, s->stream>>>(s->elem_D, s->T, s->elem_Dr);
+    }
+    FEA_CHECK_LAUNCH();
+    assemble(s);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_adjoint_advdiff(fea_solver* s, const float* u0, const float* target, int64_t nsteps,
+                        int64_t checkpoint_every, double* loss, float* grad_u0, float* grad_D) {
+    API_BEGIN
+    check_handle(s);
+    if (!u0 || !target || nsteps < 1 || checkpoint_every < 1)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "adjoint needs u0, target, nsteps >= 1 and checkpoint_every >= 1");
+    if (s->precision == FEA_FP64) adjoint_host<double>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
+    else adjoint_host<float>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
+    API_END
+}
+
+int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target, int64_t nsteps,
+                               int64_t checkpoint_every, double* loss, void* grad_u0, void* grad_D) {
+    API_BEGIN
+    check_handle(s);
+    if (!u0 || !target || nsteps < 1 || checkpoint_every < 1)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "adjoint needs u0, target, nsteps >= 1 and checkpoint_every >= 1");
+    if (s->precision == FEA_FP64)
+        adjoint_device<double>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
+    else adjoint_device<float>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
     API_END
 }
 

@@ -106,6 +106,7 @@ SIGNATURES = {
     "fea_time_spmv": [_P, C.c_int, C.c_int, C.POINTER(C.c_double)],
     "fea_adjoint_advdiff": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
     "fea_adjoint_advdiff_device": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
+    "fea_set_element_diffusivity_device": [_P, _P],
     "fea_batch_create": [C.POINTER(InstanceDesc), C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)],
     "fea_batch_destroy": [_P],
     "fea_batch_set_fields": [_P, C.c_int, _P, _P],
@@ -276,16 +277,41 @@ class CUDASolver:
         check(load().fea_get_idx_map(self._h, _ptr(idx), _ptr(ob)))
         return idx, ob
 
-    def adjoint_advdiff(self, u0, target, nsteps, checkpoint_every):
-        """(J, dJ/du0 node-indexed, dJ/dD per element) of the explicit advection-diffusion loss."""
+    def adjoint_advdiff(self, u0, target, nsteps, checkpoint_every, grads=True):
+        """(J, dJ/du0 node-indexed, dJ/dD per element) of the explicit advection-diffusion loss
+        (gradients None when grads is False: forward and loss only)."""
         u0 = np.ascontiguousarray(u0, dtype=np.float32)
         tg = np.ascontiguousarray(target, dtype=np.float32)
-        gu = np.zeros(self.vertices.shape[0], dtype=np.float32)
-        gd = np.zeros(self.triangles.shape[0], dtype=np.float32)
+        gu = np.zeros(self.vertices.shape[0], dtype=np.float32) if grads else None
+        gd = np.zeros(self.triangles.shape[0], dtype=np.float32) if grads else None
         J = C.c_double(0)
         check(load().fea_adjoint_advdiff(self._h, _ptr(u0), _ptr(tg), int(nsteps), int(checkpoint_every),
                                          C.byref(J), _ptr(gu), _ptr(gd)))
         return J.value, gu, gd
+
+    def adjoint_advdiff_device(self, u0, target, nsteps, checkpoint_every, grads=True):
+        """The same on CUDA tensors: u0 and target unknown-indexed [N] in the handle's precision;
+        returns (J, dJ/du0 [N], dJ/dD [T]) as tensors on the same device (None without grads)."""
+        import torch
+        dt = torch.float64 if self.precision == FP64 else torch.float32
+        u0 = u0.detach().to(dtype=dt).contiguous()
+        tg = target.detach().to(dtype=dt, device=u0.device).contiguous()
+        gu = torch.zeros_like(u0) if grads else None
+        gd = torch.zeros(self.triangles.shape[0], dtype=dt, device=u0.device) if grads else None
+        J = C.c_double(0)
+        torch.cuda.synchronize(u0.device)
+        check(load().fea_adjoint_advdiff_device(self._h, u0.data_ptr(), tg.data_ptr(), int(nsteps),
+                                                int(checkpoint_every), C.byref(J),
+                                                gu.data_ptr() if grads else None, gd.data_ptr() if grads else None))
+        return J.value, gu, gd
+
+    def set_element_diffusivity_device(self, D):
+        """Per-element diffusivity from a CUDA tensor [T] (handle precision)."""
+        import torch
+        dt = torch.float64 if self.precision == FP64 else torch.float32
+        D = D.detach().to(dtype=dt).contiguous()
+        torch.cuda.synchronize(D.device)
+        check(load().fea_set_element_diffusivity_device(self._h, D.data_ptr()))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -228,17 +228,29 @@ int fea_get_stream(fea_solver* s, void** stream);
 int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch);
 
 /* ---- adjoint (explicit advection-diffusion) ------------------------------
- * Loss J = 1/2 (u_N - target)^T M (u_N - target) after nsteps explicit
- * advection-diffusion steps from u0 with the current per-element diffusivity.
- * Writes J, dJ/du0 (node-indexed float[V]) and dJ/dD (float[T]).  Forward
+ * Model: nsteps steps of the advection-diffusion equation with
+ * advection_scheme 1 (A u' = B u, A = M/dt + c K_D, B = M/dt + s Adv, with
+ * c = advdiff_c, s = advection_sign and K_D = sum_e D_e K_e over the current
+ * per-element diffusivity) from u0.  Loss J = 1/2 (u_N - target)^T M
+ * (u_N - target).  Writes J, dJ/du0 and dJ/dD (per element) from the
+ * hand-written adjoint: each reverse step solves with the forward operator
+ * (A is symmetric) and back-propagates through the advection term; forward
  * states are recomputed from checkpoints every `checkpoint_every` steps.
- * No reference counterpart: the reference has no differentiation. */
+ * Gradient outputs may be NULL (NULL for both: forward and loss only).  The
+ * handle's field is left at u_N.  FEA_ERR_STATE for another equation or
+ * scheme.  No reference counterpart: the reference has no differentiation.
+ * Host variant: node-indexed float[V] u0, target and dJ/du0 (0 on Dirichlet
+ * points), dJ/dD float[T]. */
 int fea_adjoint_advdiff(fea_solver* s, const float* u0, const float* target, int64_t nsteps,
                         int64_t checkpoint_every, double* loss, float* grad_u0, float* grad_D);
-/* Device-resident variant, unknown-indexed arrays in the handle's precision;
- * grad_D is [T]. */
+/* Device-resident variant: unknown-indexed [N] u0, target and dJ/du0 and
+ * per-element [T] dJ/dD, all in the handle's precision. */
 int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target, int64_t nsteps,
                                int64_t checkpoint_every, double* loss, void* grad_u0, void* grad_D);
+/* Per-element diffusivity D_e from device memory in the handle's precision
+ * ([T]); like fea_set_element_fields without the float rounding for FP64
+ * handles.  No reference counterpart. */
+int fea_set_element_diffusivity_device(fea_solver* s, const void* diffusivity);
 
 /* ---- batched Gray-Scott ---------------------------------------------------
  * Many independent meshes with their own (F, k, Du, Dv, dt), stepped together:
