@@ -147,6 +147,66 @@ def batch_workload(n=BATCH_N, seed=0):
     return insts, starts
 
 
+# Adjoint inverse problem: advection-diffusion on the 512 x 512 jittered grid
+ADJ_GRID, ADJ_STEPS, ADJ_CKPT, ADJ_DT = 512, 200, 20, 1e-2
+
+
+def adjoint_workload(F, precision):
+    """Handle, initial field u0 and target (unknown-indexed CUDA tensors) and
+    the prior diffusivity: rotating velocity (-(y-0.5), x-0.5) * 0.5 per
+    element, hidden D_e = 1e-3 exp(0.5 g) with g a 16-mode Fourier field, a
+    seeded Gaussian u0; the target is the hidden model's final field and the
+    loss is evaluated at the prior D = 1e-3."""
+    import numpy as np
+    import torch
+    from fea_gb300 import meshgen as mg
+    xyz, tri = mg.jittered_grid(ADJ_GRID, seed=0)
+    cen = xyz[tri].mean(axis=1)
+    vel = (np.stack([-(cen[:, 1] - 0.5), cen[:, 0] - 0.5, np.zeros(len(tri))], 1) * 0.5).astype(np.float32)
+    hidden = 1e-3 * np.exp(0.5 * mg.fourier_field(cen, seed=1, n_modes=16))
+    rng = np.random.default_rng(2)
+    c = rng.uniform(0.3, 0.7, 2)
+    u0n = np.exp(-((xyz[:, 0] - c[0]) ** 2 + (xyz[:, 1] - c[1]) ** 2) / 0.02)
+    p = F.default_params(equation=F.ADVECTION_DIFFUSION, advection_scheme=1, advdiff_time_step=ADJ_DT,
+                         advdiff_c=1.0, velocity_mode=1, cg_tolerance=1e-12 if precision == F.FP64 else 1e-6)
+    s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=precision, params=p)
+    s.set_element_fields(velocity=vel)
+    dt = torch.float64 if precision == F.FP64 else torch.float32
+    u0 = torch.tensor(u0n, dtype=dt, device="cuda")  # Neumann: unknowns are the nodes
+    s.set_element_diffusivity_device(torch.tensor(hidden, dtype=dt, device="cuda"))
+    s.adjoint_advdiff_device(u0, torch.zeros_like(u0), ADJ_STEPS, ADJ_STEPS, grads=False)
+    target = torch.zeros_like(u0)
+    other = torch.zeros_like(u0)
+    torch.cuda.synchronize()
+    s.get_fields_device(target.data_ptr(), other.data_ptr())
+    prior = torch.full((len(tri),), 1e-3, dtype=dt, device="cuda")
+    s.set_element_diffusivity_device(prior)
+    return s, u0, target, prior, hidden
+
+
+def bench_adjoint(F):
+    """One loss + gradients evaluation (forward, checkpointed reverse sweep) in
+    FP64 and FP32, and the forward model alone."""
+    import torch
+    out = {"workload": f"advection-diffusion inverse problem, {ADJ_GRID}x{ADJ_GRID} jittered grid, rotating "
+                       f"velocity, implicit diffusion dt {ADJ_DT:g}, {ADJ_STEPS} steps, checkpoints every "
+                       f"{ADJ_CKPT}; loss 1/2 |u_N - target|_M^2, gradients w.r.t. u0 and per-element D"}
+    for name, prec in (("fp64", F.FP64), ("fp32", F.FP32)):
+        s, u0, target, prior, _ = adjoint_workload(F, prec)
+        s.adjoint_advdiff_device(u0, target, ADJ_STEPS, ADJ_CKPT)  # warm-up (graphs, allocations)
+        t0 = time.perf_counter()
+        J, gu, gD = s.adjoint_advdiff_device(u0, target, ADJ_STEPS, ADJ_CKPT)
+        t1 = time.perf_counter()
+        s.adjoint_advdiff_device(u0, target, ADJ_STEPS, ADJ_CKPT, grads=False)
+        t2 = time.perf_counter()
+        st = s.status()
+        out[name] = {"loss_and_gradients_ms": 1000 * (t1 - t0), "forward_only_ms": 1000 * (t2 - t1), "loss": J,
+                     "grad_u0_norm": float(torch.linalg.norm(gu)), "grad_D_norm": float(torch.linalg.norm(gD)),
+                     "cg_iterations_last_solve": int(st.last_iterations[0])}
+        s.close()
+    return out
+
+
 def bench_batched(F, steps, warmup, plain_steps):
     """The 256-instance sweep in one batch vs the plain loop of single-mesh
     handles (one after another, each advancing its own graph)."""
@@ -253,6 +313,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched sweep")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint inverse-problem timing")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--grid", type=int, default=GRID_N,
@@ -360,6 +421,7 @@ def main():
     batched = None
     if not args.no_batch:
         batched = bench_batched(F, args.batch_steps, 3, args.plain_steps)
+    adjoint = None if args.no_adjoint else bench_adjoint(F)
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -385,6 +447,7 @@ def main():
                          "ms_per_launch_l2_warm": spmv_warm_ms, "peak_source": peak_kind},
             "cpu_baseline": cpu,
             "batched": batched,
+            "adjoint": adjoint,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "status_flags": int(flags),

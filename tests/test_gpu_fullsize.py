@@ -1,9 +1,15 @@
-"""Full-size accuracy of the benchmark workload: Gray-Scott on the 1024 x 1024
-jittered grid (1,048,576 vertices), the bench's CG tolerance, FP32 fields.
+"""Full-size accuracy of the benchmark workloads.
 
-One step from a generic state (three FP64 oracle steps after the initial
-condition) must stay within rel-L2 1e-5 of the FP64 oracle per field; the
-drift over ten steps from the initial condition is checked too.
+Gray-Scott on the 1024 x 1024 jittered grid (1,048,576 vertices), the bench's
+CG tolerance, FP32 fields: one step from a generic state (three FP64 oracle
+steps after the initial condition) must stay within rel-L2 1e-5 of the FP64
+oracle per field; the drift over ten steps from the initial condition is
+checked too.
+
+The advection-diffusion inverse problem on the 512 x 512 grid (200 steps,
+checkpoints every 20, FP64): adjoint directional derivatives against central
+finite differences (eps 1e-4) of the GPU forward model on 32 random
+directions, to 1e-4.
 """
 import os
 
@@ -57,3 +63,27 @@ def test_ten_step_drift_full_size(fea, workload):
     eu, ev = rel_l2(ug, S.scatter(uo)), rel_l2(vg, S.scatter(vo))
     print(f"ten-step drift rel-L2: u {eu:.3e} v {ev:.3e}")
     assert eu < 1e-5 and ev < 1e-5
+
+
+def test_adjoint_inverse_problem_full_size(fea):
+    import bench
+    import torch
+    s, u0, target, prior, _ = bench.adjoint_workload(fea, fea.FP64)
+    steps, ck, eps = bench.ADJ_STEPS, bench.ADJ_CKPT, 1e-4
+    J, gu, gD = s.adjoint_advdiff_device(u0, target, steps, ck)
+    assert J > 0
+    gen = torch.Generator(device="cuda").manual_seed(5)
+
+    def loss(u, D):
+        s.set_element_diffusivity_device(D)
+        return s.adjoint_advdiff_device(u, target, steps, ck, grads=False)[0]
+
+    worst = 0.0
+    for k in range(32):
+        du = torch.randn(u0.shape, generator=gen, device="cuda", dtype=torch.float64)
+        dD = torch.randn(prior.shape, generator=gen, device="cuda", dtype=torch.float64)
+        pred = float(gu @ du + gD @ (prior * dD))
+        fd = (loss(u0 + eps * du, prior * (1 + eps * dD)) - loss(u0 - eps * du, prior * (1 - eps * dD))) / (2 * eps)
+        worst = max(worst, abs(fd - pred) / abs(pred))
+    print(f"adjoint vs central differences, 32 directions: worst relative error {worst:.2e}")
+    assert worst < 1e-4
