@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a
 template <typename R, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a) {
     __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
+    __shared__ FV<R, 2> ut[kTile];
     __shared__ double red[32 * kNV];
     const int wib = threadIdx.x >> 5;
     const int iter = iter_of(a), par = iter & 1;
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a
         c.set(iter, (const volatile BInst*)(a.inst + i));
         if (!c.any) continue;
         Acc<R> dots[kNV];  // gamma', delta', |r'|^2
-        cgcg_rows<R, 2, WCH>(v, c, (int64_t)tile * kTile + wib * 32, a.N, sm[wib], dots);
+        cgcg_tile<R, 2, WCH>(v, c, (int64_t)tile * kTile, a.N, sm[wib], ut, dots);
         double blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;

@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
 template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
+    __shared__ FV<R, NF> ut[kBlock];
     __shared__ double red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
@@ -130,11 +131,9 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
     v.w1 = a.wb[c.par ^ 1];
     v.s1 = a.sb[c.par ^ 1];
     const int wib = threadIdx.x >> 5;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
-    for (int64_t row0 = warp * 32; row0 < a.N; row0 += nwarps * 32)
-        cgcg_rows<R, NF, WCH>(v, c, row0, a.N, sm[wib], dots);
+    for (int64_t tile0 = blockIdx.x * (int64_t)kBlock; tile0 < a.N; tile0 += (int64_t)gridDim.x * kBlock)
+        cgcg_tile<R, NF, WCH>(v, c, tile0, a.N, sm[wib], ut, dots);
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)

@@ -274,33 +274,32 @@ __device__ __forceinline__ void cg_advance(const PhaseCtl<R, NF>& c, const FV<R,
     }
 }
 
-// One Chronopoulos-Gear iteration on one warp's rows (Jacobi-preconditioned
-// CG rearranged, Chronopoulos & Gear 1989, so that an iteration needs one
-// global reduction): with u = D^-1 r, w = A u and s = A p,
+// One Chronopoulos-Gear iteration on a tile of blockDim.x consecutive rows
+// starting at tile0 (one row per thread, 32 rows per warp), Jacobi-
+// preconditioned CG rearranged (Chronopoulos & Gear 1989) so that an
+// iteration needs one global reduction: with u = D^-1 r, w = A u, s = A p,
 //   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,
 //   u' = D^-1 r,  w' = A u',  gamma' = r.u',  delta' = w'.u'.
-// The SpMV recomputes u' at each gathered column from the old r, w and s
-// there; every row owner applies the vector updates.  dots[] receives gamma',
-// delta' and |r'|^2 per field.
+// Each thread first applies the vector updates to its own row and leaves u'
+// in the tile's shared-memory slice ut[]; after a block barrier the SpMV
+// takes u' of in-tile columns from there and recomputes it from the old r, w
+// and s in global memory only for columns outside the tile (few, in the
+// solver's Morton order).  dots[] receives gamma', delta' and |r'|^2 per
+// field.  Every thread of the block must call it (it holds barriers).
 template <typename R, int NF, int WCH>
-__device__ __forceinline__ void cgcg_rows(const CgVecs<R, NF>& v, const PhaseCtl<R, NF>& c, int64_t row0, int64_t N,
-                                          FV<R, NF>* smw, Acc<R> (&dots)[3 * NF]) {
-    const FV<R, NF> wn = warp_rows<R, NF, WCH>(v.rp, v.col, v.A, row0, N, smw, [&](int32_t col) {
-        const FV<R, NF> ro = ldv(v.r0 + col, false), wo = ldv(v.w0 + col, false);
-        const FV<R, NF> d = ldv(v.dinv + col, false);
-        FV<R, NF> so = wo;
-        if (c.need_old) so = ldv(v.s0 + col, false);
-        FV<R, NF> sn, rn, un;
-        cg_advance(c, ro, wo, so, d, sn, rn, un);
-        return un;
-    });
-    const int64_t row = row0 + (threadIdx.x & 31);
+__device__ __forceinline__ void cgcg_tile(const CgVecs<R, NF>& v, const PhaseCtl<R, NF>& c, int64_t tile0,
+                                          int64_t N, FV<R, NF>* smw, FV<R, NF>* ut, Acc<R> (&dots)[3 * NF]) {
+    const int t = threadIdx.x;
+    const int64_t row = tile0 + t;
+    FV<R, NF> un;
+#pragma unroll
+    for (int f = 0; f < NF; f++) un.v[f] = 0;
     if (row < N) {
         const FV<R, NF> ro = ldv(v.r0 + row, false), wo = ldv(v.w0 + row, false), d = ldv(v.dinv + row, false);
         FV<R, NF> so = wo;
         if (c.need_old) so = ldv(v.s0 + row, false);
         FV<R, NF> x = v.x[row], p = v.p[row];
-        FV<R, NF> sn, rn, un;
+        FV<R, NF> sn, rn;
         cg_advance(c, ro, wo, so, d, sn, rn, un);
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -310,15 +309,33 @@ __device__ __forceinline__ void cgcg_rows(const CgVecs<R, NF>& v, const PhaseCtl
                 x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
             }
             dots[f].add_prod(rn.v[f], un.v[f]);
-            dots[NF + f].add_prod(wn.v[f], un.v[f]);
             dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
         }
         v.x[row] = x;
         v.p[row] = p;
         v.r1[row] = rn;
         v.s1[row] = sn;
-        v.w1[row] = wn;
     }
+    ut[t] = un;
+    __syncthreads();
+    const uint32_t span = blockDim.x;
+    const FV<R, NF> wn = warp_rows<R, NF, WCH>(v.rp, v.col, v.A, tile0 + (t & ~31), N, smw, [&](int32_t col) {
+        const uint32_t o = (uint32_t)(col - tile0);
+        if (o < span) return ut[o];
+        const FV<R, NF> ro = ldv(v.r0 + col, false), wo = ldv(v.w0 + col, false);
+        const FV<R, NF> d = ldv(v.dinv + col, false);
+        FV<R, NF> so = wo;
+        if (c.need_old) so = ldv(v.s0 + col, false);
+        FV<R, NF> sn, rn, u2;
+        cg_advance(c, ro, wo, so, d, sn, rn, u2);
+        return u2;
+    });
+    if (row < N) {
+        v.w1[row] = wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
+    }
+    __syncthreads();  // the next tile reuses ut[]
 }
 
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
