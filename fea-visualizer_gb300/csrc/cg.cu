@@ -140,6 +140,71 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
+// The same two kernels on the tile-ELL layout (variant 0): one block per
+// 256-row tile (grid-stride), the tile's operand staged in dynamic shared
+// memory (kTileRows + hmax entries).
+template <typename R, int NF>
+__device__ __forceinline__ EllView<R, NF> ell_view(const StepArgs<R, NF>& a) {
+    return EllView<R, NF>{a.As, a.lcol, a.slice_off, a.halo_off, a.halo_col};
+}
+
+template <typename R, int NF>
+__global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
+    __shared__ double red[32 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    FV<R, NF>* w = a.wb[c.par];
+    const EllView<R, NF> e = ell_view(a);
+    const int64_t ntiles = ceil_div(a.N, kTileRows);
+    Acc<R> dot[NF];
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) init_tile_ell(e, a.z, w, tile, a.N, ut, dot);
+    double blk[NF], tot[NF];
+    block_totals<NF>(dot, red, blk);
+    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
+        volatile CgState* cg = a.cg;
+        finish_spmv<R, NF>(cg, &a.run->flags, c.act, tot);
+        int any = 0;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            cg->fresh[f] = 1;
+            any |= cg->active[f];
+        }
+        signal_loop(a, any != 0);
+    }
+}
+
+template <typename R, int NF>
+__global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
+    __shared__ double red[32 * 3 * NF];
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[c.par];
+    v.w0 = a.wb[c.par];
+    v.s0 = a.sb[c.par];
+    v.r1 = a.rb[c.par ^ 1];
+    v.w1 = a.wb[c.par ^ 1];
+    v.s1 = a.sb[c.par ^ 1];
+    const EllView<R, NF> e = ell_view(a);
+    const int64_t ntiles = ceil_div(a.N, kTileRows);
+    Acc<R> dots[3 * NF];
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) cgcg_tile_ell(v, e, c, tile, a.N, ut, dots);
+    double blk[3 * NF], tot[3 * NF];
+    block_totals<3 * NF>(dots, red, blk);
+    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+        signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
+}
+
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
 // previous solution), z = D^-1 r, p = z, and the CG set-up scalars.  Also the
 // has_numerical_instability test of the state entering the step.
@@ -412,12 +477,31 @@ int g_max_grid = 0;
 
 constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
 
+// The CG kernels of a variant: WCH > 0 the windowed CSR kernels (entries per
+// lane and window), 0 the tile-ELL kernels with their dynamic shared memory.
+template <typename R, int NF, int WCH>
+struct CgKernels {
+    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init<R, NF, WCH>;
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter<R, NF, WCH>;
+    static size_t smem(const StepArgs<R, NF>&) { return 0; }
+};
+template <typename R, int NF>
+struct CgKernels<R, NF, 0> {
+    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init_ell<R, NF>;
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_ell<R, NF>;
+    static size_t smem(const StepArgs<R, NF>& a) { return sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax); }
+};
+
 template <typename R, int NF, int WCH>
 struct Grids {
+    using K = CgKernels<R, NF, WCH>;
     int spmv, iter, rhs, stream;
-    explicit Grids(int64_t N) {
-        spmv = wave_grid(k_cgcg_init<R, NF, WCH>, ceil_div(N, kBlock));
-        iter = wave_grid(k_cgcg_iter<R, NF, WCH>, ceil_div(N, kBlock));
+    size_t smem;
+    explicit Grids(const StepArgs<R, NF>& a) {
+        const int64_t N = a.N;
+        smem = K::smem(a);
+        spmv = wave_grid(K::init, ceil_div(N, kBlock), smem);
+        iter = wave_grid(K::iter, ceil_div(N, kBlock), smem);
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -442,7 +526,8 @@ struct LoopArgs {
 template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     LoopArgs<R, NF> L(base, lf, 1);
-    const Grids<R, NF, WCH> g(base.N);
+    const Grids<R, NF, WCH> g(base);
+    using K = CgKernels<R, NF, WCH>;
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
     G.graph = top;
@@ -454,14 +539,14 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a1);
+    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a1);
+    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, k_cgcg_init<R, NF, WCH>, g.spmv, kBlock, L.a2);
+    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, k_cgcg_iter<R, NF, WCH>, g.iter, kBlock, L.a2);
+    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -482,7 +567,8 @@ int read_flag(const int* d, cudaStream_t st) {
 template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
-    const Grids<R, NF, WCH> g(base.N);
+    const Grids<R, NF, WCH> g(base);
+    using K = CgKernels<R, NF, WCH>;
     k_start<R, NF><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_flag(&lf->step, st)) {
@@ -493,10 +579,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                 k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            k_cgcg_init<R, NF, WCH><<<g.spmv, kBlock, 0, st>>>(*la);
+            K::init<<<g.spmv, kBlock, g.smem, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                k_cgcg_iter<R, NF, WCH><<<g.iter, kBlock, 0, st>>>(*la);
+                K::iter<<<g.iter, kBlock, g.smem, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -515,6 +601,7 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
 template <typename R, int NF, int EQ>
 void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags* lf, cudaStream_t st) {
     switch (wch) {
+    case 0: G ? build_graph_t<R, NF, EQ, 0>(*G, a, lf) : run_stream_t<R, NF, EQ, 0>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -581,14 +668,21 @@ void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st) {
     FEA_CHECK_LAUNCH();
 }
 
+template <typename R, int NF, int WCH>
+void probe_t(const StepArgs<R, NF>& a, cudaStream_t st) {
+    const Grids<R, NF, WCH> g(a);
+    CgKernels<R, NF, WCH>::iter<<<g.iter, kBlock, g.smem, st>>>(a);
+    FEA_CHECK_LAUNCH();
+}
+
 template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     switch (wch) {
-    case 4: k_cgcg_iter<R, NF, 4><<<Grids<R, NF, 4>(a.N).iter, kBlock, 0, st>>>(a); break;
-    case 16: k_cgcg_iter<R, NF, 16><<<Grids<R, NF, 16>(a.N).iter, kBlock, 0, st>>>(a); break;
-    default: k_cgcg_iter<R, NF, 8><<<Grids<R, NF, 8>(a.N).iter, kBlock, 0, st>>>(a); break;
+    case 0: probe_t<R, NF, 0>(a, st); break;
+    case 4: probe_t<R, NF, 4>(a, st); break;
+    case 16: probe_t<R, NF, 16>(a, st); break;
+    default: probe_t<R, NF, 8>(a, st); break;
     }
-    FEA_CHECK_LAUNCH();
 }
 
 #define FEA_INST_STEP(R, NF)                                                                              \

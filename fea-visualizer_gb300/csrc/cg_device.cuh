@@ -338,6 +338,126 @@ __device__ __forceinline__ void cgcg_tile(const CgVecs<R, NF>& v, const PhaseCtl
     __syncthreads();  // the next tile reuses ut[]
 }
 
+// ---- tile-ELL bodies (layout: tile_ell.cu) -------------------------------------
+
+template <typename R, int NF>
+struct EllView {
+    const FV<R, NF>* As;
+    const uint16_t* lcol;
+    const int32_t* slice_off;
+    const int32_t* halo_off;
+    const int32_t* halo_col;
+};
+
+// Product of tile `tile` with the operand staged in ut[] (tile rows, then the
+// tile's halo): thread t returns row tile*kTileRows + t.  Warp w reads slice
+// w column by column: each step loads 32 consecutive values and 16-bit local
+// indices and gathers from shared memory; entries are summed in row order.
+template <typename R, int NF>
+__device__ __forceinline__ FV<R, NF> ell_rows(const EllView<R, NF>& e, int64_t tile, const FV<R, NF>* ut) {
+    const int t = threadIdx.x;
+    const int64_t s = tile * (kTileRows / 32) + (t >> 5);
+    const int32_t b = ldg(e.slice_off + s);
+    const int32_t w = (ldg(e.slice_off + s + 1) - b) >> 5;
+    const FV<R, NF>* ap = e.As + b + (t & 31);
+    const uint16_t* lp = e.lcol + b + (t & 31);
+    FV<R, NF> acc;
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc.v[f] = 0;
+#pragma unroll 4
+    for (int k = 0; k < w; k++) {
+        const FV<R, NF> a = ldv(ap + 32 * k, false);
+        const FV<R, NF> g = ut[__ldg(lp + 32 * k)];
+#pragma unroll
+        for (int f = 0; f < NF; f++) acc.v[f] = fma(a.v[f], g.v[f], acc.v[f]);
+    }
+    return acc;
+}
+
+// u' of one unknown from the old r, w, s and D^-1 in global memory.
+template <typename R, int NF>
+__device__ __forceinline__ FV<R, NF> cg_u_at(const CgVecs<R, NF>& v, const PhaseCtl<R, NF>& c, int64_t i) {
+    const FV<R, NF> ro = ldv(v.r0 + i, false), wo = ldv(v.w0 + i, false), d = ldv(v.dinv + i, false);
+    FV<R, NF> so = wo;
+    if (c.need_old) so = ldv(v.s0 + i, false);
+    FV<R, NF> sn, rn, un;
+    cg_advance(c, ro, wo, so, d, sn, rn, un);
+    return un;
+}
+
+// One Chronopoulos-Gear iteration on tile `tile` in the tile-ELL layout (the
+// recurrences as in cgcg_tile).  Each thread updates its row and stages u';
+// the tile's halo columns get u' recomputed from the old r, w, s; after a
+// barrier every gathered operand comes from shared memory.  ut[] holds
+// kTileRows + the layout's largest halo.  Every thread of the block calls it.
+template <typename R, int NF>
+__device__ __forceinline__ void cgcg_tile_ell(const CgVecs<R, NF>& v, const EllView<R, NF>& e,
+                                              const PhaseCtl<R, NF>& c, int64_t tile, int64_t N, FV<R, NF>* ut,
+                                              Acc<R> (&dots)[3 * NF]) {
+    const int t = threadIdx.x;
+    const int64_t row = tile * kTileRows + t;
+    FV<R, NF> un;
+#pragma unroll
+    for (int f = 0; f < NF; f++) un.v[f] = 0;
+    if (row < N) {
+        const FV<R, NF> ro = ldv(v.r0 + row, false), wo = ldv(v.w0 + row, false), d = ldv(v.dinv + row, false);
+        FV<R, NF> so = wo;
+        if (c.need_old) so = ldv(v.s0 + row, false);
+        FV<R, NF> x = v.x[row], p = v.p[row];
+        FV<R, NF> sn, rn;
+        cg_advance(c, ro, wo, so, d, sn, rn, un);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            if (c.act[f]) {
+                const R ui = d.v[f] * ro.v[f];
+                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+            }
+            dots[f].add_prod(rn.v[f], un.v[f]);
+            dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+        }
+        v.x[row] = x;
+        v.p[row] = p;
+        v.r1[row] = rn;
+        v.s1[row] = sn;
+    }
+    ut[t] = un;
+    const int32_t h0 = ldg(e.halo_off + tile), h1 = ldg(e.halo_off + tile + 1);
+    for (int32_t h = h0 + t; h < h1; h += blockDim.x) ut[kTileRows + (h - h0)] = cg_u_at(v, c, ldg(e.halo_col + h));
+    __syncthreads();
+    const FV<R, NF> wn = ell_rows(e, tile, ut);
+    if (row < N) {
+        v.w1[row] = wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
+    }
+    __syncthreads();  // the next tile reuses ut[]
+}
+
+// Set-up product w = A z on tile `tile` in the tile-ELL layout, z.w into dot[].
+template <typename R, int NF>
+__device__ __forceinline__ void init_tile_ell(const EllView<R, NF>& e, const FV<R, NF>* __restrict__ z,
+                                              FV<R, NF>* __restrict__ w, int64_t tile, int64_t N, FV<R, NF>* ut,
+                                              Acc<R> (&dot)[NF]) {
+    const int t = threadIdx.x;
+    const int64_t row = tile * kTileRows + t;
+    FV<R, NF> zr;
+#pragma unroll
+    for (int f = 0; f < NF; f++) zr.v[f] = 0;
+    if (row < N) zr = ldv(z + row, false);
+    ut[t] = zr;
+    const int32_t h0 = ldg(e.halo_off + tile), h1 = ldg(e.halo_off + tile + 1);
+    for (int32_t h = h0 + t; h < h1; h += blockDim.x) ut[kTileRows + (h - h0)] = ldv(z + ldg(e.halo_col + h), false);
+    __syncthreads();
+    const FV<R, NF> wr = ell_rows(e, tile, ut);
+    if (row < N) {
+        w[row] = wr;
+#pragma unroll
+        for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
+    }
+    __syncthreads();
+}
+
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
 // (S: CgState or a batched instance's state; flags receives FEA_STATUS_*.)
 template <typename R, int NF, typename S>
@@ -417,14 +537,14 @@ __device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act
 
 template <typename... P>
 cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...), int grid, int block,
-                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg) {
+                           const typename std::tuple_element<0, std::tuple<P...>>::type& arg, size_t smem = 0) {
     auto local = arg;
     void* argv[] = {(void*)&local};
     cudaKernelNodeParams kp = {};
     kp.func = (void*)fn;
     kp.gridDim = dim3((unsigned)grid);
     kp.blockDim = dim3((unsigned)block);
-    kp.sharedMemBytes = 0;
+    kp.sharedMemBytes = (unsigned int)smem;
     kp.kernelParams = argv;
     cudaGraphNode_t n;
     FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
@@ -444,11 +564,14 @@ cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphCondition
 }
 
 // Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
-// calculator), capped by the work and by the partial-sum stride.
+// calculator, with `smem` bytes of dynamic shared memory, opted in above the
+// default 48 KB), capped by the work and by the partial-sum stride.
 template <typename K>
-int wave_grid(K kernel, int64_t work_blocks) {
+int wave_grid(K kernel, int64_t work_blocks, size_t smem = 0) {
+    if (smem > 48 * 1024)
+        FEA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     int64_t g = (int64_t)num_sms() * per_sm;
     if (g > max_grid_blocks()) g = max_grid_blocks();

@@ -32,6 +32,31 @@ int64_t build_idx_map(const uint8_t* ob, int64_t V, int bc, int32_t* idx, cudaSt
 void build_pattern(Pattern& P, DeviceArena& keep, const uint32_t* tri, int64_t T, const uint8_t* ob,
                    const int32_t* idx, int bc, int64_t N, cudaStream_t st);
 
+// ---- tile-ELL operator layout (tile_ell.cu) ----------------------------------------
+// Tiles of kTileRows solver-order rows (one row per thread of a kBlock-thread
+// block), 32-row slices stored column by column, 16-bit tile-local column
+// indices into [tile rows | tile halo].
+constexpr int kTileRows = kBlock;
+constexpr size_t kEllSmemBudget = 96 * 1024;  // largest staged operand per block
+struct TileEll {
+    int64_t E = 0;  // stored entries, padding included
+    int ntiles = 0, hmax = 0;
+    int32_t* slice_off = nullptr;  // [ntiles * 8 + 1] first entry of each slice
+    int32_t* halo_off = nullptr;   // [ntiles + 1]
+    int32_t* halo_col = nullptr;   // sorted distinct out-of-tile columns per tile
+    uint16_t* lcol = nullptr;      // [E] local column index
+    int32_t* emap = nullptr;       // [E] CSR slot of each entry, -1 for padding
+    bool ok = false;
+};
+// From host copies of a solver-order CSR pattern.  Returns false (L.ok false)
+// when a tile's halo does not fit the 16-bit indices or `smem_budget` bytes of
+// shared memory at fv_bytes per operand.
+bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& col, int64_t N, size_t fv_bytes,
+                    size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st);
+// As[k] = A[emap[k]] (0 for padding): the layout's copy of operator values.
+template <typename R, int NF>
+void fill_tile_ell(const TileEll& L, const FV<R, NF>* A, FV<R, NF>* As, cudaStream_t st);
+
 // ---- assembly (assemble.cu) ---------------------------------------------------
 template <typename R>
 void element_matrices(const float* xyz, const uint32_t* tri, int64_t T, int vel_mode, const float vel[3],
@@ -124,6 +149,13 @@ struct StepArgs {
     R* ut;                  // Newmark predictors
     R* vt;
     const R* rhs;           // EQ_GIVEN: right-hand side [N]
+    // tile-ELL copy of A (the CG kernels' layout when ell.ok)
+    const FV<R, NF>* As;
+    const uint16_t* lcol;
+    const int32_t* slice_off;
+    const int32_t* halo_off;
+    const int32_t* halo_col;
+    int hmax;
     const StepParams* prm;
     CgState* cg;
     RunState* run;

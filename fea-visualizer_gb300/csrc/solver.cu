@@ -157,6 +157,8 @@ struct fea_solver {
     int32_t* emap = nullptr;        // [nnz] solver slot -> assembly slot
     int32_t* idx_c = nullptr;       // [V] node -> solver index (-1 on Dirichlet points)
     void *Kc = nullptr, *Mc = nullptr, *Advc = nullptr;        // values in solver order
+    TileEll ell;                    // the CG kernels' layout of Pc (tile_ell.cu)
+    void *S1 = nullptr, *S0 = nullptr, *S2 = nullptr;          // tile-ELL copies of A1, A0, A2
     std::vector<float> h_xyz;       // host copy of the points (ordering keys)
     uint8_t* adv_present = nullptr;
     Fields F;
@@ -171,7 +173,7 @@ struct fea_solver {
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
-    int lanes = 8;  // SpMV variant: entries per lane and window (4, 8, 16)
+    int lanes = 8;  // CG kernel variant: 0 tile-ELL, else CSR entries per lane and window (4, 8, 16)
     bool op_dirty = true;
     int op_kind = -1;
     bool acc_valid = false;
@@ -252,9 +254,10 @@ uint64_t spread3(uint32_t x) {  // 21 bits -> every third bit of 63
 
 // The solver's ordering of the unknowns: sorted by the 63-bit Morton key of
 // their points (coordinates quantised to 21 bits over the bounding box), ties
-// by unknown number.  Neighbouring points get nearby numbers, so the columns a
-// warp gathers sit in few cache lines.  Computed on the host once per mesh and
-// boundary condition.
+// by unknown number, then by stored-entry count within each tile of
+// kTileRows rows.  Neighbouring points get nearby numbers, so a tile is a
+// compact patch whose rows mostly reference each other.  Computed on the host
+// once per mesh and boundary condition.
 void build_ordering(fea_solver* s) {
     cudaStream_t st = s->stream;
     const int64_t V = s->V, N = s->N;
@@ -283,11 +286,18 @@ void build_ordering(fea_solver* s) {
         key.emplace_back(m, idx[i]);
     }
     std::sort(key.begin(), key.end());
+    // within each tile of kTileRows rows, rows by stored-entry count, so the
+    // 32-row slices of the tile-ELL layout carry little padding (the tile's
+    // row set, hence its locality, is that of the Morton order)
+    std::vector<int32_t> rp(N + 1);
+    FEA_CUDA_TRY(cudaMemcpyAsync(rp.data(), s->P.row_ptr, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
     std::vector<int32_t> pos(N), inv(N);
-    for (int64_t c = 0; c < N; c++) {
-        inv[c] = key[c].second;
-        pos[key[c].second] = (int32_t)c;
-    }
+    for (int64_t c = 0; c < N; c++) inv[c] = key[c].second;
+    for (int64_t t0 = 0; t0 < N; t0 += kTileRows)
+        std::stable_sort(inv.begin() + t0, inv.begin() + std::min<int64_t>(N, t0 + kTileRows),
+                         [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] < rp[b + 1] - rp[b]; });
+    for (int64_t c = 0; c < N; c++) pos[inv[c]] = (int32_t)c;
     s->pos = s->mat_mem.alloc<int32_t>(N);
     s->inv = s->mat_mem.alloc<int32_t>(N);
     s->emap = s->mat_mem.alloc<int32_t>(s->P.nnz);
@@ -308,6 +318,8 @@ void build_context(fea_solver* s) {
     s->mat_mem.release();
     s->P = Pattern{};
     s->Pc = Pattern{};
+    s->ell = TileEll{};
+    s->S1 = s->S0 = s->S2 = nullptr;
     s->F = Fields{};
     cudaStream_t st = s->stream;
     s->idx = s->mat_mem.alloc<int32_t>(s->V);
@@ -315,6 +327,20 @@ void build_context(fea_solver* s) {
     build_pattern(s->P, s->mat_mem, s->tri, s->T, s->ob, s->idx, s->bc, s->N, st);
     const int64_t N = s->N, nnz = s->P.nnz, T = s->T;
     build_ordering(s);
+    {
+        std::vector<int32_t> rp(N + 1), col(nnz);
+        FEA_CUDA_TRY(cudaMemcpyAsync(rp.data(), s->Pc.row_ptr, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, st));
+        if (nnz > 0)
+            FEA_CUDA_TRY(cudaMemcpyAsync(col.data(), s->Pc.col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, st));
+        FEA_CUDA_TRY(cudaStreamSynchronize(st));
+        build_tile_ell(rp, col, N, 2 * rsize(s), kEllSmemBudget, s->ell, s->mat_mem, st);
+        if (s->ell.ok) {
+            s->S1 = ralloc(s->mat_mem, s, s->ell.E);
+            s->S0 = ralloc(s->mat_mem, s, s->ell.E);
+            s->S2 = ralloc(s->mat_mem, s, 2 * s->ell.E);
+        }
+        s->lanes = s->ell.ok ? 0 : 8;
+    }
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
     s->Mloc = s->mat_mem.alloc<double>(9 * T);
     s->Aloc = s->mat_mem.alloc<double>(9 * T);
@@ -417,6 +443,15 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
     a.a = (R*)F.a;
     a.ut = (R*)F.ut;
     a.vt = (R*)F.vt;
+    if (s->ell.ok) {
+        if constexpr (NF == 1) a.As = (const FV<R, 1>*)(init_op ? s->S0 : s->S1);
+        else a.As = (const FV<R, 2>*)s->S2;
+        a.lcol = s->ell.lcol;
+        a.slice_off = s->ell.slice_off;
+        a.halo_off = s->ell.halo_off;
+        a.halo_col = s->ell.halo_col;
+        a.hmax = s->ell.hmax;
+    }
     a.prm = s->d_prm;
     a.cg = s->d_cg;
     a.run = s->d_run;
@@ -476,6 +511,7 @@ void update_operator(fea_solver* s, int kind) {
         c.f[1] = {dt, (double)p.rd_Dv, 1.0, 0.0};
         combine_operator<R, 2>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
                                s->stream);
+        fill_tile_ell<R, 2>(s->ell, (const FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->S2, s->stream);
     } else {
         OpCoef<1> c{};
         c.f[0] = {dt, 0.0, 1.0, 0.0};
@@ -498,9 +534,11 @@ void update_operator(fea_solver* s, int kind) {
             m.f[0] = {1.0, 0.0, 1.0, 0.0};
             combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, m, (FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->F.d0,
                                    s->stream);
+            fill_tile_ell<R, 1>(s->ell, (const FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->S0, s->stream);
         }
         combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
                                s->stream);
+        fill_tile_ell<R, 1>(s->ell, (const FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->S1, s->stream);
     }
 }
 
@@ -1259,10 +1297,11 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[3] = {4, 8, 16};
+    const int cand[4] = {0, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
+        if (l == 0 && !s->ell.ok) continue;
         probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
