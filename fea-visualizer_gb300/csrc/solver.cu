@@ -1322,6 +1322,16 @@ int fea_autotune(fea_solver* s) {
     API_END
 }
 
+int fea_set_cg_variant(fea_solver* s, int variant) {
+    API_BEGIN
+    check_handle(s);
+    if (variant != 0 && variant != 4 && variant != 8 && variant != 16)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 4, 8 or 16");
+    if (variant == 0 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
+    s->lanes = variant;
+    API_END
+}
+
 int fea_get_stream(fea_solver* s, void** stream) {
     API_BEGIN
     check_handle(s);

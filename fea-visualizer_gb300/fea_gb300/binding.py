@@ -102,6 +102,7 @@ SIGNATURES = {
     "fea_get_matrix": [_P, C.c_int, _P, _P, _P, _P],
     "fea_get_idx_map": [_P, _P, _P],
     "fea_autotune": [_P],
+    "fea_set_cg_variant": [_P, C.c_int],
     "fea_get_stream": [_P, C.POINTER(C.c_void_p)],
     "fea_time_spmv": [_P, C.c_int, C.c_int, C.POINTER(C.c_double)],
     "fea_adjoint_advdiff": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
@@ -249,6 +250,10 @@ class CUDASolver:
     def autotune(self):
         check(load().fea_autotune(self._h))
         return self.info.rows_per_warp_lanes
+
+    def set_cg_variant(self, variant: int):
+        """0: tile-ELL kernels; 4, 8, 16: windowed CSR kernels."""
+        check(load().fea_set_cg_variant(self._h, int(variant)))
 
     def stream(self) -> int:
         """cudaStream_t of the handle, as an integer."""

@@ -116,7 +116,7 @@ typedef struct {
     int64_t max_row_nonzeros;    /* FEMContext::compute_max_row_nonzeros (:207-219) */
     int precision;               /* FEA_FP32 / FEA_FP64 */
     int boundary_condition;
-    int rows_per_warp_lanes;     /* lanes per CSR row chosen for the SpMV */
+    int rows_per_warp_lanes;     /* CG kernel variant (fea_autotune): 0 tile-ELL, else CSR window */
     int64_t device_bytes;        /* device memory held by the handle */
 } fea_info;
 
@@ -208,11 +208,16 @@ int fea_get_matrix(fea_solver* s, int which, int32_t* row_ptr, int32_t* col, voi
 /* Node -> unknown map (FEMContext::idx_map, int32[V]) and boundary flags. */
 int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
 
-/* Pick the window size of the warp-cooperative CSR kernels (4, 8 or 16
- * entries per lane and window) by timing one CG iteration of each candidate
- * on this mesh; the choice is kept in fea_info.rows_per_warp_lanes.  Leaves
- * the fields unchanged. */
+/* CG kernel variants: 0 = tile-ELL layout (256-row tiles, 32-row slices
+ * stored column-wise, operand and halo staged in shared memory; the default
+ * when the mesh's halos fit), 4 / 8 / 16 = warp-cooperative CSR with that
+ * many entries per lane and window.  fea_autotune times one CG iteration of
+ * each candidate on this mesh and keeps the fastest (fea_info.
+ * rows_per_warp_lanes); the fields are left unchanged. */
 int fea_autotune(fea_solver* s);
+/* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
+ * FEA_ERR_UNSUPPORTED for 0 when the layout is unavailable on this mesh). */
+int fea_set_cg_variant(fea_solver* s, int variant);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
  * their own work or events after it. */

@@ -270,11 +270,38 @@ def test_step_determinism(fea):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("lanes", [2, 4, 8, 16])
-def test_autotune_choice_is_valid(fea, lanes):
+def test_autotune_choice_is_valid(fea):
     xyz, tri = mg.jittered_grid(129, seed=1)
     s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
-    assert s.autotune() in (2, 4, 8, 16)
+    assert s.info.rows_per_warp_lanes == 0  # the tile-ELL layout is the default
+    assert s.autotune() in (0, 4, 8, 16)
+    with pytest.raises(fea.FeaError):
+        s.set_cg_variant(3)
+
+
+@pytest.mark.parametrize("name", ["grid33", "ico3", "cyl"])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_cg_variants_agree(fea, oracle_mod, name, bc):
+    """Every CG kernel variant steps to the oracle's result (Gray-Scott, two fields)."""
+    xyz, tri = MESHES[name]()
+    u0, v0 = mg.gray_scott_patches(xyz, seed=6, side=0.3) if np.ptp(xyz[:, 2]) == 0 else \
+        mg.sphere_patches(xyz / np.linalg.norm(xyz, axis=1, keepdims=True), seed=6, n_patches=5, radius=0.4)
+    kw = dict(rd_time_step=0.5, rd_Du=2e-3, rd_Dv=1e-3, rd_feed_rate=0.04, rd_kill_rate=0.06)
+    S = oracle_mod.System(xyz, tri, bc=bc)
+    p = None
+    outs = []
+    for variant in (0, 4, 8, 16):
+        s = _solver(fea, xyz, tri, bc, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-7, **kw)
+        s.set_cg_variant(variant)
+        s.set_fields(u0, v0)
+        s.advance_time(2)
+        outs.append(s.get_fields())
+        p = s.params
+    uo, vo, *_ = oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
+                             S.gather(v0), 2, Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate,
+                             reaction_mode=1)
+    for variant, (ug, vg) in zip((0, 4, 8, 16), outs):
+        assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, variant
 
 
 def test_boundary_condition_switch(fea, oracle_mod):
