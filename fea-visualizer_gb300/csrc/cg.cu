@@ -148,7 +148,26 @@ __device__ __forceinline__ EllView<R, NF> ell_view(const StepArgs<R, NF>& a) {
     return EllView<R, NF>{a.As, a.lcol, a.slice_off, a.halo_off, a.halo_col};
 }
 
-template <typename R, int NF>
+// Tile loop of the tile-ELL kernels: block b takes tiles b, b + G, ...;
+// consecutive tiles alternate the two staging buffers of ut (each kTileRows +
+// hmax entries of dynamic shared memory), and every tile's slice and halo
+// references are loaded one tile ahead.
+template <typename R, int NF, typename Body>
+__device__ __forceinline__ void ell_tiles(const StepArgs<R, NF>& a, FV<R, NF>* ut, Body body) {
+    const EllView<R, NF> e = ell_view(a);
+    const int64_t ntiles = ceil_div(a.N, kTileRows);
+    const int stride = kTileRows + a.hmax;
+    EllTileRef ref = ell_ref(e, (int64_t)blockIdx.x, ntiles);
+    int buf = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const EllTileRef next = ell_ref(e, tile + gridDim.x, ntiles);
+        body(e, tile, ref, ut + buf * stride);
+        ref = next;
+        buf ^= 1;
+    }
+}
+
+template <typename R, int NF, int KPRE>
 __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
@@ -156,10 +175,10 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     FV<R, NF>* w = a.wb[c.par];
-    const EllView<R, NF> e = ell_view(a);
-    const int64_t ntiles = ceil_div(a.N, kTileRows);
     Acc<R> dot[NF];
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) init_tile_ell(e, a.z, w, tile, a.N, ut, dot);
+    ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
+        init_tile_ell<R, NF, KPRE>(e, a.z, w, tile, ref, a.N, buf, dot);
+    });
     double blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
     if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
@@ -175,7 +194,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     }
 }
 
-template <typename R, int NF>
+template <typename R, int NF, int KPRE>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
@@ -195,10 +214,10 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     v.r1 = a.rb[c.par ^ 1];
     v.w1 = a.wb[c.par ^ 1];
     v.s1 = a.sb[c.par ^ 1];
-    const EllView<R, NF> e = ell_view(a);
-    const int64_t ntiles = ceil_div(a.N, kTileRows);
     Acc<R> dots[3 * NF];
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) cgcg_tile_ell(v, e, c, tile, a.N, ut, dots);
+    ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
+        cgcg_tile_ell<R, NF, KPRE>(v, e, c, tile, ref, a.N, buf, dots);
+    });
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -485,12 +504,18 @@ struct CgKernels {
     static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter<R, NF, WCH>;
     static size_t smem(const StepArgs<R, NF>&) { return 0; }
 };
-template <typename R, int NF>
-struct CgKernels<R, NF, 0> {
-    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init_ell<R, NF>;
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_ell<R, NF>;
-    static size_t smem(const StepArgs<R, NF>& a) { return sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax); }
+// Variants 0 and 1: the tile-ELL kernels with 8 or 4 entries per row
+// prefetched into registers; two staging buffers of kTileRows + hmax entries.
+template <typename R, int NF, int KPRE>
+struct EllKernels {
+    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init_ell<R, NF, KPRE>;
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_ell<R, NF, KPRE>;
+    static size_t smem(const StepArgs<R, NF>& a) { return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax); }
 };
+template <typename R, int NF>
+struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
 
 template <typename R, int NF, int WCH>
 struct Grids {
@@ -602,6 +627,7 @@ template <typename R, int NF, int EQ>
 void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags* lf, cudaStream_t st) {
     switch (wch) {
     case 0: G ? build_graph_t<R, NF, EQ, 0>(*G, a, lf) : run_stream_t<R, NF, EQ, 0>(a, lf, st); break;
+    case 1: G ? build_graph_t<R, NF, EQ, 1>(*G, a, lf) : run_stream_t<R, NF, EQ, 1>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -679,6 +705,7 @@ template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     switch (wch) {
     case 0: probe_t<R, NF, 0>(a, st); break;
+    case 1: probe_t<R, NF, 1>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;

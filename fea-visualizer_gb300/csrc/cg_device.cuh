@@ -349,30 +349,66 @@ struct EllView {
     const int32_t* halo_col;
 };
 
-// Product of tile `tile` with the operand staged in ut[] (tile rows, then the
-// tile's halo): thread t returns row tile*kTileRows + t.  Warp w reads slice
-// w column by column: each step loads 32 consecutive values and 16-bit local
-// indices and gathers from shared memory; entries are summed in row order.
+// Where a warp's slice and its tile's halo sit in the layout: loaded one
+// tile ahead, so no load of a tile waits on another.
+struct EllTileRef {
+    int32_t sb, sw;  // the warp's slice: first entry, width (entries per row)
+    int32_t h0, h1;  // the tile's halo range
+};
+
 template <typename R, int NF>
-__device__ __forceinline__ FV<R, NF> ell_rows(const EllView<R, NF>& e, int64_t tile, const FV<R, NF>* ut) {
-    const int t = threadIdx.x;
-    const int64_t s = tile * (kTileRows / 32) + (t >> 5);
-    const int32_t b = ldg(e.slice_off + s);
-    const int32_t w = (ldg(e.slice_off + s + 1) - b) >> 5;
-    const FV<R, NF>* ap = e.As + b + (t & 31);
-    const uint16_t* lp = e.lcol + b + (t & 31);
-    FV<R, NF> acc;
-#pragma unroll
-    for (int f = 0; f < NF; f++) acc.v[f] = 0;
-#pragma unroll 4
-    for (int k = 0; k < w; k++) {
-        const FV<R, NF> a = ldv(ap + 32 * k, false);
-        const FV<R, NF> g = ut[__ldg(lp + 32 * k)];
-#pragma unroll
-        for (int f = 0; f < NF; f++) acc.v[f] = fma(a.v[f], g.v[f], acc.v[f]);
+__device__ __forceinline__ EllTileRef ell_ref(const EllView<R, NF>& e, int64_t tile, int64_t ntiles) {
+    EllTileRef r{0, 0, 0, 0};
+    if (tile < ntiles) {
+        const int64_t s = tile * (kTileRows / 32) + (threadIdx.x >> 5);
+        r.sb = ldg(e.slice_off + s);
+        r.sw = (ldg(e.slice_off + s + 1) - r.sb) >> 5;
+        r.h0 = ldg(e.halo_off + tile);
+        r.h1 = ldg(e.halo_off + tile + 1);
     }
-    return acc;
+    return r;
 }
+
+// The first KPRE entries of the thread's row in its slice, loaded into
+// registers before the tile's operand is staged (their loads do not depend on
+// it); ell_finish multiplies them and any remaining entries with ut[].
+template <typename R, int NF, int KPRE>
+struct EllRow {
+    FV<R, NF> a[KPRE];
+    uint32_t l[KPRE];
+    __device__ __forceinline__ void load(const EllView<R, NF>& e, const EllTileRef& r) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int k = 0; k < KPRE; k++) {
+            if (k < r.sw) {
+                a[k] = ldv(e.As + r.sb + 32 * k + lane, false);
+                l[k] = __ldg(e.lcol + r.sb + 32 * k + lane);
+            }
+        }
+    }
+    __device__ __forceinline__ FV<R, NF> finish(const EllView<R, NF>& e, const EllTileRef& r,
+                                                const FV<R, NF>* ut) const {
+        const int lane = threadIdx.x & 31;
+        FV<R, NF> acc;
+#pragma unroll
+        for (int f = 0; f < NF; f++) acc.v[f] = 0;
+#pragma unroll
+        for (int k = 0; k < KPRE; k++) {
+            if (k < r.sw) {
+                const FV<R, NF> g = ut[l[k]];
+#pragma unroll
+                for (int f = 0; f < NF; f++) acc.v[f] = fma(a[k].v[f], g.v[f], acc.v[f]);
+            }
+        }
+        for (int k = KPRE; k < r.sw; k++) {
+            const FV<R, NF> av = ldv(e.As + r.sb + 32 * k + lane, false);
+            const FV<R, NF> g = ut[__ldg(e.lcol + r.sb + 32 * k + lane)];
+#pragma unroll
+            for (int f = 0; f < NF; f++) acc.v[f] = fma(av.v[f], g.v[f], acc.v[f]);
+        }
+        return acc;
+    }
+};
 
 // u' of one unknown from the old r, w, s and D^-1 in global memory.
 template <typename R, int NF>
@@ -386,16 +422,21 @@ __device__ __forceinline__ FV<R, NF> cg_u_at(const CgVecs<R, NF>& v, const Phase
 }
 
 // One Chronopoulos-Gear iteration on tile `tile` in the tile-ELL layout (the
-// recurrences as in cgcg_tile).  Each thread updates its row and stages u';
-// the tile's halo columns get u' recomputed from the old r, w, s; after a
-// barrier every gathered operand comes from shared memory.  ut[] holds
-// kTileRows + the layout's largest halo.  Every thread of the block calls it.
-template <typename R, int NF>
+// recurrences as in cgcg_tile).  Each thread updates its row and stages u' in
+// ut[] (this tile's buffer: kTileRows + the layout's largest halo); the
+// tile's halo columns get u' recomputed from the old r, w, s; after one block
+// barrier every gathered operand comes from shared memory.  All loads of the
+// tile are issued before the barrier.  The caller alternates two ut buffers
+// between consecutive tiles, which makes the one barrier enough.  Every
+// thread of the block calls it.
+template <typename R, int NF, int KPRE>
 __device__ __forceinline__ void cgcg_tile_ell(const CgVecs<R, NF>& v, const EllView<R, NF>& e,
-                                              const PhaseCtl<R, NF>& c, int64_t tile, int64_t N, FV<R, NF>* ut,
-                                              Acc<R> (&dots)[3 * NF]) {
+                                              const PhaseCtl<R, NF>& c, int64_t tile, const EllTileRef& ref,
+                                              int64_t N, FV<R, NF>* ut, Acc<R> (&dots)[3 * NF]) {
     const int t = threadIdx.x;
     const int64_t row = tile * kTileRows + t;
+    EllRow<R, NF, KPRE> er;
+    er.load(e, ref);
     FV<R, NF> un;
 #pragma unroll
     for (int f = 0; f < NF; f++) un.v[f] = 0;
@@ -422,40 +463,41 @@ __device__ __forceinline__ void cgcg_tile_ell(const CgVecs<R, NF>& v, const EllV
         v.s1[row] = sn;
     }
     ut[t] = un;
-    const int32_t h0 = ldg(e.halo_off + tile), h1 = ldg(e.halo_off + tile + 1);
-    for (int32_t h = h0 + t; h < h1; h += blockDim.x) ut[kTileRows + (h - h0)] = cg_u_at(v, c, ldg(e.halo_col + h));
+    for (int32_t h = ref.h0 + t; h < ref.h1; h += blockDim.x)
+        ut[kTileRows + (h - ref.h0)] = cg_u_at(v, c, ldg(e.halo_col + h));
     __syncthreads();
-    const FV<R, NF> wn = ell_rows(e, tile, ut);
+    const FV<R, NF> wn = er.finish(e, ref, ut);
     if (row < N) {
         v.w1[row] = wn;
 #pragma unroll
         for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
     }
-    __syncthreads();  // the next tile reuses ut[]
 }
 
-// Set-up product w = A z on tile `tile` in the tile-ELL layout, z.w into dot[].
-template <typename R, int NF>
+// Set-up product w = A z on tile `tile` in the tile-ELL layout, z.w into dot[]
+// (same staging and buffer alternation as cgcg_tile_ell).
+template <typename R, int NF, int KPRE>
 __device__ __forceinline__ void init_tile_ell(const EllView<R, NF>& e, const FV<R, NF>* __restrict__ z,
-                                              FV<R, NF>* __restrict__ w, int64_t tile, int64_t N, FV<R, NF>* ut,
-                                              Acc<R> (&dot)[NF]) {
+                                              FV<R, NF>* __restrict__ w, int64_t tile, const EllTileRef& ref,
+                                              int64_t N, FV<R, NF>* ut, Acc<R> (&dot)[NF]) {
     const int t = threadIdx.x;
     const int64_t row = tile * kTileRows + t;
+    EllRow<R, NF, KPRE> er;
+    er.load(e, ref);
     FV<R, NF> zr;
 #pragma unroll
     for (int f = 0; f < NF; f++) zr.v[f] = 0;
     if (row < N) zr = ldv(z + row, false);
     ut[t] = zr;
-    const int32_t h0 = ldg(e.halo_off + tile), h1 = ldg(e.halo_off + tile + 1);
-    for (int32_t h = h0 + t; h < h1; h += blockDim.x) ut[kTileRows + (h - h0)] = ldv(z + ldg(e.halo_col + h), false);
+    for (int32_t h = ref.h0 + t; h < ref.h1; h += blockDim.x)
+        ut[kTileRows + (h - ref.h0)] = ldv(z + ldg(e.halo_col + h), false);
     __syncthreads();
-    const FV<R, NF> wr = ell_rows(e, tile, ut);
+    const FV<R, NF> wr = er.finish(e, ref, ut);
     if (row < N) {
         w[row] = wr;
 #pragma unroll
         for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wr.v[f]);
     }
-    __syncthreads();
 }
 
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.

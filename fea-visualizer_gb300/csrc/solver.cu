@@ -173,7 +173,7 @@ struct fea_solver {
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
-    int lanes = 8;  // CG kernel variant: 0 tile-ELL, else CSR entries per lane and window (4, 8, 16)
+    int lanes = 8;  // CG kernel variant: 0/1 tile-ELL (8/4 entries prefetched), 4/8/16 CSR window
     bool op_dirty = true;
     int op_kind = -1;
     bool acc_valid = false;
@@ -1297,11 +1297,11 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[4] = {0, 4, 8, 16};
+    const int cand[5] = {0, 1, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
-        if (l == 0 && !s->ell.ok) continue;
+        if (l <= 1 && !s->ell.ok) continue;
         probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
@@ -1325,9 +1325,9 @@ int fea_autotune(fea_solver* s) {
 int fea_set_cg_variant(fea_solver* s, int variant) {
     API_BEGIN
     check_handle(s);
-    if (variant != 0 && variant != 4 && variant != 8 && variant != 16)
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 4, 8 or 16");
-    if (variant == 0 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
+    if (variant != 0 && variant != 1 && variant != 4 && variant != 8 && variant != 16)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 4, 8 or 16");
+    if (variant <= 1 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
     s->lanes = variant;
     API_END
 }

@@ -208,15 +208,17 @@ int fea_get_matrix(fea_solver* s, int which, int32_t* row_ptr, int32_t* col, voi
 /* Node -> unknown map (FEMContext::idx_map, int32[V]) and boundary flags. */
 int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
 
-/* CG kernel variants: 0 = tile-ELL layout (256-row tiles, 32-row slices
- * stored column-wise, operand and halo staged in shared memory; the default
- * when the mesh's halos fit), 4 / 8 / 16 = warp-cooperative CSR with that
- * many entries per lane and window.  fea_autotune times one CG iteration of
- * each candidate on this mesh and keeps the fastest (fea_info.
- * rows_per_warp_lanes); the fields are left unchanged. */
+/* CG kernel variants: 0 and 1 = tile-ELL layout (256-row tiles, 32-row
+ * slices stored column-wise, operand and halo staged in shared memory; the
+ * first 8 (variant 0, the default when the mesh's halos fit) or 4 (variant 1)
+ * entries of each row prefetched into registers), 4 / 8 / 16 = warp-
+ * cooperative CSR with that many entries per lane and window.  fea_autotune
+ * times one CG iteration of each candidate on this mesh and keeps the
+ * fastest (fea_info.rows_per_warp_lanes); the fields are left unchanged. */
 int fea_autotune(fea_solver* s);
 /* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
- * FEA_ERR_UNSUPPORTED for 0 when the layout is unavailable on this mesh). */
+ * FEA_ERR_UNSUPPORTED for 0 or 1 when the layout is unavailable on this
+ * mesh). */
 int fea_set_cg_variant(fea_solver* s, int variant);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
