@@ -19,6 +19,7 @@
 #include <cmath>
 
 #include "cg_device.cuh"
+#include "tma.cuh"
 
 namespace fea {
 
@@ -218,6 +219,217 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
         cgcg_tile_ell<R, NF, KPRE>(v, e, c, tile, ref, a.N, buf, dots);
     });
+    double blk[3 * NF], tot[3 * NF];
+    block_totals<3 * NF>(dots, red, blk);
+    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+        signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
+}
+
+// ---- variant 2: tile-ELL streamed through shared memory by bulk copies ----------
+//
+// Every input a tile streams is a few contiguous ranges: its operator values
+// and 16-bit local columns (the tile's slices are consecutive) and its 256
+// rows of r, w, s, D^-1, x and p.  Thread 0 moves them into one of two stages
+// of shared memory with bulk copies (cp.async.bulk, completing on the stage's
+// mbarrier) two tiles ahead of the tile being computed, so the block computes
+// on data already in shared memory while the next tile's data is in flight.
+// The halo operands of the next tile are gathered into registers during the
+// current tile and staged after its product.  Every wait is bounded: on
+// expiry the kernel raises FEA_STATUS_BREAKDOWN, waits (bounded) for the
+// copies it issued and leaves the tile loop.
+
+// Byte offsets of one stage (all 16-byte aligned).
+template <typename R, int NF>
+struct StageLayout {
+    size_t A, L, V, U, bar, bytes;
+    __host__ __device__ StageLayout(int emax, int hmax) {
+        const size_t fv = sizeof(FV<R, NF>);
+        auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        A = 0;
+        L = al(A + fv * (size_t)emax);
+        V = al(L + 2 * (size_t)emax);
+        U = al(V + 6 * fv * (size_t)kTileRows);
+        bar = al(U + fv * (size_t)(kTileRows + hmax));
+        bytes = al(bar + 8);
+    }
+};
+
+// The vectors a stage holds, in this order.
+enum { kVr = 0, kVw = 1, kVs = 2, kVd = 3, kVx = 4, kVp = 5 };
+
+// Thread 0: bulk copies of tile `tile` into stage S (after the block's last
+// read of S and a proxy fence).
+template <typename R, int NF>
+__device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const StepArgs<R, NF>& a,
+                           const CgVecs<R, NF>& v, int64_t tile) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(S + L.bar);
+    const int32_t e0 = a.slice_off[tile * (kTileRows / 32)];
+    const int32_t e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
+    const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
+    const uint32_t nL = (uint32_t)(e1 - e0) * 2u;
+    const uint32_t nV = (uint32_t)kTileRows * (uint32_t)sizeof(FV<R, NF>);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(bar, nA + nL + 6 * nV);
+    if (nA) {
+        bulk_g2s(S + L.A, a.As + e0, nA, bar);
+        bulk_g2s(S + L.L, a.lcol + e0, nL, bar);
+    }
+    const int64_t r0 = tile * kTileRows;
+    const FV<R, NF>* src[6] = {v.r0 + r0, v.w0 + r0, v.s0 + r0, v.dinv + r0, v.x + r0, v.p + r0};
+#pragma unroll
+    for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
+}
+
+template <typename R, int NF>
+__global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ double red[32 * 3 * NF];
+    const StageLayout<R, NF> L(a.emax, a.hmax);
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[c.par];
+    v.w0 = a.wb[c.par];
+    v.s0 = a.sb[c.par];
+    v.r1 = a.rb[c.par ^ 1];
+    v.w1 = a.wb[c.par ^ 1];
+    v.s1 = a.sb[c.par ^ 1];
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5;
+    const int64_t ntiles = ceil_div(a.N, kTileRows), G = gridDim.x;
+    unsigned char* stg[2] = {dyn_smem, dyn_smem + L.bytes};
+    auto bar_of = [&](int b) { return reinterpret_cast<uint64_t*>(stg[b] + L.bar); };
+    auto ut_of = [&](int b) { return reinterpret_cast<FV<R, NF>*>(stg[b] + L.U); };
+    __shared__ int armed[2];
+    if (t == 0) {
+        mbar_init(bar_of(0), 1);
+        mbar_init(bar_of(1), 1);
+        mbar_fence_init();
+        armed[0] = armed[1] = 0;
+        const int64_t t0 = blockIdx.x;
+        if (t0 < ntiles) {
+            stage_tile(stg[0], L, a, v, t0);
+            armed[0] = 1;
+        }
+        if (t0 + G < ntiles) {
+            stage_tile(stg[1], L, a, v, t0 + G);
+            armed[1] = 1;
+        }
+    }
+    // halo of the first tile, straight into stage 0
+    if ((int64_t)blockIdx.x < ntiles) {
+        const int32_t h0 = a.halo_off[blockIdx.x], h1 = a.halo_off[blockIdx.x + 1];
+        for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
+    }
+    __syncthreads();
+    Acc<R> dots[3 * NF];
+    uint32_t phase[2] = {0u, 0u};
+    bool ok = true;
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += G, k++) {
+        const int b = k & 1;
+        FV<R, NF>* ut = ut_of(b);
+        // the next tile's halo operands (old r, w, s and D^-1 in global memory)
+        const int64_t nt = tile + G;
+        int32_t nh0 = 0, nh1 = 0;
+        if (nt < ntiles) {
+            nh0 = a.halo_off[nt];
+            nh1 = a.halo_off[nt + 1];
+        }
+        const int32_t nh = nh0 + t;
+        FV<R, NF> hr, hw, hs, hd;
+        if (nh < nh1) {
+            const int32_t col = a.halo_col[nh];
+            hr = ldv(v.r0 + col, false);
+            hw = ldv(v.w0 + col, false);
+            hd = ldv(v.dinv + col, false);
+            hs = hw;
+            if (c.need_old) hs = ldv(v.s0 + col, false);
+        }
+        // this warp's slice within the tile
+        const int64_t sl = tile * (kTileRows / 32) + wib;
+        const int32_t e0 = a.slice_off[tile * (kTileRows / 32)];
+        const int32_t sb = a.slice_off[sl] - e0, sw = (a.slice_off[sl + 1] - a.slice_off[sl]) >> 5;
+        const bool got = mbar_wait(bar_of(b), phase[b]);
+        phase[b] ^= 1u;
+        if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+        }
+        if (t == 0) armed[b] = 0;
+        const FV<R, NF>* V = reinterpret_cast<const FV<R, NF>*>(stg[b] + L.V);
+        const int64_t row = tile * kTileRows + t;
+        FV<R, NF> un;
+#pragma unroll
+        for (int f = 0; f < NF; f++) un.v[f] = 0;
+        if (row < a.N) {
+            const FV<R, NF> ro = V[kVr * kTileRows + t], wo = V[kVw * kTileRows + t], d = V[kVd * kTileRows + t];
+            FV<R, NF> so = wo;
+            if (c.need_old) so = V[kVs * kTileRows + t];
+            FV<R, NF> x = V[kVx * kTileRows + t], p = V[kVp * kTileRows + t];
+            FV<R, NF> sn, rn;
+            cg_advance(c, ro, wo, so, d, sn, rn, un);
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (c.act[f]) {
+                    const R ui = d.v[f] * ro.v[f];
+                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
+                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                }
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            v.x[row] = x;
+            v.p[row] = p;
+            v.r1[row] = rn;
+            v.s1[row] = sn;
+        }
+        ut[t] = un;
+        __syncthreads();
+        const FV<R, NF>* As = reinterpret_cast<const FV<R, NF>*>(stg[b] + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stg[b] + L.L) + sb + lane;
+        FV<R, NF> wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) wn.v[f] = 0;
+#pragma unroll 4
+        for (int j = 0; j < sw; j++) {
+            const FV<R, NF> av = As[32 * j];
+            const FV<R, NF> g = ut[Ls[32 * j]];
+#pragma unroll
+            for (int f = 0; f < NF; f++) wn.v[f] = fma(av.v[f], g.v[f], wn.v[f]);
+        }
+        if (row < a.N) {
+            v.w1[row] = wn;
+#pragma unroll
+            for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
+        }
+        // the next tile's halo into the other stage (free since the last tile)
+        if (nh < nh1) {
+            FV<R, NF> sn, rn, u2;
+            cg_advance(c, hr, hw, hs, hd, sn, rn, u2);
+            ut_of(b ^ 1)[kTileRows + (nh - nh0)] = u2;
+        }
+        for (int32_t h = nh + kBlock; h < nh1; h += kBlock)
+            ut_of(b ^ 1)[kTileRows + (h - nh0)] = cg_u_at(v, c, a.halo_col[h]);
+        __syncthreads();  // this stage is free again
+        if (t == 0 && tile + 2 * G < ntiles) {
+            stage_tile(stg[b], L, a, v, tile + 2 * G);
+            armed[b] = 1;
+        }
+    }
+    if (!ok) {
+        if (t == 0) {
+            atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            for (int b = 0; b < 2; b++)  // copies still in flight land before the block exits
+                if (armed[b]) mbar_wait(bar_of(b), phase[b]);
+        }
+        __syncthreads();
+    }
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -502,7 +714,8 @@ template <typename R, int NF, int WCH>
 struct CgKernels {
     static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init<R, NF, WCH>;
     static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter<R, NF, WCH>;
-    static size_t smem(const StepArgs<R, NF>&) { return 0; }
+    static size_t smem_init(const StepArgs<R, NF>&) { return 0; }
+    static size_t smem_iter(const StepArgs<R, NF>&) { return 0; }
 };
 // Variants 0 and 1: the tile-ELL kernels with 8 or 4 entries per row
 // prefetched into registers; two staging buffers of kTileRows + hmax entries.
@@ -510,23 +723,33 @@ template <typename R, int NF, int KPRE>
 struct EllKernels {
     static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init_ell<R, NF, KPRE>;
     static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_ell<R, NF, KPRE>;
-    static size_t smem(const StepArgs<R, NF>& a) { return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax); }
+    static size_t smem_init(const StepArgs<R, NF>& a) {
+        return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
+    }
+    static size_t smem_iter(const StepArgs<R, NF>& a) { return smem_init(a); }
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
+// Variant 2: the streamed iteration; its set-up product is variant 1's.
+template <typename R, int NF>
+struct CgKernels<R, NF, 2> : EllKernels<R, NF, 4> {
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF>;
+    static size_t smem_iter(const StepArgs<R, NF>& a) { return 2 * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
+};
 
 template <typename R, int NF, int WCH>
 struct Grids {
     using K = CgKernels<R, NF, WCH>;
     int spmv, iter, rhs, stream;
-    size_t smem;
+    size_t smem_init, smem_iter;
     explicit Grids(const StepArgs<R, NF>& a) {
         const int64_t N = a.N;
-        smem = K::smem(a);
-        spmv = wave_grid(K::init, ceil_div(N, kBlock), smem);
-        iter = wave_grid(K::iter, ceil_div(N, kBlock), smem);
+        smem_init = K::smem_init(a);
+        smem_iter = K::smem_iter(a);
+        spmv = wave_grid(K::init, ceil_div(N, kBlock), smem_init);
+        iter = wave_grid(K::iter, ceil_div(N, kBlock), smem_iter);
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -564,14 +787,14 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, k_rhs<R, NF, EQ, kRowLanes>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem);
+    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem);
+    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem_iter);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem);
+    s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem);
+    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem_iter);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -604,10 +827,10 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                 k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            K::init<<<g.spmv, kBlock, g.smem, st>>>(*la);
+            K::init<<<g.spmv, kBlock, g.smem_init, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                K::iter<<<g.iter, kBlock, g.smem, st>>>(*la);
+                K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(*la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -628,6 +851,7 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     switch (wch) {
     case 0: G ? build_graph_t<R, NF, EQ, 0>(*G, a, lf) : run_stream_t<R, NF, EQ, 0>(a, lf, st); break;
     case 1: G ? build_graph_t<R, NF, EQ, 1>(*G, a, lf) : run_stream_t<R, NF, EQ, 1>(a, lf, st); break;
+    case 2: G ? build_graph_t<R, NF, EQ, 2>(*G, a, lf) : run_stream_t<R, NF, EQ, 2>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -697,7 +921,7 @@ void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st) {
 template <typename R, int NF, int WCH>
 void probe_t(const StepArgs<R, NF>& a, cudaStream_t st) {
     const Grids<R, NF, WCH> g(a);
-    CgKernels<R, NF, WCH>::iter<<<g.iter, kBlock, g.smem, st>>>(a);
+    CgKernels<R, NF, WCH>::iter<<<g.iter, kBlock, g.smem_iter, st>>>(a);
     FEA_CHECK_LAUNCH();
 }
 
@@ -706,11 +930,22 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     switch (wch) {
     case 0: probe_t<R, NF, 0>(a, st); break;
     case 1: probe_t<R, NF, 1>(a, st); break;
+    case 2: probe_t<R, NF, 2>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;
     }
 }
+
+// Shared memory the streamed iteration needs on this layout (0 = unavailable).
+template <typename R, int NF>
+size_t stream_smem_bytes(int emax, int hmax) {
+    return 2 * StageLayout<R, NF>(emax, hmax).bytes;
+}
+template size_t stream_smem_bytes<float, 1>(int, int);
+template size_t stream_smem_bytes<float, 2>(int, int);
+template size_t stream_smem_bytes<double, 1>(int, int);
+template size_t stream_smem_bytes<double, 2>(int, int);
 
 #define FEA_INST_STEP(R, NF)                                                                              \
     template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \

@@ -41,6 +41,7 @@ constexpr size_t kEllSmemBudget = 96 * 1024;  // largest staged operand per bloc
 struct TileEll {
     int64_t E = 0;  // stored entries, padding included
     int ntiles = 0, hmax = 0;
+    int emax = 0;                  // stored entries of the largest tile
     int32_t* slice_off = nullptr;  // [ntiles * 8 + 1] first entry of each slice
     int32_t* halo_off = nullptr;   // [ntiles + 1]
     int32_t* halo_col = nullptr;   // sorted distinct out-of-tile columns per tile
@@ -135,6 +136,8 @@ struct StepArgs {
     const R* M;             // mass values [nnz]
     const R* K;             // stiffness values [nnz] (diffusivity-scaled)
     const R* Adv;           // advection values [nnz]
+    // Per-row vectors hold whole tiles: ceil(N / kTileRows) * kTileRows rows
+    // (the streamed CG kernels copy 256-row tiles of them).
     FV<R, NF>* x;           // unknown of the solve (warm start and result)
     FV<R, NF>* b;
     FV<R, NF>* z;           // D^-1 r of the initial residual
@@ -155,7 +158,7 @@ struct StepArgs {
     const int32_t* slice_off;
     const int32_t* halo_off;
     const int32_t* halo_col;
-    int hmax;
+    int hmax, emax;
     const StepParams* prm;
     CgState* cg;
     RunState* run;
@@ -201,6 +204,11 @@ template <typename R, int NF>
 void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st);
 template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
+// Dynamic shared memory of the streamed CG iteration (variant 2) for a
+// tile-ELL layout with the given largest tile and halo.
+template <typename R, int NF>
+size_t stream_smem_bytes(int emax, int hmax);
+constexpr size_t kStreamSmemLimit = 220 * 1024;  // per block, below the 227 KB opt-in maximum
 
 int max_grid_blocks();
 

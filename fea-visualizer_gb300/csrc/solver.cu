@@ -158,6 +158,7 @@ struct fea_solver {
     int32_t* idx_c = nullptr;       // [V] node -> solver index (-1 on Dirichlet points)
     void *Kc = nullptr, *Mc = nullptr, *Advc = nullptr;        // values in solver order
     TileEll ell;                    // the CG kernels' layout of Pc (tile_ell.cu)
+    bool stream_ok = false;         // the streamed iteration (variant 2) fits in shared memory
     void *S1 = nullptr, *S0 = nullptr, *S2 = nullptr;          // tile-ELL copies of A1, A0, A2
     std::vector<float> h_xyz;       // host copy of the points (ordering keys)
     uint8_t* adv_present = nullptr;
@@ -173,7 +174,7 @@ struct fea_solver {
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
-    int lanes = 8;  // CG kernel variant: 0/1 tile-ELL (8/4 entries prefetched), 4/8/16 CSR window
+    int lanes = 8;  // CG kernel variant: 0/1 tile-ELL (8/4 entries prefetched), 2 streamed, 4/8/16 CSR window
     bool op_dirty = true;
     int op_kind = -1;
     bool acc_valid = false;
@@ -187,7 +188,7 @@ namespace {
 
 size_t rsize(const fea_solver* s) { return s->precision == FEA_FP64 ? 8 : 4; }
 
-int64_t pad4(int64_t n) { return (n + 3) & ~(int64_t)3; }
+int64_t pad_tiles(int64_t n) { return ceil_div(n, kTileRows) * kTileRows; }
 
 void* ralloc(DeviceArena& ar, const fea_solver* s, int64_t n) {
     if (s->precision == FEA_FP64) return ar.alloc<double>(n);
@@ -319,6 +320,7 @@ void build_context(fea_solver* s) {
     s->P = Pattern{};
     s->Pc = Pattern{};
     s->ell = TileEll{};
+    s->stream_ok = false;
     s->S1 = s->S0 = s->S2 = nullptr;
     s->F = Fields{};
     cudaStream_t st = s->stream;
@@ -339,6 +341,10 @@ void build_context(fea_solver* s) {
             s->S0 = ralloc(s->mat_mem, s, s->ell.E);
             s->S2 = ralloc(s->mat_mem, s, 2 * s->ell.E);
         }
+        // both field counts fit when the two-field stages do
+        s->stream_ok = s->ell.ok && (s->precision == FEA_FP64
+                                         ? stream_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax)
+                                         : stream_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax)) <= kStreamSmemLimit;
         s->lanes = s->ell.ok ? 0 : 8;
     }
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
@@ -362,34 +368,38 @@ void build_context(fea_solver* s) {
     s->adv_present = s->mat_mem.alloc<uint8_t>(nnz);
     Fields& F = s->F;
     F.N = N;
-    F.u = ralloc(s->mat_mem, s, N);
-    F.v = ralloc(s->mat_mem, s, N);
-    F.a = ralloc(s->mat_mem, s, N);
-    F.ut = ralloc(s->mat_mem, s, N);
-    F.vt = ralloc(s->mat_mem, s, N);
-    F.uv = ralloc(s->mat_mem, s, 2 * N);
+    // every per-row vector holds whole tiles (Nt rows, zero beyond N): the
+    // streamed CG kernels copy 256-row tiles of them into shared memory
+    const int64_t Nt = ceil_div(N, kTileRows) * kTileRows;
+    F.u = ralloc(s->mat_mem, s, Nt);
+    F.v = ralloc(s->mat_mem, s, Nt);
+    F.a = ralloc(s->mat_mem, s, Nt);
+    F.ut = ralloc(s->mat_mem, s, Nt);
+    F.vt = ralloc(s->mat_mem, s, Nt);
+    F.uv = ralloc(s->mat_mem, s, 2 * Nt);
     F.A1 = ralloc(s->mat_mem, s, nnz);
-    F.d1 = ralloc(s->mat_mem, s, N);
-    F.b1 = ralloc(s->mat_mem, s, N);
-    const int64_t Np = pad4(N);  // every buffer of a group starts 16-byte aligned
+    F.d1 = ralloc(s->mat_mem, s, Nt);
+    F.b1 = ralloc(s->mat_mem, s, Nt);
+    const int64_t Np = Nt;  // every buffer of a group starts on a tile boundary
     F.r1 = ralloc(s->mat_mem, s, 6 * Np);  // r, w, s: two buffers each
-    F.z1 = ralloc(s->mat_mem, s, N);
+    F.z1 = ralloc(s->mat_mem, s, Nt);
     F.p1 = ralloc(s->mat_mem, s, 2 * Np);
-    F.q1 = ralloc(s->mat_mem, s, N);
+    F.q1 = ralloc(s->mat_mem, s, Nt);
     F.A0 = ralloc(s->mat_mem, s, nnz);
-    F.d0 = ralloc(s->mat_mem, s, N);
+    F.d0 = ralloc(s->mat_mem, s, Nt);
     F.A2 = ralloc(s->mat_mem, s, 2 * nnz);
-    F.d2 = ralloc(s->mat_mem, s, 2 * N);
-    F.b2 = ralloc(s->mat_mem, s, 2 * N);
+    F.d2 = ralloc(s->mat_mem, s, 2 * Nt);
+    F.b2 = ralloc(s->mat_mem, s, 2 * Nt);
     F.r2 = ralloc(s->mat_mem, s, 12 * Np);
-    F.z2 = ralloc(s->mat_mem, s, 2 * N);
+    F.z2 = ralloc(s->mat_mem, s, 2 * Nt);
     F.p2 = ralloc(s->mat_mem, s, 4 * Np);
-    F.q2 = ralloc(s->mat_mem, s, 2 * N);
+    F.q2 = ralloc(s->mat_mem, s, 2 * Nt);
     // every vector starts at zero (the direction buffers are read with weight
     // beta = 0 only after a write, but a zero start keeps them finite)
     const std::pair<void*, int64_t> zeroed[] = {
-        {F.u, N}, {F.v, N}, {F.a, N}, {F.ut, N}, {F.vt, N}, {F.uv, 2 * N}, {F.b1, N}, {F.r1, 6 * Np}, {F.z1, N},
-        {F.p1, 2 * Np}, {F.q1, N}, {F.b2, 2 * N}, {F.r2, 12 * Np}, {F.z2, 2 * N}, {F.p2, 4 * Np}, {F.q2, 2 * N}};
+        {F.u, Nt}, {F.v, Nt}, {F.a, Nt}, {F.ut, Nt}, {F.vt, Nt}, {F.uv, 2 * Nt}, {F.d1, Nt}, {F.b1, Nt},
+        {F.r1, 6 * Np}, {F.z1, Nt}, {F.p1, 2 * Np}, {F.q1, Nt}, {F.d0, Nt}, {F.d2, 2 * Nt}, {F.b2, 2 * Nt},
+        {F.r2, 12 * Np}, {F.z2, 2 * Nt}, {F.p2, 4 * Np}, {F.q2, 2 * Nt}};
     for (const auto& zv : zeroed)
         FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
     F.interleaved = false;
@@ -423,19 +433,19 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.A = (const FV<R, 1>*)(init_op ? F.A0 : F.A1);
         a.dinv = (const FV<R, 1>*)(init_op ? F.d0 : F.d1);
         a.b = (FV<R, 1>*)F.b1;
-        set_rws(a, (FV<R, 1>*)F.r1, pad4(s->N));
+        set_rws(a, (FV<R, 1>*)F.r1, pad_tiles(s->N));
         a.z = (FV<R, 1>*)F.z1;
         a.pp[0] = (FV<R, 1>*)F.p1;
-        a.pp[1] = a.pp[0] + pad4(s->N);
+        a.pp[1] = a.pp[0] + pad_tiles(s->N);
         a.q = (FV<R, 1>*)F.q1;
     } else {
         a.A = (const FV<R, 2>*)F.A2;
         a.dinv = (const FV<R, 2>*)F.d2;
         a.b = (FV<R, 2>*)F.b2;
-        set_rws(a, (FV<R, 2>*)F.r2, pad4(s->N));
+        set_rws(a, (FV<R, 2>*)F.r2, pad_tiles(s->N));
         a.z = (FV<R, 2>*)F.z2;
         a.pp[0] = (FV<R, 2>*)F.p2;
-        a.pp[1] = a.pp[0] + pad4(s->N);
+        a.pp[1] = a.pp[0] + pad_tiles(s->N);
         a.q = (FV<R, 2>*)F.q2;
     }
     a.u = (R*)F.u;
@@ -451,6 +461,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.halo_off = s->ell.halo_off;
         a.halo_col = s->ell.halo_col;
         a.hmax = s->ell.hmax;
+        a.emax = s->ell.emax;
     }
     a.prm = s->d_prm;
     a.cg = s->d_cg;
@@ -732,7 +743,7 @@ double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int6
     DeviceArena tmp;
     R* ck = tmp.alloc<R>(nck * N);
     R* seg = tmp.alloc<R>((ckpt + 1) * N);
-    R* mu = tmp.alloc<R>(N);
+    R* mu = tmp.alloc<R>(pad_tiles(N));  // x of the solves: whole tiles
     R* uN = tmp.alloc<R>(N);
     R* lam_f = lam ? lam : tmp.alloc<R>(N);
     double* J = tmp.alloc<double>(1);
@@ -746,7 +757,7 @@ double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int6
     adjoint_loss<R>(s->Pc, (const R*)s->Mc, u, t, lam_f, s->d_part, max_grid_blocks(), s->d_tickets + 5, J, st);
     if (grads) {
         FEA_CUDA_TRY(cudaMemsetAsync(gD, 0, sizeof(double) * (size_t)s->T, st));
-        FEA_CUDA_TRY(cudaMemsetAsync(mu, 0, rb, st));
+        FEA_CUDA_TRY(cudaMemsetAsync(mu, 0, sizeof(R) * (size_t)pad_tiles(N), st));
         StepArgs<R, 1> a = make_args<R, 1>(s, false);
         a.x = (FV<R, 1>*)mu;
         a.rhs = lam_f;
@@ -1297,11 +1308,12 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[5] = {0, 1, 4, 8, 16};
+    const int cand[6] = {0, 1, 2, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
-        if (l <= 1 && !s->ell.ok) continue;
+        if (l <= 2 && !s->ell.ok) continue;
+        if (l == 2 && !s->stream_ok) continue;
         probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
@@ -1325,9 +1337,11 @@ int fea_autotune(fea_solver* s) {
 int fea_set_cg_variant(fea_solver* s, int variant) {
     API_BEGIN
     check_handle(s);
-    if (variant != 0 && variant != 1 && variant != 4 && variant != 8 && variant != 16)
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 4, 8 or 16");
-    if (variant <= 1 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
+    if (variant != 0 && variant != 1 && variant != 2 && variant != 4 && variant != 8 && variant != 16)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 4, 8 or 16");
+    if (variant <= 2 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
+    if (variant == 2 && !s->stream_ok)
+        return fail(FEA_ERR_UNSUPPORTED, "streamed tiles exceed the shared memory on this mesh");
     s->lanes = variant;
     API_END
 }

@@ -91,9 +91,13 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
             }
         }
     }
+    int64_t emax = 0;
+    for (int64_t t = 0; t < ntiles; t++)
+        emax = std::max<int64_t>(emax, slice_off[(t + 1) * (kTileRows / 32)] - slice_off[t * (kTileRows / 32)]);
     L.E = E;
     L.ntiles = (int)ntiles;
     L.hmax = (int)hmax;
+    L.emax = (int)emax;
     L.slice_off = keep.alloc<int32_t>(nslices + 1);
     L.halo_off = keep.alloc<int32_t>(ntiles + 1);
     L.halo_col = keep.alloc<int32_t>(std::max<int64_t>(1, (int64_t)halo_col.size()));
