@@ -392,6 +392,15 @@ def main():
     # dominant kernel: one CG iteration, timed alone on the same operator
     spmv_ms = s.time_spmv(reps=20, flush_l2=True)
     spmv_warm_ms = s.time_spmv(reps=20, flush_l2=False)
+    # every CG kernel variant on the same operator (L2 flushed), then back to the autotuned one
+    variant_ms = {}
+    for var in (0, 1, 2, 3, 4, 8, 16):
+        try:
+            s.set_cg_variant(var)
+        except F.FeaError:
+            continue
+        variant_ms[str(var)] = s.time_spmv(reps=10, flush_l2=True)
+    s.set_cg_variant(lanes)
     peak, peak_kind = measured_peak_hbm()
     bytes_spmv = iter_bytes(N, nnz)
     achieved = bytes_spmv / (spmv_ms * 1e-3) / 1e9
@@ -436,7 +445,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config(int(V), int(tri.shape[0]), int(nnz),
-                             {"parallelism": "replicas" if world > 1 else "single gpu", "lanes_per_row": lanes,
+                             {"parallelism": "replicas" if world > 1 else "single gpu", "cg_variant": lanes,
                               "cg_iterations_per_step": iters / args.steps,
                               "one_launch_ms_per_step": one_launch_ms / args.steps}),
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": 4 * V},
@@ -444,7 +453,8 @@ def main():
                          "frac": achieved / peak, "traffic": None,
                          "kernel": "k_cgcg_iter (one CG iteration: paired u,v SpMV with fused vector updates)",
                          "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": spmv_ms,
-                         "ms_per_launch_l2_warm": spmv_warm_ms, "peak_source": peak_kind},
+                         "ms_per_launch_l2_warm": spmv_warm_ms, "peak_source": peak_kind,
+                         "variant": lanes, "ms_per_launch_by_variant": variant_ms},
             "cpu_baseline": cpu,
             "batched": batched,
             "adjoint": adjoint,

@@ -280,10 +280,15 @@ __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const 
     for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
 }
 
-template <typename R, int NF>
+// Thread t's halo slot: slots are dealt round-robin over the warps, so every
+// warp stages about the same share of a tile's halo.
+__device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
+
+template <typename R, int NF, int NS>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ double red[32 * 3 * NF];
+    __shared__ int armed[NS];
     const StageLayout<R, NF> L(a.emax, a.hmax);
     PhaseCtl<R, NF> c;
     c.load(a.cg);
@@ -300,61 +305,74 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     v.r1 = a.rb[c.par ^ 1];
     v.w1 = a.wb[c.par ^ 1];
     v.s1 = a.sb[c.par ^ 1];
-    const int t = threadIdx.x, lane = t & 31, wib = t >> 5;
-    const int64_t ntiles = ceil_div(a.N, kTileRows), G = gridDim.x;
-    unsigned char* stg[2] = {dyn_smem, dyn_smem + L.bytes};
-    auto bar_of = [&](int b) { return reinterpret_cast<uint64_t*>(stg[b] + L.bar); };
-    auto ut_of = [&](int b) { return reinterpret_cast<FV<R, NF>*>(stg[b] + L.U); };
-    __shared__ int armed[2];
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
+    const int64_t ntiles = ceil_div(a.N, kTileRows), G = gridDim.x, t0 = blockIdx.x;
+    auto stage = [&](int b) { return dyn_smem + (size_t)b * L.bytes; };
+    auto bar_of = [&](int b) { return reinterpret_cast<uint64_t*>(stage(b) + L.bar); };
+    auto ut_of = [&](int b) { return reinterpret_cast<FV<R, NF>*>(stage(b) + L.U); };
+    // halo column of slot j of tile `tile` (-1: none) and the tile's halo count
+    auto halo_ref = [&](int64_t tile, int32_t& col, int32_t& cnt) {
+        col = -1;
+        cnt = 0;
+        if (tile < ntiles) {
+            const int32_t h0 = a.halo_off[tile];
+            cnt = a.halo_off[tile + 1] - h0;
+            if (j < cnt) col = a.halo_col[h0 + j];
+        }
+    };
+    // this warp's slice of tile `tile`: offset in the tile's entries, width
+    auto slice_ref = [&](int64_t tile, int32_t& sb, int32_t& sw) {
+        sb = sw = 0;
+        if (tile < ntiles) {
+            const int64_t sl = tile * (kTileRows / 32) + wib;
+            const int32_t s0 = a.slice_off[sl];
+            sb = s0 - a.slice_off[tile * (kTileRows / 32)];
+            sw = (a.slice_off[sl + 1] - s0) >> 5;
+        }
+    };
     if (t == 0) {
-        mbar_init(bar_of(0), 1);
-        mbar_init(bar_of(1), 1);
+        for (int b = 0; b < NS; b++) {
+            mbar_init(bar_of(b), 1);
+            armed[b] = 0;
+        }
         mbar_fence_init();
-        armed[0] = armed[1] = 0;
-        const int64_t t0 = blockIdx.x;
-        if (t0 < ntiles) {
-            stage_tile(stg[0], L, a, v, t0);
-            armed[0] = 1;
-        }
-        if (t0 + G < ntiles) {
-            stage_tile(stg[1], L, a, v, t0 + G);
-            armed[1] = 1;
-        }
+        for (int b = 0; b < NS; b++)
+            if (t0 + b * G < ntiles) {
+                stage_tile(stage(b), L, a, v, t0 + b * G);
+                armed[b] = 1;
+            }
     }
-    // halo of the first tile, straight into stage 0
-    if ((int64_t)blockIdx.x < ntiles) {
-        const int32_t h0 = a.halo_off[blockIdx.x], h1 = a.halo_off[blockIdx.x + 1];
+    // the first tile's halo, straight into stage 0 (every slot, also beyond 256)
+    if (t0 < ntiles) {
+        const int32_t h0 = a.halo_off[t0], h1 = a.halo_off[t0 + 1];
         for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
     }
+    int32_t hcol, hcnt, sb, sw;
+    halo_ref(t0 + G, hcol, hcnt);  // the next tile's halo slot
+    slice_ref(t0, sb, sw);
     __syncthreads();
     Acc<R> dots[3 * NF];
-    uint32_t phase[2] = {0u, 0u};
+    uint32_t phase[NS];
+#pragma unroll
+    for (int b = 0; b < NS; b++) phase[b] = 0u;
     bool ok = true;
-    int k = 0;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += G, k++) {
-        const int b = k & 1;
+    int b = 0;
+    for (int64_t tile = t0; tile < ntiles; tile += G) {
         FV<R, NF>* ut = ut_of(b);
-        // the next tile's halo operands (old r, w, s and D^-1 in global memory)
-        const int64_t nt = tile + G;
-        int32_t nh0 = 0, nh1 = 0;
-        if (nt < ntiles) {
-            nh0 = a.halo_off[nt];
-            nh1 = a.halo_off[nt + 1];
-        }
-        const int32_t nh = nh0 + t;
+        const int bn = b + 1 == NS ? 0 : b + 1;
+        // operands of the next tile's halo slot (column loaded one tile ago)
         FV<R, NF> hr, hw, hs, hd;
-        if (nh < nh1) {
-            const int32_t col = a.halo_col[nh];
-            hr = ldv(v.r0 + col, false);
-            hw = ldv(v.w0 + col, false);
-            hd = ldv(v.dinv + col, false);
+        if (hcol >= 0) {
+            hr = ldv(v.r0 + hcol, false);
+            hw = ldv(v.w0 + hcol, false);
+            hd = ldv(v.dinv + hcol, false);
             hs = hw;
-            if (c.need_old) hs = ldv(v.s0 + col, false);
+            if (c.need_old) hs = ldv(v.s0 + hcol, false);
         }
-        // this warp's slice within the tile
-        const int64_t sl = tile * (kTileRows / 32) + wib;
-        const int32_t e0 = a.slice_off[tile * (kTileRows / 32)];
-        const int32_t sb = a.slice_off[sl] - e0, sw = (a.slice_off[sl + 1] - a.slice_off[sl]) >> 5;
+        // references of the tile after next and of the next tile's slice
+        int32_t hcol2, hcnt2, sb2, sw2;
+        halo_ref(tile + 2 * G, hcol2, hcnt2);
+        slice_ref(tile + G, sb2, sw2);
         const bool got = mbar_wait(bar_of(b), phase[b]);
         phase[b] ^= 1u;
         if (!__syncthreads_and(got)) {
@@ -362,7 +380,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             break;
         }
         if (t == 0) armed[b] = 0;
-        const FV<R, NF>* V = reinterpret_cast<const FV<R, NF>*>(stg[b] + L.V);
+        const FV<R, NF>* V = reinterpret_cast<const FV<R, NF>*>(stage(b) + L.V);
         const int64_t row = tile * kTileRows + t;
         FV<R, NF> un;
 #pragma unroll
@@ -391,15 +409,15 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         }
         ut[t] = un;
         __syncthreads();
-        const FV<R, NF>* As = reinterpret_cast<const FV<R, NF>*>(stg[b] + L.A) + sb + lane;
-        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stg[b] + L.L) + sb + lane;
+        const FV<R, NF>* As = reinterpret_cast<const FV<R, NF>*>(stage(b) + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage(b) + L.L) + sb + lane;
         FV<R, NF> wn;
 #pragma unroll
         for (int f = 0; f < NF; f++) wn.v[f] = 0;
 #pragma unroll 4
-        for (int j = 0; j < sw; j++) {
-            const FV<R, NF> av = As[32 * j];
-            const FV<R, NF> g = ut[Ls[32 * j]];
+        for (int k = 0; k < sw; k++) {
+            const FV<R, NF> av = As[32 * k];
+            const FV<R, NF> g = ut[Ls[32 * k]];
 #pragma unroll
             for (int f = 0; f < NF; f++) wn.v[f] = fma(av.v[f], g.v[f], wn.v[f]);
         }
@@ -408,25 +426,33 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
 #pragma unroll
             for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
         }
-        // the next tile's halo into the other stage (free since the last tile)
-        if (nh < nh1) {
+        // the next tile's halo into its stage (free since that stage's last tile)
+        if (hcol >= 0) {
             FV<R, NF> sn, rn, u2;
             cg_advance(c, hr, hw, hs, hd, sn, rn, u2);
-            ut_of(b ^ 1)[kTileRows + (nh - nh0)] = u2;
+            ut_of(bn)[kTileRows + j] = u2;
         }
-        for (int32_t h = nh + kBlock; h < nh1; h += kBlock)
-            ut_of(b ^ 1)[kTileRows + (h - nh0)] = cg_u_at(v, c, a.halo_col[h]);
+        if (hcnt > kBlock && tile + G < ntiles) {  // halos beyond 256 columns: the rest directly
+            const int32_t h0 = a.halo_off[tile + G];
+            for (int32_t h = kBlock + t; h < hcnt; h += kBlock)
+                ut_of(bn)[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0 + h]);
+        }
         __syncthreads();  // this stage is free again
-        if (t == 0 && tile + 2 * G < ntiles) {
-            stage_tile(stg[b], L, a, v, tile + 2 * G);
+        if (t == 0 && tile + NS * G < ntiles) {
+            stage_tile(stage(b), L, a, v, tile + NS * G);
             armed[b] = 1;
         }
+        hcol = hcol2;
+        hcnt = hcnt2;
+        sb = sb2;
+        sw = sw2;
+        b = bn;
     }
     if (!ok) {
         if (t == 0) {
             atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
-            for (int b = 0; b < 2; b++)  // copies still in flight land before the block exits
-                if (armed[b]) mbar_wait(bar_of(b), phase[b]);
+            for (int q = 0; q < NS; q++)  // copies still in flight land before the block exits
+                if (armed[q]) mbar_wait(bar_of(q), phase[q]);
         }
         __syncthreads();
     }
@@ -732,12 +758,17 @@ template <typename R, int NF>
 struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
-// Variant 2: the streamed iteration; its set-up product is variant 1's.
-template <typename R, int NF>
-struct CgKernels<R, NF, 2> : EllKernels<R, NF, 4> {
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF>;
-    static size_t smem_iter(const StepArgs<R, NF>& a) { return 2 * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
+// Variants 2 and 3: the streamed iteration with 2 or 3 stages; the set-up
+// product is variant 1's.
+template <typename R, int NF, int NS>
+struct StreamKernels : EllKernels<R, NF, 4> {
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS>;
+    static size_t smem_iter(const StepArgs<R, NF>& a) { return NS * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
 };
+template <typename R, int NF>
+struct CgKernels<R, NF, 2> : StreamKernels<R, NF, 2> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 3> : StreamKernels<R, NF, 3> {};
 
 template <typename R, int NF, int WCH>
 struct Grids {
@@ -852,6 +883,7 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     case 0: G ? build_graph_t<R, NF, EQ, 0>(*G, a, lf) : run_stream_t<R, NF, EQ, 0>(a, lf, st); break;
     case 1: G ? build_graph_t<R, NF, EQ, 1>(*G, a, lf) : run_stream_t<R, NF, EQ, 1>(a, lf, st); break;
     case 2: G ? build_graph_t<R, NF, EQ, 2>(*G, a, lf) : run_stream_t<R, NF, EQ, 2>(a, lf, st); break;
+    case 3: G ? build_graph_t<R, NF, EQ, 3>(*G, a, lf) : run_stream_t<R, NF, EQ, 3>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -931,21 +963,22 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     case 0: probe_t<R, NF, 0>(a, st); break;
     case 1: probe_t<R, NF, 1>(a, st); break;
     case 2: probe_t<R, NF, 2>(a, st); break;
+    case 3: probe_t<R, NF, 3>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;
     }
 }
 
-// Shared memory the streamed iteration needs on this layout (0 = unavailable).
+// Shared memory of one stage of the streamed iteration on this layout.
 template <typename R, int NF>
-size_t stream_smem_bytes(int emax, int hmax) {
-    return 2 * StageLayout<R, NF>(emax, hmax).bytes;
+size_t stream_stage_bytes(int emax, int hmax) {
+    return StageLayout<R, NF>(emax, hmax).bytes;
 }
-template size_t stream_smem_bytes<float, 1>(int, int);
-template size_t stream_smem_bytes<float, 2>(int, int);
-template size_t stream_smem_bytes<double, 1>(int, int);
-template size_t stream_smem_bytes<double, 2>(int, int);
+template size_t stream_stage_bytes<float, 1>(int, int);
+template size_t stream_stage_bytes<float, 2>(int, int);
+template size_t stream_stage_bytes<double, 1>(int, int);
+template size_t stream_stage_bytes<double, 2>(int, int);
 
 #define FEA_INST_STEP(R, NF)                                                                              \
     template void build_step_graph<R, NF>(StepGraph&, const StepArgs<R, NF>&, int, int, LoopFlags*);     \

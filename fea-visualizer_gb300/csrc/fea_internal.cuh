@@ -204,10 +204,11 @@ template <typename R, int NF>
 void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st);
 template <typename R, int NF>
 void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
-// Dynamic shared memory of the streamed CG iteration (variant 2) for a
-// tile-ELL layout with the given largest tile and halo.
+// Dynamic shared memory of one stage of the streamed CG iteration (variants
+// 2 and 3 hold 2 and 3 stages) for a tile-ELL layout with the given largest
+// tile and halo.
 template <typename R, int NF>
-size_t stream_smem_bytes(int emax, int hmax);
+size_t stream_stage_bytes(int emax, int hmax);
 constexpr size_t kStreamSmemLimit = 220 * 1024;  // per block, below the 227 KB opt-in maximum
 
 int max_grid_blocks();

@@ -158,7 +158,7 @@ struct fea_solver {
     int32_t* idx_c = nullptr;       // [V] node -> solver index (-1 on Dirichlet points)
     void *Kc = nullptr, *Mc = nullptr, *Advc = nullptr;        // values in solver order
     TileEll ell;                    // the CG kernels' layout of Pc (tile_ell.cu)
-    bool stream_ok = false;         // the streamed iteration (variant 2) fits in shared memory
+    int stream_stages = 0;          // stages of the streamed iteration that fit in shared memory (0, 2 or 3)
     void *S1 = nullptr, *S0 = nullptr, *S2 = nullptr;          // tile-ELL copies of A1, A0, A2
     std::vector<float> h_xyz;       // host copy of the points (ordering keys)
     uint8_t* adv_present = nullptr;
@@ -174,7 +174,7 @@ struct fea_solver {
     bool stream_mode = false;  // FEA_LAUNCH_MODE=stream: kernel-by-kernel launches
     RunState* h_run = nullptr;  // pinned
     StepGraph graph, init_graph;
-    int lanes = 8;  // CG kernel variant: 0/1 tile-ELL (8/4 entries prefetched), 2 streamed, 4/8/16 CSR window
+    int lanes = 8;  // CG kernel variant: 0/1 tile-ELL (8/4 entries prefetched), 2/3 streamed (stages), 4/8/16 CSR window
     bool op_dirty = true;
     int op_kind = -1;
     bool acc_valid = false;
@@ -320,7 +320,7 @@ void build_context(fea_solver* s) {
     s->P = Pattern{};
     s->Pc = Pattern{};
     s->ell = TileEll{};
-    s->stream_ok = false;
+    s->stream_stages = 0;
     s->S1 = s->S0 = s->S2 = nullptr;
     s->F = Fields{};
     cudaStream_t st = s->stream;
@@ -342,9 +342,9 @@ void build_context(fea_solver* s) {
             s->S2 = ralloc(s->mat_mem, s, 2 * s->ell.E);
         }
         // both field counts fit when the two-field stages do
-        s->stream_ok = s->ell.ok && (s->precision == FEA_FP64
-                                         ? stream_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax)
-                                         : stream_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax)) <= kStreamSmemLimit;
+        const size_t stage = s->precision == FEA_FP64 ? stream_stage_bytes<double, 2>(s->ell.emax, s->ell.hmax)
+                                                      : stream_stage_bytes<float, 2>(s->ell.emax, s->ell.hmax);
+        s->stream_stages = !s->ell.ok ? 0 : 3 * stage <= kStreamSmemLimit ? 3 : 2 * stage <= kStreamSmemLimit ? 2 : 0;
         s->lanes = s->ell.ok ? 0 : 8;
     }
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
@@ -1308,12 +1308,12 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[6] = {0, 1, 2, 4, 8, 16};
+    const int cand[7] = {0, 1, 2, 3, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
-        if (l <= 2 && !s->ell.ok) continue;
-        if (l == 2 && !s->stream_ok) continue;
+        if (l <= 3 && !s->ell.ok) continue;
+        if ((l == 2 || l == 3) && s->stream_stages < l) continue;
         probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
@@ -1337,10 +1337,10 @@ int fea_autotune(fea_solver* s) {
 int fea_set_cg_variant(fea_solver* s, int variant) {
     API_BEGIN
     check_handle(s);
-    if (variant != 0 && variant != 1 && variant != 2 && variant != 4 && variant != 8 && variant != 16)
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 4, 8 or 16");
-    if (variant <= 2 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
-    if (variant == 2 && !s->stream_ok)
+    if (variant < 0 || (variant > 3 && variant != 4 && variant != 8 && variant != 16))
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 8 or 16");
+    if (variant <= 3 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
+    if ((variant == 2 || variant == 3) && s->stream_stages < variant)
         return fail(FEA_ERR_UNSUPPORTED, "streamed tiles exceed the shared memory on this mesh");
     s->lanes = variant;
     API_END

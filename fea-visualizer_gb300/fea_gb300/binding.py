@@ -252,8 +252,8 @@ class CUDASolver:
         return self.info.rows_per_warp_lanes
 
     def set_cg_variant(self, variant: int):
-        """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 2: tile-ELL streamed by bulk copies;
-        4, 8, 16: windowed CSR kernels."""
+        """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 2, 3: tile-ELL streamed by bulk copies
+        (2 or 3 stages); 4, 8, 16: windowed CSR kernels."""
         check(load().fea_set_cg_variant(self._h, int(variant)))
 
     def stream(self) -> int:

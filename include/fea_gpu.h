@@ -211,16 +211,17 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
 /* CG kernel variants: 0 and 1 = tile-ELL layout (256-row tiles, 32-row
  * slices stored column-wise, operand and halo staged in shared memory; the
  * first 8 (variant 0, the default when the mesh's halos fit) or 4 (variant 1)
- * entries of each row prefetched into registers), 2 = the same layout with
- * each tile's operator entries and row vectors moved into shared memory by
- * bulk asynchronous copies two tiles ahead, 4 / 8 / 16 = warp-cooperative
- * CSR with that many entries per lane and window.  fea_autotune
+ * entries of each row prefetched into registers), 2 and 3 = the same layout
+ * with each tile's operator entries and row vectors moved into 2 or 3
+ * shared-memory stages by bulk asynchronous copies ahead of the tile being
+ * computed, 4 / 8 / 16 = warp-cooperative CSR with that many entries per
+ * lane and window.  fea_autotune
  * times one CG iteration of each candidate on this mesh and keeps the
  * fastest (fea_info.rows_per_warp_lanes); the fields are left unchanged. */
 int fea_autotune(fea_solver* s);
 /* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
- * FEA_ERR_UNSUPPORTED for 0, 1 or 2 when the layout, or for 2 the shared
- * memory of its stages, is unavailable on this mesh). */
+ * FEA_ERR_UNSUPPORTED for 0 to 3 when the layout, or for 2 and 3 the shared
+ * memory of their stages, is unavailable on this mesh). */
 int fea_set_cg_variant(fea_solver* s, int variant);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
