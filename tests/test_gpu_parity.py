@@ -276,7 +276,7 @@ def test_autotune_choice_is_valid(fea):
     assert s.info.rows_per_warp_lanes == 0  # the tile-ELL layout is the default
     assert s.autotune() in (0, 1, 2, 3, 4, 8, 16)
     with pytest.raises(fea.FeaError):
-        s.set_cg_variant(3)
+        s.set_cg_variant(5)
 
 
 @pytest.mark.parametrize("name", ["grid33", "ico3", "cyl"])
