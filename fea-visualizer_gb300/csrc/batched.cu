@@ -91,6 +91,13 @@ struct BArgs {
     double* part;           // [ntiles * kNV] tile partials
     unsigned int* iticket;  // [ninst] tiles finished per instance in this phase
     int probe;              // timing probe: every tile, no state update
+    // tile-ELL copy of A (variants 0 and 1)
+    const FV<R, 2>* As;
+    const uint16_t* lcol;
+    const int32_t* slice_off;
+    const int32_t* halo_off;
+    const int32_t* halo_col;
+    int hmax;
     cudaGraphConditionalHandle cond;
     int* cont;
     int use_graph;
@@ -334,6 +341,92 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a
     phase_end(a, kIterNext);
 }
 
+// The same two kernels on the tile-ELL layout of the stacked matrix (the
+// instances' tiles are the layout's tiles): the tile's operand and halo staged
+// in shared memory, two staging buffers alternating over processed tiles.
+template <typename R>
+__device__ __forceinline__ EllView<R, 2> bell_view(const BArgs<R>& a) {
+    return EllView<R, 2>{a.As, a.lcol, a.slice_off, a.halo_off, a.halo_col};
+}
+
+template <typename R, int KPRE>
+__global__ void __launch_bounds__(kBlock) kb_init_ell(BArgs<R> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
+    __shared__ double red[32 * kNV];
+    const int iter = iter_of(a);
+    FV<R, 2>* w = a.wb[iter & 1];
+    const EllView<R, 2> e = bell_view(a);
+    const int stride = kTileRows + a.hmax;
+    int buf = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        PhaseCtl<R, 2> c;
+        c.set(iter, (const volatile BInst*)(a.inst + i));
+        if (!c.any && !a.probe) continue;
+        Acc<R> dot[2];
+        init_tile_ell<R, 2, KPRE>(e, a.z, w, tile, ell_ref(e, tile, a.ntiles), a.N, ut + buf * stride, dot);
+        buf ^= 1;
+        double blk[2], tot[2];
+        block_totals<2>(dot, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<2>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
+            volatile BInst* s = a.inst + i;
+            finish_spmv<R, 2>(s, &a.inst[i].flags, c.act, tot);
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                s->fresh[f] = 1;
+                nact += s->active[f];
+            }
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterKeep);
+}
+
+template <typename R, int KPRE>
+__global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
+    __shared__ double red[32 * kNV];
+    const int iter = iter_of(a), par = iter & 1;
+    CgVecs<R, 2> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.p;
+    v.r0 = a.rb[par];
+    v.w0 = a.wb[par];
+    v.s0 = a.sb[par];
+    v.r1 = a.rb[par ^ 1];
+    v.w1 = a.wb[par ^ 1];
+    v.s1 = a.sb[par ^ 1];
+    const EllView<R, 2> e = bell_view(a);
+    const int stride = kTileRows + a.hmax;
+    int buf = 0;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        PhaseCtl<R, 2> c;
+        c.set(iter, (const volatile BInst*)(a.inst + i));
+        if (!c.any) continue;
+        Acc<R> dots[kNV];
+        cgcg_tile_ell<R, 2, KPRE>(v, e, c, tile, ell_ref(e, tile, a.ntiles), a.N, ut + buf * stride, dots);
+        buf ^= 1;
+        double blk[kNV], tot[kNV];
+        block_totals<kNV>(dots, red, blk);
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+            volatile BInst* s = a.inst + i;
+            if (finish_cgcg<R, 2>(s, &a.inst[i].flags, c.act, tot))
+                atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
+        }
+    }
+    phase_end(a, kIterNext);
+}
+
 // After the first solve loop: zero right-hand sides give x = 0, then one
 // FP64-accurate true-residual pass r = b - A x; fields still above their
 // threshold restart CG from there.
@@ -526,7 +619,9 @@ struct fea_batch {
     int precision = FEA_FP32;
     int ninst = 0, ntiles = 0;
     int64_t N = 0, nnz = 0;
-    int wch = 8;  // entries per lane and window of the CG kernels (autotuned)
+    int wch = 8;  // CG kernel variant (autotuned): 0/1 tile-ELL (8/4 entries prefetched), 4/8 CSR window
+    TileEll ell;  // tile-ELL layout of the stacked matrix
+    void* As = nullptr;
     std::vector<int64_t> V, node_off;
     DeviceArena mem;
     int32_t *rp = nullptr, *col = nullptr, *tile_inst = nullptr, *inst_tile = nullptr, *node_map = nullptr;
@@ -576,6 +671,14 @@ BArgs<R> make_bargs(fea_batch* B) {
     a.ctl = B->ctl;
     a.part = B->part;
     a.iticket = B->iticket;
+    if (B->ell.ok) {
+        a.As = (const FV<R, 2>*)B->As;
+        a.lcol = B->ell.lcol;
+        a.slice_off = B->ell.slice_off;
+        a.halo_off = B->ell.halo_off;
+        a.halo_col = B->ell.halo_col;
+        a.hmax = B->ell.hmax;
+    }
     return a;
 }
 
@@ -590,13 +693,35 @@ struct BLoop {
     }
 };
 
-template <typename R, int WCH>
+// The CG kernels of a variant: 4 and 8 the windowed CSR kernels, 0 and 1 the
+// tile-ELL kernels with 8 or 4 entries prefetched.
+template <typename R, int V>
+struct BKernels {
+    static constexpr void (*init)(BArgs<R>) = kb_init<R, V>;
+    static constexpr void (*iter)(BArgs<R>) = kb_iter<R, V>;
+    static size_t smem(const fea_batch*) { return 0; }
+};
+template <typename R, int KPRE>
+struct BEllKernels {
+    static constexpr void (*init)(BArgs<R>) = kb_init_ell<R, KPRE>;
+    static constexpr void (*iter)(BArgs<R>) = kb_iter_ell<R, KPRE>;
+    static size_t smem(const fea_batch* B) { return 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + B->ell.hmax); }
+};
+template <typename R>
+struct BKernels<R, 0> : BEllKernels<R, 8> {};
+template <typename R>
+struct BKernels<R, 1> : BEllKernels<R, 4> {};
+
+template <typename R, int V>
 struct BGrids {
+    using K = BKernels<R, V>;
     int rhs, init, iter, stream;
+    size_t smem;
     explicit BGrids(const fea_batch* B) {
+        smem = K::smem(B);
         rhs = wave_grid(kb_rhs<R>, B->ntiles);
-        init = wave_grid(kb_init<R, WCH>, B->ntiles);
-        iter = wave_grid(kb_iter<R, WCH>, B->ntiles);
+        init = wave_grid(K::init, B->ntiles, smem);
+        iter = wave_grid(K::iter, B->ntiles, smem);
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(B->N, kBlock)));
     }
 };
@@ -607,6 +732,7 @@ template <typename R, int WCH>
 void build_batch_graph_t(fea_batch* B) {
     BLoop<R> L(make_bargs<R>(B), B->flags, 1);
     const BGrids<R, WCH> g(B);
+    using K = BKernels<R, WCH>;
     StepGraph& G = B->graph;
     cudaGraph_t top;
     FEA_CUDA_TRY(cudaGraphCreate(&top, 0));
@@ -619,14 +745,14 @@ void build_batch_graph_t(fea_batch* B) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, kb_rhs<R>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, kb_init<R, WCH>, g.init, kBlock, L.a1);
+    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, kb_iter<R, WCH>, g.iter, kBlock, L.a1);
+    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem);
     s = add_kernel(step_body, s, kb_refine<R>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, kb_init<R, WCH>, g.init, kBlock, L.a2);
+    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, kb_iter<R, WCH>, g.iter, kBlock, L.a2);
+    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem);
     add_kernel(step_body, s, kb_stepctl<R>, 1, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
     G.lanes = WCH;
@@ -645,18 +771,23 @@ template <typename R, int WCH>
 void run_batch_stream_t(fea_batch* B) {
     BLoop<R> L(make_bargs<R>(B), B->flags, 0);
     const BGrids<R, WCH> g(B);
+    using K = BKernels<R, WCH>;
     cudaStream_t st = B->stream;
     kb_start<R><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_int(&B->flags->step, st)) {
         kb_rhs<R><<<g.rhs, kBlock, 0, st>>>(L.a1);
+        FEA_CHECK_LAUNCH();
         for (int loop = 0; loop < 2; loop++) {
             const BArgs<R>& la = loop ? L.a2 : L.a1;
-            if (loop) kb_refine<R><<<g.rhs, kBlock, 0, st>>>(L.a2);
-            kb_init<R, WCH><<<g.init, kBlock, 0, st>>>(la);
+            if (loop) {
+                kb_refine<R><<<g.rhs, kBlock, 0, st>>>(L.a2);
+                FEA_CHECK_LAUNCH();
+            }
+            K::init<<<g.init, kBlock, g.smem, st>>>(la);
             FEA_CHECK_LAUNCH();
             while (read_int(la.cont, st)) {
-                kb_iter<R, WCH><<<g.iter, kBlock, 0, st>>>(la);
+                K::iter<<<g.iter, kBlock, g.smem, st>>>(la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -670,32 +801,50 @@ void run_batch_stream_t(fea_batch* B) {
 template <typename R>
 void run_batch(fea_batch* B) {
     if (B->stream_mode) {
-        if (B->wch == 4) run_batch_stream_t<R, 4>(B);
-        else run_batch_stream_t<R, 8>(B);
+        switch (B->wch) {
+        case 0: run_batch_stream_t<R, 0>(B); break;
+        case 1: run_batch_stream_t<R, 1>(B); break;
+        case 4: run_batch_stream_t<R, 4>(B); break;
+        default: run_batch_stream_t<R, 8>(B); break;
+        }
         return;
     }
     if (!B->graph.exec || B->graph.lanes != B->wch) {
         B->graph.destroy();
-        if (B->wch == 4) build_batch_graph_t<R, 4>(B);
-        else build_batch_graph_t<R, 8>(B);
+        switch (B->wch) {
+        case 0: build_batch_graph_t<R, 0>(B); break;
+        case 1: build_batch_graph_t<R, 1>(B); break;
+        case 4: build_batch_graph_t<R, 4>(B); break;
+        default: build_batch_graph_t<R, 8>(B); break;
+        }
     }
     FEA_CUDA_TRY(cudaGraphLaunch(B->graph.exec, B->stream));
 }
 
-// One set-up SpMV (w = A z over every tile) with the given window size: the
+template <typename R, int V>
+void batch_probe_t(fea_batch* B, const BArgs<R>& a) {
+    const BGrids<R, V> g(B);
+    BKernels<R, V>::init<<<g.init, kBlock, g.smem, B->stream>>>(a);
+    FEA_CHECK_LAUNCH();
+}
+
+// One set-up SpMV (w = A z over every tile) of the given variant: the
 // autotuning probe.  It writes only CG scratch that every solve recomputes.
 template <typename R>
-void batch_probe(fea_batch* B, int wch) {
+void batch_probe(fea_batch* B, int var) {
     BArgs<R> a = make_bargs<R>(B);
     a.probe = 1;
     a.use_graph = 0;
     a.cont = &B->flags->probe;
-    if (wch == 4) kb_init<R, 4><<<BGrids<R, 4>(B).init, kBlock, 0, B->stream>>>(a);
-    else kb_init<R, 8><<<BGrids<R, 8>(B).init, kBlock, 0, B->stream>>>(a);
-    FEA_CHECK_LAUNCH();
+    switch (var) {
+    case 0: batch_probe_t<R, 0>(B, a); break;
+    case 1: batch_probe_t<R, 1>(B, a); break;
+    case 4: batch_probe_t<R, 4>(B, a); break;
+    default: batch_probe_t<R, 8>(B, a); break;
+    }
 }
 
-// Pick the window size of the CG kernels by timing the set-up SpMV.
+// Pick the CG kernel variant by timing the set-up SpMV of each candidate.
 template <typename R>
 void autotune_batch(fea_batch* B) {
     cudaEvent_t e0, e1;
@@ -703,7 +852,8 @@ void autotune_batch(fea_batch* B) {
     FEA_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     int pick = 8;
-    for (int w : {4, 8}) {
+    for (int w : {0, 1, 4, 8}) {
+        if (w <= 1 && !B->ell.ok) continue;
         for (int rep = 0; rep < 13; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, B->stream));
             batch_probe<R>(B, w);
@@ -874,6 +1024,17 @@ void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
         fea_destroy(H.h[i]);
         H.h[i] = nullptr;
     }
+    {  // tile-ELL layout of the stacked matrix
+        std::vector<int32_t> hrp(Nr + 1), hcol(nnz);
+        FEA_CUDA_TRY(cudaMemcpyAsync(hrp.data(), B->rp, sizeof(int32_t) * (Nr + 1), cudaMemcpyDeviceToHost, st));
+        if (nnz > 0)
+            FEA_CUDA_TRY(cudaMemcpyAsync(hcol.data(), B->col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, st));
+        FEA_CUDA_TRY(cudaStreamSynchronize(st));
+        if (build_tile_ell(hrp, hcol, Nr, sizeof(FV<R, 2>), kEllSmemBudget, B->ell, B->mem, st)) {
+            B->As = B->mem.alloc<FV<R, 2>>(B->ell.E);
+            fill_tile_ell<R, 2>(B->ell, (const FV<R, 2>*)B->A, (FV<R, 2>*)B->As, st);
+        }
+    }
     autotune_batch<R>(B);
     FEA_CUDA_TRY(cudaStreamSynchronize(st));
 }
@@ -1009,6 +1170,21 @@ int fea_batch_synchronize(fea_batch* B) {
     BATCH_API_BEGIN
     check_batch(B);
     FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    BATCH_API_END
+}
+
+int fea_batch_cg_variant(fea_batch* B, int set, int* variant) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    if (!variant) return fail(FEA_ERR_INVALID_ARGUMENT, "null variant");
+    if (!set) {
+        *variant = B->wch;
+        return FEA_OK;
+    }
+    const int v = *variant;
+    if (v != 0 && v != 1 && v != 4 && v != 8) return fail(FEA_ERR_INVALID_ARGUMENT, "batch CG variant must be 0, 1, 4 or 8");
+    if (v <= 1 && !B->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable for this batch");
+    B->wch = v;
     BATCH_API_END
 }
 

@@ -115,6 +115,7 @@ SIGNATURES = {
     "fea_batch_advance_time": [_P, _I64],
     "fea_batch_synchronize": [_P],
     "fea_batch_get_status": [_P, _P, _P],
+    "fea_batch_cg_variant": [_P, C.c_int, C.POINTER(C.c_int)],
     "fea_pcg_solve_csr_noalloc": [_I64, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int, _P,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double)],
 }
@@ -382,6 +383,17 @@ class BatchSolver:
 
     def synchronize(self):
         check(load().fea_batch_synchronize(self._h))
+
+    @property
+    def cg_variant(self) -> int:
+        v = C.c_int(0)
+        check(load().fea_batch_cg_variant(self._h, 0, C.byref(v)))
+        return v.value
+
+    def set_cg_variant(self, variant: int):
+        """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 4, 8: windowed CSR kernels."""
+        v = C.c_int(int(variant))
+        check(load().fea_batch_cg_variant(self._h, 1, C.byref(v)))
 
     def status(self):
         """(flags uint32[n], iterations int32[n, 2] of the last solve)."""

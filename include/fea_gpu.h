@@ -231,8 +231,8 @@ int fea_get_stream(fea_solver* s, void** stream);
 /* Diagnostics: mean device time in ms of one CG iteration kernel (the step
  * loop's dominant kernel: the CSR SpMV with the vector updates fused) over
  * `reps` launches on the current operator of the current equation, each
- * launch preceded by a 256 MiB write that evicts the L2 cache when
- * flush_l2 != 0.  CUDA events on the handle's stream.  The probe masks every
+ * launch preceded by a 256 MiB read that evicts the L2 cache (leaving clean
+ * lines) when flush_l2 != 0.  CUDA events on the handle's stream.  The probe masks every
  * field, so the fields are written back unchanged; only CG scratch, which the
  * next step recomputes, changes. */
 int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch);
@@ -293,6 +293,11 @@ int fea_batch_advance_time(fea_batch* b, int64_t nsteps);
 int fea_batch_synchronize(fea_batch* b);
 /* flags: uint32[num_instances]; iterations: int32[2*num_instances] (last solve) */
 int fea_batch_get_status(fea_batch* b, uint32_t* flags, int32_t* iterations);
+/* CG kernel variant of the batch: 0 / 1 tile-ELL (8 / 4 entries prefetched;
+ * FEA_ERR_UNSUPPORTED when the layout is unavailable), 4 / 8 windowed CSR.
+ * fea_batch_create picks the fastest by timing; *variant receives the
+ * current one when `set` is 0. */
+int fea_batch_cg_variant(fea_batch* b, int set, int* variant);
 
 /* ---- solve without device allocation ---------------------------------------
  * No counterpart in the reference.  Solves A x = b with Jacobi-preconditioned

@@ -105,6 +105,7 @@ def test_batched_repeatable_and_masked(fea):
     runs = []
     for _ in range(2):
         B = fea.BatchSolver(insts, cg_tolerance=1e-6)
+        B.set_cg_variant(0)  # bit-for-bit comparisons need the same kernels
         for i, d in enumerate(insts):
             B.set_fields(i, *_start(d, 7 + i))
         B.advance_time(5)
@@ -122,6 +123,8 @@ def test_blowup_freezes_only_its_instance(fea):
     starts = [_start(d, 30 + i) for i, d in enumerate(insts)]
     ref = fea.BatchSolver(insts, cg_tolerance=1e-6)
     bad = fea.BatchSolver(insts, cg_tolerance=1e-6)
+    ref.set_cg_variant(0)
+    bad.set_cg_variant(0)
     for i, (u, v) in enumerate(starts):
         ref.set_fields(i, u, v)
         if i == 1:
@@ -142,6 +145,24 @@ def test_blowup_freezes_only_its_instance(fea):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 4, 8])
+def test_batched_variants_match_oracle(fea, oracle_mod, variant):
+    insts = _instances()
+    B = fea.BatchSolver(insts, cg_tolerance=1e-7)
+    B.set_cg_variant(variant)
+    assert B.cg_variant == variant
+    for i, d in enumerate(insts):
+        B.set_fields(i, *_start(d, 50 + i))
+    B.advance_time(2)
+    for i, d in enumerate(insts):
+        S = oracle_mod.System(d["vertices"], d["triangles"], bc=d["boundary_condition"])
+        u0, v0 = _start(d, 50 + i)
+        uo, vo, *_ = oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, d["time_step"],
+                                 S.gather(u0.astype(np.float32)), S.gather(v0.astype(np.float32)), 2, **_okw(d))
+        ug, vg = B.get_fields(i)
+        assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, (variant, i)
+
+
 def test_batch_arguments(fea):
     insts = _instances()[:2]
     B = fea.BatchSolver(insts)
@@ -149,3 +170,5 @@ def test_batch_arguments(fea):
         B.get_fields(2)
     with pytest.raises(fea.FeaError):
         B.advance_time(-1)
+    with pytest.raises(fea.FeaError):
+        B.set_cg_variant(2)
