@@ -21,8 +21,10 @@ LIB = os.path.join(LIB_DIR, "libfea_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no floating-point contraction (the export's color polynomial and
+# other host arithmetic round at every operation on x86 and Arm alike)
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-fvisibility=hidden", f"-I{INCLUDE}", f"-I{CSRC}"]
+         "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
 def nvcc() -> str:

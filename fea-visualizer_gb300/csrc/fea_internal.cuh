@@ -229,6 +229,20 @@ template <typename R>
 void adjoint_grad_D(const double* Kloc, const uint32_t* tri, const int32_t* idx_c, int64_t T, double c, const R* mu,
                     const R* u, double* gD, cudaStream_t st);
 
+// ---- after the solve (surface.cu) ------------------------------------------------
+// Vertex -> incident triangles (vt_ptr [V+1], vt_tri [3T], ascending per vertex).
+void build_vertex_triangles(const uint32_t* tri, int64_t T, int64_t V, int32_t* vt_ptr, int32_t* vt_tri,
+                            cudaStream_t st);
+// Extruded smooth normals: face[3T] scratch, out[3V].
+void smooth_normals(const float* xyz, const uint32_t* tri, int64_t T, int64_t V, const int32_t* vt_ptr,
+                    const int32_t* vt_tri, const float* nrm, const float* val, float e, float* face, float* out,
+                    cudaStream_t st);
+// Export clipping: slots pos[18T], pval[6T], used[6T]; triangles otri[12T]
+// (slot numbers, -1 when not emitted).
+void ply_clip(const float* xyz, const uint32_t* tri, int64_t T, const float* nrm, const float* val, float e,
+              float threshold, int mesh_type, float* pos, float* pval, uint8_t* used, int32_t* otri,
+              cudaStream_t st);
+
 // Solver-order view of a handle's assembled mesh: what the batched solver
 // copies out of a single-mesh handle built for each of its instances.
 struct MeshView {

@@ -4,6 +4,9 @@
 // (mesh, idx_map, assembled matrices; src/FEM/FEMContext.cpp) and of a Solver
 // implementation (state fields u, v and advance_time; include/FEM/Solver.hpp).
 #include <algorithm>
+#include <charconv>
+#include <cstdio>
+#include <unordered_map>
 #include <cstdarg>
 #include <cstring>
 #include <new>
@@ -192,6 +195,8 @@ struct fea_solver {
     float cur_vel[3] = {1.f, 0.f, 0.f};
     int cur_vel_mode = 0;
     float* d_nodes = nullptr;  // node-indexed staging buffer [V] for host field copies
+    int32_t* vt_ptr = nullptr;  // vertex -> triangles (built on first use)
+    int32_t* vt_tri = nullptr;
 };
 
 namespace fea {
@@ -884,6 +889,172 @@ MeshView mesh_view(const fea_solver* s) {
     return m;
 }
 
+// ---- after the solve: smooth normals and the .ply export ----------------------------
+
+// The displayed field (v for Gray-Scott, u otherwise; 0 on Dirichlet points),
+// node-indexed, into the handle's staging buffer.
+void stage_node_values(fea_solver* s) {
+    const int which = displayed_field(s->prm);
+    Fields& F = s->F;
+    const int64_t V = s->V;
+    if (s->precision == FEA_FP64) {
+        if (F.interleaved)
+            k_scatter_nodes<double><<<launch_grid(V), kBlock, 0, s->stream>>>((double*)F.uv, s->idx_c, V, s->d_nodes,
+                                                                               2, which);
+        else
+            k_scatter_nodes<double><<<launch_grid(V), kBlock, 0, s->stream>>>(
+                (double*)(which ? F.v : F.u), s->idx_c, V, s->d_nodes, 1, 0);
+    } else {
+        if (F.interleaved)
+            k_scatter_nodes<float><<<launch_grid(V), kBlock, 0, s->stream>>>((float*)F.uv, s->idx_c, V, s->d_nodes, 2,
+                                                                              which);
+        else
+            k_scatter_nodes<float><<<launch_grid(V), kBlock, 0, s->stream>>>((float*)(which ? F.v : F.u), s->idx_c,
+                                                                              V, s->d_nodes, 1, 0);
+    }
+    FEA_CHECK_LAUNCH();
+}
+
+void ensure_vertex_triangles(fea_solver* s) {
+    if (s->vt_ptr) return;
+    s->vt_ptr = s->mesh_mem.alloc<int32_t>(s->V + 1);
+    s->vt_tri = s->mesh_mem.alloc<int32_t>(3 * s->T);
+    build_vertex_triangles(s->tri, s->T, s->V, s->vt_ptr, s->vt_tri, s->stream);
+}
+
+// nrm and out: device float[3V]
+void smooth_normals_dev(fea_solver* s, const float* nrm, float e, float* out) {
+    ensure_vertex_triangles(s);
+    stage_node_values(s);
+    DeviceArena tmp;
+    float* face = tmp.alloc<float>(3 * s->T);
+    smooth_normals(s->xyz, s->tri, s->T, s->V, s->vt_ptr, s->vt_tri, nrm, s->d_nodes, e, face, out, s->stream);
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+}
+
+struct PlyGeometry {
+    std::vector<float> pos, val;
+    std::vector<uint32_t> tri;
+};
+
+struct PosKey {
+    uint32_t b[3];
+    bool operator==(const PosKey& o) const { return b[0] == o.b[0] && b[1] == o.b[1] && b[2] == o.b[2]; }
+};
+struct PosKeyHash {
+    size_t operator()(const PosKey& k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint32_t x : k.b) h = (h ^ x) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+uint32_t key_bits(float f) {
+    if (f == 0.0f) f = 0.0f;  // -0 and +0 are the same position
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+
+// Clipping on the device, then the reference's first-seen numbering of the
+// positions (an exact-equality position map) on the host.
+void ply_geometry(fea_solver* s, const float* nrm_host, float e, float thr, int mesh_type, PlyGeometry& g) {
+    const int64_t V = s->V, T = s->T;
+    cudaStream_t st = s->stream;
+    DeviceArena tmp;
+    float* nrm = tmp.alloc<float>(3 * V);
+    float* pos = tmp.alloc<float>(18 * T);
+    float* pval = tmp.alloc<float>(6 * T);
+    uint8_t* used = tmp.alloc<uint8_t>(6 * T);
+    int32_t* otri = tmp.alloc<int32_t>(12 * T);
+    FEA_CUDA_TRY(cudaMemcpyAsync(nrm, nrm_host, sizeof(float) * 3 * V, cudaMemcpyHostToDevice, st));
+    stage_node_values(s);
+    ply_clip(s->xyz, s->tri, T, nrm, s->d_nodes, e, thr, mesh_type, pos, pval, used, otri, st);
+    std::vector<float> hpos(18 * T), hval(6 * T);
+    std::vector<uint8_t> hused(6 * T);
+    std::vector<int32_t> htri(12 * T);
+    FEA_CUDA_TRY(cudaMemcpyAsync(hpos.data(), pos, sizeof(float) * 18 * T, cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(hval.data(), pval, sizeof(float) * 6 * T, cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(hused.data(), used, 6 * T, cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(htri.data(), otri, sizeof(int32_t) * 12 * T, cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    std::unordered_map<PosKey, uint32_t, PosKeyHash> map;
+    std::vector<uint32_t> slot_idx(6 * T, 0);
+    g.pos.clear();
+    g.val.clear();
+    g.tri.clear();
+    for (int64_t k = 0; k < T; k++) {
+        for (int j = 0; j < 6; j++) {  // the order of the reference's add_clipped_position calls
+            const int64_t q = 6 * k + j;
+            if (!hused[q]) continue;
+            const float* p = &hpos[3 * q];
+            const PosKey key{{key_bits(p[0]), key_bits(p[1]), key_bits(p[2])}};
+            auto it = map.find(key);
+            if (it == map.end()) {
+                const uint32_t idx = (uint32_t)g.val.size();
+                map.emplace(key, idx);
+                g.pos.insert(g.pos.end(), p, p + 3);
+                g.val.push_back(hval[q]);
+                slot_idx[q] = idx;
+            } else {
+                slot_idx[q] = it->second;
+            }
+        }
+        for (int m = 0; m < 4; m++) {
+            const int32_t* t3 = &htri[12 * k + 3 * m];
+            if (t3[0] < 0) continue;
+            for (int i = 0; i < 3; i++) g.tri.push_back(slot_idx[t3[i]]);
+        }
+    }
+}
+
+void append_float(std::string& out, float x) {
+    char buf[64];
+    const auto r = std::to_chars(buf, buf + sizeof(buf), x);  // shortest round-trip form, as std::format("{}")
+    out.append(buf, r.ptr);
+}
+
+// Surface::export_to_ply's file (Surface.cpp:254-284): ASCII PLY, float
+// x y z red green blue per vertex (color from the polynomial color map,
+// ColorMap::get_color, ColorMap.cpp:12-14), "3 a b c" per face.
+void write_ply(const char* path, const PlyGeometry& g, const float* coeffs) {
+    std::string out;
+    const size_t nv = g.val.size(), nf = g.tri.size() / 3;
+    out.reserve(64 * nv + 24 * nf + 256);
+    out += "ply\nformat ascii 1.0\nelement vertex " + std::to_string(nv) +
+           "\nproperty float x\nproperty float y\nproperty float z\nproperty float red\nproperty float green\n"
+           "property float blue\nelement face " +
+           std::to_string(nf) + "\nproperty list uchar uint vertex_indices\nend_header\n";
+    for (size_t i = 0; i < nv; i++) {
+        const float t = g.val[i];
+        float col[3];
+        for (int ch = 0; ch < 3; ch++) {  // c0 + t (c1 + t (c2 + ... + t c6))
+            float acc = coeffs[3 * 6 + ch];
+            for (int k = 5; k >= 0; k--) acc = coeffs[3 * k + ch] + t * acc;
+            col[ch] = acc;
+        }
+        const float v6[6] = {g.pos[3 * i], g.pos[3 * i + 1], g.pos[3 * i + 2], col[0], col[1], col[2]};
+        for (int j = 0; j < 6; j++) {
+            append_float(out, v6[j]);
+            out += j < 5 ? ' ' : '\n';
+        }
+    }
+    for (size_t f = 0; f < nf; f++)
+        out += "3 " + std::to_string(g.tri[3 * f]) + " " + std::to_string(g.tri[3 * f + 1]) + " " +
+               std::to_string(g.tri[3 * f + 2]) + "\n";
+    FILE* fh = fopen(path, "wb");
+    if (!fh) {
+        set_error("cannot open %s for writing", path);
+        throw Error{FEA_ERR_INVALID_ARGUMENT};
+    }
+    const size_t wrote = fwrite(out.data(), 1, out.size(), fh);
+    const int closed = fclose(fh);
+    if (wrote != out.size() || closed != 0) {
+        set_error("writing %s failed", path);
+        throw Error{FEA_ERR_INVALID_ARGUMENT};
+    }
+}
+
 // Device partial-reduction storage sized for the widest grid.
 void alloc_run_state(fea_solver* s) {
     s->d_prm = s->run_mem.alloc<StepParams>(1);
@@ -1130,6 +1301,62 @@ int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target
     if (s->precision == FEA_FP64)
         adjoint_device<double>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
     else adjoint_device<float>(s, u0, target, nsteps, checkpoint_every, loss, grad_u0, grad_D);
+    API_END
+}
+
+int fea_smooth_normals(fea_solver* s, const float* normals, float vertex_extrusion, float* out) {
+    API_BEGIN
+    check_handle(s);
+    if (!normals || !out) return fail(FEA_ERR_INVALID_ARGUMENT, "null normals or output");
+    DeviceArena tmp;
+    float* nrm = tmp.alloc<float>(3 * s->V);
+    float* res = tmp.alloc<float>(3 * s->V);
+    FEA_CUDA_TRY(cudaMemcpyAsync(nrm, normals, sizeof(float) * 3 * s->V, cudaMemcpyHostToDevice, s->stream));
+    smooth_normals_dev(s, nrm, vertex_extrusion, res);
+    FEA_CUDA_TRY(cudaMemcpyAsync(out, res, sizeof(float) * 3 * s->V, cudaMemcpyDeviceToHost, s->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int fea_smooth_normals_device(fea_solver* s, const float* normals, float vertex_extrusion, float* out) {
+    API_BEGIN
+    check_handle(s);
+    if (!normals || !out) return fail(FEA_ERR_INVALID_ARGUMENT, "null normals or output");
+    smooth_normals_dev(s, normals, vertex_extrusion, out);
+    API_END
+}
+
+int fea_ply_geometry(fea_solver* s, const float* normals, float vertex_extrusion, float threshold, int mesh_type,
+                     float* positions, float* values, int64_t max_vertices, uint32_t* triangles,
+                     int64_t max_triangles, int64_t* num_vertices, int64_t* num_triangles) {
+    API_BEGIN
+    check_handle(s);
+    if (!normals || !num_vertices || !num_triangles) return fail(FEA_ERR_INVALID_ARGUMENT, "null argument");
+    if (mesh_type < FEA_MESH_OPEN || mesh_type > FEA_MESH_MIRRORED) return fail(FEA_ERR_INVALID_ARGUMENT, "bad mesh type");
+    PlyGeometry g;
+    ply_geometry(s, normals, vertex_extrusion, threshold, mesh_type, g);
+    const int64_t nv = (int64_t)g.val.size(), nt = (int64_t)g.tri.size() / 3;
+    *num_vertices = nv;
+    *num_triangles = nt;
+    if (positions && values && nv <= max_vertices) {
+        memcpy(positions, g.pos.data(), sizeof(float) * 3 * nv);
+        memcpy(values, g.val.data(), sizeof(float) * nv);
+    }
+    if (triangles && nt <= max_triangles) memcpy(triangles, g.tri.data(), sizeof(uint32_t) * 3 * nt);
+    API_END
+}
+
+int fea_export_ply(fea_solver* s, const char* path, const float* normals, float vertex_extrusion, float threshold,
+                   int mesh_type, const float* color_coeffs) {
+    API_BEGIN
+    check_handle(s);
+    if (!path || !normals) return fail(FEA_ERR_INVALID_ARGUMENT, "null path or normals");
+    if (mesh_type < FEA_MESH_OPEN || mesh_type > FEA_MESH_MIRRORED) return fail(FEA_ERR_INVALID_ARGUMENT, "bad mesh type");
+    float gray[21] = {0.f};
+    gray[3] = gray[4] = gray[5] = 1.0f;  // color = (t, t, t)
+    PlyGeometry g;
+    ply_geometry(s, normals, vertex_extrusion, threshold, mesh_type, g);
+    write_ply(path, g, color_coeffs ? color_coeffs : gray);
     API_END
 }
 

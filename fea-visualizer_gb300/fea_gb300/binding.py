@@ -22,6 +22,7 @@ FP32, FP64 = 0, 1
 STIFFNESS, MASS, ADVECTION = 0, 1, 2
 
 STATUS_BLOWUP, STATUS_NONFINITE, STATUS_NOT_CONVERGED, STATUS_BREAKDOWN = 1, 2, 4, 8
+MESH_OPEN, MESH_CLOSED, MESH_MIRRORED = 0, 1, 2
 
 ERRORS = {
     -1: "invalid argument", -2: "CUDA error", -3: "no CUDA device", -4: "bad mesh",
@@ -108,6 +109,11 @@ SIGNATURES = {
     "fea_adjoint_advdiff": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
     "fea_adjoint_advdiff_device": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
     "fea_set_element_diffusivity_device": [_P, _P],
+    "fea_smooth_normals": [_P, _P, C.c_float, _P],
+    "fea_smooth_normals_device": [_P, _P, C.c_float, _P],
+    "fea_export_ply": [_P, C.c_char_p, _P, C.c_float, C.c_float, C.c_int, _P],
+    "fea_ply_geometry": [_P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _I64, _P, _I64, C.POINTER(C.c_int64),
+                         C.POINTER(C.c_int64)],
     "fea_batch_create": [C.POINTER(InstanceDesc), C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)],
     "fea_batch_destroy": [_P],
     "fea_batch_set_fields": [_P, C.c_int, _P, _P],
@@ -319,6 +325,35 @@ class CUDASolver:
         D = D.detach().to(dtype=dt).contiguous()
         torch.cuda.synchronize(D.device)
         check(load().fea_set_element_diffusivity_device(self._h, D.data_ptr()))
+
+    # -- after the solve (Surface::calculate_normals, Surface::export_to_ply) -----
+    def smooth_normals(self, normals, vertex_extrusion):
+        """Extruded smooth normals of the displayed field -> float32[V, 3] (unnormalised)."""
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros_like(n)
+        check(load().fea_smooth_normals(self._h, _ptr(n), float(vertex_extrusion), _ptr(out)))
+        return out
+
+    def ply_geometry(self, normals, vertex_extrusion=0.25, threshold=0.0, mesh_type=MESH_OPEN):
+        """(positions float32[n, 3], values float32[n], triangles uint32[m, 3]) of the clipped export."""
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        nv, nt = C.c_int64(0), C.c_int64(0)
+        args = (float(vertex_extrusion), float(threshold), int(mesh_type))
+        check(load().fea_ply_geometry(self._h, _ptr(n), *args, None, None, 0, None, 0, C.byref(nv), C.byref(nt)))
+        pos = np.zeros((nv.value, 3), dtype=np.float32)
+        val = np.zeros(nv.value, dtype=np.float32)
+        tri = np.zeros((nt.value, 3), dtype=np.uint32)
+        check(load().fea_ply_geometry(self._h, _ptr(n), *args, _ptr(pos), _ptr(val), nv.value, _ptr(tri), nt.value,
+                                      C.byref(nv), C.byref(nt)))
+        return pos, val, tri
+
+    def export_ply(self, path, normals, vertex_extrusion=0.25, threshold=0.0, mesh_type=MESH_OPEN,
+                   color_coeffs=None):
+        """Surface::export_to_ply of the displayed field (color_coeffs: 7 RGB polynomial coefficients)."""
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        cc = None if color_coeffs is None else np.ascontiguousarray(color_coeffs, dtype=np.float32).reshape(21)
+        check(load().fea_export_ply(self._h, os.fsencode(path), _ptr(n), float(vertex_extrusion), float(threshold),
+                                    int(mesh_type), _ptr(cc)))
 
     def close(self):
         if getattr(self, "_h", None):

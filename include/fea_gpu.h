@@ -237,6 +237,40 @@ int fea_get_stream(fea_solver* s, void** stream);
  * next step recomputes, changes. */
 int fea_time_spmv(fea_solver* s, int reps, int flush_l2, double* ms_per_launch);
 
+/* ---- after the solve: extruded smooth normals, .ply export ---------------
+ * Smooth normals of the extruded surface (shaders/FEM/smooth_normals.glsl:
+ * 30-57, Surface::calculate_normals, Surface.cpp:287-306): every triangle's
+ * corners move along `normals` by min(1, vertex_extrusion * max(0, value)) of
+ * the displayed field (as fea_get_values); the cross product of the moved
+ * triangle's edges is added to its three vertices, unnormalised.  The sums
+ * run in ascending triangle order (the shader's atomics have no fixed order).
+ * normals, out: float[3V], host (or device for the _device variant). */
+int fea_smooth_normals(fea_solver* s, const float* normals, float vertex_extrusion, float* out);
+int fea_smooth_normals_device(fea_solver* s, const float* normals, float vertex_extrusion, float* out);
+
+/* MeshType, include/Utils/Surface.hpp:25-29 */
+#define FEA_MESH_OPEN 0
+#define FEA_MESH_CLOSED 1
+#define FEA_MESH_MIRRORED 2
+
+/* Surface::export_to_ply (Surface.cpp:138-285) of the displayed field: the
+ * triangles clipped at `threshold` on the extruded surface (plus the
+ * projected copies for FEA_MESH_CLOSED / FEA_MESH_MIRRORED), positions
+ * numbered in the reference's first-seen order, written as ASCII PLY with the
+ * color of each vertex's value from the polynomial color map
+ * c0 + t (c1 + t (... + t c6)) (ColorMap::get_color, ColorMap.cpp:12-14);
+ * color_coeffs: float[21] (7 RGB coefficients), NULL for gray (t, t, t).
+ * normals: host float[3V]. */
+int fea_export_ply(fea_solver* s, const char* path, const float* normals, float vertex_extrusion, float threshold,
+                   int mesh_type, const float* color_coeffs);
+/* The same geometry in memory: positions float[3 n], values float[n],
+ * triangles uint32[3 m]; *num_vertices = n, *num_triangles = m (the arrays
+ * are filled when n <= max_vertices and m <= max_triangles; call with NULL
+ * arrays to size them). */
+int fea_ply_geometry(fea_solver* s, const float* normals, float vertex_extrusion, float threshold, int mesh_type,
+                     float* positions, float* values, int64_t max_vertices, uint32_t* triangles,
+                     int64_t max_triangles, int64_t* num_vertices, int64_t* num_triangles);
+
 /* ---- adjoint (explicit advection-diffusion) ------------------------------
  * Model: nsteps steps of the advection-diffusion equation with
  * advection_scheme 1 (A u' = B u, A = M/dt + c K_D, B = M/dt + s Adv, with

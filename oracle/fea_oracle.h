@@ -19,8 +19,10 @@
  *     preconditioner: zero initial guess, stop when |r|^2 < tol^2 |b|^2,
  *     at most 2N iterations (Eigen's documented defaults)
  * plus the extensions the GPU path implements (consistent Gray-Scott reaction,
- * explicit advection, Newmark-beta wave, per-element diffusivity/velocity) and
- * an FP64 adjoint of the implicit advection-diffusion step.
+ * explicit advection, Newmark-beta wave, per-element diffusivity/velocity),
+ * an FP64 adjoint of the implicit advection-diffusion step, and the steps
+ * after the solve: extruded smooth normals (shaders/FEM/smooth_normals.glsl)
+ * and the iso-clipped .ply geometry (src/Utils/Surface.cpp:138-285).
  *
  * Parity status: UNPINNED against reference outputs -- the reference publishes
  * no golden vectors and cannot be compiled here (Eigen and glm are absent).
@@ -111,6 +113,22 @@ double fo_adjoint_advdiff_f64(int64_t N, int64_t T, const int32_t* row_ptr, cons
                               const uint32_t* tri, const fo_params* prm, const double* u0,
                               const double* target, int64_t nsteps, int64_t ckpt,
                               double* grad_u0, double* grad_D);
+
+/* Extruded smooth normals (shaders/FEM/smooth_normals.glsl:30-57): for each
+ * triangle, cross(b' - a', c' - a') of its corners moved along `normals` by
+ * min(1, extrusion * max(0, value)), added to its three vertices (in triangle
+ * order).  out: float[3V]. */
+void fo_smooth_normals_f32(int64_t V, int64_t T, const float* xyz, const uint32_t* tri, const float* normals,
+                           const float* values, float extrusion, float* out);
+
+/* Geometry of Surface::export_to_ply (Surface.cpp:138-285): clipped
+ * positions (first-seen order, exact-equality dedup), their values, and the
+ * output triangles.  mesh_type 0 Open, 1 Closed, 2 Mirrored.  Returns the
+ * vertex count; *ntri receives the triangle count (arrays hold at most
+ * cap_v / cap_t). */
+int64_t fo_ply_clip(int64_t V, int64_t T, const float* xyz, const uint32_t* tri, const float* normals,
+                    const float* values, float extrusion, float threshold, int mesh_type, float* pos_out,
+                    float* val_out, int64_t cap_v, uint32_t* tri_out, int64_t cap_t, int64_t* ntri);
 
 #ifdef __cplusplus
 }

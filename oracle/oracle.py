@@ -90,6 +90,11 @@ def lib():
             f = getattr(L, f"fo_instability_{s}")
             f.restype = C.c_int
             f.argtypes = [i64, p, p]
+        L.fo_smooth_normals_f32.restype = None
+        L.fo_smooth_normals_f32.argtypes = [i64, i64, p, p, p, p, C.c_float, p]
+        L.fo_ply_clip.restype = i64
+        L.fo_ply_clip.argtypes = [i64, i64, p, p, p, p, C.c_float, C.c_float, C.c_int, p, p, i64, p, i64,
+                                  C.POINTER(C.c_int64)]
         L.fo_adjoint_advdiff_f64.restype = C.c_double
         L.fo_adjoint_advdiff_f64.argtypes = [i64, i64, p, p, p, p, p, p, p, p, p,
                                              C.POINTER(Params), p, p, i64, i64, p, p]
@@ -292,3 +297,33 @@ def params(equation, dt, **kw) -> Params:
     p.warm_start = kw.get("warm_start", 1)
     p.nthreads = kw.get("nthreads", 1)
     return p
+
+
+def smooth_normals(xyz, tri, normals, values, extrusion):
+    """Extruded smooth normals (smooth_normals.glsl), summed in triangle order -> float32[V, 3]."""
+    xyz = _c(xyz, np.float32)
+    tri = _c(tri, np.uint32)
+    nrm = _c(normals, np.float32)
+    val = _c(values, np.float32)
+    out = np.zeros((xyz.shape[0], 3), dtype=np.float32)
+    lib().fo_smooth_normals_f32(xyz.shape[0], tri.shape[0], _ptr(xyz), _ptr(tri), _ptr(nrm), _ptr(val),
+                                float(extrusion), _ptr(out))
+    return out
+
+
+def ply_clip(xyz, tri, normals, values, extrusion, threshold, mesh_type):
+    """Geometry of Surface::export_to_ply -> (positions float32[n, 3], values float32[n], triangles uint32[m, 3])."""
+    xyz = _c(xyz, np.float32)
+    tri = _c(tri, np.uint32)
+    nrm = _c(normals, np.float32)
+    val = _c(values, np.float32)
+    T = tri.shape[0]
+    cap_v, cap_t = 6 * T + 1, 4 * T + 1
+    pos = np.zeros((cap_v, 3), dtype=np.float32)
+    pv = np.zeros(cap_v, dtype=np.float32)
+    tout = np.zeros((cap_t, 3), dtype=np.uint32)
+    nt = C.c_int64(0)
+    n = lib().fo_ply_clip(xyz.shape[0], T, _ptr(xyz), _ptr(tri), _ptr(nrm), _ptr(val), float(extrusion),
+                          float(threshold), int(mesh_type), _ptr(pos), _ptr(pv), cap_v, _ptr(tout), cap_t,
+                          C.byref(nt))
+    return pos[:n].copy(), pv[:n].copy(), tout[:nt.value].copy()
