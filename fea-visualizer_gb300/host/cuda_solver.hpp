@@ -31,11 +31,15 @@ enum class Equation { Heat = FEA_HEAT, Wave = FEA_WAVE, Advection_Diffusion = FE
                       Reaction_Diffusion = FEA_REACTION_DIFFUSION };
 enum class BoundaryCondition { Dirichlet = FEA_DIRICHLET, Neumann = FEA_NEUMANN };
 
+enum class MeshType { Open = FEA_MESH_OPEN, Closed = FEA_MESH_CLOSED, Mirrored = FEA_MESH_MIRRORED };
+
 struct Surface {
     std::vector<std::array<float, 3>> vertices;
+    std::vector<std::array<float, 3>> normals;  // Surface::normals (Surface.cpp:91-102)
     std::vector<std::array<uint32_t, 3>> triangles;
     std::vector<bool> on_boundary;  // empty: detected on the device
     std::vector<float> values;
+    std::vector<std::array<float, 3>> calculated_normals;  // the smooth-normals output
     int num_boundary_points = 0;
 };
 
@@ -115,6 +119,25 @@ public:
         int out = 0;
         check(fea_has_numerical_instability(handle_, &out), "fea_has_numerical_instability");
         return out != 0;
+    }
+
+    // Surface::calculate_normals (Surface.cpp:287-306) on the solver's field.
+    void calculate_normals(float vertex_extrusion) {
+        Surface& s = *fem_ctx->surface;
+        s.calculated_normals.resize(s.vertices.size());
+        check(fea_smooth_normals(handle_, reinterpret_cast<const float*>(s.normals.data()), vertex_extrusion,
+                                 reinterpret_cast<float*>(s.calculated_normals.data())),
+              "fea_smooth_normals");
+    }
+
+    // Surface::export_to_ply (Surface.cpp:138-285); coeffs: the color map's
+    // 7 RGB coefficients (nullptr: gray).
+    void export_to_ply(const char* path, float vertex_extrusion = 0.25f, float threshold = 0.0f,
+                       MeshType mesh_type = MeshType::Open, const float* coeffs = nullptr) {
+        const Surface& s = *fem_ctx->surface;
+        check(fea_export_ply(handle_, path, reinterpret_cast<const float*>(s.normals.data()), vertex_extrusion,
+                             threshold, static_cast<int>(mesh_type), coeffs),
+              "fea_export_ply");
     }
 
     fea_solver* handle() { return handle_; }

@@ -42,7 +42,8 @@ def test_heat_frames_through_shim(fea, oracle_mod, tmp_path, bc):
         fh.write(u0.tobytes())
     out = tmp_path / "out.bin"
     frames = 5
-    subprocess.run([exe, str(mesh), str(out), "0", str(bc), str(frames)], check=True)
+    ply = tmp_path / "out.ply"
+    subprocess.run([exe, str(mesh), str(out), "0", str(bc), str(frames), str(ply)], check=True)
     raw = np.fromfile(out, dtype=np.float32)
     vals, unstable = raw[:-1], raw[-1:].view(np.int32)[0]
     assert unstable == 0
@@ -56,3 +57,8 @@ def test_heat_frames_through_shim(fea, oracle_mod, tmp_path, bc):
     assert rel_l2(vals, S.scatter(u)) < 1e-5
     if bc == 0:
         assert np.all(vals[S.on_boundary == 1] == 0)
+    # the export at the end of the loop (threshold 0, Open): geometry as the oracle's
+    normals = np.tile(np.array([0.0, 0.0, 1.0], np.float32), (len(xyz), 1))
+    P, _, T = oracle_mod.ply_clip(xyz, tri, normals, vals, 0.25, 0.0, 0)
+    lines = ply.read_text().splitlines()
+    assert lines[0] == "ply" and lines[2] == f"element vertex {len(P)}" and lines[9] == f"element face {len(T)}"
