@@ -316,6 +316,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint inverse-problem timing")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--cg-variant", type=int, default=None,
+                    help="CG kernel variant instead of the autotuned one (profiling captures)")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="vertices per side (other sizes are for profiling captures, not bench lines)")
     args = ap.parse_args()
@@ -342,6 +344,9 @@ def main():
     p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=CG_TOL, **PARAMS)
     s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=F.FP32, params=p)
     lanes = s.autotune()
+    if args.cg_variant is not None:
+        s.set_cg_variant(args.cg_variant)
+        lanes = args.cg_variant
     info = s.info
     N, nnz, V = info.num_unknowns, info.nnz, info.num_vertices
     s.set_fields(u0, v0)
