@@ -114,6 +114,15 @@ double fo_adjoint_advdiff_f64(int64_t N, int64_t T, const int32_t* row_ptr, cons
                               const double* target, int64_t nsteps, int64_t ckpt,
                               double* grad_u0, double* grad_D);
 
+/* FP64 adjoint of the mass-weighted Gray-Scott step (the loss 1/2 |x_N - t|_M^2
+ * over the fields whose target is not NULL).  Returns the loss; writes dJ/du0,
+ * dJ/dv0 [N] and grad_params[4] = dJ/dF, dJ/dk, dJ/dDu, dJ/dDv.  prm: the
+ * Gray-Scott parameters (dt, Du, Dv, F, k, tol, max_iter, warm_start). */
+double fo_adjoint_gray_scott_f64(int64_t N, const int32_t* row_ptr, const int32_t* col, const double* M,
+                                 const double* K, const fo_params* prm, const double* u0, const double* v0,
+                                 const double* target_u, const double* target_v, int64_t nsteps, int64_t ckpt,
+                                 double* grad_u0, double* grad_v0, double* grad_params);
+
 /* Extruded smooth normals (shaders/FEM/smooth_normals.glsl:30-57): for each
  * triangle, cross(b' - a', c' - a') of its corners moved along `normals` by
  * min(1, extrusion * max(0, value)), added to its three vertices (in triangle

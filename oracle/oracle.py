@@ -90,6 +90,8 @@ def lib():
             f = getattr(L, f"fo_instability_{s}")
             f.restype = C.c_int
             f.argtypes = [i64, p, p]
+        L.fo_adjoint_gray_scott_f64.restype = C.c_double
+        L.fo_adjoint_gray_scott_f64.argtypes = [i64, p, p, p, p, C.POINTER(Params), p, p, p, p, i64, i64, p, p, p]
         L.fo_smooth_normals_f32.restype = None
         L.fo_smooth_normals_f32.argtypes = [i64, i64, p, p, p, p, C.c_float, p]
         L.fo_ply_clip.restype = i64
@@ -260,6 +262,20 @@ class System:
             self.N, _ptr(self.row_ptr), _ptr(self.col), _ptr(_c(val, self.dtype)), _ptr(b), _ptr(x),
             float(tol), int(max_iter), 1 if x0 is None else 0, int(nthreads), C.byref(rr))
         return x, int(it), rr.value
+
+    def adjoint_gray_scott(self, params: Params, u0, v0, target_u, target_v, nsteps, ckpt):
+        """FP64 adjoint of the mass-weighted Gray-Scott loss -> (J, dJ/du0, dJ/dv0, [dF, dk, dDu, dDv])."""
+        u0 = _c(u0, np.float64)
+        v0 = _c(v0, np.float64)
+        tu = None if target_u is None else _c(target_u, np.float64)
+        tv = None if target_v is None else _c(target_v, np.float64)
+        gu = np.zeros(self.N)
+        gv = np.zeros(self.N)
+        gp = np.zeros(4)
+        J = lib().fo_adjoint_gray_scott_f64(self.N, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.M), _ptr(self.K),
+                                            C.byref(params), _ptr(u0), _ptr(v0), _ptr(tu), _ptr(tv), int(nsteps),
+                                            int(ckpt), _ptr(gu), _ptr(gv), _ptr(gp))
+        return J, gu, gv, gp
 
     def adjoint_advdiff(self, params: Params, D, u0, target, nsteps, ckpt):
         """FP64 adjoint of the explicit advection-diffusion step -> (J, dJ/du0, dJ/dD)."""

@@ -337,3 +337,39 @@ def test_golden_known_counts():
     assert ico["num_boundary"] == 0
     tube = gold["meshes"]["tube"]
     assert tube["num_boundary"] == 192
+
+
+def test_gray_scott_adjoint_matches_finite_differences(oracle_mod):
+    """FP64 adjoint of the mass-weighted Gray-Scott loss vs central differences,
+    for the initial fields and for F, k, Du, Dv."""
+    xyz, tri = mg.jittered_grid(9, seed=3)
+    S = oracle_mod.System(xyz, tri, bc=oracle_mod.NEUMANN)
+    rng = np.random.default_rng(2)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=1, side=0.3)
+    u0, v0 = S.gather(u0), S.gather(v0)
+    tu, tv = rng.uniform(size=S.N), rng.uniform(size=S.N)
+    base = dict(Du=2e-3, Dv=1e-3, F=0.04, k=0.06, reaction_mode=1, tol=1e-15)
+    nsteps, ck = 6, 4
+
+    def run(u, v, **over):
+        kw = dict(base)
+        kw.update(over)
+        p = oracle_mod.params(oracle_mod.REACTION_DIFFUSION, 0.5, **kw)
+        return S.adjoint_gray_scott(p, u, v, tu, tv, nsteps, ck)
+
+    J, gu, gv, gp = run(u0, v0)
+    eps = 1e-6
+    for _ in range(3):
+        du, dv = rng.normal(size=S.N), rng.normal(size=S.N)
+        fd = (run(u0 + eps * du, v0 + eps * dv)[0] - run(u0 - eps * du, v0 - eps * dv)[0]) / (2 * eps)
+        pred = gu @ du + gv @ dv
+        assert abs(fd - pred) <= 1e-6 * abs(pred)
+    for j, name in enumerate(("F", "k", "Du", "Dv")):
+        h = 1e-5 * base[name]
+        fd = (run(u0, v0, **{name: base[name] + h})[0] - run(u0, v0, **{name: base[name] - h})[0]) / (2 * h)
+        assert abs(fd - gp[j]) <= 1e-5 * abs(gp[j]), name
+    # a dropped target drops its term
+    p = oracle_mod.params(oracle_mod.REACTION_DIFFUSION, 0.5, **base)
+    J_u_only = S.adjoint_gray_scott(p, u0, v0, tu, None, nsteps, ck)[0]
+    J_v_only = S.adjoint_gray_scott(p, u0, v0, None, tv, nsteps, ck)[0]
+    assert abs(J_u_only + J_v_only - J) <= 1e-12 * J
