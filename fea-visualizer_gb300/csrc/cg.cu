@@ -531,8 +531,12 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                 bs[NF - 1].add(-((R)P.F + (R)P.k) * v);
             }
             if constexpr (EQ == EQ_GIVEN) {  // adjoint values may be large: only non-finite stops
-                bs[0].add(a.rhs[row]);
-                if (!isfinite(xr.v[0])) flags |= FEA_STATUS_NONFINITE;
+                const FV<R, NF> g = a.rhs[row];
+#pragma unroll
+                for (int f = 0; f < NF; f++) {
+                    bs[f].add(g.v[f]);
+                    if (!isfinite(xr.v[f])) flags |= FEA_STATUS_NONFINITE;
+                }
             } else if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_NEWMARK_INIT) {
                 flags |= check_value(a.u[row]) | check_value(a.v[row]);
             } else if constexpr (EQ == EQ_WAVE_NEWMARK) {
@@ -718,7 +722,10 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK || EQ == EQ_NEWMARK_INIT) {
             flags |= check_value(a.u[i]) | check_value(a.v[i]);
         } else if constexpr (EQ == EQ_GIVEN) {
-            if (!isfinite(a.x[i].v[0])) flags |= FEA_STATUS_NONFINITE;
+            const FV<R, NF> x = a.x[i];
+#pragma unroll
+            for (int f = 0; f < NF; f++)
+                if (!isfinite(x.v[f])) flags |= FEA_STATUS_NONFINITE;
         } else {
             const FV<R, NF> x = a.x[i];
 #pragma unroll
@@ -906,6 +913,7 @@ void dispatch_kind(StepGraph* G, const StepArgs<R, NF>& a, int kind, int wch, Lo
         switch (kind) {
         case EQ_GS_REF: dispatch_variant<R, 2, EQ_GS_REF>(G, a, wch, lf, st); break;
         case EQ_GS_CONSISTENT: dispatch_variant<R, 2, EQ_GS_CONSISTENT>(G, a, wch, lf, st); break;
+        case EQ_GIVEN: dispatch_variant<R, 2, EQ_GIVEN>(G, a, wch, lf, st); break;
         default: throw Error{FEA_ERR_UNSUPPORTED};
         }
     }

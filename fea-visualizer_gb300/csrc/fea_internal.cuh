@@ -151,7 +151,7 @@ struct StepArgs {
     R* a;                   // acceleration (Newmark)
     R* ut;                  // Newmark predictors
     R* vt;
-    const R* rhs;           // EQ_GIVEN: right-hand side [N]
+    const FV<R, NF>* rhs;   // EQ_GIVEN: right-hand side [N]
     // tile-ELL copy of A (the CG kernels' layout when ell.ok)
     const FV<R, NF>* As;
     const uint16_t* lcol;
@@ -242,6 +242,18 @@ void smooth_normals(const float* xyz, const uint32_t* tri, int64_t T, int64_t V,
 void ply_clip(const float* xyz, const uint32_t* tri, int64_t T, const float* nrm, const float* val, float e,
               float threshold, int mesh_type, float* pos, float* pval, uint8_t* used, int32_t* otri,
               cudaStream_t st);
+
+// Gray-Scott (mass-weighted reaction) adjoint: lam = M (x - t) for the fields
+// whose use flag is set, *J = 1/2 (x - t).lam; and one reverse step from
+// mu = A^-1 lam (x0/x1: the step's input and output), accumulating
+// g[4] += (dJ/dF, dJ/dk, dJ/dDu, dJ/dDv) of the step.
+template <typename R>
+void adjoint_gs_loss(const Pattern& P, const R* M, const FV<R, 2>* x, const FV<R, 2>* t, int use_u, int use_v,
+                     FV<R, 2>* lam, double* part, int stride, unsigned int* ticket, double* J, cudaStream_t st);
+template <typename R>
+void adjoint_gs_step(const Pattern& P, const R* M, const R* K, const FV<R, 2>* mu, const FV<R, 2>* x0,
+                     const FV<R, 2>* x1, double dt, double F, double k, FV<R, 2>* lam, double* part, int stride,
+                     unsigned int* ticket, double* g, cudaStream_t st);
 
 // Solver-order view of a handle's assembled mesh: what the batched solver
 // copies out of a single-mesh handle built for each of its instances.

@@ -727,16 +727,16 @@ void ensure_operator(fea_solver* s, int kind) {
 // `ckpt` steps.
 
 // One solve A mu = lam with the graph g (built on first use).
-template <typename R>
-void run_given(fea_solver* s, StepGraph& g, const StepArgs<R, 1>& a) {
+template <typename R, int NF>
+void run_given(fea_solver* s, StepGraph& g, const StepArgs<R, NF>& a) {
     long long ctl[2] = {1, 0};  // steps_left, steps_done
     FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, ctl, sizeof(ctl), cudaMemcpyHostToDevice, s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
     if (s->stream_mode) {
-        run_steps_stream<R, 1>(a, EQ_GIVEN, s->lanes, s->d_flags, s->stream);
+        run_steps_stream<R, NF>(a, EQ_GIVEN, s->lanes, s->d_flags, s->stream);
         return;
     }
-    if (!g.exec) build_step_graph<R, 1>(g, a, EQ_GIVEN, s->lanes, s->d_flags);
+    if (!g.exec) build_step_graph<R, NF>(g, a, EQ_GIVEN, s->lanes, s->d_flags);
     FEA_CUDA_TRY(cudaGraphLaunch(g.exec, s->stream));
 }
 
@@ -776,7 +776,7 @@ double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int6
         FEA_CUDA_TRY(cudaMemsetAsync(mu, 0, sizeof(R) * (size_t)pad_tiles(N), st));
         StepArgs<R, 1> a = make_args<R, 1>(s, false);
         a.x = (FV<R, 1>*)mu;
-        a.rhs = lam_f;
+        a.rhs = (const FV<R, 1>*)lam_f;
         StepGraph g;
         const double dt = time_step(s->prm), c = s->prm.advdiff_c, sign = s->prm.advection_sign;
         try {
@@ -788,7 +788,7 @@ double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int6
                     FEA_CUDA_TRY(cudaMemcpyAsync(seg + (n - n0 + 1) * N, u, rb, d2d, st));
                 }
                 for (int64_t n = n1 - 1; n >= n0; n--) {
-                    run_given<R>(s, g, a);  // mu = A^-1 lam, warm-started from the previous mu
+                    run_given<R, 1>(s, g, a);  // mu = A^-1 lam, warm-started from the previous mu
                     adjoint_grad_D<R>(s->Kloc, s->tri, s->idx_c, s->T, c, mu, seg + (n - n0 + 1) * N, gD, st);
                     adjoint_lambda<R>(s->Pc, (const R*)s->Mc, (const R*)s->Advc, dt, sign, mu, lam_f, st);
                 }
@@ -806,6 +806,150 @@ double adjoint_core(fea_solver* s, const R* u0, const R* t, int64_t nsteps, int6
     FEA_CUDA_TRY(cudaMemcpyAsync(&h, J, sizeof(double), cudaMemcpyDeviceToHost, st));
     FEA_CUDA_TRY(cudaStreamSynchronize(st));
     return h;
+}
+
+// ---- adjoint of the mass-weighted Gray-Scott step (kernels in adjoint.cu) ---------
+// x0, t: solver-order (u, v) pairs; use_u / use_v select the loss terms.
+// Leaves lam = (dJ/du0, dJ/dv0) in solver order, adds (dJ/dF, dJ/dk, dJ/dDu,
+// dJ/dDv) into g[4] (device), and the handle's fields at the final state.
+template <typename R>
+double adjoint_gs_core(fea_solver* s, const FV<R, 2>* x0, const FV<R, 2>* t, int use_u, int use_v, int64_t nsteps,
+                       int64_t ckpt, bool grads, FV<R, 2>* lam, double* g) {
+    if (step_kind(s->prm) != EQ_GS_CONSISTENT) {
+        set_error("the Gray-Scott adjoint needs equation FEA_REACTION_DIFFUSION with reaction_mode 1");
+        throw Error{FEA_ERR_STATE};
+    }
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N;
+    const size_t xb = sizeof(FV<R, 2>) * (size_t)N;
+    const auto d2d = cudaMemcpyDeviceToDevice;
+    ckpt = std::min(ckpt, nsteps);
+    const int64_t nck = ceil_div(nsteps, ckpt);
+    ensure_layout<R>(s, true);  // the forward steps update the operator to the current parameters
+    DeviceArena tmp;
+    FV<R, 2>* ck = tmp.alloc<FV<R, 2>>(nck * N);
+    FV<R, 2>* seg = tmp.alloc<FV<R, 2>>((ckpt + 1) * N);
+    FV<R, 2>* mu = tmp.alloc<FV<R, 2>>(pad_tiles(N));  // x of the solves: whole tiles
+    FV<R, 2>* xN = tmp.alloc<FV<R, 2>>(N);
+    double* J = tmp.alloc<double>(1);
+    FV<R, 2>* x = (FV<R, 2>*)s->F.uv;
+    FEA_CUDA_TRY(cudaMemcpyAsync(x, x0, xb, d2d, st));
+    for (int64_t sg = 0; sg < nck; sg++) {  // forward sweep, a checkpoint per segment
+        FEA_CUDA_TRY(cudaMemcpyAsync(ck + sg * N, x, xb, d2d, st));
+        advance<R>(s, std::min(ckpt, nsteps - sg * ckpt));
+    }
+    FEA_CUDA_TRY(cudaMemcpyAsync(xN, x, xb, d2d, st));
+    adjoint_gs_loss<R>(s->Pc, (const R*)s->Mc, x, t, use_u, use_v, lam, s->d_part, max_grid_blocks(),
+                       s->d_tickets + 5, J, st);
+    if (grads) {
+        FEA_CUDA_TRY(cudaMemsetAsync(mu, 0, sizeof(FV<R, 2>) * (size_t)pad_tiles(N), st));
+        StepArgs<R, 2> a = make_args<R, 2>(s, false);
+        a.x = mu;
+        a.rhs = lam;
+        StepGraph gr;
+        const fea_params& p = s->prm;
+        const double dt = p.rd_time_step, F = p.rd_feed_rate, kr = p.rd_kill_rate;
+        try {
+            for (int64_t sg = nck - 1; sg >= 0; sg--) {
+                const int64_t n0 = sg * ckpt, n1 = std::min(n0 + ckpt, nsteps);
+                FEA_CUDA_TRY(cudaMemcpyAsync(x, ck + sg * N, xb, d2d, st));
+                FEA_CUDA_TRY(cudaMemcpyAsync(seg, x, xb, d2d, st));
+                for (int64_t n = n0; n < n1; n++) {  // x^{n0+1} .. x^{n1}
+                    advance<R>(s, 1);
+                    FEA_CUDA_TRY(cudaMemcpyAsync(seg + (n - n0 + 1) * N, x, xb, d2d, st));
+                }
+                for (int64_t n = n1 - 1; n >= n0; n--) {
+                    run_given<R, 2>(s, gr, a);  // mu = A^-1 lam (both fields), warm-started
+                    adjoint_gs_step<R>(s->Pc, (const R*)s->Mc, (const R*)s->Kc, mu, seg + (n - n0) * N,
+                                       seg + (n - n0 + 1) * N, dt, F, kr, lam, s->d_part, max_grid_blocks(),
+                                       s->d_tickets + 6, g, st);
+                }
+            }
+        } catch (...) {
+            cudaStreamSynchronize(st);
+            gr.destroy();
+            throw;
+        }
+        FEA_CUDA_TRY(cudaStreamSynchronize(st));
+        gr.destroy();
+    }
+    FEA_CUDA_TRY(cudaMemcpyAsync(x, xN, xb, d2d, st));
+    double h = 0;
+    FEA_CUDA_TRY(cudaMemcpyAsync(&h, J, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    return h;
+}
+
+// Node-indexed float arrays (NULL targets drop their loss terms).
+template <typename R>
+void adjoint_gs_host(fea_solver* s, const float* u0, const float* v0, const float* tu, const float* tv,
+                     int64_t nsteps, int64_t ckpt, double* loss, float* gu, float* gv, double* gparams) {
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N, V = s->V;
+    DeviceArena tmp;
+    FV<R, 2>* x0 = tmp.alloc<FV<R, 2>>(N);
+    FV<R, 2>* t = tmp.alloc<FV<R, 2>>(N);
+    FV<R, 2>* lam = tmp.alloc<FV<R, 2>>(N);
+    double* g = tmp.alloc<double>(4);
+    FEA_CUDA_TRY(cudaMemsetAsync(t, 0, sizeof(FV<R, 2>) * (size_t)N, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(g, 0, 4 * sizeof(double), st));
+    const std::pair<const float*, std::pair<R*, int>> ins[4] = {
+        {u0, {(R*)x0, 0}}, {v0, {(R*)x0, 1}}, {tu, {(R*)t, 0}}, {tv, {(R*)t, 1}}};
+    for (const auto& in : ins) {
+        if (!in.first) continue;
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->d_nodes, in.first, sizeof(float) * V, cudaMemcpyHostToDevice, st));
+        k_gather_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(s->d_nodes, s->idx_c, V, in.second.first, 2,
+                                                              in.second.second);
+        FEA_CHECK_LAUNCH();
+    }
+    const bool grads = gu || gv || gparams;
+    const double J = adjoint_gs_core<R>(s, x0, t, tu != nullptr, tv != nullptr, nsteps, ckpt, grads, lam, g);
+    if (loss) *loss = J;
+    float* outs[2] = {gu, gv};
+    for (int f = 0; f < 2; f++) {
+        if (!outs[f]) continue;
+        k_scatter_nodes<R><<<launch_grid(V), kBlock, 0, st>>>((const R*)lam, s->idx_c, V, s->d_nodes, 2, f);
+        FEA_CHECK_LAUNCH();
+        FEA_CUDA_TRY(cudaMemcpyAsync(outs[f], s->d_nodes, sizeof(float) * V, cudaMemcpyDeviceToHost, st));
+        FEA_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    if (gparams) FEA_CUDA_TRY(cudaMemcpyAsync(gparams, g, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// Unknown-indexed device arrays in the handle's precision.
+template <typename R>
+void adjoint_gs_device(fea_solver* s, const void* u0, const void* v0, const void* tu, const void* tv,
+                       int64_t nsteps, int64_t ckpt, double* loss, void* gu, void* gv, double* gparams) {
+    cudaStream_t st = s->stream;
+    const int64_t N = s->N;
+    DeviceArena tmp;
+    FV<R, 2>* x0 = tmp.alloc<FV<R, 2>>(N);
+    FV<R, 2>* t = tmp.alloc<FV<R, 2>>(N);
+    FV<R, 2>* lam = tmp.alloc<FV<R, 2>>(N);
+    double* g = tmp.alloc<double>(4);
+    FEA_CUDA_TRY(cudaMemsetAsync(t, 0, sizeof(FV<R, 2>) * (size_t)N, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(g, 0, 4 * sizeof(double), st));
+    const std::pair<const void*, std::pair<R*, int>> ins[4] = {
+        {u0, {(R*)x0, 0}}, {v0, {(R*)x0, 1}}, {tu, {(R*)t, 0}}, {tv, {(R*)t, 1}}};
+    if (N > 0)
+        for (const auto& in : ins) {
+            if (!in.first) continue;
+            k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)in.first, s->pos, N, in.second.first, 2,
+                                                                   in.second.second);
+            FEA_CHECK_LAUNCH();
+        }
+    const bool grads = gu || gv || gparams;
+    const double J = adjoint_gs_core<R>(s, x0, t, tu != nullptr, tv != nullptr, nsteps, ckpt, grads, lam, g);
+    if (loss) *loss = J;
+    void* outs[2] = {gu, gv};
+    for (int f = 0; f < 2; f++)
+        if (outs[f] && N > 0) {
+            k_copy_from_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)lam, s->pos, N, (R*)outs[f], 2, f);
+            FEA_CHECK_LAUNCH();
+        }
+    if (gparams) FEA_CUDA_TRY(cudaMemcpyAsync(gparams, g, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FEA_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
 // Node-indexed float inputs and outputs (the host entry point).
@@ -1357,6 +1501,38 @@ int fea_export_ply(fea_solver* s, const char* path, const float* normals, float 
     PlyGeometry g;
     ply_geometry(s, normals, vertex_extrusion, threshold, mesh_type, g);
     write_ply(path, g, color_coeffs ? color_coeffs : gray);
+    API_END
+}
+
+int fea_adjoint_gray_scott(fea_solver* s, const float* u0, const float* v0, const float* target_u,
+                           const float* target_v, int64_t nsteps, int64_t checkpoint_every, double* loss,
+                           float* grad_u0, float* grad_v0, double* grad_params) {
+    API_BEGIN
+    check_handle(s);
+    if (!u0 || !v0 || nsteps < 1 || checkpoint_every < 1)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "adjoint needs u0, v0, nsteps >= 1 and checkpoint_every >= 1");
+    if (s->precision == FEA_FP64)
+        adjoint_gs_host<double>(s, u0, v0, target_u, target_v, nsteps, checkpoint_every, loss, grad_u0, grad_v0,
+                                grad_params);
+    else
+        adjoint_gs_host<float>(s, u0, v0, target_u, target_v, nsteps, checkpoint_every, loss, grad_u0, grad_v0,
+                               grad_params);
+    API_END
+}
+
+int fea_adjoint_gray_scott_device(fea_solver* s, const void* u0, const void* v0, const void* target_u,
+                                  const void* target_v, int64_t nsteps, int64_t checkpoint_every, double* loss,
+                                  void* grad_u0, void* grad_v0, double* grad_params) {
+    API_BEGIN
+    check_handle(s);
+    if (!u0 || !v0 || nsteps < 1 || checkpoint_every < 1)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "adjoint needs u0, v0, nsteps >= 1 and checkpoint_every >= 1");
+    if (s->precision == FEA_FP64)
+        adjoint_gs_device<double>(s, u0, v0, target_u, target_v, nsteps, checkpoint_every, loss, grad_u0, grad_v0,
+                                  grad_params);
+    else
+        adjoint_gs_device<float>(s, u0, v0, target_u, target_v, nsteps, checkpoint_every, loss, grad_u0, grad_v0,
+                                 grad_params);
     API_END
 }
 

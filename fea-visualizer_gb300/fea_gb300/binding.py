@@ -109,6 +109,8 @@ SIGNATURES = {
     "fea_adjoint_advdiff": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
     "fea_adjoint_advdiff_device": [_P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P],
     "fea_set_element_diffusivity_device": [_P, _P],
+    "fea_adjoint_gray_scott": [_P, _P, _P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P, _P],
+    "fea_adjoint_gray_scott_device": [_P, _P, _P, _P, _P, _I64, _I64, C.POINTER(C.c_double), _P, _P, _P],
     "fea_smooth_normals": [_P, _P, C.c_float, _P],
     "fea_smooth_normals_device": [_P, _P, C.c_float, _P],
     "fea_export_ply": [_P, C.c_char_p, _P, C.c_float, C.c_float, C.c_int, _P],
@@ -317,6 +319,27 @@ class CUDASolver:
                                                 int(checkpoint_every), C.byref(J),
                                                 gu.data_ptr() if grads else None, gd.data_ptr() if grads else None))
         return J.value, gu, gd
+
+    def adjoint_gray_scott_device(self, u0, v0, target_u, target_v, nsteps, checkpoint_every, grads=True):
+        """Gray-Scott adjoint on CUDA tensors (unknown-indexed [N], handle precision; a None target drops
+        its loss term) -> (J, dJ/du0, dJ/dv0, numpy [dJ/dF, dJ/dk, dJ/dDu, dJ/dDv]); gradients None
+        without grads."""
+        import torch
+        dt = torch.float64 if self.precision == FP64 else torch.float32
+        u0 = u0.detach().to(dtype=dt).contiguous()
+        v0 = v0.detach().to(dtype=dt, device=u0.device).contiguous()
+        tu = None if target_u is None else target_u.detach().to(dtype=dt, device=u0.device).contiguous()
+        tv = None if target_v is None else target_v.detach().to(dtype=dt, device=u0.device).contiguous()
+        gu = torch.zeros_like(u0) if grads else None
+        gv = torch.zeros_like(u0) if grads else None
+        gp = np.zeros(4) if grads else None
+        J = C.c_double(0)
+        torch.cuda.synchronize(u0.device)
+        check(load().fea_adjoint_gray_scott_device(
+            self._h, u0.data_ptr(), v0.data_ptr(), None if tu is None else tu.data_ptr(),
+            None if tv is None else tv.data_ptr(), int(nsteps), int(checkpoint_every), C.byref(J),
+            gu.data_ptr() if grads else None, gv.data_ptr() if grads else None, _ptr(gp)))
+        return J.value, gu, gv, gp
 
     def set_element_diffusivity_device(self, D):
         """Per-element diffusivity from a CUDA tensor [T] (handle precision)."""

@@ -291,6 +291,27 @@ int fea_adjoint_advdiff(fea_solver* s, const float* u0, const float* target, int
  * per-element [T] dJ/dD, all in the handle's precision. */
 int fea_adjoint_advdiff_device(fea_solver* s, const void* u0, const void* target, int64_t nsteps,
                                int64_t checkpoint_every, double* loss, void* grad_u0, void* grad_D);
+/* ---- adjoint (mass-weighted Gray-Scott) ------------------------------------
+ * Model: nsteps Gray-Scott steps with reaction_mode 1 (A_f x_f' = M w_f(u, v),
+ * A_f = M/dt + D_f K; CPUSolver.cpp:127-145 with the mass-weighted reaction)
+ * from (u0, v0).  Loss J = 1/2 |u_N - target_u|_M^2 + 1/2 |v_N - target_v|_M^2
+ * (a NULL target drops its term).  Writes J, dJ/du0, dJ/dv0 and
+ * grad_params[4] = dJ/dF, dJ/dk, dJ/dDu, dJ/dDv from the hand-written
+ * adjoint: each reverse step solves with the forward operators (the paired
+ * SPD solve) and back-propagates through the reaction's Jacobian; forward
+ * states are recomputed from checkpoints.  Outputs may be NULL.  The handle's
+ * fields are left at the final state.  FEA_ERR_STATE for another equation or
+ * reaction mode.  No reference counterpart.  Host variant: node-indexed
+ * float[V] arrays (gradients 0 on Dirichlet points). */
+int fea_adjoint_gray_scott(fea_solver* s, const float* u0, const float* v0, const float* target_u,
+                           const float* target_v, int64_t nsteps, int64_t checkpoint_every, double* loss,
+                           float* grad_u0, float* grad_v0, double* grad_params);
+/* Device-resident variant: unknown-indexed [N] arrays in the handle's
+ * precision. */
+int fea_adjoint_gray_scott_device(fea_solver* s, const void* u0, const void* v0, const void* target_u,
+                                  const void* target_v, int64_t nsteps, int64_t checkpoint_every, double* loss,
+                                  void* grad_u0, void* grad_v0, double* grad_params);
+
 /* Per-element diffusivity D_e from device memory in the handle's precision
  * ([T]); like fea_set_element_fields without the float rounding for FP64
  * handles.  No reference counterpart. */

@@ -124,3 +124,79 @@ def test_adjoint_argument_errors(fea):
     assert ei.value.code == -6
     with pytest.raises(fea.FeaError):
         s.adjoint_advdiff(u, u, 0, 1)
+
+
+def _gs_problem(fea, oracle_mod, mesh, bc=1):
+    import torch
+    xyz, tri = mesh
+    kw = dict(rd_time_step=0.5, rd_Du=2e-3, rd_Dv=1e-3, rd_feed_rate=0.04, rd_kill_rate=0.06)
+    p = fea.default_params(equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-13, **kw)
+    s = fea.CUDASolver(xyz, tri, boundary_condition=bc, precision=fea.FP64, params=p)
+    S = oracle_mod.System(xyz, tri, bc=bc)
+    planar = np.ptp(xyz[:, 2]) == 0
+    u0, v0 = (mg.gray_scott_patches(xyz, seed=1, side=0.3) if planar else
+              mg.sphere_patches(xyz / np.linalg.norm(xyz, axis=1, keepdims=True), seed=1, n_patches=4, radius=0.4))
+    u0, v0 = S.gather(u0), S.gather(v0)
+    rng = np.random.default_rng(9)
+    tu, tv = rng.uniform(size=S.N), rng.uniform(size=S.N)
+    op = oracle_mod.params(oracle_mod.REACTION_DIFFUSION, f32(0.5), Du=f32(2e-3), Dv=f32(1e-3), F=f32(0.04),
+                           k=f32(0.06), reaction_mode=1, tol=1e-15)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    return s, S, op, p, (u0, v0, tu, tv), T
+
+
+@pytest.mark.parametrize("mesh,bc", [("grid", 1), ("grid", 0), ("ico", 1)])
+def test_gray_scott_adjoint_matches_oracle(fea, oracle_mod, mesh, bc):
+    m = mg.jittered_grid(17, seed=2) if mesh == "grid" else mg.icosphere(3)
+    s, S, op, p, (u0, v0, tu, tv), T = _gs_problem(fea, oracle_mod, m, bc)
+    J, gu, gv, gp = s.adjoint_gray_scott_device(T(u0), T(v0), T(tu), T(tv), 7, 3)
+    Jo, guo, gvo, gpo = S.adjoint_gray_scott(op, u0, v0, tu, tv, 7, 3)
+    assert abs(J - Jo) <= 1e-9 * abs(Jo)
+    assert rel_l2(gu.cpu().numpy(), guo) < 1e-8 and rel_l2(gv.cpu().numpy(), gvo) < 1e-8
+    np.testing.assert_allclose(gp, gpo, rtol=1e-8)
+    # a dropped target drops its term
+    Ju = s.adjoint_gray_scott_device(T(u0), T(v0), T(tu), None, 7, 3, grads=False)[0]
+    Jv = s.adjoint_gray_scott_device(T(u0), T(v0), None, T(tv), 7, 3, grads=False)[0]
+    assert abs(Ju + Jv - J) <= 1e-11 * abs(J)
+
+
+def test_gray_scott_adjoint_finite_differences(fea, oracle_mod):
+    """Initial fields and (F, k, Du, Dv): central differences of the GPU forward."""
+    s, S, op, p, (u0, v0, tu, tv), T = _gs_problem(fea, oracle_mod, mg.jittered_grid(21, seed=4))
+    nsteps, ck = 10, 4
+    J, gu, gv, gp = s.adjoint_gray_scott_device(T(u0), T(v0), T(tu), T(tv), nsteps, ck)
+    gu, gv = gu.cpu().numpy(), gv.cpu().numpy()
+
+    def loss(u, v):
+        return s.adjoint_gray_scott_device(T(u), T(v), T(tu), T(tv), nsteps, ck, grads=False)[0]
+
+    rng = np.random.default_rng(3)
+    eps = 1e-4
+    for _ in range(6):
+        du, dv = rng.normal(size=S.N), rng.normal(size=S.N)
+        fd = (loss(u0 + eps * du, v0 + eps * dv) - loss(u0 - eps * du, v0 - eps * dv)) / (2 * eps)
+        pred = gu @ du + gv @ dv
+        assert abs(fd - pred) <= 1e-4 * abs(pred)
+    for j, name in enumerate(("rd_feed_rate", "rd_kill_rate", "rd_Du", "rd_Dv")):
+        base = getattr(p, name)
+        lo, hi = f32(base * (1 - 1e-3)), f32(base * (1 + 1e-3))  # the ABI holds float parameters
+        setattr(p, name, hi)
+        s.set_params(p)
+        j_hi = loss(u0, v0)
+        setattr(p, name, lo)
+        s.set_params(p)
+        j_lo = loss(u0, v0)
+        setattr(p, name, base)
+        s.set_params(p)
+        fd = (j_hi - j_lo) / (hi - lo)
+        assert abs(fd - gp[j]) <= 1e-4 * abs(gp[j]), (name, fd, gp[j])
+
+
+def test_gray_scott_adjoint_state_check(fea):
+    xyz, tri = mg.icosphere(2)
+    s = fea.CUDASolver(xyz, tri, boundary_condition=1,
+                       params=fea.default_params(equation=fea.REACTION_DIFFUSION, reaction_mode=0))
+    u = np.ones(len(xyz), np.float32)
+    with pytest.raises(fea.FeaError) as ei:
+        s.adjoint_advdiff(u, u, 2, 1)
+    assert ei.value.code == -6
