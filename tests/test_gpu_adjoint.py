@@ -200,3 +200,20 @@ def test_gray_scott_adjoint_state_check(fea):
     with pytest.raises(fea.FeaError) as ei:
         s.adjoint_advdiff(u, u, 2, 1)
     assert ei.value.code == -6
+
+
+def test_gray_scott_autograd_bridge(fea, oracle_mod):
+    import torch
+    from fea_gb300.autograd import gray_scott_loss
+    s, S, op, p, (u0, v0, tu, tv), T = _gs_problem(fea, oracle_mod, mg.jittered_grid(17, seed=2))
+    u = T(u0).requires_grad_()
+    v = T(v0).requires_grad_()
+    theta = torch.tensor([p.rd_feed_rate, p.rd_kill_rate, p.rd_Du, p.rd_Dv], dtype=torch.float64,
+                         requires_grad=True)
+    J = gray_scott_loss(s, u, v, theta, T(tu), T(tv), 5, 2)
+    J.backward()
+    Jd, gu, gv, gp = s.adjoint_gray_scott_device(T(u0), T(v0), T(tu), T(tv), 5, 2)
+    assert abs(J.item() - Jd) <= 1e-12 * abs(Jd)
+    torch.testing.assert_close(u.grad, gu, rtol=1e-12, atol=0)
+    torch.testing.assert_close(v.grad, gv, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(theta.grad.numpy(), gp, rtol=1e-12)
