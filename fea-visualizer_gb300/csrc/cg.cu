@@ -249,8 +249,8 @@ struct StageLayout {
         L = al(A + fv * (size_t)emax);
         V = al(L + 2 * (size_t)emax);
         U = al(V + 6 * fv * (size_t)kTileRows);
-        bar = al(U + fv * (size_t)(kTileRows + hmax));  // full barrier (copies landed), then empty (warps done)
-        bytes = al(bar + 16);
+        bar = al(U + fv * (size_t)(kTileRows + hmax));
+        bytes = al(bar + 8);
     }
 };
 
@@ -308,8 +308,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int64_t ntiles = ceil_div(a.N, kTileRows), G = gridDim.x, t0 = blockIdx.x;
     auto stage = [&](int b) { return dyn_smem + (size_t)b * L.bytes; };
-    auto full_of = [&](int b) { return reinterpret_cast<uint64_t*>(stage(b) + L.bar); };
-    auto empty_of = [&](int b) { return reinterpret_cast<uint64_t*>(stage(b) + L.bar + 8); };
+    auto bar_of = [&](int b) { return reinterpret_cast<uint64_t*>(stage(b) + L.bar); };
     auto ut_of = [&](int b) { return reinterpret_cast<FV<R, NF>*>(stage(b) + L.U); };
     // halo column of slot j of tile `tile` (-1: none) and the tile's halo count
     auto halo_ref = [&](int64_t tile, int32_t& col, int32_t& cnt) {
@@ -333,8 +332,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     };
     if (t == 0) {
         for (int b = 0; b < NS; b++) {
-            mbar_init(full_of(b), 1);
-            mbar_init(empty_of(b), kBlock / 32);  // one arrival per warp
+            mbar_init(bar_of(b), 1);
             armed[b] = 0;
         }
         mbar_fence_init();
@@ -354,9 +352,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     slice_ref(t0, sb, sw);
     __syncthreads();
     Acc<R> dots[3 * NF];
-    uint32_t fph[NS], eph[NS];  // phases of the full and empty barriers
+    uint32_t phase[NS];
 #pragma unroll
-    for (int b = 0; b < NS; b++) fph[b] = eph[b] = 0u;
+    for (int b = 0; b < NS; b++) phase[b] = 0u;
     bool ok = true;
     int b = 0;
     for (int64_t tile = t0; tile < ntiles; tile += G) {
@@ -375,14 +373,19 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         int32_t hcol2, hcnt2, sb2, sw2;
         halo_ref(tile + 2 * G, hcol2, hcnt2);
         slice_ref(tile + G, sb2, sw2);
-        const bool got = mbar_wait(full_of(b), fph[b]);
-        fph[b] ^= 1u;
+        const bool got = mbar_wait(bar_of(b), phase[b]);
+        phase[b] ^= 1u;
+        if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+        }
+        if (t == 0) armed[b] = 0;
         const FV<R, NF>* V = reinterpret_cast<const FV<R, NF>*>(stage(b) + L.V);
         const int64_t row = tile * kTileRows + t;
         FV<R, NF> un;
 #pragma unroll
         for (int f = 0; f < NF; f++) un.v[f] = 0;
-        if (got && row < a.N) {
+        if (row < a.N) {
             const FV<R, NF> ro = V[kVr * kTileRows + t], wo = V[kVw * kTileRows + t], d = V[kVd * kTileRows + t];
             FV<R, NF> so = wo;
             if (c.need_old) so = V[kVs * kTileRows + t];
@@ -405,13 +408,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             v.s1[row] = sn;
         }
         ut[t] = un;
-        // one block barrier per tile: the staged operand is complete, and
-        // every thread's copy wait succeeded
-        if (!__syncthreads_and(got)) {
-            ok = false;
-            break;
-        }
-        if (t == 0) armed[b] = 0;
+        __syncthreads();
         const FV<R, NF>* As = reinterpret_cast<const FV<R, NF>*>(stage(b) + L.A) + sb + lane;
         const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage(b) + L.L) + sb + lane;
         FV<R, NF> wn;
@@ -429,8 +426,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
 #pragma unroll
             for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
         }
-        // the next tile's halo into its stage: that stage's last tile finished
-        // in every warp before this tile's barrier
+        // the next tile's halo into its stage (free since that stage's last tile)
         if (hcol >= 0) {
             FV<R, NF> sn, rn, u2;
             cg_advance(c, hr, hw, hs, hd, sn, rn, u2);
@@ -441,16 +437,11 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             for (int32_t h = kBlock + t; h < hcnt; h += kBlock)
                 ut_of(bn)[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0 + h]);
         }
-        // this warp is done with stage b; thread 0 re-arms it once every warp is
-        __syncwarp();
-        if (lane == 0) mbar_arrive(empty_of(b));
+        __syncthreads();  // this stage is free again
         if (t == 0 && tile + NS * G < ntiles) {
-            if (mbar_wait(empty_of(b), eph[b])) {
-                stage_tile(stage(b), L, a, v, tile + NS * G);
-                armed[b] = 1;
-            }  // else: the stage's next wait runs out and the block leaves
+            stage_tile(stage(b), L, a, v, tile + NS * G);
+            armed[b] = 1;
         }
-        if (t == 0) eph[b] ^= 1u;  // every use of the stage completes one empty phase
         hcol = hcol2;
         hcnt = hcnt2;
         sb = sb2;
@@ -461,10 +452,10 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         if (t == 0) {
             atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
             for (int q = 0; q < NS; q++)  // copies still in flight land before the block exits
-                if (armed[q]) mbar_wait(full_of(q), fph[q] ^ (q == b ? 1u : 0u));
+                if (armed[q]) mbar_wait(bar_of(q), phase[q]);
         }
+        __syncthreads();
     }
-    __syncthreads();
     double blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
