@@ -4,7 +4,7 @@
 
 One step = the reference's Gray-Scott advance_time (CPUSolver.cpp:127-145):
 mass-weighted reaction right-hand side for u and v, then the two SPD solves
-(M/dt + D K) x = b with Jacobi-PCG, FP32 fields and FP64-accurate reductions.
+(M/dt + D K) x = b with Jacobi-PCG, FP32 fields and float-float reductions.
 Workload (synthetic, seeded): Du 2e-5, Dv 1e-5, F 0.037, k 0.06, dt 1, Neumann,
 u = 1, v = 0 with 20 squares of side 0.05 at u = 0.5, v = 0.25, plus U(-0.01,
 0.01) noise.  Timed steps continue from the warm-up state.
@@ -48,7 +48,7 @@ def workload():
 def config(V, T, nnz, extra=None):
     c = {"workload": f"gray-scott {GRID_N}x{GRID_N} jittered grid", "vertices": V, "triangles": T,
          "nnz": nnz, "reaction": "mass-weighted (consistent)", "bc": "neumann", "dt": 1.0, "Du": 2e-5,
-         "Dv": 1e-5, "F": 0.037, "k": 0.06, "cg": f"jacobi-pcg, |r| < {CG_TOL:g} |b|, warm start, FP64-accurate dots",
+         "Dv": 1e-5, "F": 0.037, "k": 0.06, "cg": f"jacobi-pcg, |r| < {CG_TOL:g} |b|, warm start, float-float dots and scalars",
          "l2": "flushed before every timed step (256 MiB write)"}
     if extra:
         c.update(extra)

@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_loss(int64_t N, const int32_t* _
                                                      const int32_t* __restrict__ col, const R* __restrict__ M,
                                                      const R* __restrict__ u, const R* __restrict__ t, R* lam,
                                                      double* part, int stride, unsigned int* ticket, double* J) {
-    __shared__ double red[32];
+    __shared__ typename Acc<R>::Packed red[32];
     Acc<R> acc[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         Acc<R> s;
@@ -29,13 +29,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_loss(int64_t N, const int32_t* _
             const int32_t c = col[e];
             s.add_prod(M[e], u[c] - t[c]);
         }
-        const R l = (R)s.value();
+        const R l = s.rounded();
         lam[i] = l;
         acc[0].add_prod(u[i] - t[i], l);
     }
-    double blk[1], tot[1];
+    Acc<R> blk[1], tot[1];
     block_totals<1>(acc, red, blk);
-    if (last_block_commit<1>(blk, part, stride, ticket, red, tot) && threadIdx.x == 0) *J = 0.5 * tot[0];
+    if (grid_commit<1>(blk, part, stride, ticket, red, tot) && threadIdx.x == 0) *J = 0.5 * tot[0].value();
 }
 
 // lam_i = (sum_e M_e mu_c) / dt + s sum_e Adv_{c,i} mu_c over row i's entries
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kBlock) k_gs_adj_loss(int64_t N, const int32_t
                                                         const FV<R, 2>* __restrict__ tg, int use_u, int use_v,
                                                         FV<R, 2>* lam, double* part, int stride,
                                                         unsigned int* ticket, double* J) {
-    __shared__ double red[32];
+    __shared__ typename Acc<R>::Packed red[32];
     Acc<R> acc[1];
     const int use[2] = {use_u, use_v};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
@@ -110,14 +110,14 @@ __global__ void __launch_bounds__(kBlock) k_gs_adj_loss(int64_t N, const int32_t
         FV<R, 2> l;
 #pragma unroll
         for (int f = 0; f < 2; f++) {
-            l.v[f] = use[f] ? (R)s[f].value() : (R)0;
+            l.v[f] = use[f] ? s[f].rounded() : (R)0;
             if (use[f]) acc[0].add_prod(xi.v[f] - ti.v[f], l.v[f]);
         }
         lam[i] = l;
     }
-    double blk[1], tot[1];
+    Acc<R> blk[1], tot[1];
     block_totals<1>(acc, red, blk);
-    if (last_block_commit<1>(blk, part, stride, ticket, red, tot) && threadIdx.x == 0) *J = 0.5 * tot[0];
+    if (grid_commit<1>(blk, part, stride, ticket, red, tot) && threadIdx.x == 0) *J = 0.5 * tot[0].value();
 }
 
 template <typename R>

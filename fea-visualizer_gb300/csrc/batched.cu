@@ -4,8 +4,8 @@
 // one mesh with its own (F, k, Du, Dv, dt) and follows the Gray-Scott step of
 // CPUSolver.cpp:127-145 with the mass-weighted reaction, b = M (x/dt + f(x))
 // for x = (u, v), solved with the single-mesh solver's CG: the Jacobi-
-// preconditioned Chronopoulos-Gear iteration with FP64-accurate inner products
-// and one true-residual refinement pass per solve.
+// preconditioned Chronopoulos-Gear iteration with float-float inner products
+// and scalars, and one true-residual refinement pass per solve.
 //
 // Layout.  The instances' systems are stacked block-diagonally into one CSR
 // matrix, each in its own solver order (a single-mesh handle built per
@@ -43,6 +43,8 @@ struct BPrm {
 // CG and step state of one instance.
 struct BInst {
     double rz[2], rr[2], pq[2], thr[2], bb[2], alpha[2], beta[2];
+    float ffrz[2][2], ffalpha[2][2], ffthr[2][2];  // FP32: float-float copies
+    float falpha[2], fbeta[2];                       // FP32: rounded coefficients
     int active[2], fresh[2], iters[2];
     int iter;  // iterations of the current solve
     int max_iter;
@@ -108,29 +110,28 @@ struct BArgs {
 // partials in tile order and returns true in all its threads, with the totals
 // in out[] (valid in thread 0).  The instance's ticket is reset for the next
 // phase.
-template <int NV>
-__device__ bool inst_commit(const double (&blk)[NV], double* part, int tile, int t0, int nt, unsigned int* ticket,
-                            double* smem, double (&out)[NV]) {
+template <int NV, typename R>
+__device__ bool inst_commit(const Acc<R> (&blk)[NV], double* part, int tile, int t0, int nt, unsigned int* ticket,
+                            typename Acc<R>::Packed* smem, Acc<R> (&out)[NV]) {
+    using P = typename Acc<R>::Packed;
+    static_assert(sizeof(P) == sizeof(double), "partials use 8-byte slots");
+    P* pp = reinterpret_cast<P*>(part);
     __shared__ bool last;
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) part[(int64_t)tile * kNV + k] = blk[k];
+        for (int k = 0; k < NV; k++) pp[(int64_t)tile * kNV + k] = blk[k].pack();
         __threadfence();
         last = atomicAdd(ticket, 1u) == (unsigned int)(nt - 1);
     }
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    double y[NV];
+    Acc<R> y[NV];
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double acc = 0.0;
-        for (int t = t0 + threadIdx.x; t < t0 + nt; t += blockDim.x) acc += __ldcg(&part[(int64_t)t * kNV + k]);
-        y[k] = acc;
-    }
-    block_sum<NV>(y, smem);
-#pragma unroll
-    for (int k = 0; k < NV; k++) out[k] = y[k];
+    for (int k = 0; k < NV; k++)
+        for (int t = t0 + threadIdx.x; t < t0 + nt; t += blockDim.x)
+            y[k].merge(Acc<R>::unpack(__ldcg(&pp[(int64_t)t * kNV + k])));
+    block_totals<NV, R>(y, smem, out);
     if (threadIdx.x == 0) *ticket = 0u;
     return true;
 }
@@ -178,7 +179,7 @@ __device__ __forceinline__ int iter_of(const BArgs<R>& a) {
 // instances whose state entering the step is unstable are frozen.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) kb_rhs(BArgs<R> a) {
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     constexpr int RPW = 32 / kLanes;      // rows per warp pass
     constexpr int RPB = kBlock / kLanes;  // rows per block pass
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -223,9 +224,9 @@ __global__ void __launch_bounds__(kBlock) kb_rhs(BArgs<R> a) {
                 FV<R, 2> bv, rv, zv;
 #pragma unroll
                 for (int f = 0; f < 2; f++) {
-                    bv.v[f] = (R)bs[f].value();
+                    bv.v[f] = bs[f].rounded();
                     bs[f].sub(ax[f]);
-                    rv.v[f] = (R)bs[f].value();
+                    rv.v[f] = bs[f].rounded();
                     zv.v[f] = d.v[f] * rv.v[f];
                     dots[f].add_prod(bv.v[f], bv.v[f]);
                     dots[2 + f].add_prod(rv.v[f], rv.v[f]);
@@ -237,30 +238,18 @@ __global__ void __launch_bounds__(kBlock) kb_rhs(BArgs<R> a) {
             }
         }
         raise_inst(s, flags);
-        double blk[kNV], tot[kNV];
+        Acc<R> blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
             volatile BInst* vs = s;
             const int stop = (atomicOr(&s->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
             const double tol = a.ctl->tol;
-            const double tiny = sizeof(R) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
             vs->stop = stop;
             vs->iter = 0;
             int nact = 0;
 #pragma unroll
-            for (int f = 0; f < 2; f++) {
-                const double bb = tot[f], rr = tot[2 + f], rz = tot[4 + f];
-                const double thr = tol * tol * bb;
-                vs->bb[f] = bb;
-                vs->thr[f] = thr < tiny ? tiny : thr;
-                vs->rr[f] = rr;
-                vs->rz[f] = rz;
-                vs->iters[f] = 0;
-                vs->fresh[f] = 1;
-                vs->active[f] = (!stop && bb > 0.0 && rr >= vs->thr[f]) ? 1 : 0;
-                nact += vs->active[f];
-            }
+            for (int f = 0; f < 2; f++) nact += start_solve<R>(vs, f, stop, tol, tot[f], tot[2 + f], tot[4 + f]);
             if (nact) atomicAdd(&a.ctl->n_next, nact);
         }
     }
@@ -272,7 +261,7 @@ __global__ void __launch_bounds__(kBlock) kb_rhs(BArgs<R> a) {
 template <typename R, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a) {
     __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     const int wib = threadIdx.x >> 5;
     const int iter = iter_of(a);
     FV<R, 2>* w = a.wb[iter & 1];
@@ -283,7 +272,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a
         if (!c.any && !a.probe) continue;
         Acc<R> dot[2];
         init_rows<R, 2, WCH>(a.rp, a.col, a.A, a.z, w, (int64_t)tile * kTile + wib * 32, a.N, sm[wib], dot);
-        double blk[2], tot[2];
+        Acc<R> blk[2], tot[2];
         block_totals<2>(dot, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<2>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
@@ -306,7 +295,7 @@ template <typename R, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a) {
     __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
     __shared__ FV<R, 2> ut[kTile];
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     const int wib = threadIdx.x >> 5;
     const int iter = iter_of(a), par = iter & 1;
     CgVecs<R, 2> v;
@@ -329,7 +318,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a
         if (!c.any) continue;
         Acc<R> dots[kNV];  // gamma', delta', |r'|^2
         cgcg_tile<R, 2, WCH>(v, c, (int64_t)tile * kTile, a.N, sm[wib], ut, dots);
-        double blk[kNV], tot[kNV];
+        Acc<R> blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
@@ -353,7 +342,7 @@ template <typename R, int KPRE>
 __global__ void __launch_bounds__(kBlock) kb_init_ell(BArgs<R> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     const int iter = iter_of(a);
     FV<R, 2>* w = a.wb[iter & 1];
     const EllView<R, 2> e = bell_view(a);
@@ -367,7 +356,7 @@ __global__ void __launch_bounds__(kBlock) kb_init_ell(BArgs<R> a) {
         Acc<R> dot[2];
         init_tile_ell<R, 2, KPRE>(e, a.z, w, tile, ell_ref(e, tile, a.ntiles), a.N, ut + buf * stride, dot);
         buf ^= 1;
-        double blk[2], tot[2];
+        Acc<R> blk[2], tot[2];
         block_totals<2>(dot, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<2>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
@@ -389,7 +378,7 @@ template <typename R, int KPRE>
 __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     const int iter = iter_of(a), par = iter & 1;
     CgVecs<R, 2> v;
     v.rp = a.rp;
@@ -415,7 +404,7 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
         Acc<R> dots[kNV];
         cgcg_tile_ell<R, 2, KPRE>(v, e, c, tile, ell_ref(e, tile, a.ntiles), a.N, ut + buf * stride, dots);
         buf ^= 1;
-        double blk[kNV], tot[kNV];
+        Acc<R> blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
@@ -428,11 +417,11 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
 }
 
 // After the first solve loop: zero right-hand sides give x = 0, then one
-// FP64-accurate true-residual pass r = b - A x; fields still above their
+// float-float true-residual pass r = b - A x; fields still above their
 // threshold restart CG from there.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) kb_refine(BArgs<R> a) {
-    __shared__ double red[32 * kNV];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
     constexpr int RPW = 32 / kLanes;
     constexpr int RPB = kBlock / kLanes;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -481,7 +470,7 @@ __global__ void __launch_bounds__(kBlock) kb_refine(BArgs<R> a) {
                         Acc<R> t;
                         t.add(bv.v[f]);
                         t.sub(ax[f]);
-                        rv.v[f] = (R)t.value();
+                        rv.v[f] = t.rounded();
                         zv.v[f] = d.v[f] * rv.v[f];
                         dots[f].add_prod(rv.v[f], rv.v[f]);
                         dots[2 + f].add_prod(rv.v[f], zv.v[f]);
@@ -491,7 +480,7 @@ __global__ void __launch_bounds__(kBlock) kb_refine(BArgs<R> a) {
                 }
             }
         }
-        double blk[4], tot[4];
+        Acc<R> blk[4], tot[4];
         block_totals<4>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
         if (inst_commit<4>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
@@ -502,9 +491,10 @@ __global__ void __launch_bounds__(kBlock) kb_refine(BArgs<R> a) {
                 w->active[f] = 0;
                 w->fresh[f] = 1;
                 if (refine && !zero[f] && w->bb[f] > 0.0) {
-                    w->rr[f] = tot[f];
-                    if (tot[f] >= w->thr[f]) {
-                        w->rz[f] = tot[2 + f];
+                    const double rr = tot[f].value();
+                    w->rr[f] = rr;
+                    if (rr >= w->thr[f]) {
+                        set_gamma(w, f, tot[2 + f]);
                         w->active[f] = 1;
                         nact++;
                     }

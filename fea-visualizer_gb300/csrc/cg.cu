@@ -10,11 +10,13 @@
 // body is ONE kernel per CG iteration (the Chronopoulos-Gear form below): the
 // vector updates are fused into the SpMV, and a single grid-wide reduction
 // gives every scalar of the next iteration.
-// Inner products: FP32 products are accumulated exactly as float-float pairs
-// per thread and per warp, then in FP64 across warps and blocks (the GB300's
-// FP64 pipe is narrow, so FP64 arithmetic is kept off the per-element path).
-// The block partials are combined by the last block to finish, in a fixed
-// order, so every reduction is deterministic.
+// Inner products: FP32 products are accumulated as float-float pairs (about
+// 48 significant bits) per thread, warp, block and grid, and the CG scalars
+// are updated in float-float arithmetic too: the GB300's FP64 pipe is narrow
+// enough that a few FP64 instructions per warp at the end of every iteration
+// cost microseconds, so the FP32 iteration runs none.  The block partials are
+// combined by the last block to finish, in a fixed order, so every reduction
+// is deterministic.
 #include <algorithm>
 #include <cmath>
 
@@ -29,28 +31,11 @@ namespace {
 // Returns true in the last block, with totals in out[] valid in thread 0.
 template <typename R, int NV>
 __device__ __forceinline__ bool grid_reduce(Acc<R> (&acc)[NV], double* part, int stride, unsigned int* ticket,
-                                            double (&out)[NV]) {
-    __shared__ double sm[32 * NV];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
-        if (lane == 0) sm[wid * NV + k] = acc[k].value();
-    }
-    __syncthreads();
-    double x[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++) x[k] = 0.0;
-    if (threadIdx.x == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        for (int w = 0; w < nw; w++)
-#pragma unroll
-            for (int k = 0; k < NV; k++) x[k] += sm[w * NV + k];
-    }
-    __syncthreads();
-    // x[] holds the block totals in thread 0; the last block sums them.
-    return last_block_commit<NV>(x, part, stride, ticket, sm, out);
+                                            Acc<R> (&out)[NV]) {
+    __shared__ typename Acc<R>::Packed sm[32 * NV];
+    Acc<R> blk[NV];
+    block_totals<NV, R>(acc, sm, blk);
+    return grid_commit<NV, R>(blk, part, stride, ticket, sm, out);
 }
 
 // Threads are grouped LANES per CSR row; a warp covers 32/LANES consecutive
@@ -86,7 +71,7 @@ struct RowMap {
 template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
-    __shared__ double red[32 * NF];
+    __shared__ typename Acc<R>::Packed red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     FV<R, NF>* w = a.wb[c.par];
@@ -96,9 +81,9 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
     Acc<R> dot[NF];
     for (int64_t row0 = warp * 32; row0 < a.N; row0 += nwarps * 32)
         init_rows<R, NF, WCH>(a.rp, a.col, a.A, a.z, w, row0, a.N, sm[wib], dot);
-    double blk[NF], tot[NF];
+    Acc<R> blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
-    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
+    if (grid_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
         volatile CgState* cg = a.cg;
         finish_spmv<R, NF>(cg, &a.run->flags, c.act, tot);
         int any = 0;
@@ -115,7 +100,7 @@ template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepArgs<R, NF> a) {
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ FV<R, NF> ut[kBlock];
-    __shared__ double red[32 * 3 * NF];
+    __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     CgVecs<R, NF> v;
@@ -135,9 +120,9 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
     for (int64_t tile0 = blockIdx.x * (int64_t)kBlock; tile0 < a.N; tile0 += (int64_t)gridDim.x * kBlock)
         cgcg_tile<R, NF, WCH>(v, c, tile0, a.N, sm[wib], ut, dots);
-    double blk[3 * NF], tot[3 * NF];
+    Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
-    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+    if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
@@ -172,7 +157,7 @@ template <typename R, int NF, int KPRE>
 __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
-    __shared__ double red[32 * NF];
+    __shared__ typename Acc<R>::Packed red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     FV<R, NF>* w = a.wb[c.par];
@@ -180,9 +165,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
         init_tile_ell<R, NF, KPRE>(e, a.z, w, tile, ref, a.N, buf, dot);
     });
-    double blk[NF], tot[NF];
+    Acc<R> blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
-    if (last_block_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
+    if (grid_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
         volatile CgState* cg = a.cg;
         finish_spmv<R, NF>(cg, &a.run->flags, c.act, tot);
         int any = 0;
@@ -199,7 +184,7 @@ template <typename R, int NF, int KPRE>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
-    __shared__ double red[32 * 3 * NF];
+    __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     CgVecs<R, NF> v;
@@ -219,9 +204,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
         cgcg_tile_ell<R, NF, KPRE>(v, e, c, tile, ref, a.N, buf, dots);
     });
-    double blk[3 * NF], tot[3 * NF];
+    Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
-    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+    if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
@@ -287,7 +272,7 @@ __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3)
 template <typename R, int NF, int NS>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
-    __shared__ double red[32 * 3 * NF];
+    __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     __shared__ int armed[NS];
     const StageLayout<R, NF> L(a.emax, a.hmax);
     PhaseCtl<R, NF> c;
@@ -396,8 +381,8 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             for (int f = 0; f < NF; f++) {
                 if (c.act[f]) {
                     const R ui = d.v[f] * ro.v[f];
-                    p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                    x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                    p.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], p.v[f], ui);
+                    x.v[f] = fmar(c.alpha[f], p.v[f], x.v[f]);
                 }
                 dots[f].add_prod(rn.v[f], un.v[f]);
                 dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
@@ -419,7 +404,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             const FV<R, NF> av = As[32 * k];
             const FV<R, NF> g = ut[Ls[32 * k]];
 #pragma unroll
-            for (int f = 0; f < NF; f++) wn.v[f] = fma(av.v[f], g.v[f], wn.v[f]);
+            for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
         }
         if (row < a.N) {
             v.w1[row] = wn;
@@ -456,9 +441,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         }
         __syncthreads();
     }
-    double blk[3 * NF], tot[3 * NF];
+    Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
-    if (last_block_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+    if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
@@ -552,9 +537,9 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
             FV<R, NF> bv, rv, pv;
 #pragma unroll
             for (int f = 0; f < NF; f++) {
-                bv.v[f] = (R)bs[f].value();
+                bv.v[f] = bs[f].rounded();
                 bs[f].sub(ax[f]);
-                rv.v[f] = (R)bs[f].value();
+                rv.v[f] = bs[f].rounded();
                 pv.v[f] = d.v[f] * rv.v[f];
                 dots[f].add_prod(bv.v[f], bv.v[f]);
                 dots[NF + f].add_prod(rv.v[f], rv.v[f]);
@@ -566,7 +551,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
         }
     }
     raise_flags(a.run, flags);
-    double tot[3 * NF];
+    Acc<R> tot[3 * NF];
     if (grid_reduce<R, 3 * NF>(dots, a.part, a.part_stride, a.tickets + 2, tot) && threadIdx.x == 0) {
         CgState* cg = a.cg;
         RunState* run = a.run;
@@ -575,26 +560,15 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
         cg->iter = 0;
         cg->max_iter = run->max_iter;
         int any = 0;
-        const double tiny = sizeof(R) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
 #pragma unroll
-        for (int f = 0; f < NF; f++) {
-            const double bb = tot[f], rr = tot[NF + f], rz = tot[2 * NF + f];
-            double thr = run->tol * run->tol * bb;
-            cg->bb[f] = bb;
-            cg->thr[f] = thr < tiny ? tiny : thr;
-            cg->rr[f] = rr;
-            cg->rz[f] = rz;
-            cg->iters[f] = 0;
-            cg->fresh[f] = 1;  // the first direction is p = z
-            cg->active[f] = (!stop && bb > 0.0 && rr >= cg->thr[f]) ? 1 : 0;
-            any |= cg->active[f];
-        }
+        for (int f = 0; f < NF; f++)
+            any |= start_solve<R>((volatile CgState*)cg, f, stop, run->tol, tot[f], tot[NF + f], tot[2 * NF + f]);
         signal_loop(a, any != 0);
     }
 }
 
 // After the first CG loop: zero right-hand sides give x = 0 (Eigen's
-// early exit), then one FP64-accurate true-residual pass r = b - A x.  Fields
+// early exit), then one float-float true-residual pass r = b - A x.  Fields
 // whose true residual is still above the threshold restart CG from there.
 template <typename R, int NF, int LANES>
 __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
@@ -643,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                     Acc<R> t;
                     t.add(bv.v[f]);
                     t.sub(ax[f]);
-                    rv.v[f] = (R)t.value();
+                    rv.v[f] = t.rounded();
                     pv.v[f] = d.v[f] * rv.v[f];
                     dots[f].add_prod(rv.v[f], rv.v[f]);
                     dots[NF + f].add_prod(rv.v[f], pv.v[f]);
@@ -653,7 +627,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
             }
         }
     }
-    double tot[2 * NF];
+    Acc<R> tot[2 * NF];
     if (grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot) && threadIdx.x == 0) {
         int any = 0;
 #pragma unroll
@@ -661,9 +635,10 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
             cg->active[f] = 0;
             cg->fresh[f] = 1;
             if (refine && !zero[f] && cg->bb[f] > 0.0) {
-                cg->rr[f] = tot[f];
-                if (tot[f] >= cg->thr[f]) {
-                    cg->rz[f] = tot[NF + f];
+                const double rr = tot[f].value();
+                cg->rr[f] = rr;
+                if (rr >= cg->thr[f]) {
+                    set_gamma((volatile CgState*)cg, f, tot[NF + f]);
                     cg->active[f] = 1;
                     any = 1;
                 }
@@ -949,6 +924,8 @@ __global__ void k_probe_state(CgState* cg) {
         cg->fresh[f] = 0;
         cg->alpha[f] = 0.0;
         cg->beta[f] = 0.0;
+        cg->falpha[f] = 0.f;
+        cg->fbeta[f] = 0.f;
     }
 }
 

@@ -18,10 +18,20 @@ template <>
 struct Acc<double> {
     double s = 0.0;
     __device__ __forceinline__ void add(double x) { s += x; }
-    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fmar(a, b, s); }
     __device__ __forceinline__ void sub(const Acc& o) { s -= o.s; }
     __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ double rounded() const { return s; }
+    __device__ __forceinline__ void merge(const Acc& o) { s += o.s; }
     __device__ __forceinline__ void shfl_add(int off) { s += __shfl_xor_sync(0xffffffffu, s, off); }
+    // storage of a block's total in an 8-byte partial slot
+    using Packed = double;
+    __device__ __forceinline__ Packed pack() const { return s; }
+    __device__ __forceinline__ static Acc unpack(Packed x) {
+        Acc a;
+        a.s = x;
+        return a;
+    }
 };
 
 // float-float: value = hi + lo with |lo| <= ulp(hi)/2 (Knuth two-sum plus the
@@ -48,13 +58,93 @@ struct Acc<float> {
         lo = __fsub_rn(lo, o.lo);
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    // hi + lo rounded once to float.  The pair's exact sum fits a double, so
+    // this equals (float)value() without touching the FP64 pipe.
+    __device__ __forceinline__ float rounded() const { return __fadd_rn(hi, lo); }
+    __device__ __forceinline__ void merge(const Acc& o) {
+        add(o.hi);
+        lo = __fadd_rn(lo, o.lo);
+    }
     __device__ __forceinline__ void shfl_add(int off) {
-        const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
-        const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
-        add(oh);
-        lo = __fadd_rn(lo, ol);
+        Acc o;
+        o.hi = __shfl_xor_sync(0xffffffffu, hi, off);
+        o.lo = __shfl_xor_sync(0xffffffffu, lo, off);
+        merge(o);
+    }
+    using Packed = float2;
+    __device__ __forceinline__ Packed pack() const { return make_float2(hi, lo); }
+    __device__ __forceinline__ static Acc unpack(Packed x) {
+        Acc a;
+        a.hi = x.x;
+        a.lo = x.y;
+        return a;
     }
 };
+
+// ---- float-float scalars ------------------------------------------------------
+// The CG scalars of FP32 solvers (alpha, beta, gamma, the convergence test)
+// are computed in float-float arithmetic (about 48 significant bits), so that
+// no FP64 instruction runs inside a CG iteration.  Knuth / Dekker error-free
+// transformations, rounded intrinsics throughout.
+using FF = Acc<float>;
+
+__device__ __forceinline__ FF ff_quick(float a, float b) {  // |a| >= |b|
+    FF r;
+    r.hi = __fadd_rn(a, b);
+    r.lo = __fsub_rn(b, __fsub_rn(r.hi, a));
+    return r;
+}
+__device__ __forceinline__ FF ff_of(double x) {
+    FF r;
+    r.hi = __double2float_rn(x);
+    r.lo = __double2float_rn(x - (double)r.hi);
+    return r;
+}
+__device__ __forceinline__ FF ff_load(const volatile float (&p)[2]) {
+    FF r;
+    r.hi = p[0];
+    r.lo = p[1];
+    return r;
+}
+__device__ __forceinline__ void ff_store(volatile float (&p)[2], const FF& x) {
+    p[0] = x.hi;
+    p[1] = x.lo;
+}
+__device__ __forceinline__ FF ff_two(float a, float b) {  // any magnitudes
+    FF r;
+    r.hi = __fadd_rn(a, b);
+    const float bb = __fsub_rn(r.hi, a);
+    r.lo = __fadd_rn(__fsub_rn(a, __fsub_rn(r.hi, bb)), __fsub_rn(b, bb));
+    return r;
+}
+// a - b with both pairs' errors carried (accurate under cancellation).
+__device__ __forceinline__ FF ff_sub(const FF& a, const FF& b) {
+    FF s = ff_two(a.hi, -b.hi);
+    const FF t = ff_two(a.lo, -b.lo);
+    s = ff_quick(s.hi, __fadd_rn(s.lo, t.hi));
+    return ff_quick(s.hi, __fadd_rn(s.lo, t.lo));
+}
+__device__ __forceinline__ FF ff_mul(const FF& a, const FF& b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return ff_quick(p, e);
+}
+// Long division: q1 = a/b in float, then the quotient of the exact remainder.
+__device__ __forceinline__ FF ff_div(const FF& a, const FF& b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    FF q;
+    q.hi = q1;
+    q.lo = 0.f;
+    const FF r = ff_sub(a, ff_mul(q, b));
+    return ff_quick(q1, __fdiv_rn(r.hi, b.hi));
+}
+__device__ __forceinline__ FF ff_norm(const FF& a) { return ff_two(a.hi, a.lo); }
+// a < b for normalised pairs
+__device__ __forceinline__ bool ff_less(const FF& a, const FF& b) {
+    return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
 
 // Loop condition: stored for host-driven loops, and set on the graph's
 // conditional node when the kernel runs inside the step graph.  Called by one
@@ -112,25 +202,62 @@ __device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
     return ldv(p, false);
 }
 
+// Block totals of NV accumulators: warp sums by shuffles, then thread 0
+// merges the warps' sums in warp order.  The accumulator type carries through
+// (float-float pairs for FP32 solvers: no FP64 instruction), and the result is
+// valid in thread 0 (empty elsewhere).  sm holds 32 * NV packed values.
 template <int NV, typename R>
-__device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], double* sm, double (&blk)[NV]) {
+__device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], typename Acc<R>::Packed* sm, Acc<R> (&blk)[NV]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[k].shfl_add(o);
-        if (lane == 0) sm[wid * NV + k] = acc[k].value();
+        if (lane == 0) sm[wid * NV + k] = acc[k].pack();
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < NV; k++) blk[k] = 0.0;
+    for (int k = 0; k < NV; k++) blk[k] = Acc<R>();
     if (threadIdx.x == 0) {
         const int nw = (blockDim.x + 31) >> 5;
         for (int w = 0; w < nw; w++)
 #pragma unroll
-            for (int k = 0; k < NV; k++) blk[k] += sm[w * NV + k];
+            for (int k = 0; k < NV; k++) blk[k].merge(Acc<R>::unpack(sm[w * NV + k]));
     }
     __syncthreads();
+}
+
+// Last-block-done reduction of block totals held in thread 0: every block
+// stores its NV totals, packed, to part[k * stride + blockIdx.x] (8-byte
+// slots); the block that finishes last merges all partials in a fixed order
+// (the result does not depend on which block finished last) and returns true
+// in all its threads with the totals in out[] (valid in thread 0).  The
+// ticket counter is reset for the next launch.
+template <int NV, typename R>
+__device__ bool grid_commit(const Acc<R> (&blk)[NV], double* part, int stride, unsigned int* ticket,
+                            typename Acc<R>::Packed* sm, Acc<R> (&out)[NV]) {
+    using P = typename Acc<R>::Packed;
+    static_assert(sizeof(P) == sizeof(double), "partials use 8-byte slots");
+    P* pp = reinterpret_cast<P*>(part);
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) pp[k * stride + blockIdx.x] = blk[k].pack();
+        __threadfence();
+        const unsigned int t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    Acc<R> y[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            y[k].merge(Acc<R>::unpack(__ldcg(&pp[k * stride + b])));
+    block_totals<NV, R>(y, sm, out);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
 }
 
 // ---- CG building blocks ----------------------------------------------------------
@@ -153,8 +280,13 @@ struct PhaseCtl {
         for (int f = 0; f < NF; f++) {
             act[f] = st->active[f];
             fresh[f] = st->fresh[f] != 0;
-            beta[f] = fresh[f] ? (R)0 : (R)st->beta[f];
-            alpha[f] = act[f] ? (R)st->alpha[f] : (R)0;
+            if constexpr (sizeof(R) == 4) {  // coefficients stored rounded: no conversion here
+                beta[f] = fresh[f] ? (R)0 : st->fbeta[f];
+                alpha[f] = act[f] ? st->falpha[f] : (R)0;
+            } else {
+                beta[f] = fresh[f] ? (R)0 : (R)st->beta[f];
+                alpha[f] = act[f] ? (R)st->alpha[f] : (R)0;
+            }
             need_old |= !fresh[f];
             any |= act[f] != 0;
         }
@@ -268,8 +400,8 @@ __device__ __forceinline__ void cg_advance(const PhaseCtl<R, NF>& c, const FV<R,
                                            FV<R, NF>& rn, FV<R, NF>& un) {
 #pragma unroll
     for (int f = 0; f < NF; f++) {
-        sn.v[f] = c.fresh[f] ? wo.v[f] : fma(c.beta[f], so.v[f], wo.v[f]);
-        rn.v[f] = c.act[f] ? fma(-c.alpha[f], sn.v[f], ro.v[f]) : ro.v[f];
+        sn.v[f] = c.fresh[f] ? wo.v[f] : fmar(c.beta[f], so.v[f], wo.v[f]);
+        rn.v[f] = c.act[f] ? fmar(-c.alpha[f], sn.v[f], ro.v[f]) : ro.v[f];
         un.v[f] = d.v[f] * rn.v[f];
     }
 }
@@ -305,8 +437,8 @@ __device__ __forceinline__ void cgcg_tile(const CgVecs<R, NF>& v, const PhaseCtl
         for (int f = 0; f < NF; f++) {
             if (c.act[f]) {
                 const R ui = d.v[f] * ro.v[f];
-                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                p.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], p.v[f], ui);
+                x.v[f] = fmar(c.alpha[f], p.v[f], x.v[f]);
             }
             dots[f].add_prod(rn.v[f], un.v[f]);
             dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
@@ -397,14 +529,14 @@ struct EllRow {
             if (k < r.sw) {
                 const FV<R, NF> g = ut[l[k]];
 #pragma unroll
-                for (int f = 0; f < NF; f++) acc.v[f] = fma(a[k].v[f], g.v[f], acc.v[f]);
+                for (int f = 0; f < NF; f++) acc.v[f] = fmar(a[k].v[f], g.v[f], acc.v[f]);
             }
         }
         for (int k = KPRE; k < r.sw; k++) {
             const FV<R, NF> av = ldv(e.As + r.sb + 32 * k + lane, false);
             const FV<R, NF> g = ut[__ldg(e.lcol + r.sb + 32 * k + lane)];
 #pragma unroll
-            for (int f = 0; f < NF; f++) acc.v[f] = fma(av.v[f], g.v[f], acc.v[f]);
+            for (int f = 0; f < NF; f++) acc.v[f] = fmar(av.v[f], g.v[f], acc.v[f]);
         }
         return acc;
     }
@@ -451,8 +583,8 @@ __device__ __forceinline__ void cgcg_tile_ell(const CgVecs<R, NF>& v, const EllV
         for (int f = 0; f < NF; f++) {
             if (c.act[f]) {
                 const R ui = d.v[f] * ro.v[f];
-                p.v[f] = c.fresh[f] ? ui : fma(c.beta[f], p.v[f], ui);
-                x.v[f] = fma(c.alpha[f], p.v[f], x.v[f]);
+                p.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], p.v[f], ui);
+                x.v[f] = fmar(c.alpha[f], p.v[f], x.v[f]);
             }
             dots[f].add_prod(rn.v[f], un.v[f]);
             dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
@@ -500,21 +632,60 @@ __device__ __forceinline__ void init_tile_ell(const EllView<R, NF>& e, const FV<
     }
 }
 
+// gamma = r.z of the running solve (and its float-float copy for FP32).
+template <typename R, typename S>
+__device__ __forceinline__ void set_gamma(volatile S* s, int f, const Acc<R>& g) {
+    s->rz[f] = g.value();
+    if constexpr (sizeof(R) == 4) ff_store(s->ffrz[f], ff_norm(g));
+}
+
+// CG scalars of a solve's start, per field: |b|^2, the threshold tol^2 |b|^2
+// (at least the smallest normal number of R), |r|^2 and gamma = r.z.  The
+// FP32 solver keeps float-float copies of gamma and the threshold for its
+// iterations.  Returns whether the field iterates.
+template <typename R, typename S>
+__device__ __forceinline__ int start_solve(volatile S* s, int f, int stop, double tol, const Acc<R>& bb_a,
+                                           const Acc<R>& rr_a, const Acc<R>& rz_a) {
+    const double tiny = sizeof(R) == 4 ? 1.1754943508222875e-38 : 2.2250738585072014e-308;
+    const double bb = bb_a.value(), rr = rr_a.value();
+    double thr = tol * tol * bb;
+    thr = thr < tiny ? tiny : thr;
+    s->bb[f] = bb;
+    s->thr[f] = thr;
+    s->rr[f] = rr;
+    set_gamma(s, f, rz_a);
+    if constexpr (sizeof(R) == 4) ff_store(s->ffthr[f], ff_of(thr));
+    s->iters[f] = 0;
+    s->fresh[f] = 1;  // the first direction is p = z
+    s->active[f] = (!stop && bb > 0.0 && rr >= thr) ? 1 : 0;
+    return s->active[f];
+}
+
 // After the SpMV phase: alpha = r.z / p.q, or breakdown.
 // (S: CgState or a batched instance's state; flags receives FEA_STATUS_*.)
 template <typename R, int NF, typename S>
-__device__ void finish_spmv(volatile S* cg, unsigned int* flags, const int (&act)[NF], const double* tot) {
+__device__ void finish_spmv(volatile S* cg, unsigned int* flags, const int (&act)[NF], const Acc<R>* tot) {
 #pragma unroll
     for (int f = 0; f < NF; f++) {
         if (!act[f]) continue;
-        cg->pq[f] = tot[f];
-        const double al = cg->rz[f] / tot[f];
-        if (!(tot[f] > 0.0) || !isfinite(al)) {
+        bool ok;
+        if constexpr (sizeof(R) == 4) {
+            const FF pq = ff_norm(tot[f]);
+            const FF al = ff_div(ff_load(cg->ffrz[f]), pq);
+            ok = pq.hi > 0.f && isfinite(al.hi);
+            if (ok) {
+                ff_store(cg->ffalpha[f], al);
+                cg->falpha[f] = al.rounded();
+            }
+        } else {
+            const double al = cg->rz[f] / tot[f].s;
+            ok = tot[f].s > 0.0 && isfinite(al);
+            if (ok) cg->alpha[f] = al;
+        }
+        if (!ok) {
             cg->active[f] = 0;
             cg->iters[f] = cg->iter;
             atomicOr(flags, FEA_STATUS_BREAKDOWN);
-        } else {
-            cg->alpha[f] = al;
         }
     }
 }
@@ -523,9 +694,10 @@ __device__ void finish_spmv(volatile S* cg, unsigned int* flags, const int (&act
 // beta = gamma'/gamma and alpha = gamma' / (delta' - beta gamma'/alpha) for
 // the next iteration; iteration count and the max_iter limit.  tot holds
 // gamma' = r.u, delta' = w.u and r.r per field.  Returns whether another
-// iteration runs.
+// iteration runs.  The FP32 solver does this in float-float arithmetic and
+// stores |r|^2 as a double only when a field stops iterating.
 template <typename R, int NF, typename S>
-__device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act)[NF], const double* tot) {
+__device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act)[NF], const Acc<R>* tot) {
     const int it = cg->iter + 1;
     cg->iter = it;
     int any = 0;
@@ -533,32 +705,54 @@ __device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act
     for (int f = 0; f < NF; f++) {
         cg->fresh[f] = 0;
         if (!act[f]) continue;
-        const double g = tot[f], d = tot[NF + f], rr = tot[2 * NF + f];
-        cg->rr[f] = rr;
-        if (!isfinite(rr)) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            atomicOr(flags, FEA_STATUS_BREAKDOWN);
+        const Acc<R>& rr = tot[2 * NF + f];
+        int state;  // 0: iterates, 1: converged, 2: breakdown
+        if constexpr (sizeof(R) == 4) {
+            const FF r2 = ff_norm(rr);
+            if (!isfinite(r2.hi)) {
+                state = 2;
+            } else if (ff_less(r2, ff_load(cg->ffthr[f]))) {
+                state = 1;
+            } else {
+                const FF g = ff_norm(tot[f]), d = ff_norm(tot[NF + f]);
+                const FF beta = ff_div(g, ff_load(cg->ffrz[f]));
+                const FF den = ff_sub(d, ff_div(ff_mul(beta, g), ff_load(cg->ffalpha[f])));
+                const FF alpha = ff_div(g, den);
+                state = (!(den.hi > 0.f) || !isfinite(alpha.hi) || !isfinite(beta.hi)) ? 2 : 0;
+                if (state == 0) {
+                    cg->fbeta[f] = beta.rounded();
+                    cg->falpha[f] = alpha.rounded();
+                    ff_store(cg->ffalpha[f], alpha);
+                    ff_store(cg->ffrz[f], g);
+                }
+            }
+        } else {
+            const double g = tot[f].s, d = tot[NF + f].s, r2 = rr.s;
+            if (!isfinite(r2)) {
+                state = 2;
+            } else if (r2 < cg->thr[f]) {
+                state = 1;
+            } else {
+                const double beta = g / cg->rz[f];
+                const double den = d - beta * g / cg->alpha[f];
+                const double alpha = g / den;
+                state = (!(den > 0.0) || !isfinite(alpha) || !isfinite(beta)) ? 2 : 0;
+                if (state == 0) {
+                    cg->beta[f] = beta;
+                    cg->alpha[f] = alpha;
+                    cg->rz[f] = g;
+                }
+            }
+            cg->rr[f] = r2;
+        }
+        if (state == 0) {
+            any = 1;
             continue;
         }
-        if (rr < cg->thr[f]) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            continue;
-        }
-        const double beta = g / cg->rz[f];
-        const double den = d - beta * g / cg->alpha[f];
-        const double alpha = g / den;
-        if (!(den > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
-            cg->active[f] = 0;
-            cg->iters[f] = it;
-            atomicOr(flags, FEA_STATUS_BREAKDOWN);
-            continue;
-        }
-        cg->beta[f] = beta;
-        cg->alpha[f] = alpha;
-        cg->rz[f] = g;
-        any = 1;
+        if constexpr (sizeof(R) == 4) cg->rr[f] = rr.value();
+        cg->active[f] = 0;
+        cg->iters[f] = it;
+        if (state == 2) atomicOr(flags, FEA_STATUS_BREAKDOWN);
     }
     const bool cont = any && it < cg->max_iter;
     if (any && !cont) {
@@ -566,6 +760,7 @@ __device__ bool finish_cgcg(volatile S* cg, unsigned int* flags, const int (&act
 #pragma unroll
         for (int f = 0; f < NF; f++)
             if (cg->active[f]) {
+                if constexpr (sizeof(R) == 4) cg->rr[f] = tot[2 * NF + f].value();
                 cg->active[f] = 0;
                 cg->iters[f] = it;
             }

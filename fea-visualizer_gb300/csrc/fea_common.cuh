@@ -114,6 +114,11 @@ __device__ bool last_block_commit(const double (&blk)[NV], double* part, int str
     return true;
 }
 
+// Fused multiply-add in the operands' own precision (the float overload runs
+// on the FP32 pipe; nothing here may promote to double, whose pipe is narrow).
+__device__ __forceinline__ float fmar(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmar(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 // Round-to-nearest arithmetic without contraction, so that FP32 operator
 // values match the reference's per-entry evaluation bit for bit.
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }

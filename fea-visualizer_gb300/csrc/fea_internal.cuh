@@ -107,6 +107,10 @@ struct StepParams {
 
 struct CgState {
     double rz[2], rr[2], pq[2], thr[2], bb[2], alpha[2], beta[2];
+    // FP32 solvers: float-float (hi, lo) gamma, alpha and threshold, and the
+    // coefficients alpha, beta rounded to float for the vector updates
+    float ffrz[2][2], ffalpha[2][2], ffthr[2][2];
+    float falpha[2], fbeta[2];
     int active[2];
     int fresh[2];  // the next direction is p = z (first iteration of a loop)
     int iters[2];
@@ -214,7 +218,7 @@ constexpr size_t kStreamSmemLimit = 220 * 1024;  // per block, below the 227 KB 
 int max_grid_blocks();
 
 // ---- adjoint of the explicit advection-diffusion step (adjoint.cu) ----------------
-// lam = M (u - t), *J = 1/2 (u - t).lam  (FP64-accurate; one block-partial
+// lam = M (u - t), *J = 1/2 (u - t).lam  (exact accumulators; one block-partial
 // reduction through part/ticket).
 template <typename R>
 void adjoint_loss(const Pattern& P, const R* M, const R* u, const R* t, R* lam, double* part, int stride,

@@ -15,10 +15,13 @@
 // The array is shared by all calls on a device and keeps the last call's
 // contents: each call clears the loop state before use, and calls that
 // overlap on the GPU (other streams, other host threads) race on it.
+//
+// Inner products and the initial residual accumulate in the solvers' exact
+// accumulators (float-float pairs in FP32), block and grid totals included.
 #include <cmath>
 #include <mutex>
 
-#include "fea_internal.cuh"
+#include "cg_device.cuh"
 
 namespace fea {
 namespace {
@@ -55,35 +58,39 @@ struct NaArgs {
     R *r, *p, *q, *dinv;
 };
 
-template <int NV>
-__device__ __forceinline__ bool na_reduce(double (&acc)[NV], double* part, unsigned int* ticket,
-                                          double (&out)[NV]) {
-    __shared__ double sm[32 * NV];
-    block_sum<NV>(acc, sm);
-    return last_block_commit<NV>(acc, part, kNaMaxBlocks, ticket, sm, out);
+template <int NV, typename R>
+__device__ __forceinline__ bool na_reduce(Acc<R> (&acc)[NV], double* part, unsigned int* ticket, double (&out)[NV]) {
+    __shared__ typename Acc<R>::Packed sm[32 * NV];
+    Acc<R> blk[NV], tot[NV];
+    block_totals<NV, R>(acc, sm, blk);
+    const bool last = grid_commit<NV, R>(blk, part, kNaMaxBlocks, ticket, sm, tot);
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = tot[k].value();
+    return last;
 }
 
 // r = b - A x, D^-1, p = D^-1 r and the set-up scalars.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) k_na_init(NaArgs<R> a, double tol, int max_iter) {
-    double acc[3] = {0.0, 0.0, 0.0};
+    Acc<R> acc[3];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
-        double ax = 0.0;
+        Acc<R> t;
         R d = 0;
         for (int32_t e = a.rp[i]; e < a.rp[i + 1]; e++) {
             const int32_t c = a.col[e];
-            ax = fma((double)a.val[e], (double)a.x[c], ax);
+            t.add_prod(-a.val[e], a.x[c]);
             if (c == i) d += a.val[e];
         }
         const R bi = a.b[i];
-        const R ri = (R)((double)bi - ax);
+        t.add(bi);
+        const R ri = t.rounded();
         const R di = d != (R)0 ? (R)1 / d : (R)1;
         a.r[i] = ri;
         a.dinv[i] = di;
         a.p[i] = di * ri;
-        acc[0] += (double)bi * bi;
-        acc[1] += (double)ri * ri;
-        acc[2] += (double)ri * (di * ri);
+        acc[0].add_prod(bi, bi);
+        acc[1].add_prod(ri, ri);
+        acc[2].add_prod(ri, di * ri);
     }
     double tot[3];
     if (na_reduce<3>(acc, a.part, &a.st->ticket[0], tot) && threadIdx.x == 0) {
@@ -104,12 +111,12 @@ __global__ void __launch_bounds__(kBlock) k_na_init(NaArgs<R> a, double tol, int
 template <typename R>
 __global__ void __launch_bounds__(kBlock) k_na_spmv(NaArgs<R> a) {
     if (!a.st->active) return;
-    double acc[1] = {0.0};
+    Acc<R> acc[1];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         R s = 0;
-        for (int32_t e = a.rp[i]; e < a.rp[i + 1]; e++) s = fma(a.val[e], a.p[a.col[e]], s);
+        for (int32_t e = a.rp[i]; e < a.rp[i + 1]; e++) s = fmar(a.val[e], a.p[a.col[e]], s);
         a.q[i] = s;
-        acc[0] += (double)a.p[i] * s;
+        acc[0].add_prod(a.p[i], s);
     }
     double tot[1];
     if (na_reduce<1>(acc, a.part, &a.st->ticket[1], tot) && threadIdx.x == 0) {
@@ -130,13 +137,13 @@ template <typename R>
 __global__ void __launch_bounds__(kBlock) k_na_update(NaArgs<R> a) {
     if (!a.st->active) return;
     const R alpha = (R)a.st->alpha;
-    double acc[2] = {0.0, 0.0};
+    Acc<R> acc[2];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
-        a.x[i] = fma(alpha, a.p[i], a.x[i]);
-        const R ri = fma(-alpha, a.q[i], a.r[i]);
+        a.x[i] = fmar(alpha, a.p[i], a.x[i]);
+        const R ri = fmar(-alpha, a.q[i], a.r[i]);
         a.r[i] = ri;
-        acc[0] += (double)ri * (a.dinv[i] * ri);
-        acc[1] += (double)ri * ri;
+        acc[0].add_prod(ri, a.dinv[i] * ri);
+        acc[1].add_prod(ri, ri);
     }
     double tot[2];
     if (na_reduce<2>(acc, a.part, &a.st->ticket[2], tot) && threadIdx.x == 0) {
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(kBlock) k_na_dir(NaArgs<R> a) {
     if (!a.st->active) return;
     const R beta = (R)a.st->beta;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
-        a.p[i] = fma(beta, a.p[i], a.dinv[i] * a.r[i]);
+        a.p[i] = fmar(beta, a.p[i], a.dinv[i] * a.r[i]);
 }
 
 // Eigen's early exit: a zero right-hand side gives x = 0.
