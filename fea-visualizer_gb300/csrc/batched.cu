@@ -127,10 +127,7 @@ __device__ bool inst_commit(const Acc<R> (&blk)[NV], double* part, int tile, int
     if (!last) return false;
     __threadfence();
     Acc<R> y[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-        for (int t = t0 + threadIdx.x; t < t0 + nt; t += blockDim.x)
-            y[k].merge(Acc<R>::unpack(__ldcg(&pp[(int64_t)t * kNV + k])));
+    merge_partials<NV, R>(y, pp, 1, kNV, t0, (int64_t)t0 + nt);  // tile t, value k at pp[t * kNV + k]
     block_totals<NV, R>(y, smem, out);
     if (threadIdx.x == 0) *ticket = 0u;
     return true;

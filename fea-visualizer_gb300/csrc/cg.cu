@@ -242,14 +242,12 @@ struct StageLayout {
 // The vectors a stage holds, in this order.
 enum { kVr = 0, kVw = 1, kVs = 2, kVd = 3, kVx = 4, kVp = 5 };
 
-// Thread 0: bulk copies of tile `tile` into stage S (after the block's last
-// read of S and a proxy fence).
+// Thread 0: bulk copies of tile `tile` (entries e0 .. e1 of the tile-ELL
+// arrays) into stage S, after the block's last read of S and a proxy fence.
 template <typename R, int NF>
 __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const StepArgs<R, NF>& a,
-                           const CgVecs<R, NF>& v, int64_t tile) {
+                           const CgVecs<R, NF>& v, int64_t tile, int32_t e0, int32_t e1) {
     uint64_t* bar = reinterpret_cast<uint64_t*>(S + L.bar);
-    const int32_t e0 = a.slice_off[tile * (kTileRows / 32)];
-    const int32_t e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
     const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
     const uint32_t nL = (uint32_t)(e1 - e0) * 2u;
     const uint32_t nV = (uint32_t)kTileRows * (uint32_t)sizeof(FV<R, NF>);
@@ -269,7 +267,17 @@ __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const 
 // warp stages about the same share of a tile's halo.
 __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
 
-template <typename R, int NF, int NS>
+// The per-tile references (entry ranges, slice offsets, halo lists) are loaded
+// ahead of use in a software pipeline, so that no load waits on another
+// within a tile: a tile's halo offset is loaded one tile before its halo
+// column, which is loaded one tile before the column's operands are gathered,
+// which happens one tile before the tile itself.
+//
+// LATE = false: thread 0 refills a stage after a third block barrier at the
+// end of the tile that used it.  LATE = true: after the next tile's first
+// barrier, which already orders every read of the stage before the refill;
+// two barriers per tile.
+template <typename R, int NF, int NS, bool LATE>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
@@ -295,16 +303,16 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     auto stage = [&](int b) { return dyn_smem + (size_t)b * L.bytes; };
     auto bar_of = [&](int b) { return reinterpret_cast<uint64_t*>(stage(b) + L.bar); };
     auto ut_of = [&](int b) { return reinterpret_cast<FV<R, NF>*>(stage(b) + L.U); };
-    // halo column of slot j of tile `tile` (-1: none) and the tile's halo count
-    auto halo_ref = [&](int64_t tile, int32_t& col, int32_t& cnt) {
-        col = -1;
-        cnt = 0;
+    // first halo entry and halo count of tile `tile` (0, 0 past the end)
+    auto halo_head = [&](int64_t tile, int32_t& h0, int32_t& cnt) {
+        h0 = cnt = 0;
         if (tile < ntiles) {
-            const int32_t h0 = a.halo_off[tile];
+            h0 = a.halo_off[tile];
             cnt = a.halo_off[tile + 1] - h0;
-            if (j < cnt) col = a.halo_col[h0 + j];
         }
     };
+    // halo column of this thread's slot (-1: none)
+    auto halo_col = [&](int32_t h0, int32_t cnt) { return j < cnt ? a.halo_col[h0 + j] : -1; };
     // this warp's slice of tile `tile`: offset in the tile's entries, width
     auto slice_ref = [&](int64_t tile, int32_t& sb, int32_t& sw) {
         sb = sw = 0;
@@ -315,6 +323,14 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             sw = (a.slice_off[sl + 1] - s0) >> 5;
         }
     };
+    // entry range of tile `tile` (thread 0's copies)
+    auto entries = [&](int64_t tile, int32_t& e0, int32_t& e1) {
+        e0 = e1 = 0;
+        if (tile < ntiles) {
+            e0 = a.slice_off[tile * (kTileRows / 32)];
+            e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
+        }
+    };
     if (t == 0) {
         for (int b = 0; b < NS; b++) {
             mbar_init(bar_of(b), 1);
@@ -323,7 +339,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         mbar_fence_init();
         for (int b = 0; b < NS; b++)
             if (t0 + b * G < ntiles) {
-                stage_tile(stage(b), L, a, v, t0 + b * G);
+                int32_t e0, e1;
+                entries(t0 + b * G, e0, e1);
+                stage_tile(stage(b), L, a, v, t0 + b * G, e0, e1);
                 armed[b] = 1;
             }
     }
@@ -332,9 +350,18 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         const int32_t h0 = a.halo_off[t0], h1 = a.halo_off[t0 + 1];
         for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
     }
-    int32_t hcol, hcnt, sb, sw;
-    halo_ref(t0 + G, hcol, hcnt);  // the next tile's halo slot
+    // pipeline registers: halo column and count of the next tile, halo head
+    // of the tile after next, this tile's slice, and (thread 0) the entry
+    // range of the next refill
+    int32_t hcol, hcnt, hh0, hhc, sb, sw, re0 = 0, re1 = 0;
+    {
+        int32_t h0;
+        halo_head(t0 + G, h0, hcnt);
+        hcol = halo_col(h0, hcnt);
+    }
+    halo_head(t0 + 2 * G, hh0, hhc);
     slice_ref(t0, sb, sw);
+    if (t == 0) entries(t0 + NS * G, re0, re1);
     __syncthreads();
     Acc<R> dots[3 * NF];
     uint32_t phase[NS];
@@ -342,6 +369,8 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     for (int b = 0; b < NS; b++) phase[b] = 0u;
     bool ok = true;
     int b = 0;
+    int64_t refill = -1;  // LATE: tile whose stage (the previous one) thread 0 refills next
+    int bprev = 0;
     for (int64_t tile = t0; tile < ntiles; tile += G) {
         FV<R, NF>* ut = ut_of(b);
         const int bn = b + 1 == NS ? 0 : b + 1;
@@ -354,17 +383,30 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             hs = hw;
             if (c.need_old) hs = ldv(v.s0 + hcol, false);
         }
-        // references of the tile after next and of the next tile's slice
-        int32_t hcol2, hcnt2, sb2, sw2;
-        halo_ref(tile + 2 * G, hcol2, hcnt2);
+        // references further ahead, each from values already loaded
+        const int32_t hcol2 = halo_col(hh0, hhc), hcnt2 = hhc;
+        int32_t hh0n, hhcn, sb2, sw2;
+        halo_head(tile + 3 * G, hh0n, hhcn);
         slice_ref(tile + G, sb2, sw2);
+        const int32_t ce0 = re0, ce1 = re1;
+        if (t == 0) entries((LATE ? tile : tile + G) + NS * G, re0, re1);  // the next refill
         const bool got = mbar_wait(bar_of(b), phase[b]);
         phase[b] ^= 1u;
         if (!__syncthreads_and(got)) {
             ok = false;
             break;
         }
-        if (t == 0) armed[b] = 0;
+        if (t == 0) {
+            armed[b] = 0;
+            if (LATE && refill >= 0) {
+                stage_tile(stage(bprev), L, a, v, refill, ce0, ce1);
+                armed[bprev] = 1;
+            }
+        }
+        if (LATE) {
+            refill = tile + NS * G < ntiles ? tile + NS * G : -1;
+            bprev = b;
+        }
         const FV<R, NF>* V = reinterpret_cast<const FV<R, NF>*>(stage(b) + L.V);
         const int64_t row = tile * kTileRows + t;
         FV<R, NF> un;
@@ -422,13 +464,17 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             for (int32_t h = kBlock + t; h < hcnt; h += kBlock)
                 ut_of(bn)[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0 + h]);
         }
-        __syncthreads();  // this stage is free again
-        if (t == 0 && tile + NS * G < ntiles) {
-            stage_tile(stage(b), L, a, v, tile + NS * G);
-            armed[b] = 1;
+        if (!LATE) {
+            __syncthreads();  // this stage is free again
+            if (t == 0 && tile + NS * G < ntiles) {
+                stage_tile(stage(b), L, a, v, tile + NS * G, ce0, ce1);
+                armed[b] = 1;
+            }
         }
         hcol = hcol2;
         hcnt = hcnt2;
+        hh0 = hh0n;
+        hhc = hhcn;
         sb = sb2;
         sw = sw2;
         b = bn;
@@ -740,17 +786,22 @@ template <typename R, int NF>
 struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
-// Variants 2 and 3: the streamed iteration with 2 or 3 stages; the set-up
-// product is variant 1's.
-template <typename R, int NF, int NS>
+// Variants 2 and 3: the streamed iteration with 2 or 3 stages, refilled
+// after a third barrier per tile; 6 and 7: the same, refilled after the next
+// tile's first barrier.  The set-up product is variant 1's.
+template <typename R, int NF, int NS, bool LATE>
 struct StreamKernels : EllKernels<R, NF, 4> {
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS>;
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS, LATE>;
     static size_t smem_iter(const StepArgs<R, NF>& a) { return NS * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
 };
 template <typename R, int NF>
-struct CgKernels<R, NF, 2> : StreamKernels<R, NF, 2> {};
+struct CgKernels<R, NF, 2> : StreamKernels<R, NF, 2, false> {};
 template <typename R, int NF>
-struct CgKernels<R, NF, 3> : StreamKernels<R, NF, 3> {};
+struct CgKernels<R, NF, 3> : StreamKernels<R, NF, 3, false> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 6> : StreamKernels<R, NF, 2, true> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 7> : StreamKernels<R, NF, 3, true> {};
 
 template <typename R, int NF, int WCH>
 struct Grids {
@@ -866,6 +917,8 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     case 1: G ? build_graph_t<R, NF, EQ, 1>(*G, a, lf) : run_stream_t<R, NF, EQ, 1>(a, lf, st); break;
     case 2: G ? build_graph_t<R, NF, EQ, 2>(*G, a, lf) : run_stream_t<R, NF, EQ, 2>(a, lf, st); break;
     case 3: G ? build_graph_t<R, NF, EQ, 3>(*G, a, lf) : run_stream_t<R, NF, EQ, 3>(a, lf, st); break;
+    case 6: G ? build_graph_t<R, NF, EQ, 6>(*G, a, lf) : run_stream_t<R, NF, EQ, 6>(a, lf, st); break;
+    case 7: G ? build_graph_t<R, NF, EQ, 7>(*G, a, lf) : run_stream_t<R, NF, EQ, 7>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -949,6 +1002,8 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     case 1: probe_t<R, NF, 1>(a, st); break;
     case 2: probe_t<R, NF, 2>(a, st); break;
     case 3: probe_t<R, NF, 3>(a, st); break;
+    case 6: probe_t<R, NF, 6>(a, st); break;
+    case 7: probe_t<R, NF, 7>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;

@@ -202,8 +202,8 @@ __device__ __forceinline__ FV<R, NF> ldfv(const FV<R, NF>* p) {
     return ldv(p, false);
 }
 
-// Block totals of NV accumulators: warp sums by shuffles, then thread 0
-// merges the warps' sums in warp order.  The accumulator type carries through
+// Block totals of NV accumulators: warp sums by shuffles, then a shuffle tree
+// over the warps' sums in warp 0 (a fixed order).  The accumulator type carries through
 // (float-float pairs for FP32 solvers: no FP64 instruction), and the result is
 // valid in thread 0 (empty elsewhere).  sm holds 32 * NV packed values.
 template <int NV, typename R>
@@ -218,13 +218,48 @@ __device__ __forceinline__ void block_totals(Acc<R> (&acc)[NV], typename Acc<R>:
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NV; k++) blk[k] = Acc<R>();
-    if (threadIdx.x == 0) {
+    if (wid == 0) {  // lane w holds warp w's sums; a shuffle tree over the warps
         const int nw = (blockDim.x + 31) >> 5;
-        for (int w = 0; w < nw; w++)
+        if (lane < nw)
 #pragma unroll
-            for (int k = 0; k < NV; k++) blk[k].merge(Acc<R>::unpack(sm[w * NV + k]));
+            for (int k = 0; k < NV; k++) blk[k] = Acc<R>::unpack(sm[lane * NV + k]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            if (o < nw)
+#pragma unroll
+                for (int k = 0; k < NV; k++) blk[k].shfl_add(o);
+        if (lane != 0)
+#pragma unroll
+            for (int k = 0; k < NV; k++) blk[k] = Acc<R>();
     }
     __syncthreads();
+}
+
+// y[k] += partials p[k * vstride + b * pstride] for b in [b0, b1), thread t
+// taking b0 + t, b0 + t + blockDim.x, ...  The loads of kMergeBatch partials
+// per value are all issued before the first merge, so the block pays one L2
+// round trip per batch rather than one per partial.
+constexpr int kMergeBatch = 2;
+template <int NV, typename R>
+__device__ __forceinline__ void merge_partials(Acc<R> (&y)[NV], const typename Acc<R>::Packed* p, int64_t vstride,
+                                               int64_t pstride, int64_t b0, int64_t b1) {
+    using P = typename Acc<R>::Packed;
+    const int64_t step = (int64_t)kMergeBatch * blockDim.x;
+    for (int64_t base = b0 + threadIdx.x; base < b1; base += step) {
+        P v[kMergeBatch][NV];
+#pragma unroll
+        for (int u = 0; u < kMergeBatch; u++) {
+            const int64_t b = base + (int64_t)u * blockDim.x;
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                if (b < b1) v[u][k] = __ldcg(&p[k * vstride + b * pstride]);
+        }
+#pragma unroll
+        for (int u = 0; u < kMergeBatch; u++)
+            if (base + (int64_t)u * blockDim.x < b1)
+#pragma unroll
+                for (int k = 0; k < NV; k++) y[k].merge(Acc<R>::unpack(v[u][k]));
+    }
 }
 
 // Last-block-done reduction of block totals held in thread 0: every block
@@ -251,10 +286,7 @@ __device__ bool grid_commit(const Acc<R> (&blk)[NV], double* part, int stride, u
     if (!is_last) return false;
     __threadfence();
     Acc<R> y[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            y[k].merge(Acc<R>::unpack(__ldcg(&pp[k * stride + b])));
+    merge_partials<NV, R>(y, pp, stride, 1, 0, (int64_t)gridDim.x);
     block_totals<NV, R>(y, sm, out);
     if (threadIdx.x == 0) *ticket = 0u;
     return true;

@@ -1712,6 +1712,18 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary) {
     API_END
 }
 
+// Whether CG variant l runs on this handle: FEA_OK, FEA_ERR_INVALID_ARGUMENT
+// (no such variant) or FEA_ERR_UNSUPPORTED (its layout or shared memory does
+// not fit this mesh).
+static int variant_check(const fea_solver* s, int l) {
+    const bool csr = l == 4 || l == 8 || l == 16;
+    const int stages = (l == 2 || l == 6) ? 2 : (l == 3 || l == 7) ? 3 : 0;
+    if (!csr && l != 0 && l != 1 && stages == 0) return FEA_ERR_INVALID_ARGUMENT;
+    if (!csr && !s->ell.ok) return FEA_ERR_UNSUPPORTED;
+    if (s->stream_stages < stages) return FEA_ERR_UNSUPPORTED;
+    return FEA_OK;
+}
+
 int fea_autotune(fea_solver* s) {
     API_BEGIN
     check_handle(s);
@@ -1722,12 +1734,11 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[7] = {0, 1, 2, 3, 4, 8, 16};
+    const int cand[9] = {0, 1, 2, 3, 6, 7, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
-        if (l <= 3 && !s->ell.ok) continue;
-        if ((l == 2 || l == 3) && s->stream_stages < l) continue;
+        if (variant_check(s, l)) continue;
         probe_any(s, kind, l, true);
         for (int rep = 0; rep < 23; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, s->stream));
@@ -1751,11 +1762,14 @@ int fea_autotune(fea_solver* s) {
 int fea_set_cg_variant(fea_solver* s, int variant) {
     API_BEGIN
     check_handle(s);
-    if (variant < 0 || (variant > 3 && variant != 4 && variant != 8 && variant != 16))
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 8 or 16");
-    if (variant <= 3 && !s->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable on this mesh");
-    if ((variant == 2 || variant == 3) && s->stream_stages < variant)
-        return fail(FEA_ERR_UNSUPPORTED, "streamed tiles exceed the shared memory on this mesh");
+    switch (variant_check(s, variant)) {
+    case FEA_ERR_INVALID_ARGUMENT:
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 6, 7, 8 or 16");
+    case FEA_ERR_UNSUPPORTED:
+        return fail(FEA_ERR_UNSUPPORTED, s->ell.ok ? "streamed tiles exceed the shared memory on this mesh"
+                                                   : "tile-ELL layout unavailable on this mesh");
+    default: break;
+    }
     s->lanes = variant;
     API_END
 }
