@@ -382,8 +382,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     iters = st1.total_iterations - st0.total_iterations
-    # per step: rhs, 2 x init, refine, stepctl; one kernel per CG iteration; per call: start, final check
-    launches = args.steps * 5 + iters + 2 * args.steps
+    # per step: rhs, 2 x init, refine, stepctl; the CG iteration kernels (counted on the device,
+    # with the copies that close an unrolled loop pass); per call: start, final check
+    launches = args.steps * 5 + (st1.cg_launches - st0.cg_launches) + 2 * args.steps
     value = world * args.steps / (total_ms / 1000.0)
 
     # one K-step graph launch (no flush between steps) for reference

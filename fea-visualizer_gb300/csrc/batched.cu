@@ -60,6 +60,7 @@ struct BCtl {
     long long steps_left, steps_done;
     int iter;             // CG iteration of the running solve loop: buffer parity
     int n_next;           // (instance, field) solves left active by this phase
+    int live;             // the same count after the last phase that ended
     unsigned int ticket;  // blocks finished in this phase
     int refine;
     double tol;
@@ -151,6 +152,7 @@ __device__ void phase_end(const BArgs<R>& a, int iter_mode) {
         __threadfence();
         BCtl* c = a.ctl;
         const int n = atomicExch(&c->n_next, 0);
+        c->live = n;
         c->ticket = 0u;
         if (iter_mode == kIterNext) c->iter = c->iter + 1;
         if (iter_mode == kIterReset) c->iter = 0;
@@ -169,6 +171,18 @@ __device__ __forceinline__ void raise_inst(BInst* s, unsigned int f) {
 template <typename R>
 __device__ __forceinline__ int iter_of(const BArgs<R>& a) {
     return ((const volatile BCtl*)a.ctl)->iter;
+}
+
+// The CG loop body chains kBatchUnroll iteration kernels (each pass of a
+// graph WHILE loop costs a few microseconds of relaunch).  A kernel that
+// finds no solve left running is one of the extra copies of the last pass:
+// it leaves the state alone and only confirms the loop's end.
+constexpr int kBatchUnroll = 4;
+template <typename R>
+__device__ __forceinline__ bool batch_stopped(const BArgs<R>& a) {
+    if (a.probe || ((const volatile BCtl*)a.ctl)->live > 0) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+    return true;
 }
 
 // Right-hand side b = M (x/dt + f(x)) of every unfrozen instance, initial
@@ -290,6 +304,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a
 // One Chronopoulos-Gear iteration of every instance that still iterates.
 template <typename R, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a) {
+    if (batch_stopped(a)) return;
     __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
     __shared__ FV<R, 2> ut[kTile];
     __shared__ typename Acc<R>::Packed red[32 * kNV];
@@ -373,6 +388,7 @@ __global__ void __launch_bounds__(kBlock) kb_init_ell(BArgs<R> a) {
 
 template <typename R, int KPRE>
 __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
+    if (batch_stopped(a)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
     __shared__ typename Acc<R>::Packed red[32 * kNV];
@@ -713,8 +729,14 @@ struct BGrids {
     }
 };
 
-// start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter } -> refine -> init
-//          -> WHILE(cg2) { iter } -> stepctl } -> final_check
+template <typename R>
+void add_batch_iterations(cudaGraph_t body, void (*iter)(BArgs<R>), int grid, const BArgs<R>& a, size_t smem) {
+    cudaGraphNode_t n = nullptr;
+    for (int u = 0; u < kBatchUnroll; u++) n = add_kernel(body, n, iter, grid, kBlock, a, smem);
+}
+
+// start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter x 4 } -> refine -> init
+//          -> WHILE(cg2) { iter x 4 } -> stepctl } -> final_check
 template <typename R, int WCH>
 void build_batch_graph_t(fea_batch* B) {
     BLoop<R> L(make_bargs<R>(B), B->flags, 1);
@@ -735,11 +757,11 @@ void build_batch_graph_t(fea_batch* B) {
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem);
+    add_batch_iterations(body1, K::iter, g.iter, L.a1, g.smem);
     s = add_kernel(step_body, s, kb_refine<R>, g.rhs, kBlock, L.a2);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem);
+    add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem);
     add_kernel(step_body, s, kb_stepctl<R>, 1, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
     G.lanes = WCH;

@@ -7,9 +7,9 @@
 // iterations.  The compute-shader path (cgm.glsl:104-149, GPUSolver.cpp:326-361)
 // runs the same recurrences with a host round trip per stage; here the loop is
 // a CUDA graph WHILE node over time steps with a WHILE node per solve whose
-// body is ONE kernel per CG iteration (the Chronopoulos-Gear form below): the
-// vector updates are fused into the SpMV, and a single grid-wide reduction
-// gives every scalar of the next iteration.
+// body chains eight copies of ONE kernel per CG iteration (the Chronopoulos-
+// Gear form below): the vector updates are fused into the SpMV, and a single
+// grid-wide reduction gives every scalar of the next iteration.
 // Inner products: FP32 products are accumulated as float-float pairs (about
 // 48 significant bits) per thread, warp, block and grid, and the CG scalars
 // are updated in float-float arithmetic too: the GB300's FP64 pipe is narrow
@@ -36,6 +36,20 @@ __device__ __forceinline__ bool grid_reduce(Acc<R> (&acc)[NV], double* part, int
     Acc<R> blk[NV];
     block_totals<NV, R>(acc, sm, blk);
     return grid_commit<NV, R>(blk, part, stride, ticket, sm, out);
+}
+
+// The loop body holds kLoopUnroll iteration kernels, since every pass of a
+// graph WHILE loop costs a few microseconds of relaunch; a kernel that finds
+// every field of its solve stopped is one of the extra copies of the last
+// pass: it leaves the state alone and only confirms the loop's end.
+constexpr int kLoopUnroll = 8;
+template <typename R, int NF>
+__device__ __forceinline__ bool solve_stopped(const StepArgs<R, NF>& a, const PhaseCtl<R, NF>& c) {
+    if (a.probe) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.run->cg_launches += 1;
+    if (c.any) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+    return true;
 }
 
 // Threads are grouped LANES per CSR row; a warp covers 32/LANES consecutive
@@ -103,6 +117,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
+    if (solve_stopped(a, c)) return;
     CgVecs<R, NF> v;
     v.rp = a.rp;
     v.col = a.col;
@@ -187,6 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
+    if (solve_stopped(a, c)) return;
     CgVecs<R, NF> v;
     v.rp = a.rp;
     v.col = a.col;
@@ -285,6 +301,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     const StageLayout<R, NF> L(a.emax, a.hmax);
     PhaseCtl<R, NF> c;
     c.load(a.cg);
+    if (solve_stopped(a, c)) return;
     CgVecs<R, NF> v;
     v.rp = a.rp;
     v.col = a.col;
@@ -832,8 +849,16 @@ struct LoopArgs {
     }
 };
 
-// Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter }
-//              -> refine -> init -> WHILE(cg2) { iter } -> [post] -> stepctl }
+// A CG loop body: kLoopUnroll iteration kernels in a chain.
+template <typename R, int NF>
+void add_iterations(cudaGraph_t body, void (*iter)(StepArgs<R, NF>), int grid, const StepArgs<R, NF>& a,
+                    size_t smem) {
+    cudaGraphNode_t n = nullptr;
+    for (int u = 0; u < kLoopUnroll; u++) n = add_kernel(body, n, iter, grid, kBlock, a, smem);
+}
+
+// Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter x 8 }
+//              -> refine -> init -> WHILE(cg2) { iter x 8 } -> [post] -> stepctl }
 //              -> final_check
 template <typename R, int NF, int EQ, int WCH>
 void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
@@ -854,11 +879,11 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_kernel(body1, nullptr, K::iter, g.iter, kBlock, L.a1, g.smem_iter);
+    add_iterations(body1, K::iter, g.iter, L.a1, g.smem_iter);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_kernel(body2, nullptr, K::iter, g.iter, kBlock, L.a2, g.smem_iter);
+    add_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);

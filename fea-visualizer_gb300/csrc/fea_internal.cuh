@@ -121,6 +121,7 @@ struct CgState {
 
 struct RunState {
     long long steps_left, steps_done, total_iters;
+    long long cg_launches;  // iteration kernels run (timing probes excluded)
     unsigned int flags;
     int last_iters[2];
     double last_rel[2];
@@ -172,6 +173,7 @@ struct StepArgs {
     cudaGraphConditionalHandle cond;  // loop condition set by this kernel (graph mode)
     int* cont;              // the same condition, also stored here for host-driven loops
     int use_graph;          // 1: kernels run as graph nodes and set `cond`
+    int probe;              // 1: a timing probe (iterates with every field masked)
 };
 
 // Loop-condition slots in device memory for host-driven (stream) execution.

@@ -688,6 +688,7 @@ StepArgs<R, NF> probe_args(fea_solver* s, int kind) {
     set_x<R, NF>(s, a, kind);
     a.cont = &s->d_flags->probe;
     a.use_graph = 0;
+    a.probe = 1;
     return a;
 }
 
@@ -1655,6 +1656,7 @@ int fea_get_status(fea_solver* s, fea_status* out) {
     out->last_rel_residual[1] = r.last_rel[1];
     out->steps_done = r.steps_done;
     out->total_iterations = r.total_iters;
+    out->cg_launches = r.cg_launches;
     API_END
 }
 

@@ -65,6 +65,7 @@ class Status(C.Structure):
     _fields_ = [
         ("flags", C.c_uint32), ("last_iterations", C.c_int32 * 2),
         ("last_rel_residual", C.c_double * 2), ("steps_done", C.c_int64), ("total_iterations", C.c_int64),
+        ("cg_launches", C.c_int64),
     ]
 
 

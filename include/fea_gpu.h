@@ -126,6 +126,8 @@ typedef struct {
     double last_rel_residual[2]; /* |r| / |b| at exit of that solve */
     int64_t steps_done;          /* steps completed by the last fea_advance_time */
     int64_t total_iterations;    /* CG iterations summed over all solves */
+    int64_t cg_launches;         /* CG iteration kernels launched, including the copies
+                                    that close an unrolled loop pass without iterating */
 } fea_status;
 
 typedef struct fea_solver fea_solver;

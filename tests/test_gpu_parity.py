@@ -270,6 +270,35 @@ def test_step_determinism(fea):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("variant", [2, 4])
+def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
+    """The step graph chains 8 iteration kernels per pass of each CG loop; the
+    copies that run after a solve has stopped change nothing.  The same steps
+    launched kernel by kernel (loop conditions read on the host) give the
+    same fields bit for bit and the same iteration counts, and launch exactly
+    one kernel per iteration."""
+    xyz, tri = mg.jittered_grid(65, seed=2)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=1, side=0.1)
+    res = {}
+    for mode in ("graph", "stream"):
+        if mode == "stream":
+            monkeypatch.setenv("FEA_LAUNCH_MODE", "stream")
+        else:
+            monkeypatch.delenv("FEA_LAUNCH_MODE", raising=False)
+        s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=1.0,
+                    rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+        s.set_cg_variant(variant)
+        s.set_fields(u0, v0)
+        s.advance_time(4)
+        st = s.status()
+        res[mode] = (s.get_fields(), st.total_iterations, st.cg_launches, list(st.last_iterations))
+    (fg, ig, lg, lig), (fs, is_, ls, lis) = res["graph"], res["stream"]
+    assert np.array_equal(fg[0], fs[0]) and np.array_equal(fg[1], fs[1])
+    assert ig == is_ and lig == lis and ig > 0
+    assert ls == is_
+    assert ig <= lg <= ig + 4 * 2 * 7  # 4 steps, 2 solve loops each, at most 7 stopped copies per loop
+
+
 def test_autotune_choice_is_valid(fea):
     xyz, tri = mg.jittered_grid(129, seed=1)
     s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
