@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_init(BArgs<R> a
 // One Chronopoulos-Gear iteration of every instance that still iterates.
 template <typename R, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a) {
+    grid_dependency_wait();
     if (batch_stopped(a)) return;
     __shared__ FV<R, 2> sm[kBlock / 32][32 * WCH];
     __shared__ FV<R, 2> ut[kTile];
@@ -339,6 +340,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a
                 atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
         }
     }
+    grid_launch_dependents();
     phase_end(a, kIterNext);
 }
 
@@ -388,6 +390,7 @@ __global__ void __launch_bounds__(kBlock) kb_init_ell(BArgs<R> a) {
 
 template <typename R, int KPRE>
 __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
+    grid_dependency_wait();
     if (batch_stopped(a)) return;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, 2>* ut = reinterpret_cast<FV<R, 2>*>(dyn_smem);
@@ -426,6 +429,7 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
                 atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
         }
     }
+    grid_launch_dependents();
     phase_end(a, kIterNext);
 }
 
@@ -729,10 +733,15 @@ struct BGrids {
     }
 };
 
+// The iteration kernels of a loop pass, chained by programmatic edges.
 template <typename R>
 void add_batch_iterations(cudaGraph_t body, void (*iter)(BArgs<R>), int grid, const BArgs<R>& a, size_t smem) {
-    cudaGraphNode_t n = nullptr;
-    for (int u = 0; u < kBatchUnroll; u++) n = add_kernel(body, n, iter, grid, kBlock, a, smem);
+    cudaGraphNode_t prev = nullptr;
+    for (int u = 0; u < kBatchUnroll; u++) {
+        cudaGraphNode_t n = add_kernel(body, nullptr, iter, grid, kBlock, a, smem);
+        if (prev) add_programmatic_edge(body, prev, n);
+        prev = n;
+    }
 }
 
 // start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter x 4 } -> refine -> init

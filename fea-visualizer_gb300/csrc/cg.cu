@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ FV<R, NF> ut[kBlock];
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
+    grid_dependency_wait();
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     if (solve_stopped(a, c)) return;
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_iter(StepAr
     Acc<R> dots[3 * NF];  // gamma', delta', |r'|^2
     for (int64_t tile0 = blockIdx.x * (int64_t)kBlock; tile0 < a.N; tile0 += (int64_t)gridDim.x * kBlock)
         cgcg_tile<R, NF, WCH>(v, c, tile0, a.N, sm[wib], ut, dots);
+    grid_launch_dependents();
     Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -200,6 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
+    grid_dependency_wait();
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     if (solve_stopped(a, c)) return;
@@ -220,6 +223,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
         cgcg_tile_ell<R, NF, KPRE>(v, e, c, tile, ref, a.N, buf, dots);
     });
+    grid_launch_dependents();
     Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
     if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
@@ -279,6 +283,33 @@ __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const 
     for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
 }
 
+// The first copies of a stage in two parts: the tile's operator entries
+// (constant through a solve; issued before the dependency wait) raise the
+// expected bytes without arriving, and its rows of r, w, s, D^-1, x and p
+// arrive with theirs once the previous iteration's vectors are visible.
+template <typename R, int NF>
+__device__ void stage_entries(unsigned char* S, const StageLayout<R, NF>& L, const StepArgs<R, NF>& a, int32_t e0,
+                              int32_t e1) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(S + L.bar);
+    const uint32_t nA = (uint32_t)(e1 - e0) * (uint32_t)sizeof(FV<R, NF>);
+    const uint32_t nL = (uint32_t)(e1 - e0) * 2u;
+    if (!nA) return;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, nA + nL);
+    bulk_g2s(S + L.A, a.As + e0, nA, bar);
+    bulk_g2s(S + L.L, a.lcol + e0, nL, bar);
+}
+template <typename R, int NF>
+__device__ void stage_rows(unsigned char* S, const StageLayout<R, NF>& L, const CgVecs<R, NF>& v, int64_t tile) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(S + L.bar);
+    const uint32_t nV = (uint32_t)kTileRows * (uint32_t)sizeof(FV<R, NF>);
+    mbar_arrive_expect_tx(bar, 6 * nV);
+    const int64_t r0 = tile * kTileRows;
+    const FV<R, NF>* src[6] = {v.r0 + r0, v.w0 + r0, v.s0 + r0, v.dinv + r0, v.x + r0, v.p + r0};
+#pragma unroll
+    for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
+}
+
 // Thread t's halo slot: slots are dealt round-robin over the warps, so every
 // warp stages about the same share of a tile's halo.
 __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
@@ -299,22 +330,6 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
     __shared__ int armed[NS];
     const StageLayout<R, NF> L(a.emax, a.hmax);
-    PhaseCtl<R, NF> c;
-    c.load(a.cg);
-    if (solve_stopped(a, c)) return;
-    CgVecs<R, NF> v;
-    v.rp = a.rp;
-    v.col = a.col;
-    v.A = a.A;
-    v.dinv = a.dinv;
-    v.x = a.x;
-    v.p = a.pp[0];
-    v.r0 = a.rb[c.par];
-    v.w0 = a.wb[c.par];
-    v.s0 = a.sb[c.par];
-    v.r1 = a.rb[c.par ^ 1];
-    v.w1 = a.wb[c.par ^ 1];
-    v.s1 = a.sb[c.par ^ 1];
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int64_t ntiles = ceil_div(a.N, kTileRows), G = gridDim.x, t0 = blockIdx.x;
     auto stage = [&](int b) { return dyn_smem + (size_t)b * L.bytes; };
@@ -348,6 +363,10 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
         }
     };
+    // Before the dependency wait, only what no earlier kernel writes: the
+    // stages' barriers, the first tiles' operator entries (bulk copies) and
+    // the tile references.  Under a programmatic launch this overlaps the end
+    // of the previous iteration.
     if (t == 0) {
         for (int b = 0; b < NS; b++) {
             mbar_init(bar_of(b), 1);
@@ -358,14 +377,9 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
             if (t0 + b * G < ntiles) {
                 int32_t e0, e1;
                 entries(t0 + b * G, e0, e1);
-                stage_tile(stage(b), L, a, v, t0 + b * G, e0, e1);
+                stage_entries(stage(b), L, a, e0, e1);
                 armed[b] = 1;
             }
-    }
-    // the first tile's halo, straight into stage 0 (every slot, also beyond 256)
-    if (t0 < ntiles) {
-        const int32_t h0 = a.halo_off[t0], h1 = a.halo_off[t0 + 1];
-        for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
     }
     // pipeline registers: halo column and count of the next tile, halo head
     // of the tile after next, this tile's slice, and (thread 0) the entry
@@ -379,11 +393,42 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     halo_head(t0 + 2 * G, hh0, hhc);
     slice_ref(t0, sb, sw);
     if (t == 0) entries(t0 + NS * G, re0, re1);
+    grid_dependency_wait();
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    if (solve_stopped(a, c)) {
+        if (t == 0)  // the entry copies land before the block exits
+            for (int b = 0; b < NS; b++)
+                if (armed[b]) {
+                    mbar_arrive(bar_of(b));
+                    mbar_wait(bar_of(b), 0u);
+                }
+        return;
+    }
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[c.par];
+    v.w0 = a.wb[c.par];
+    v.s0 = a.sb[c.par];
+    v.r1 = a.rb[c.par ^ 1];
+    v.w1 = a.wb[c.par ^ 1];
+    v.s1 = a.sb[c.par ^ 1];
+    if (t == 0)
+        for (int b = 0; b < NS; b++)
+            if (armed[b]) stage_rows(stage(b), L, v, t0 + b * G);
+    // the first tile's halo, straight into stage 0 (every slot, also beyond 256)
+    if (t0 < ntiles) {
+        const int32_t h0 = a.halo_off[t0], h1 = a.halo_off[t0 + 1];
+        for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
+    }
     __syncthreads();
     Acc<R> dots[3 * NF];
-    uint32_t phase[NS];
-#pragma unroll
-    for (int b = 0; b < NS; b++) phase[b] = 0u;
+    uint32_t phases = 0u;  // bit b: parity of stage b's next phase (a register, not a local array)
     bool ok = true;
     int b = 0;
     int64_t refill = -1;  // LATE: tile whose stage (the previous one) thread 0 refills next
@@ -407,8 +452,8 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         slice_ref(tile + G, sb2, sw2);
         const int32_t ce0 = re0, ce1 = re1;
         if (t == 0) entries((LATE ? tile : tile + G) + NS * G, re0, re1);  // the next refill
-        const bool got = mbar_wait(bar_of(b), phase[b]);
-        phase[b] ^= 1u;
+        const bool got = mbar_wait(bar_of(b), (phases >> b) & 1u);
+        phases ^= 1u << b;
         if (!__syncthreads_and(got)) {
             ok = false;
             break;
@@ -496,11 +541,12 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
         sw = sw2;
         b = bn;
     }
+    grid_launch_dependents();
     if (!ok) {
         if (t == 0) {
             atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
             for (int q = 0; q < NS; q++)  // copies still in flight land before the block exits
-                if (armed[q]) mbar_wait(bar_of(q), phase[q]);
+                if (armed[q]) mbar_wait(bar_of(q), (phases >> q) & 1u);
         }
         __syncthreads();
     }
@@ -849,12 +895,18 @@ struct LoopArgs {
     }
 };
 
-// A CG loop body: kLoopUnroll iteration kernels in a chain.
+// A CG loop body: kLoopUnroll iteration kernels in a chain whose edges are
+// programmatic, so that each launch is scheduled while the previous one
+// finishes its reduction (the kernels wait for it before reading its output).
 template <typename R, int NF>
 void add_iterations(cudaGraph_t body, void (*iter)(StepArgs<R, NF>), int grid, const StepArgs<R, NF>& a,
                     size_t smem) {
-    cudaGraphNode_t n = nullptr;
-    for (int u = 0; u < kLoopUnroll; u++) n = add_kernel(body, n, iter, grid, kBlock, a, smem);
+    cudaGraphNode_t prev = nullptr;
+    for (int u = 0; u < kLoopUnroll; u++) {
+        cudaGraphNode_t n = add_kernel(body, nullptr, iter, grid, kBlock, a, smem);
+        if (prev) add_programmatic_edge(body, prev, n);
+        prev = n;
+    }
 }
 
 // Step graph:  start -> WHILE(step) { rhs -> init -> WHILE(cg1) { iter x 8 }

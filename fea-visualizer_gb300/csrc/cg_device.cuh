@@ -146,6 +146,15 @@ __device__ __forceinline__ bool ff_less(const FF& a, const FF& b) {
     return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
 }
 
+// Programmatic dependent launch.  wait: block until the kernel this one
+// depends on programmatically has completed and its memory is visible (a
+// no-op without such a dependency).  launch_dependents: this block no longer
+// holds back the launch of kernels that depend on this one.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Loop condition: stored for host-driven loops, and set on the graph's
 // conditional node when the kernel runs inside the step graph.  Called by one
 // thread only (concurrent cudaGraphSetConditional calls are undefined).
@@ -818,6 +827,16 @@ cudaGraphNode_t add_kernel(cudaGraph_t g, cudaGraphNode_t dep, void (*fn)(P...),
     cudaGraphNode_t n;
     FEA_CUDA_TRY(cudaGraphAddKernelNode(&n, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp));
     return n;
+}
+
+// from -> to as a programmatic dependency: `to` may be scheduled once every
+// block of `from` has called grid_launch_dependents (or exited); it reads
+// what `from` wrote only after grid_dependency_wait.
+inline void add_programmatic_edge(cudaGraph_t g, cudaGraphNode_t from, cudaGraphNode_t to) {
+    cudaGraphEdgeData ed = {};
+    ed.from_port = cudaGraphKernelNodePortProgrammatic;
+    ed.type = cudaGraphDependencyTypeProgrammatic;
+    FEA_CUDA_TRY(cudaGraphAddDependencies(g, &from, &to, &ed, 1));
 }
 
 cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraph_t* body) {
