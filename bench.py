@@ -108,6 +108,12 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (read + write) per in-loop launch of the CG iteration kernel, by
+# variant: the mean of five consecutive launches of the same workload in one
+# ncu capture without cache control (profiles/k_cgcg_iter_stream_gray_scott_1024.md).
+IN_LOOP_TRAFFIC = {7: 167.2e6}
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -493,7 +499,10 @@ def main():
                               "one_launch_ms_per_step": one_launch_ms / args.steps}),
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": 4 * V},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": IN_LOOP_TRAFFIC.get(lanes),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, in-loop launches, "
+                                           "--cache-control none" if lanes in IN_LOOP_TRAFFIC else
+                                           "no capture of this variant",
                          "kernel": "k_cgcg_iter (one CG iteration: paired u,v SpMV with fused vector updates)",
                          "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": iter_ms,
                          "ms_per_launch_how": "in the step graph: pinned iteration counts "
