@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -65,7 +66,9 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        # raw samples: a temporary file unless FEA_CLOCKS_DIR names a folder to keep them in
+        self.path = os.path.join(os.environ.get("FEA_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"fea_clocks_rank{index}.csv")
 
     def __enter__(self):
         try:
