@@ -393,7 +393,22 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     halo_head(t0 + 2 * G, hh0, hhc);
     slice_ref(t0, sb, sw);
     if (t == 0) entries(t0 + NS * G, re0, re1);
+    int32_t fh0, fcnt;  // the first tile's halo; this thread's slot t of it
+    halo_head(t0, fh0, fcnt);
+    const int32_t fcol = t < fcnt ? a.halo_col[fh0 + t] : -1;
     grid_dependency_wait();
+    // the slot's operands from both parity buffers, in flight with the state
+    // load that tells which parity is current
+    FV<R, NF> fr[2], fw[2], fs[2], fd;
+    if (fcol >= 0) {
+        fd = ldv(a.dinv + fcol, false);
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            fr[q] = ldv(a.rb[q] + fcol, false);
+            fw[q] = ldv(a.wb[q] + fcol, false);
+            fs[q] = ldv(a.sb[q] + fcol, false);
+        }
+    }
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     if (solve_stopped(a, c)) {
@@ -421,11 +436,15 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     if (t == 0)
         for (int b = 0; b < NS; b++)
             if (armed[b]) stage_rows(stage(b), L, v, t0 + b * G);
-    // the first tile's halo, straight into stage 0 (every slot, also beyond 256)
-    if (t0 < ntiles) {
-        const int32_t h0 = a.halo_off[t0], h1 = a.halo_off[t0 + 1];
-        for (int32_t h = h0 + t; h < h1; h += kBlock) ut_of(0)[kTileRows + (h - h0)] = cg_u_at(v, c, a.halo_col[h]);
+    // the first tile's halo, straight into stage 0 (slots beyond 256 directly)
+    if (fcol >= 0) {
+        const bool q = c.par != 0;  // selects, not a dynamic index (keeps the pairs in registers)
+        const FV<R, NF> ro = q ? fr[1] : fr[0], wo = q ? fw[1] : fw[0], so = q ? fs[1] : fs[0];
+        FV<R, NF> sn, rn, u2;
+        cg_advance(c, ro, wo, c.need_old ? so : wo, fd, sn, rn, u2);
+        ut_of(0)[kTileRows + t] = u2;
     }
+    for (int32_t h = kBlock + t; h < fcnt; h += kBlock) ut_of(0)[kTileRows + h] = cg_u_at(v, c, a.halo_col[fh0 + h]);
     __syncthreads();
     Acc<R> dots[3 * NF];
     uint32_t phases = 0u;  // bit b: parity of stage b's next phase (a register, not a local array)
