@@ -88,6 +88,10 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
     __shared__ typename Acc<R>::Packed red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
+    if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
+        if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+        return;
+    }
     FV<R, NF>* w = a.wb[c.par];
     const int wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -177,6 +181,10 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     __shared__ typename Acc<R>::Packed red[32 * NF];
     PhaseCtl<R, NF> c;
     c.load(a.cg);
+    if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
+        if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+        return;
+    }
     FV<R, NF>* w = a.wb[c.par];
     Acc<R> dot[NF];
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
