@@ -304,6 +304,17 @@ def bench_batched(F, steps, warmup, plain_steps):
                       "every CG iteration touches more than the L2 size (~0.6 GB)"}
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The largest of the ranks' values: a replica job takes as long as its
+    slowest rank.  Without a process group, the value itself."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads):
     """The reference's Eigen-semantics CPU step (the oracle's FP32 port):
     A = M/dt + D K rebuilt every step, zero initial guess, tol = FLT_EPSILON."""
@@ -415,10 +426,7 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
     st1 = s.status()
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, "cuda")
     iters = st1.total_iterations - st0.total_iterations
     # per step: rhs, 2 x init, refine, stepctl; the CG iteration kernels (counted on the device,
     # with the copies that close an unrolled loop pass); per call: start, final check
@@ -472,7 +480,7 @@ def main():
         F.binding.check(lib.fea_advance_time(s._h, 1))
         F.binding.check(lib.fea_get_values(s._h, C.c_void_p(outv.ctypes.data)))
         vals[:] = outv
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     e2e = world * args.steps / e2e_s
 
     flags = s.status().flags
