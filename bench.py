@@ -449,7 +449,7 @@ def main():
     spmv_warm_ms = s.time_spmv(reps=20, flush_l2=False)
     # every CG kernel variant on the same operator (L2 flushed), then back to the autotuned one
     variant_ms = {}
-    for var in (0, 1, 2, 3, 6, 7, 4, 8, 16):
+    for var in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16):
         try:
             s.set_cg_variant(var)
         except F.FeaError:

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepAr
         if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
         return;
     }
-    FV<R, NF>* w = a.wb[c.par];
+    FV<R, NF>* w = a.wb[a.defer ? 0 : c.par];
     const int wib = threadIdx.x >> 5;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
         return;
     }
-    FV<R, NF>* w = a.wb[c.par];
+    FV<R, NF>* w = a.wb[a.defer ? 0 : c.par];
     Acc<R> dot[NF];
     ell_tiles(a, ut, [&](const EllView<R, NF>& e, int64_t tile, const EllTileRef& ref, FV<R, NF>* buf) {
         init_tile_ell<R, NF, KPRE>(e, a.z, w, tile, ref, a.N, buf, dot);
@@ -332,7 +332,7 @@ __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3)
 // end of the tile that used it.  LATE = true: after the next tile's first
 // barrier, which already orders every read of the stage before the refill;
 // two barriers per tile.
-template <typename R, int NF, int NS, bool LATE>
+template <typename R, int NF, int NS, bool LATE, bool DEFER>
 __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ typename Acc<R>::Packed red[32 * 3 * NF];
@@ -405,29 +405,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     halo_head(t0, fh0, fcnt);
     const int32_t fcol = t < fcnt ? a.halo_col[fh0 + t] : -1;
     grid_dependency_wait();
-    // the slot's operands from both parity buffers, in flight with the state
-    // load that tells which parity is current
-    FV<R, NF> fr[2], fw[2], fs[2], fd;
-    if (fcol >= 0) {
-        fd = ldv(a.dinv + fcol, false);
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            fr[q] = ldv(a.rb[q] + fcol, false);
-            fw[q] = ldv(a.wb[q] + fcol, false);
-            fs[q] = ldv(a.sb[q] + fcol, false);
-        }
-    }
     PhaseCtl<R, NF> c;
-    c.load(a.cg);
-    if (solve_stopped(a, c)) {
-        if (t == 0)  // the entry copies land before the block exits
-            for (int b = 0; b < NS; b++)
-                if (armed[b]) {
-                    mbar_arrive(bar_of(b));
-                    mbar_wait(bar_of(b), 0u);
-                }
-        return;
-    }
     CgVecs<R, NF> v;
     v.rp = a.rp;
     v.col = a.col;
@@ -435,22 +413,131 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     v.dinv = a.dinv;
     v.x = a.x;
     v.p = a.pp[0];
-    v.r0 = a.rb[c.par];
-    v.w0 = a.wb[c.par];
-    v.s0 = a.sb[c.par];
-    v.r1 = a.rb[c.par ^ 1];
-    v.w1 = a.wb[c.par ^ 1];
-    v.s1 = a.sb[c.par ^ 1];
-    if (t == 0)
-        for (int b = 0; b < NS; b++)
-            if (armed[b]) stage_rows(stage(b), L, v, t0 + b * G);
-    // the first tile's halo, straight into stage 0 (slots beyond 256 directly)
-    if (fcol >= 0) {
-        const bool q = c.par != 0;  // selects, not a dynamic index (keeps the pairs in registers)
-        const FV<R, NF> ro = q ? fr[1] : fr[0], wo = q ? fw[1] : fw[0], so = q ? fs[1] : fs[0];
-        FV<R, NF> sn, rn, u2;
-        cg_advance(c, ro, wo, c.need_old ? so : wo, fd, sn, rn, u2);
-        ut_of(0)[kTileRows + t] = u2;
+    if constexpr (!DEFER) {
+        // the slot's operands from both parity buffers, in flight with the
+        // state load that tells which parity is current
+        FV<R, NF> fr[2], fw[2], fs[2], fd;
+        if (fcol >= 0) {
+            fd = ldv(a.dinv + fcol, false);
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                fr[q] = ldv(a.rb[q] + fcol, false);
+                fw[q] = ldv(a.wb[q] + fcol, false);
+                fs[q] = ldv(a.sb[q] + fcol, false);
+            }
+        }
+        c.load(a.cg);
+        if (solve_stopped(a, c)) {
+            if (t == 0)  // the entry copies land before the block exits
+                for (int b = 0; b < NS; b++)
+                    if (armed[b]) {
+                        mbar_arrive(bar_of(b));
+                        mbar_wait(bar_of(b), 0u);
+                    }
+            return;
+        }
+        v.r0 = a.rb[c.par];
+        v.w0 = a.wb[c.par];
+        v.s0 = a.sb[c.par];
+        v.r1 = a.rb[c.par ^ 1];
+        v.w1 = a.wb[c.par ^ 1];
+        v.s1 = a.sb[c.par ^ 1];
+        if (t == 0)
+            for (int b = 0; b < NS; b++)
+                if (armed[b]) stage_rows(stage(b), L, v, t0 + b * G);
+        // the first tile's halo, straight into stage 0 (slots beyond 256 directly)
+        if (fcol >= 0) {
+            const bool q = c.par != 0;  // selects, not a dynamic index (keeps the pairs in registers)
+            const FV<R, NF> ro = q ? fr[1] : fr[0], wo = q ? fw[1] : fw[0], so = q ? fs[1] : fs[0];
+            FV<R, NF> sn, rn, u2;
+            cg_advance(c, ro, wo, c.need_old ? so : wo, fd, sn, rn, u2);
+            ut_of(0)[kTileRows + t] = u2;
+        }
+    } else {
+        // Deferred finish.  The node's buffer parity q is static, so the
+        // rows' copies and the first halo loads start at once; meanwhile
+        // every block reads the state of parity q ^ 1 and, when the previous
+        // launch left an iteration pending, merges that launch's block
+        // partials (fixed order: every block gets the same scalars) and
+        // finishes it.  Block 0 publishes the state of parity q.
+        const int q = a.par;
+        v.r0 = a.rb[q];
+        v.w0 = a.wb[q];
+        v.s0 = a.sb[q];
+        v.r1 = a.rb[q ^ 1];
+        v.w1 = a.wb[q ^ 1];
+        v.s1 = a.sb[q ^ 1];
+        if (t == 0)
+            for (int b = 0; b < NS; b++)
+                if (armed[b]) stage_rows(stage(b), L, v, t0 + b * G);
+        FV<R, NF> fr, fw, fs, fd;
+        if (fcol >= 0) {
+            fr = ldv(v.r0 + fcol, false);
+            fw = ldv(v.w0 + fcol, false);
+            fs = ldv(v.s0 + fcol, false);
+            fd = ldv(v.dinv + fcol, false);
+        }
+        __shared__ CgState st;
+        __shared__ unsigned int sflags;
+        {
+            const int* src = reinterpret_cast<const int*>(q ? a.cg_alt : a.cg);
+            int* dst = reinterpret_cast<int*>(&st);
+            for (int k = t; k < (int)(sizeof(CgState) / 4); k += kBlock) dst[k] = __ldcg(src + k);
+        }
+        if (t == 0) sflags = 0u;
+        __syncthreads();
+        const bool had_pending = st.pending != 0;
+        if (had_pending && !a.probe) {
+            Acc<R> y[3 * NF], tot[3 * NF];
+            const auto* pp =
+                reinterpret_cast<const typename Acc<R>::Packed*>(a.part + (q ? 8 * (int64_t)a.part_stride : 0));
+            merge_partials<3 * NF, R>(y, pp, a.part_stride, 1, 0, (int64_t)gridDim.x);
+            block_totals<3 * NF, R>(y, red, tot);
+            if (t == 0) {
+                int act[NF];
+#pragma unroll
+                for (int f = 0; f < NF; f++) act[f] = st.active[f];
+                finish_cgcg<R, NF>((volatile CgState*)&st, &sflags, act, tot);
+                st.pending = 0;
+            }
+            __syncthreads();
+        }
+        c.set(st.iter, (const volatile CgState*)&st);
+        c.par = q;
+        // Only a solve's first launch iterates without finishing one: a
+        // launch that would iterate on a state with neither (an inconsistent
+        // state) stops the solve instead, so the loop always ends.
+        const bool stray = !a.probe && !had_pending && c.any && c.need_old;
+        const bool go = c.any && !stray;
+        if (t == 0 && blockIdx.x == 0 && !a.probe) {
+            a.run->cg_launches += 1;
+            if (sflags) atomicOr(&a.run->flags, sflags);
+            CgState* out = q ? a.cg : a.cg_alt;
+            const int* src = reinterpret_cast<const int*>(&st);
+            int* dst = reinterpret_cast<int*>(out);
+            for (int k = 0; k < (int)(sizeof(CgState) / 4); k++) dst[k] = src[k];
+            if (go) {  // this launch iterates; the next one finishes it
+                out->pending = 1;
+#pragma unroll
+                for (int f = 0; f < NF; f++) out->fresh[f] = 0;
+            } else if (stray) {
+#pragma unroll
+                for (int f = 0; f < NF; f++) out->active[f] = 0;
+                atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            }
+            signal_loop(a, go);
+        }
+        if (!go && !a.probe) {  // every field stopped: the stages' copies land, then the block leaves
+            if (t == 0)
+                for (int b = 0; b < NS; b++)
+                    if (armed[b]) mbar_wait(bar_of(b), 0u);
+            return;
+        }
+        if (fcol >= 0) {
+            FV<R, NF> sn, rn, u2;
+            cg_advance(c, fr, fw, c.need_old ? fs : fw, fd, sn, rn, u2);
+            ut_of(0)[kTileRows + t] = u2;
+        }
     }
     for (int32_t h = kBlock + t; h < fcnt; h += kBlock) ut_of(0)[kTileRows + h] = cg_u_at(v, c, a.halo_col[fh0 + h]);
     __syncthreads();
@@ -579,8 +666,15 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     }
     Acc<R> blk[3 * NF], tot[3 * NF];
     block_totals<3 * NF>(dots, red, blk);
-    if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0)
+    if constexpr (DEFER) {  // the block's partials of parity q; the next launch merges them
+        if (t == 0 && !a.probe) {
+            auto* pp = reinterpret_cast<typename Acc<R>::Packed*>(a.part + (a.par ? 0 : 8 * (int64_t)a.part_stride));
+#pragma unroll
+            for (int k = 0; k < 3 * NF; k++) pp[k * a.part_stride + blockIdx.x] = blk[k].pack();
+        }
+    } else if (grid_commit<3 * NF>(blk, a.part, a.part_stride, a.tickets + 1, red, tot) && threadIdx.x == 0) {
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
+    }
 }
 
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
@@ -699,6 +793,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
 #pragma unroll
         for (int f = 0; f < NF; f++)
             any |= start_solve<R>((volatile CgState*)cg, f, stop, run->tol, tot[f], tot[NF + f], tot[2 * NF + f]);
+        cg->pending = 0;
         signal_loop(a, any != 0);
     }
 }
@@ -758,7 +853,7 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                     dots[f].add_prod(rv.v[f], rv.v[f]);
                     dots[NF + f].add_prod(rv.v[f], pv.v[f]);
                 }
-                a.rb[cg->iter & 1][row] = rv;  // the restart continues the iteration parity
+                a.rb[a.defer ? 0 : (cg->iter & 1)][row] = rv;  // the restart's buffer parity
                 a.z[row] = pv;
             }
         }
@@ -879,9 +974,9 @@ struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
 // Variants 2 and 3: the streamed iteration with 2 or 3 stages, refilled
 // after a third barrier per tile; 6 and 7: the same, refilled after the next
 // tile's first barrier.  The set-up product is variant 1's.
-template <typename R, int NF, int NS, bool LATE>
+template <typename R, int NF, int NS, bool LATE, bool DEFER = false>
 struct StreamKernels : EllKernels<R, NF, 4> {
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS, LATE>;
+    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS, LATE, DEFER>;
     static size_t smem_iter(const StepArgs<R, NF>& a) { return NS * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
 };
 template <typename R, int NF>
@@ -892,6 +987,13 @@ template <typename R, int NF>
 struct CgKernels<R, NF, 6> : StreamKernels<R, NF, 2, true> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 7> : StreamKernels<R, NF, 3, true> {};
+// Variants 10 and 11: variants 2 and 7 with the deferred finish: no grid-wide
+// last-block step at the end of an iteration; the next launch merges the
+// block partials in every block and finishes the iteration at its start.
+template <typename R, int NF>
+struct CgKernels<R, NF, 10> : StreamKernels<R, NF, 2, false, true> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 11> : StreamKernels<R, NF, 3, true, true> {};
 
 template <typename R, int NF, int WCH>
 struct Grids {
@@ -925,12 +1027,17 @@ struct LoopArgs {
 // A CG loop body: kLoopUnroll iteration kernels in a chain whose edges are
 // programmatic, so that each launch is scheduled while the previous one
 // finishes its reduction (the kernels wait for it before reading its output).
+// Deferred-finish variants get node u the buffer parity u & 1 (kLoopUnroll
+// is even, so every pass starts at parity 0 as every solve does).
+static_assert(kLoopUnroll % 2 == 0, "loop passes keep the buffer parity");
 template <typename R, int NF>
 void add_iterations(cudaGraph_t body, void (*iter)(StepArgs<R, NF>), int grid, const StepArgs<R, NF>& a,
                     size_t smem) {
     cudaGraphNode_t prev = nullptr;
     for (int u = 0; u < kLoopUnroll; u++) {
-        cudaGraphNode_t n = add_kernel(body, nullptr, iter, grid, kBlock, a, smem);
+        StepArgs<R, NF> au = a;
+        au.par = a.defer ? (u & 1) : 0;
+        cudaGraphNode_t n = add_kernel(body, nullptr, iter, grid, kBlock, au, smem);
         if (prev) add_programmatic_edge(body, prev, n);
         prev = n;
     }
@@ -998,8 +1105,17 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
             K::init<<<g.spmv, kBlock, g.smem_init, st>>>(*la);
             FEA_CHECK_LAUNCH();
             while (read_flag(la->cont, st)) {
-                K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(*la);
-                FEA_CHECK_LAUNCH();
+                if (la->defer) {  // parities 0 and 1, so the final state lands in parity 1 as in the graph
+                    StepArgs<R, NF> aq = *la;
+                    for (int q = 0; q < 2; q++) {
+                        aq.par = q;
+                        K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(aq);
+                        FEA_CHECK_LAUNCH();
+                    }
+                } else {
+                    K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(*la);
+                    FEA_CHECK_LAUNCH();
+                }
             }
         }
         if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK) {
@@ -1023,6 +1139,8 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     case 3: G ? build_graph_t<R, NF, EQ, 3>(*G, a, lf) : run_stream_t<R, NF, EQ, 3>(a, lf, st); break;
     case 6: G ? build_graph_t<R, NF, EQ, 6>(*G, a, lf) : run_stream_t<R, NF, EQ, 6>(a, lf, st); break;
     case 7: G ? build_graph_t<R, NF, EQ, 7>(*G, a, lf) : run_stream_t<R, NF, EQ, 7>(a, lf, st); break;
+    case 10: G ? build_graph_t<R, NF, EQ, 10>(*G, a, lf) : run_stream_t<R, NF, EQ, 10>(a, lf, st); break;
+    case 11: G ? build_graph_t<R, NF, EQ, 11>(*G, a, lf) : run_stream_t<R, NF, EQ, 11>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -1084,6 +1202,7 @@ __global__ void k_probe_state(CgState* cg) {
         cg->falpha[f] = 0.f;
         cg->fbeta[f] = 0.f;
     }
+    cg->pending = 0;
 }
 
 template <typename R, int NF>
@@ -1108,6 +1227,8 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     case 3: probe_t<R, NF, 3>(a, st); break;
     case 6: probe_t<R, NF, 6>(a, st); break;
     case 7: probe_t<R, NF, 7>(a, st); break;
+    case 10: probe_t<R, NF, 10>(a, st); break;
+    case 11: probe_t<R, NF, 11>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;

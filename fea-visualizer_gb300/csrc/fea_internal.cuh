@@ -116,7 +116,8 @@ struct CgState {
     int iters[2];
     int iter;
     int max_iter;
-    int stop;  // this step is skipped (bad state detected at its start)
+    int stop;     // this step is skipped (bad state detected at its start)
+    int pending;  // deferred-finish kernels: the last kernel's iteration awaits its scalars
 };
 
 struct RunState {
@@ -166,8 +167,15 @@ struct StepArgs {
     int hmax, emax;
     const StepParams* prm;
     CgState* cg;
+    // Deferred-finish variants: the state is double-buffered (cg and cg_alt),
+    // the partials too (part and part + 8 * part_stride); the iteration kernel
+    // with node parity `par` reads state and partials of parity par ^ 1 and
+    // writes parity par, where parity 1 is `cg` / `part`.  Every solve's
+    // iterations then start at buffer parity 0 (defer = 1).
+    CgState* cg_alt;
+    int defer, par;
     RunState* run;
-    double* part;           // block partials [8 * part_stride]
+    double* part;           // block partials [16 * part_stride]
     int part_stride;
     unsigned int* tickets;  // [8]
     cudaGraphConditionalHandle cond;  // loop condition set by this kernel (graph mode)
@@ -218,6 +226,10 @@ size_t stream_stage_bytes(int emax, int hmax);
 constexpr size_t kStreamSmemLimit = 220 * 1024;  // per block, below the 227 KB opt-in maximum
 
 int max_grid_blocks();
+
+// CG variants whose iteration kernels finish the previous launch's iteration
+// at their start (deferred finish; see StepArgs::defer).
+constexpr bool is_deferred_variant(int l) { return l == 10 || l == 11; }
 
 // ---- adjoint of the explicit advection-diffusion step (adjoint.cu) ----------------
 // lam = M (u - t), *J = 1/2 (u - t).lam  (exact accumulators; one block-partial

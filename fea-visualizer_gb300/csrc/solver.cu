@@ -480,7 +480,9 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.emax = s->ell.emax;
     }
     a.prm = s->d_prm;
-    a.cg = s->d_cg;
+    a.cg = s->d_cg + 1;
+    a.cg_alt = s->d_cg;
+    a.defer = is_deferred_variant(s->lanes) ? 1 : 0;
     a.run = s->d_run;
     a.part = s->d_part;
     a.part_stride = max_grid_blocks();
@@ -1203,15 +1205,15 @@ void write_ply(const char* path, const PlyGeometry& g, const float* coeffs) {
 // Device partial-reduction storage sized for the widest grid.
 void alloc_run_state(fea_solver* s) {
     s->d_prm = s->run_mem.alloc<StepParams>(1);
-    s->d_cg = s->run_mem.alloc<CgState>(1);
+    s->d_cg = s->run_mem.alloc<CgState>(2);
     s->d_run = s->run_mem.alloc<RunState>(1);
-    s->d_part = s->run_mem.alloc<double>(8 * (int64_t)max_grid_blocks());
+    s->d_part = s->run_mem.alloc<double>(16 * (int64_t)max_grid_blocks());
     s->d_tickets = s->run_mem.alloc<unsigned int>(8);
     s->d_flags = s->run_mem.alloc<LoopFlags>(1);
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_flags, 0, sizeof(LoopFlags), s->stream));
     const char* mode = getenv("FEA_LAUNCH_MODE");
     s->stream_mode = mode && strcmp(mode, "stream") == 0;
-    FEA_CUDA_TRY(cudaMemsetAsync(s->d_cg, 0, sizeof(CgState), s->stream));
+    FEA_CUDA_TRY(cudaMemsetAsync(s->d_cg, 0, 2 * sizeof(CgState), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_run, 0, sizeof(RunState), s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(s->d_tickets, 0, 8 * sizeof(unsigned int), s->stream));
     FEA_CUDA_TRY(cudaMallocHost(&s->h_run, sizeof(RunState)));
@@ -1719,7 +1721,7 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary) {
 // not fit this mesh).
 static int variant_check(const fea_solver* s, int l) {
     const bool csr = l == 4 || l == 8 || l == 16;
-    const int stages = (l == 2 || l == 6) ? 2 : (l == 3 || l == 7) ? 3 : 0;
+    const int stages = (l == 2 || l == 6 || l == 10) ? 2 : (l == 3 || l == 7 || l == 11) ? 3 : 0;
     if (!csr && l != 0 && l != 1 && stages == 0) return FEA_ERR_INVALID_ARGUMENT;
     if (!csr && !s->ell.ok) return FEA_ERR_UNSUPPORTED;
     if (s->stream_stages < stages) return FEA_ERR_UNSUPPORTED;
@@ -1736,7 +1738,7 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[9] = {0, 1, 2, 3, 6, 7, 4, 8, 16};
+    const int cand[11] = {0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
@@ -1766,7 +1768,7 @@ int fea_set_cg_variant(fea_solver* s, int variant) {
     check_handle(s);
     switch (variant_check(s, variant)) {
     case FEA_ERR_INVALID_ARGUMENT:
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 6, 7, 8 or 16");
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 6, 7, 8, 10, 11 or 16");
     case FEA_ERR_UNSUPPORTED:
         return fail(FEA_ERR_UNSUPPORTED, s->ell.ok ? "streamed tiles exceed the shared memory on this mesh"
                                                    : "tile-ELL layout unavailable on this mesh");

@@ -270,13 +270,14 @@ def test_step_determinism(fea):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("variant", [2, 4])
+@pytest.mark.parametrize("variant", [2, 4, 10, 11])
 def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
     """The step graph chains 8 iteration kernels per pass of each CG loop; the
     copies that run after a solve has stopped change nothing.  The same steps
     launched kernel by kernel (loop conditions read on the host) give the
     same fields bit for bit and the same iteration counts, and launch exactly
-    one kernel per iteration."""
+    one kernel per iteration (deferred-finish variants 10 and 11: pairs of
+    launches, one more launch per solve to finish its last iteration)."""
     xyz, tri = mg.jittered_grid(65, seed=2)
     u0, v0 = mg.gray_scott_patches(xyz, seed=1, side=0.1)
     res = {}
@@ -295,15 +296,19 @@ def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
     (fg, ig, lg, lig), (fs, is_, ls, lis) = res["graph"], res["stream"]
     assert np.array_equal(fg[0], fs[0]) and np.array_equal(fg[1], fs[1])
     assert ig == is_ and lig == lis and ig > 0
-    assert ls == is_
-    assert ig <= lg <= ig + 4 * 2 * 7  # 4 steps, 2 solve loops each, at most 7 stopped copies per loop
+    if variant in (10, 11):
+        assert is_ < ls <= is_ + 4 * 2 * 2  # 4 steps, 2 solve loops each, at most 2 launches past the last iteration
+        assert ig < lg <= ig + 4 * 2 * 8
+    else:
+        assert ls == is_
+        assert ig <= lg <= ig + 4 * 2 * 7  # 4 steps, 2 solve loops each, at most 7 stopped copies per loop
 
 
 def test_autotune_choice_is_valid(fea):
     xyz, tri = mg.jittered_grid(129, seed=1)
     s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
     assert s.info.rows_per_warp_lanes == 0  # the tile-ELL layout is the default
-    assert s.autotune() in (0, 1, 2, 3, 6, 7, 4, 8, 16)
+    assert s.autotune() in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16)
     with pytest.raises(fea.FeaError):
         s.set_cg_variant(5)
 
@@ -319,7 +324,7 @@ def test_cg_variants_agree(fea, oracle_mod, name, bc):
     S = oracle_mod.System(xyz, tri, bc=bc)
     p = None
     outs = []
-    for variant in (0, 1, 2, 3, 6, 7, 4, 8, 16):
+    for variant in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16):
         s = _solver(fea, xyz, tri, bc, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-7, **kw)
         s.set_cg_variant(variant)
         s.set_fields(u0, v0)
@@ -329,7 +334,7 @@ def test_cg_variants_agree(fea, oracle_mod, name, bc):
     uo, vo, *_ = oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
                              S.gather(v0), 2, Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate,
                              reaction_mode=1)
-    for variant, (ug, vg) in zip((0, 1, 2, 3, 6, 7, 4, 8, 16), outs):
+    for variant, (ug, vg) in zip((0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16), outs):
         assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, variant
 
 
