@@ -112,9 +112,10 @@ class Clocks:
 
 
 # DRAM bytes (read + write) per in-loop launch of the CG iteration kernel, by
-# variant: the mean of five consecutive launches of the same workload in one
-# ncu capture without cache control (profiles/k_cgcg_iter_stream_gray_scott_1024.md).
-IN_LOOP_TRAFFIC = {7: 167.2e6}
+# variant: the mean of six consecutive launches of the step loop of this
+# workload in one ncu capture without cache control
+# (profiles/k_cgcg_iter_stream_gray_scott_1024.md).
+IN_LOOP_TRAFFIC = {10: 165.4e6, 11: 168.9e6}
 
 
 def measured_peak_hbm():
