@@ -218,15 +218,17 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
  * shared-memory stages by bulk asynchronous copies ahead of the tile being
  * computed, 6 and 7 = variants 2 and 3 with each stage refilled after the
  * next tile's first block barrier (two barriers per tile instead of three),
- * 4 / 8 / 16 = warp-cooperative CSR with that many entries per lane and
- * window.  fea_autotune
+ * 10 and 11 = variants 2 and 7 whose iterations are finished by the next
+ * launch (every block merges the block partials at its start) instead of
+ * by the last block to end, 4 / 8 / 16 = warp-cooperative CSR with that many
+ * entries per lane and window.  fea_autotune
  * times one CG iteration of each candidate on this mesh and keeps the
  * fastest (fea_info.rows_per_warp_lanes); the fields are left unchanged. */
 int fea_autotune(fea_solver* s);
 /* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
- * FEA_ERR_UNSUPPORTED for 0 to 3, 6 and 7 when the layout, or for the
- * streamed variants the shared memory of their stages, is unavailable on
- * this mesh). */
+ * FEA_ERR_UNSUPPORTED for 0 to 3, 6, 7, 10 and 11 when the layout, or for
+ * the streamed variants the shared memory of their stages, is unavailable
+ * on this mesh). */
 int fea_set_cg_variant(fea_solver* s, int variant);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
