@@ -263,7 +263,9 @@ class CUDASolver:
 
     def set_cg_variant(self, variant: int):
         """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 2, 3: tile-ELL streamed by bulk copies
-        (2 or 3 stages); 4, 8, 16: windowed CSR kernels."""
+        (2 or 3 stages); 6, 7: the same with two block barriers per tile; 10, 11: variants 2 and 7
+        with the deferred finish (each launch finishes the previous one's iteration); 4, 8, 16:
+        windowed CSR kernels."""
         check(load().fea_set_cg_variant(self._h, int(variant)))
 
     def stream(self) -> int:
