@@ -304,6 +304,32 @@ def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
         assert ig <= lg <= ig + 4 * 2 * 7  # 4 steps, 2 solve loops each, at most 7 stopped copies per loop
 
 
+@pytest.mark.parametrize("pair", [(2, 10), (7, 11)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_deferred_finish_bit_identical(fea, pair, precision):
+    """Variants 10 and 11 finish each iteration at the start of the next
+    launch (every block merges the block partials) instead of in the last
+    block of the launch; the partials, their merge order and the scalar
+    arithmetic are the same, so the fields match variants 2 and 7 bit for
+    bit, with the same iteration counts."""
+    xyz, tri = mg.jittered_grid(97, seed=4)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=2, side=0.1)
+    prec = fea.FP32 if precision == "fp32" else fea.FP64
+    res = []
+    for variant in pair:
+        s = _solver(fea, xyz, tri, 0, precision=prec, equation=fea.REACTION_DIFFUSION, reaction_mode=1,
+                    rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06,
+                    cg_tolerance=1e-6 if precision == "fp32" else 1e-10)
+        s.set_cg_variant(variant)
+        s.set_fields(u0, v0)
+        s.advance_time(6)
+        st = s.status()
+        res.append((s.get_fields(), st.total_iterations, list(st.last_iterations), st.flags))
+    (fa, ia, la, ga), (fb, ib, lb, gb) = res
+    assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1])
+    assert ia == ib and la == lb and ga == gb and ia > 0
+
+
 def test_autotune_choice_is_valid(fea):
     xyz, tri = mg.jittered_grid(129, seed=1)
     s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
