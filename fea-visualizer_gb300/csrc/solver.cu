@@ -361,7 +361,9 @@ void build_context(fea_solver* s) {
         const size_t stage = s->precision == FEA_FP64 ? stream_stage_bytes<double, 2>(s->ell.emax, s->ell.hmax)
                                                       : stream_stage_bytes<float, 2>(s->ell.emax, s->ell.hmax);
         s->stream_stages = !s->ell.ok ? 0 : 3 * stage <= kStreamSmemLimit ? 3 : 2 * stage <= kStreamSmemLimit ? 2 : 0;
-        s->lanes = s->ell.ok ? 0 : 8;
+        // default variant: the streamed deferred-finish kernel with as many
+        // stages as fit, else the tile-ELL kernel, else windowed CSR
+        s->lanes = !s->ell.ok ? 8 : s->stream_stages >= 3 ? 11 : s->stream_stages >= 2 ? 10 : 0;
     }
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
     s->Mloc = s->mat_mem.alloc<double>(9 * T);

@@ -212,8 +212,8 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
 
 /* CG kernel variants: 0 and 1 = tile-ELL layout (256-row tiles, 32-row
  * slices stored column-wise, operand and halo staged in shared memory; the
- * first 8 (variant 0, the default when the mesh's halos fit) or 4 (variant 1)
- * entries of each row prefetched into registers), 2 and 3 = the same layout
+ * first 8 (variant 0) or 4 (variant 1) entries of each row prefetched into
+ * registers), 2 and 3 = the same layout
  * with each tile's operator entries and row vectors moved into 2 or 3
  * shared-memory stages by bulk asynchronous copies ahead of the tile being
  * computed, 6 and 7 = variants 2 and 3 with each stage refilled after the
@@ -221,9 +221,11 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
  * 10 and 11 = variants 2 and 7 whose iterations are finished by the next
  * launch (every block merges the block partials at its start) instead of
  * by the last block to end, 4 / 8 / 16 = warp-cooperative CSR with that many
- * entries per lane and window.  fea_autotune
- * times one CG iteration of each candidate on this mesh and keeps the
- * fastest (fea_info.rows_per_warp_lanes); the fields are left unchanged. */
+ * entries per lane and window.  A new handle starts on variant 11 (10 when
+ * only two stages fit in shared memory, 0 when none do, 8 without the
+ * tile-ELL layout).  fea_autotune times one CG iteration of each candidate
+ * on this mesh and keeps the fastest (fea_info.rows_per_warp_lanes); the
+ * fields are left unchanged. */
 int fea_autotune(fea_solver* s);
 /* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
  * FEA_ERR_UNSUPPORTED for 0 to 3, 6, 7, 10 and 11 when the layout, or for
