@@ -460,18 +460,18 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     bytes_spmv = iter_bytes(N, nnz)
 
-    # end to end through the C ABI with host buffers (values = v, CPUSolver.cpp:130,144)
+    # end to end through the C ABI with a host buffer: like surface->values,
+    # one page-locked array that every step reads (set_values) and rewrites
+    # (get_values) (values = v, CPUSolver.cpp:130,144)
     hv = torch.empty(V, dtype=torch.float32).pin_memory()
-    hout = torch.empty(V, dtype=torch.float32).pin_memory()
     vals = hv.numpy()
-    outv = hout.numpy()
     lib = F.load()
     import ctypes as C
     s.set_fields(start_u, start_v)  # one untimed pass through the calls, then back to the start
     vals[:] = start_v
     F.binding.check(lib.fea_set_values(s._h, C.c_void_p(vals.ctypes.data)))
     F.binding.check(lib.fea_advance_time(s._h, 1))
-    F.binding.check(lib.fea_get_values(s._h, C.c_void_p(outv.ctypes.data)))
+    F.binding.check(lib.fea_get_values(s._h, C.c_void_p(vals.ctypes.data)))
     s.set_fields(start_u, start_v)
     vals[:] = start_v
     s.synchronize()
@@ -479,8 +479,7 @@ def main():
     for _ in range(args.steps):
         F.binding.check(lib.fea_set_values(s._h, C.c_void_p(vals.ctypes.data)))
         F.binding.check(lib.fea_advance_time(s._h, 1))
-        F.binding.check(lib.fea_get_values(s._h, C.c_void_p(outv.ctypes.data)))
-        vals[:] = outv
+        F.binding.check(lib.fea_get_values(s._h, C.c_void_p(vals.ctypes.data)))
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
     e2e = world * args.steps / e2e_s
 
