@@ -34,7 +34,7 @@ namespace {
 
 constexpr int kTile = kBlock;  // rows per tile
 constexpr int kNV = 6;         // partials per tile: 3 inner products x 2 fields
-constexpr int kLanes = 8;      // lanes per row of the once-per-step kernels
+constexpr int kLanes = 1;      // threads per row of the once-per-step kernels (1: no shuffle reductions)
 
 struct BPrm {
     double dt, F, k;

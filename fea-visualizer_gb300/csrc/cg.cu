@@ -945,7 +945,7 @@ __global__ void __launch_bounds__(kBlock) k_final_check(StepArgs<R, NF> a) {
 
 int g_max_grid = 0;
 
-constexpr int kRowLanes = 8;  // lanes per row of the once-per-step kernels
+constexpr int kRowLanes = 1;  // threads per row of the once-per-step kernels (1: no shuffle reductions)
 
 // The CG kernels of a variant: WCH > 0 the windowed CSR kernels (entries per
 // lane and window), 0 the tile-ELL kernels with their dynamic shared memory.
