@@ -118,6 +118,17 @@ class Clocks:
 IN_LOOP_TRAFFIC = {10: 165.4e6, 11: 168.9e6}
 
 
+def cg_kernel_name(variant):
+    """The CG iteration kernel that runs for a variant (fea_set_cg_variant)."""
+    if variant in (0, 1):
+        return "k_cgcg_iter_ell"
+    if variant in (2, 3, 6, 7):
+        return "k_cgcg_iter_stream"
+    if variant in (10, 11):
+        return "k_cgcg_iter_stream (deferred finish)"
+    return "k_cgcg_iter"
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -514,7 +525,8 @@ def main():
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, in-loop launches, "
                                            "--cache-control none" if lanes in IN_LOOP_TRAFFIC else
                                            "no capture of this variant",
-                         "kernel": "k_cgcg_iter (one CG iteration: paired u,v SpMV with fused vector updates)",
+                         "kernel": f"{cg_kernel_name(lanes)} (one CG iteration: paired u,v product with "
+                                   f"fused vector updates)",
                          "algorithmic_bytes_per_launch": bytes_spmv, "ms_per_launch": iter_ms,
                          "ms_per_launch_how": "in the step graph: pinned iteration counts "
                                               f"{pinned_iters[0]} and {pinned_iters[1]}, difference per iteration",
