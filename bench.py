@@ -257,6 +257,59 @@ def bench_adjoint(F):
     return out
 
 
+# Gray-Scott adjoint: the (F, k, Du, Dv) gradients on the 512 x 512 jittered grid
+GS_ADJ_GRID, GS_ADJ_STEPS, GS_ADJ_CKPT, GS_ADJ_F_TARGET = 512, 50, 10, 0.04
+
+
+def bench_gs_adjoint(F):
+    """One loss + gradients evaluation of the Gray-Scott adjoint (u0, v0, F,
+    k, Du, Dv) in FP64 and FP32, and the forward model alone.  The target is
+    the v field of the same run with the feed rate at 0.04; the loss is
+    evaluated at 0.037."""
+    import numpy as np
+    import torch
+    from fea_gb300 import meshgen as mg
+    xyz, tri = mg.jittered_grid(GS_ADJ_GRID, seed=0)
+    u0n, v0n = mg.gray_scott_patches(xyz, seed=0)
+    out = {"workload": f"gray-scott inverse problem, {GS_ADJ_GRID}x{GS_ADJ_GRID} jittered grid, mass-weighted "
+                       f"reaction, dt 1, {GS_ADJ_STEPS} steps, checkpoints every {GS_ADJ_CKPT}; loss "
+                       f"1/2 |v_N - target|_M^2 (target: feed rate {GS_ADJ_F_TARGET}, evaluated at 0.037), "
+                       f"gradients w.r.t. u0, v0, F, k, Du, Dv"}
+
+    def handle(prec, feed):
+        p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=1.0, rd_Du=2e-5,
+                             rd_Dv=1e-5, rd_feed_rate=feed, rd_kill_rate=0.06,
+                             cg_tolerance=1e-12 if prec == F.FP64 else 1e-6)
+        return F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=prec, params=p)
+
+    for name, prec in (("fp64", F.FP64), ("fp32", F.FP32)):
+        dt = torch.float64 if prec == F.FP64 else torch.float32
+        u0 = torch.tensor(u0n, dtype=dt, device="cuda")  # Neumann: unknowns are the nodes
+        v0 = torch.tensor(v0n, dtype=dt, device="cuda")
+        h = handle(prec, GS_ADJ_F_TARGET)
+        torch.cuda.synchronize()
+        h.set_fields_device(u0.data_ptr(), v0.data_ptr())
+        h.advance_time(GS_ADJ_STEPS)
+        tu, tv = torch.zeros_like(u0), torch.zeros_like(v0)
+        h.synchronize()
+        h.get_fields_device(tu.data_ptr(), tv.data_ptr())
+        h.synchronize()
+        h.close()
+        s = handle(prec, 0.037)
+        s.adjoint_gray_scott_device(u0, v0, None, tv, GS_ADJ_STEPS, GS_ADJ_CKPT)  # warm-up
+        t0 = time.perf_counter()
+        J, gu, gv, gp = s.adjoint_gray_scott_device(u0, v0, None, tv, GS_ADJ_STEPS, GS_ADJ_CKPT)
+        t1 = time.perf_counter()
+        s.adjoint_gray_scott_device(u0, v0, None, tv, GS_ADJ_STEPS, GS_ADJ_CKPT, grads=False)
+        t2 = time.perf_counter()
+        out[name] = {"loss_and_gradients_ms": 1000 * (t1 - t0), "forward_only_ms": 1000 * (t2 - t1), "loss": J,
+                     "grad_u0_norm": float(torch.linalg.norm(gu)), "grad_v0_norm": float(torch.linalg.norm(gv)),
+                     "dJ_dF": float(gp[0]), "dJ_dk": float(gp[1]), "dJ_dDu": float(gp[2]),
+                     "dJ_dDv": float(gp[3]), "status_flags": int(s.status().flags)}
+        s.close()
+    return out
+
+
 def bench_batched(F, steps, warmup, plain_steps):
     """The 256-instance sweep in one batch vs the plain loop of single-mesh
     handles (one after another, each advancing its own graph)."""
@@ -502,6 +555,7 @@ def main():
     if not args.no_batch:
         batched = bench_batched(F, args.batch_steps, 3, args.plain_steps)
     adjoint = None if args.no_adjoint else bench_adjoint(F)
+    gs_adjoint = None if args.no_adjoint else bench_gs_adjoint(F)
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -538,6 +592,7 @@ def main():
             "cpu_baseline": cpu,
             "batched": batched,
             "adjoint": adjoint,
+            "gray_scott_adjoint": gs_adjoint,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "status_flags": int(flags),
