@@ -257,6 +257,59 @@ def bench_adjoint(F):
     return out
 
 
+def _timed_steps(s, nsteps):
+    """Device time of advance_time(nsteps) on the handle's stream (CUDA events)
+    and the CG iterations it took."""
+    import torch
+    st = torch.cuda.ExternalStream(s.stream())
+    it0 = s.status().total_iterations
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        e0.record(st)
+        s.advance_time(nsteps)
+        e1.record(st)
+    s.synchronize()
+    return e0.elapsed_time(e1), s.status().total_iterations - it0
+
+
+def bench_configs(F):
+    """The other single-mesh workloads, device-timed: FP64 heat on the level-5
+    icosphere (100 steps, PCG to 1e-10) and the Newmark wave on the level-8
+    icosphere (1,000 steps, FP32)."""
+    import numpy as np
+    from fea_gb300 import meshgen as mg
+    out = {}
+    xyz, tri = mg.icosphere(5)
+    p0 = mg.sphere_point(np.random.default_rng(1))
+    u0 = np.exp(-np.sum((xyz.astype(np.float64) - p0) ** 2, axis=1) / 0.02).astype(np.float32)
+    p = F.default_params(equation=F.HEAT, heat_time_step=1e-3, heat_conductivity=1.0, cg_tolerance=1e-10)
+    s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=F.FP64, params=p)
+    s.set_fields(u0, u0)
+    s.advance_time(5)  # warm-up (graph instantiation)
+    s.set_fields(u0, u0)
+    ms, its = _timed_steps(s, 100)
+    out["heat_fp64_icosphere5"] = {
+        "workload": "heat, FP64, level-5 icosphere (10,242 vertices), kappa 1, dt 1e-3, Gaussian bump, "
+                    "Jacobi-PCG to 1e-10", "steps": 100, "ms": ms, "steps_per_s": 100 / (ms / 1000),
+        "cg_iterations_per_step": its / 100, "cg_variant": s.info.rows_per_warp_lanes}
+    s.close()
+    xyz, tri = mg.icosphere(8)
+    w0 = mg.gaussian_bumps(xyz, seed=3, n_bumps=8, width2=0.05, amplitude=(-1, 1)).astype(np.float32)
+    p = F.default_params(equation=F.WAVE, wave_time_step=2e-3, wave_c=1.0, wave_scheme=1, cg_tolerance=1e-7)
+    s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, params=p)
+    s.set_fields(w0, np.zeros_like(w0))
+    s.advance_time(5)
+    s.set_fields(w0, np.zeros_like(w0))
+    ms, its = _timed_steps(s, 1000)
+    out["wave_newmark_icosphere8"] = {
+        "workload": "wave, Newmark beta 1/4 gamma 1/2, FP32, level-8 icosphere (655,362 vertices), c 1, "
+                    "dt 2e-3, eight bumps", "steps": 1000, "ms": ms, "steps_per_s": 1000 / (ms / 1000),
+        "cg_iterations_per_step": its / 1000, "cg_variant": s.info.rows_per_warp_lanes,
+        "status_flags": int(s.status().flags)}
+    s.close()
+    return out
+
+
 # Gray-Scott adjoint: the (F, k, Du, Dv) gradients on the 512 x 512 jittered grid
 GS_ADJ_GRID, GS_ADJ_STEPS, GS_ADJ_CKPT, GS_ADJ_F_TARGET = 512, 50, 10, 0.04
 
@@ -428,6 +481,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched sweep")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint inverse-problem timing")
+    ap.add_argument("--no-configs", action="store_true", help="skip the heat and wave workload timings")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cg-variant", type=int, default=None,
@@ -556,6 +610,7 @@ def main():
         batched = bench_batched(F, args.batch_steps, 3, args.plain_steps)
     adjoint = None if args.no_adjoint else bench_adjoint(F)
     gs_adjoint = None if args.no_adjoint else bench_gs_adjoint(F)
+    configs = None if args.no_configs else bench_configs(F)
     cpu = None
     if rank == 0 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
@@ -593,6 +648,7 @@ def main():
             "batched": batched,
             "adjoint": adjoint,
             "gray_scott_adjoint": gs_adjoint,
+            "other_workloads": configs,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "status_flags": int(flags),
