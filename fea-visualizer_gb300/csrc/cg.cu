@@ -238,18 +238,20 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_ell(StepArgs<R, NF> a) {
         signal_loop(a, finish_cgcg<R, NF>(a.cg, &a.run->flags, c.act, tot));
 }
 
-// ---- variant 2: tile-ELL streamed through shared memory by bulk copies ----------
+// ---- variants 2, 3, 6, 7, 10, 11: tile-ELL streamed through shared memory -------
 //
 // Every input a tile streams is a few contiguous ranges: its operator values
 // and 16-bit local columns (the tile's slices are consecutive) and its 256
-// rows of r, w, s, D^-1, x and p.  Thread 0 moves them into one of two stages
+// rows of r, w, s, D^-1, x and p.  Thread 0 moves them into one of NS stages
 // of shared memory with bulk copies (cp.async.bulk, completing on the stage's
-// mbarrier) two tiles ahead of the tile being computed, so the block computes
-// on data already in shared memory while the next tile's data is in flight.
-// The halo operands of the next tile are gathered into registers during the
+// mbarrier) stages ahead of the tile being computed, so the block computes on
+// data already in shared memory while later tiles' data is in flight.  The
+// halo operands of the next tile are gathered into registers during the
 // current tile and staged after its product.  Every wait is bounded: on
 // expiry the kernel raises FEA_STATUS_BREAKDOWN, waits (bounded) for the
-// copies it issued and leaves the tile loop.
+// copies it issued and leaves the tile loop.  The template flags choose the
+// refill point (LATE) and how an iteration is finished (DEFER: by the next
+// launch, in every block; otherwise by this launch's last block).
 
 // Byte offsets of one stage (all 16-byte aligned).
 template <typename R, int NF>
