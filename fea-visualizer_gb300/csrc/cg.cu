@@ -284,8 +284,9 @@ __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const 
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_arrive_expect_tx(bar, nA + nL + 6 * nV);
     if (nA) {
-        bulk_g2s(S + L.A, a.As + e0, nA, bar);
-        bulk_g2s(S + L.L, a.lcol + e0, nL, bar);
+        const uint64_t pol = l2_evict_first_policy();
+        bulk_g2s_hint(S + L.A, a.As + e0, nA, bar, pol);
+        bulk_g2s_hint(S + L.L, a.lcol + e0, nL, bar, pol);
     }
     const int64_t r0 = tile * kTileRows;
     const FV<R, NF>* src[6] = {v.r0 + r0, v.w0 + r0, v.s0 + r0, v.dinv + r0, v.x + r0, v.p + r0};
@@ -306,8 +307,9 @@ __device__ void stage_entries(unsigned char* S, const StageLayout<R, NF>& L, con
     if (!nA) return;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(bar, nA + nL);
-    bulk_g2s(S + L.A, a.As + e0, nA, bar);
-    bulk_g2s(S + L.L, a.lcol + e0, nL, bar);
+    const uint64_t pol = l2_evict_first_policy();
+    bulk_g2s_hint(S + L.A, a.As + e0, nA, bar, pol);
+    bulk_g2s_hint(S + L.L, a.lcol + e0, nL, bar, pol);
 }
 template <typename R, int NF>
 __device__ void stage_rows(unsigned char* S, const StageLayout<R, NF>& L, const CgVecs<R, NF>& v, int64_t tile) {
