@@ -115,7 +115,7 @@ class Clocks:
 # variant: the mean of six consecutive launches of the step loop of this
 # workload in one ncu capture without cache control
 # (profiles/k_cgcg_iter_stream_gray_scott_1024.md).
-IN_LOOP_TRAFFIC = {10: 165.4e6, 11: 168.9e6}
+IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6}
 
 
 def cg_kernel_name(variant):
