@@ -290,8 +290,9 @@ __device__ void stage_tile(unsigned char* S, const StageLayout<R, NF>& L, const 
     }
     const int64_t r0 = tile * kTileRows;
     const FV<R, NF>* src[6] = {v.r0 + r0, v.w0 + r0, v.s0 + r0, v.dinv + r0, v.x + r0, v.p + r0};
+    const uint64_t vpol = l2_evict_last_policy();
 #pragma unroll
-    for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
+    for (int k = 0; k < 6; k++) bulk_g2s_hint(S + L.V + (size_t)k * nV, src[k], nV, bar, vpol);
 }
 
 // The first copies of a stage in two parts: the tile's operator entries
@@ -318,8 +319,9 @@ __device__ void stage_rows(unsigned char* S, const StageLayout<R, NF>& L, const 
     mbar_arrive_expect_tx(bar, 6 * nV);
     const int64_t r0 = tile * kTileRows;
     const FV<R, NF>* src[6] = {v.r0 + r0, v.w0 + r0, v.s0 + r0, v.dinv + r0, v.x + r0, v.p + r0};
+    const uint64_t vpol = l2_evict_last_policy();
 #pragma unroll
-    for (int k = 0; k < 6; k++) bulk_g2s(S + L.V + (size_t)k * nV, src[k], nV, bar);
+    for (int k = 0; k < 6; k++) bulk_g2s_hint(S + L.V + (size_t)k * nV, src[k], nV, bar, vpol);
 }
 
 // Thread t's halo slot: slots are dealt round-robin over the warps, so every

@@ -79,6 +79,13 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy() {
     return pol;
 }
 
+// An L2 policy for data the next pass reads again (the iteration's vectors).
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
 // bulk_g2s with an L2 cache policy for the source's lines.
 __device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
                                               uint64_t policy) {
