@@ -126,6 +126,10 @@ def cg_kernel_name(variant):
         return "k_cgcg_iter_stream"
     if variant in (10, 11):
         return "k_cgcg_iter_stream (deferred finish)"
+    if variant in (12, 13):
+        return "k_cgcg_iter_direct"
+    if variant in (14, 15):
+        return "k_cgcg_iter_ring"
     return "k_cgcg_iter"
 
 
@@ -568,7 +572,7 @@ def main():
     spmv_warm_ms = s.time_spmv(reps=20, flush_l2=False)
     # every CG kernel variant on the same operator (L2 flushed), then back to the autotuned one
     variant_ms = {}
-    for var in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16):
+    for var in F.CG_VARIANTS:
         try:
             s.set_cg_variant(var)
         except F.FeaError:

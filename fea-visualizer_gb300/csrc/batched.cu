@@ -97,6 +97,7 @@ struct BArgs {
     // tile-ELL copy of A (variants 0 and 1)
     const FV<R, 2>* As;
     const uint16_t* lcol;
+    const uint32_t* lcol2;  // column pairs (TileEll::lcol2)
     const int32_t* slice_off;
     const int32_t* halo_off;
     const int32_t* halo_col;
@@ -681,6 +682,7 @@ BArgs<R> make_bargs(fea_batch* B) {
     if (B->ell.ok) {
         a.As = (const FV<R, 2>*)B->As;
         a.lcol = B->ell.lcol;
+        a.lcol2 = B->ell.lcol2;
         a.slice_off = B->ell.slice_off;
         a.halo_off = B->ell.halo_off;
         a.halo_col = B->ell.halo_col;

@@ -683,6 +683,661 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     }
 }
 
+// ---- variant 12: tile-ELL with direct loads, pipelined one tile ahead -------------
+//
+// Each warp multiplies its 32-row slice of a tile from registers.  The
+// slice's operator entries and 16-bit local columns go straight from global
+// memory into the registers of the row's thread (entry k of the slice's 32
+// rows is one coalesced request), and each register takes the next tile's
+// entry as soon as the product has used it, so a whole tile of work covers the
+// DRAM latency of every entry.  The rows' r, w, s, D^-1, x, p and the operands
+// of the thread's halo slot are loaded for the next tile as soon as this
+// tile's row update and halo have used their registers; the per-tile
+// references (slice offsets, halo heads and columns) run one and two tiles
+// further ahead.  No thread copies for others: the only
+// block barrier of a tile orders its u' slice, and two u' buffers alternate
+// between consecutive tiles.  The iteration is finished by the next launch
+// (deferred finish, as variants 10 and 11), and both block reductions give
+// each value to one warp: at the start, warp k merges value k of every
+// block's partials; at the end, value k of the block's threads.
+
+// Loads of data read once per iteration (the operator entries and columns):
+// no L1 allocation, first out of the L2 (policy from l2_evict_first_policy).
+template <typename T>
+__device__ __forceinline__ T ld_once(const T* p, uint64_t pol) {
+    T o;
+    if constexpr (sizeof(T) == 4) {
+        uint32_t x;
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(x) : "l"(p), "l"(pol));
+        memcpy(&o, &x, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        uint2 x;
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
+            : "=r"(x.x), "=r"(x.y)
+            : "l"(p), "l"(pol));
+        memcpy(&o, &x, 8);
+    } else {
+        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
+        uint4 x;
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w)
+            : "l"(p), "l"(pol));
+        memcpy(&o, &x, 16);
+    }
+    return o;
+}
+__device__ __forceinline__ uint32_t ld_once_u16(const uint16_t* p, uint64_t pol) {
+    unsigned short x;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(x) : "l"(p), "l"(pol));
+    return x;
+}
+// Loads of the iteration's vectors, which the next iteration reads again:
+// kept in the L2 ahead of the operator (l2_evict_last_policy).
+template <typename T>
+__device__ __forceinline__ T ld_keep(const T* p, uint64_t pol) {
+    T o;
+    if constexpr (sizeof(T) == 4) {
+        uint32_t x;
+        asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(x) : "l"(p), "l"(pol));
+        memcpy(&o, &x, 4);
+    } else if constexpr (sizeof(T) == 8) {
+        uint2 x;
+        asm volatile("ld.global.nc.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
+                     : "=r"(x.x), "=r"(x.y)
+                     : "l"(p), "l"(pol));
+        memcpy(&o, &x, 8);
+    } else {
+        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
+        uint4 x;
+        asm volatile("ld.global.nc.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+                     : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w)
+                     : "l"(p), "l"(pol));
+        memcpy(&o, &x, 16);
+    }
+    return o;
+}
+
+// Totals of NV values over nb block partials p[k * stride + b]: warp k merges
+// value k (lane l takes b = l, l + 32, ... with four loads in flight, then a
+// shuffle tree), a fixed order; lane 0 of warp k leaves total k in sm[k].
+// Needs NV <= the block's warps; every thread calls it (no barrier inside).
+template <int NV, typename R>
+__device__ __forceinline__ void merge_partials_by_warp(const typename Acc<R>::Packed* p, int64_t stride, int nb,
+                                                       typename Acc<R>::Packed* sm) {
+    using P = typename Acc<R>::Packed;
+    constexpr int B = 4;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w >= NV) return;
+    Acc<R> y;
+    for (int base = lane; base < nb; base += 32 * B) {
+        P v[B];
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (base + 32 * u < nb) v[u] = __ldcg(&p[w * stride + base + 32 * u]);
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (base + 32 * u < nb) y.merge(Acc<R>::unpack(v[u]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) y.shfl_add(o);
+    if (lane == 0) sm[w] = y.pack();
+}
+
+// Deferred finish at the start of a launch of buffer parity q (variants 12 to
+// 15): every block reads the state of parity q ^ 1 into st; when the previous
+// launch left an iteration pending, warp k merges value k of that launch's
+// block partials (a fixed order, so every block gets the same scalars) and
+// thread 0 finishes the iteration.  Block 0 publishes the state of parity q
+// and the loop condition.  Returns whether this launch iterates (c set).
+// Only a solve's first launch iterates without finishing one: a launch that
+// would iterate on a state with neither stops the solve instead.
+template <typename R, int NF>
+__device__ __forceinline__ bool deferred_head(const StepArgs<R, NF>& a, int q, CgState& st, unsigned int& sflags,
+                                              typename Acc<R>::Packed* red, PhaseCtl<R, NF>& c) {
+    using P = typename Acc<R>::Packed;
+    constexpr int NV = 3 * NF;
+    const int t = threadIdx.x;
+    {
+        const int* src = reinterpret_cast<const int*>(q ? a.cg_alt : a.cg);
+        int* dst = reinterpret_cast<int*>(&st);
+        for (int k = t; k < (int)(sizeof(CgState) / 4); k += blockDim.x) dst[k] = __ldcg(src + k);
+    }
+    if (t == 0) sflags = 0u;
+    __syncthreads();
+    const bool had_pending = st.pending != 0;
+    if (had_pending && !a.probe) {
+        const P* pp = reinterpret_cast<const P*>(a.part + (q ? 8 * (int64_t)a.part_stride : 0));
+        merge_partials_by_warp<NV, R>(pp, a.part_stride, (int)gridDim.x, red);
+        __syncthreads();
+        if (t == 0) {
+            Acc<R> tot[NV];
+#pragma unroll
+            for (int k = 0; k < NV; k++) tot[k] = Acc<R>::unpack(red[k]);
+            int act[NF];
+#pragma unroll
+            for (int f = 0; f < NF; f++) act[f] = st.active[f];
+            finish_cgcg<R, NF>((volatile CgState*)&st, &sflags, act, tot);
+            st.pending = 0;
+        }
+        __syncthreads();
+    }
+    c.set(st.iter, (const volatile CgState*)&st);
+    c.par = q;
+    const bool stray = !a.probe && !had_pending && c.any && c.need_old;
+    const bool go = c.any && !stray;
+    if (t == 0 && blockIdx.x == 0 && !a.probe) {
+        a.run->cg_launches += 1;
+        if (sflags) atomicOr(&a.run->flags, sflags);
+        CgState* out = q ? a.cg : a.cg_alt;
+        const int* src = reinterpret_cast<const int*>(&st);
+        int* dst = reinterpret_cast<int*>(out);
+        for (int k = 0; k < (int)(sizeof(CgState) / 4); k++) dst[k] = src[k];
+        if (go) {  // this launch iterates; the next one finishes it
+            out->pending = 1;
+#pragma unroll
+            for (int f = 0; f < NF; f++) out->fresh[f] = 0;
+        } else if (stray) {
+#pragma unroll
+            for (int f = 0; f < NF; f++) out->active[f] = 0;
+            atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+        }
+        signal_loop(a, go);
+    }
+    return go;
+}
+
+// The block's partials of parity q for the next launch to merge: every
+// thread's accumulators through shared memory (red: NV * blockDim.x slots),
+// value k summed by warp k.
+template <typename R, int NV>
+__device__ __forceinline__ void store_block_partials(const StepArgs<R, NV / 3>& a, int q, const Acc<R> (&dots)[NV],
+                                                     typename Acc<R>::Packed* red) {
+    using P = typename Acc<R>::Packed;
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) red[k * kBlock + t] = dots[k].pack();
+    __syncthreads();
+    if (wib < NV) {
+        Acc<R> y = Acc<R>::unpack(red[wib * kBlock + lane]);
+#pragma unroll
+        for (int i = 1; i < kBlock / 32; i++) y.merge(Acc<R>::unpack(red[wib * kBlock + lane + 32 * i]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y.shfl_add(o);
+        if (lane == 0 && !a.probe) {
+            P* pp = reinterpret_cast<P*>(a.part + (q ? 0 : 8 * (int64_t)a.part_stride));
+            pp[wib * a.part_stride + blockIdx.x] = y.pack();
+        }
+    }
+}
+
+// PAR: the launch's buffer parity (a.par), a template argument so that the
+// parity's vector pointers stay constant operands.  Indices are 32-bit (N and
+// the layout's entry count are below 2^31).
+template <typename R, int NF, int K, int PAR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_direct(StepArgs<R, NF> a) {
+    using V = FV<R, NF>;
+    using P = typename Acc<R>::Packed;
+    constexpr int NV = 3 * NF;
+    static_assert(NV <= kBlock / 32, "one warp per reduced value");
+    static_assert(K % 2 == 0, "columns come in pairs");
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ P red[NV * kBlock];
+    __shared__ CgState st;
+    __shared__ unsigned int sflags;
+    V* const ubuf = reinterpret_cast<V*>(dyn_smem);
+    const int ustride = kTileRows + a.hmax;
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
+    const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
+    auto halo_head = [&](int tile, int32_t& h0, int32_t& cnt) {
+        h0 = cnt = 0;
+        if (tile < ntiles) {
+            h0 = a.halo_off[tile];
+            cnt = a.halo_off[tile + 1] - h0;
+        }
+    };
+    auto slice_ref = [&](int tile, int32_t& sb, int32_t& sw) {
+        sb = sw = 0;
+        if (tile < ntiles) {
+            const int sl = tile * (kTileRows / 32) + wib;
+            sb = a.slice_off[sl];
+            sw = (a.slice_off[sl + 1] - sb) >> 5;
+        }
+    };
+    // Before the dependency wait, only what no earlier kernel writes: the
+    // tile references and the first tile's operator entries.
+    int32_t sb, sw, sbn, swn;
+    slice_ref(t0, sb, sw);
+    slice_ref(t0 + G, sbn, swn);
+    V av[K];
+    uint32_t lc[K / 2];  // column pairs
+    {
+        const uint64_t pol_once = l2_evict_first_policy();
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (k < sw) av[k] = ld_once(a.As + sb + 32 * k + lane, pol_once);
+#pragma unroll
+        for (int m = 0; m < K / 2; m++)
+            if (2 * m < sw) lc[m] = ld_once(a.lcol2 + sb + 32 * m + lane, pol_once);
+    }
+    // halo pipeline: this tile's head and slot column, the next tile's, and
+    // the head of the tile after next
+    int32_t h0c, hcc, h0n, hcn, hh0, hhc;
+    halo_head(t0, h0c, hcc);
+    halo_head(t0 + G, h0n, hcn);
+    halo_head(t0 + 2 * G, hh0, hhc);
+    const int32_t fcol = j < hcc ? a.halo_col[h0c + j] : -1;
+    int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
+    grid_dependency_wait();
+    constexpr int q = PAR;  // buffer parity of this launch (static per graph node)
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[q];
+    v.w0 = a.wb[q];
+    v.s0 = a.sb[q];
+    v.r1 = a.rb[q ^ 1];
+    v.w1 = a.wb[q ^ 1];
+    v.s1 = a.sb[q ^ 1];
+    // the first tile's rows and halo slot, in flight while the previous
+    // iteration is finished
+    V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
+    {
+        const uint64_t pol_keep = l2_evict_last_policy();
+        const int row = t0 * kTileRows + t;  // every vector holds whole tiles
+        if (t0 < ntiles) {
+            cr = ld_keep(v.r0 + row, pol_keep);
+            cw = ld_keep(v.w0 + row, pol_keep);
+            cs = ld_keep(v.s0 + row, pol_keep);
+            cd = ld_keep(v.dinv + row, pol_keep);
+            cx = ld_keep(v.x + row, pol_keep);
+            cp = ld_keep(v.p + row, pol_keep);
+        }
+        if (fcol >= 0) {
+            hr = ld_keep(v.r0 + fcol, pol_keep);
+            hw = ld_keep(v.w0 + fcol, pol_keep);
+            hs = ld_keep(v.s0 + fcol, pol_keep);
+            hd = ld_keep(v.dinv + fcol, pol_keep);
+        }
+    }
+    PhaseCtl<R, NF> c;
+    const bool go = deferred_head<R, NF>(a, q, st, sflags, red, c);
+    if (!go && !a.probe) return;  // every field stopped (plain loads in flight need no wait)
+    Acc<R> dots[NV];  // gamma', delta', |r'|^2 per field
+    int buf = 0;
+    for (int tile = t0; tile < ntiles; tile += G) {
+        V* ut = ubuf + buf * ustride;
+        const int row = tile * kTileRows + t;
+        V un;
+#pragma unroll
+        for (int f = 0; f < NF; f++) un.v[f] = 0;
+        if (row < a.N) {
+            V sn, rn;
+            cg_advance(c, cr, cw, c.need_old ? cs : cw, cd, sn, rn, un);
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (c.act[f]) {
+                    const R ui = cd.v[f] * cr.v[f];
+                    cp.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], cp.v[f], ui);
+                    cx.v[f] = fmar(c.alpha[f], cp.v[f], cx.v[f]);
+                }
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            v.x[row] = cx;
+            v.p[row] = cp;
+            v.r1[row] = rn;
+            v.s1[row] = sn;
+        }
+        ut[t] = un;
+        // the row's registers are free: the next tile's rows go in flight
+        // now, ahead of the halo, the barrier and the product
+        const uint64_t pol_keep = l2_evict_last_policy();
+        const int nt = tile + G;
+        if (nt < ntiles) {
+            const int nrow = nt * kTileRows + t;
+            cr = ld_keep(v.r0 + nrow, pol_keep);
+            cw = ld_keep(v.w0 + nrow, pol_keep);
+            cs = ld_keep(v.s0 + nrow, pol_keep);
+            cd = ld_keep(v.dinv + nrow, pol_keep);
+            cx = ld_keep(v.x + nrow, pol_keep);
+            cp = ld_keep(v.p + nrow, pol_keep);
+        }
+        if (j < hcc) {
+            V sn, rn, u2;
+            cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
+            ut[kTileRows + j] = u2;
+        }
+        if (hcoln >= 0) {  // the next tile's halo slot operands
+            hr = ld_keep(v.r0 + hcoln, pol_keep);
+            hw = ld_keep(v.w0 + hcoln, pol_keep);
+            hs = ld_keep(v.s0 + hcoln, pol_keep);
+            hd = ld_keep(v.dinv + hcoln, pol_keep);
+        }
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock)  // halos beyond 256 columns: directly
+            ut[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0c + h]);
+        __syncthreads();
+        // references further ahead, each from values loaded a tile ago
+        h0c = h0n;
+        hcc = hcn;
+        hcoln = j < hhc ? a.halo_col[hh0 + j] : -1;
+        h0n = hh0;
+        hcn = hhc;
+        halo_head(tile + 3 * G, hh0, hhc);
+        int32_t sb2, sw2;
+        slice_ref(tile + 2 * G, sb2, sw2);
+        // the product; each register takes the next tile's entry once used
+        const uint64_t pol_once = l2_evict_first_policy();
+        V wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) wn.v[f] = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (k < sw) {
+                const V g = ut[(k & 1) ? lc[k / 2] >> 16 : lc[k / 2] & 0xffffu];
+#pragma unroll
+                for (int f = 0; f < NF; f++) wn.v[f] = fmar(av[k].v[f], g.v[f], wn.v[f]);
+            }
+            if (k < swn) av[k] = ld_once(a.As + sbn + 32 * k + lane, pol_once);
+            if ((k & 1) && k - 1 < swn) lc[k / 2] = ld_once(a.lcol2 + sbn + 32 * (k / 2) + lane, pol_once);
+        }
+        for (int k = K; k < sw; k++) {  // rows longer than the registers hold
+            const V ak = ld_once(a.As + sb + 32 * k + lane, pol_once);
+            const V g = ut[ld_once_u16(a.lcol + sb + 32 * k + lane, pol_once)];
+#pragma unroll
+            for (int f = 0; f < NF; f++) wn.v[f] = fmar(ak.v[f], g.v[f], wn.v[f]);
+        }
+        if (row < a.N) {
+            v.w1[row] = wn;
+#pragma unroll
+            for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
+        }
+        sb = sbn;
+        sw = swn;
+        sbn = sb2;
+        swn = sw2;
+        buf ^= 1;
+    }
+    grid_launch_dependents();
+    __syncthreads();  // red[] held the start-of-launch totals
+    store_block_partials<R, NV>(a, q, dots, red);
+}
+
+// ---- variants 14 and 15: direct row loads, operator streamed by a bulk-copy ring ---
+//
+// Variant 13's structure (rows, halo and references loaded by the threads a
+// tile ahead, one block barrier per tile, deferred finish) with the operator
+// entries and their 16-bit local columns moved by bulk copies (cp.async.bulk
+// on an mbarrier per stage) into a ring of S shared-memory stages, S - 1 tiles
+// ahead of the product: the DRAM stream holds no registers, so it runs further
+// ahead than register prefetches can.  Thread 0 refills the stage of the
+// previous tile after the current tile's barrier (every warp has finished
+// that tile's product by then).  Each warp waits for its tile's stage on its
+// own, with a bounded wait; an expired wait raises FEA_STATUS_BREAKDOWN at the
+// end of the launch, after thread 0 has waited (bounded) for the copies it
+// issued.
+
+// One stage of the ring: a tile's operator entries, then its local columns.
+struct RingStage {
+    size_t A, L, bytes;
+    __host__ __device__ RingStage(int emax, size_t fv) {
+        auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
+        A = 0;
+        L = al(fv * (size_t)emax);
+        bytes = al(L + 2 * (size_t)emax);
+    }
+};
+
+// Dynamic shared memory of the ring kernels: the ring (which the end-of-launch
+// reduction reuses once every copy has landed), then the two u' buffers.
+template <typename R, int NF>
+__host__ __device__ size_t ring_bytes(int emax, int stages) {
+    const size_t ring = (size_t)stages * RingStage(emax, sizeof(FV<R, NF>)).bytes;
+    const size_t red = (size_t)3 * NF * kBlock * sizeof(typename Acc<R>::Packed);
+    return (ring > red ? ring : red + 127) & ~(size_t)127;
+}
+
+template <typename R, int NF, int S, int PAR, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF> a) {
+    using V = FV<R, NF>;
+    using P = typename Acc<R>::Packed;
+    constexpr int NV = 3 * NF;
+    static_assert(NV <= kBlock / 32, "one warp per reduced value");
+    static_assert(S >= 2 && S <= 8, "ring depth");
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    __shared__ P mred[NV];
+    __shared__ __align__(8) uint64_t bars[S];
+    __shared__ CgState st;
+    __shared__ unsigned int sflags;
+    const RingStage L(a.emax, sizeof(V));
+    unsigned char* const ring = dyn_smem;
+    V* const ubuf = reinterpret_cast<V*>(dyn_smem + ring_bytes<R, NF>(a.emax, S));
+    const int ustride = kTileRows + a.hmax;
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
+    const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
+    auto halo_head = [&](int tile, int32_t& h0, int32_t& cnt) {
+        h0 = cnt = 0;
+        if (tile < ntiles) {
+            h0 = a.halo_off[tile];
+            cnt = a.halo_off[tile + 1] - h0;
+        }
+    };
+    // this warp's slice of a tile: offset in the tile's entries, width
+    auto slice_ref = [&](int tile, int32_t& sb, int32_t& sw) {
+        sb = sw = 0;
+        if (tile < ntiles) {
+            const int sl = tile * (kTileRows / 32) + wib;
+            const int32_t s0 = a.slice_off[sl];
+            sb = s0 - a.slice_off[tile * (kTileRows / 32)];
+            sw = (a.slice_off[sl + 1] - s0) >> 5;
+        }
+    };
+    auto tile_range = [&](int tile, int32_t& e0, int32_t& e1) {
+        e0 = e1 = 0;
+        if (tile < ntiles) {
+            e0 = a.slice_off[tile * (kTileRows / 32)];
+            e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
+        }
+    };
+    auto stage_of = [&](int b) { return ring + (size_t)b * L.bytes; };
+    // thread 0: the bulk copies of one tile's entries and columns into stage b
+    auto issue = [&](int b, int32_t e0, int32_t e1) {
+        uint64_t* bar = &bars[b];
+        const uint32_t n = (uint32_t)(e1 - e0);  // a multiple of 32 entries
+        if (n == 0) {
+            mbar_arrive(bar);
+            return;
+        }
+        mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
+        const uint64_t pol = l2_evict_first_policy();
+        bulk_g2s_hint(stage_of(b) + L.A, a.As + e0, n * (uint32_t)sizeof(V), bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.L, a.lcol + e0, 2 * n, bar, pol);
+    };
+    // Before the dependency wait, only what no earlier kernel writes: the
+    // stages' barriers, the first S tiles' operator copies, the references.
+    uint32_t armed = 0;  // thread 0: bit b set while stage b has copies in flight
+    int32_t re0 = 0, re1 = 0;  // thread 0: entry range of the next refill
+    if (t == 0) {
+        for (int b = 0; b < S; b++) mbar_init(&bars[b], 1);
+        mbar_fence_init();
+        for (int b = 0; b < S; b++) {
+            int32_t e0, e1;
+            if (t0 + b * G < ntiles) {
+                tile_range(t0 + b * G, e0, e1);
+                issue(b, e0, e1);
+                armed |= 1u << b;
+            }
+        }
+        tile_range(t0 + S * G, re0, re1);
+    }
+    int32_t sb, sw, sbn, swn;
+    slice_ref(t0, sb, sw);
+    slice_ref(t0 + G, sbn, swn);
+    int32_t h0c, hcc, h0n, hcn, hh0, hhc;
+    halo_head(t0, h0c, hcc);
+    halo_head(t0 + G, h0n, hcn);
+    halo_head(t0 + 2 * G, hh0, hhc);
+    const int32_t fcol = j < hcc ? a.halo_col[h0c + j] : -1;
+    int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
+    grid_dependency_wait();
+    constexpr int q = PAR;
+    CgVecs<R, NF> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.pp[0];
+    v.r0 = a.rb[q];
+    v.w0 = a.wb[q];
+    v.s0 = a.sb[q];
+    v.r1 = a.rb[q ^ 1];
+    v.w1 = a.wb[q ^ 1];
+    v.s1 = a.sb[q ^ 1];
+    V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
+    {
+        const uint64_t pol_keep = l2_evict_last_policy();
+        const int row = t0 * kTileRows + t;  // every vector holds whole tiles
+        if (t0 < ntiles) {
+            cr = ld_keep(v.r0 + row, pol_keep);
+            cw = ld_keep(v.w0 + row, pol_keep);
+            cs = ld_keep(v.s0 + row, pol_keep);
+            cd = ld_keep(v.dinv + row, pol_keep);
+            cx = ld_keep(v.x + row, pol_keep);
+            cp = ld_keep(v.p + row, pol_keep);
+        }
+        if (fcol >= 0) {
+            hr = ld_keep(v.r0 + fcol, pol_keep);
+            hw = ld_keep(v.w0 + fcol, pol_keep);
+            hs = ld_keep(v.s0 + fcol, pol_keep);
+            hd = ld_keep(v.dinv + fcol, pol_keep);
+        }
+    }
+    PhaseCtl<R, NF> c;
+    const bool go = deferred_head<R, NF>(a, q, st, sflags, mred, c);
+    if (!go && !a.probe) {  // every field stopped: the copies land, then the block leaves
+        if (t == 0)
+            for (int b = 0; b < S; b++)
+                if (armed & (1u << b)) mbar_wait(&bars[b], 0u);
+        return;
+    }
+    Acc<R> dots[NV];
+    uint32_t phases = 0u;  // bit b: parity of stage b's next phase
+    bool bad = false;      // a stage wait expired
+    int buf = 0, b = 0, k = 0;
+    for (int tile = t0; tile < ntiles; tile += G, k++) {
+        V* ut = ubuf + buf * ustride;
+        const int row = tile * kTileRows + t;
+        V un;
+#pragma unroll
+        for (int f = 0; f < NF; f++) un.v[f] = 0;
+        if (row < a.N) {
+            V sn, rn;
+            cg_advance(c, cr, cw, c.need_old ? cs : cw, cd, sn, rn, un);
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                if (c.act[f]) {
+                    const R ui = cd.v[f] * cr.v[f];
+                    cp.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], cp.v[f], ui);
+                    cx.v[f] = fmar(c.alpha[f], cp.v[f], cx.v[f]);
+                }
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[2 * NF + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            v.x[row] = cx;
+            v.p[row] = cp;
+            v.r1[row] = rn;
+            v.s1[row] = sn;
+        }
+        ut[t] = un;
+        const uint64_t pol_keep = l2_evict_last_policy();
+        const int nt = tile + G;
+        if (nt < ntiles) {
+            const int nrow = nt * kTileRows + t;
+            cr = ld_keep(v.r0 + nrow, pol_keep);
+            cw = ld_keep(v.w0 + nrow, pol_keep);
+            cs = ld_keep(v.s0 + nrow, pol_keep);
+            cd = ld_keep(v.dinv + nrow, pol_keep);
+            cx = ld_keep(v.x + nrow, pol_keep);
+            cp = ld_keep(v.p + nrow, pol_keep);
+        }
+        if (j < hcc) {
+            V sn, rn, u2;
+            cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
+            ut[kTileRows + j] = u2;
+        }
+        if (hcoln >= 0) {
+            hr = ld_keep(v.r0 + hcoln, pol_keep);
+            hw = ld_keep(v.w0 + hcoln, pol_keep);
+            hs = ld_keep(v.s0 + hcoln, pol_keep);
+            hd = ld_keep(v.dinv + hcoln, pol_keep);
+        }
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock)
+            ut[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0c + h]);
+        __syncthreads();
+        if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
+            const int bp = b == 0 ? S - 1 : b - 1;
+            const int target = tile + (S - 1) * G;
+            if (target < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(bp, re0, re1);
+                armed |= 1u << bp;
+            }
+            tile_range(target + G, re0, re1);
+        }
+        h0c = h0n;
+        hcc = hcn;
+        hcoln = j < hhc ? a.halo_col[hh0 + j] : -1;
+        h0n = hh0;
+        hcn = hhc;
+        halo_head(tile + 3 * G, hh0, hhc);
+        int32_t sb2, sw2;
+        slice_ref(tile + 2 * G, sb2, sw2);
+        // the product from the stage
+        const bool got = mbar_wait(&bars[b], (phases >> b) & 1u);
+        phases ^= 1u << b;
+        bad |= !got;
+        if (t == 0 && got) armed &= ~(1u << b);
+        const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+        V wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) wn.v[f] = 0;
+#pragma unroll 4
+        for (int kk = 0; kk < sw; kk++) {
+            const V av = As[32 * kk];
+            const V g = ut[Ls[32 * kk]];
+#pragma unroll
+            for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
+        }
+        if (row < a.N) {
+            v.w1[row] = wn;
+#pragma unroll
+            for (int f = 0; f < NF; f++) dots[NF + f].add_prod(wn.v[f], un.v[f]);
+        }
+        sb = sbn;
+        sw = swn;
+        sbn = sb2;
+        swn = sw2;
+        buf ^= 1;
+        b = b + 1 == S ? 0 : b + 1;
+    }
+    grid_launch_dependents();
+    // every thread is done with the ring before it holds the reduction
+    if (__syncthreads_or(bad)) {
+        if (t == 0) {
+            atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            for (int q2 = 0; q2 < S; q2++)  // copies still in flight land before the ring is reused
+                if (armed & (1u << q2)) mbar_wait(&bars[q2], (phases >> q2) & 1u);
+        }
+        __syncthreads();
+    }
+    store_block_partials<R, NV>(a, q, dots, reinterpret_cast<P*>(ring));
+}
+
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
 // previous solution), z = D^-1 r, p = z, and the CG set-up scalars.  Also the
 // has_numerical_instability test of the state entering the step.
@@ -957,8 +1612,11 @@ constexpr int kRowLanes = 1;  // threads per row of the once-per-step kernels (1
 // lane and window), 0 the tile-ELL kernels with their dynamic shared memory.
 template <typename R, int NF, int WCH>
 struct CgKernels {
-    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init<R, NF, WCH>;
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter<R, NF, WCH>;
+    using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr Fn init = k_cgcg_init<R, NF, WCH>;
+    static constexpr Fn iter = k_cgcg_iter<R, NF, WCH>;
+    // the iteration kernel of a launch with buffer parity `par`
+    static Fn iter_par(int) { return iter; }
     static size_t smem_init(const StepArgs<R, NF>&) { return 0; }
     static size_t smem_iter(const StepArgs<R, NF>&) { return 0; }
 };
@@ -966,8 +1624,10 @@ struct CgKernels {
 // prefetched into registers; two staging buffers of kTileRows + hmax entries.
 template <typename R, int NF, int KPRE>
 struct EllKernels {
-    static constexpr void (*init)(StepArgs<R, NF>) = k_cgcg_init_ell<R, NF, KPRE>;
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_ell<R, NF, KPRE>;
+    using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr Fn init = k_cgcg_init_ell<R, NF, KPRE>;
+    static constexpr Fn iter = k_cgcg_iter_ell<R, NF, KPRE>;
+    static Fn iter_par(int) { return iter; }
     static size_t smem_init(const StepArgs<R, NF>& a) {
         return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
     }
@@ -982,7 +1642,9 @@ struct CgKernels<R, NF, 1> : EllKernels<R, NF, 4> {};
 // tile's first barrier.  The set-up product is variant 1's.
 template <typename R, int NF, int NS, bool LATE, bool DEFER = false>
 struct StreamKernels : EllKernels<R, NF, 4> {
-    static constexpr void (*iter)(StepArgs<R, NF>) = k_cgcg_iter_stream<R, NF, NS, LATE, DEFER>;
+    using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr Fn iter = k_cgcg_iter_stream<R, NF, NS, LATE, DEFER>;
+    static Fn iter_par(int) { return iter; }
     static size_t smem_iter(const StepArgs<R, NF>& a) { return NS * StageLayout<R, NF>(a.emax, a.hmax).bytes; }
 };
 template <typename R, int NF>
@@ -1000,6 +1662,34 @@ template <typename R, int NF>
 struct CgKernels<R, NF, 10> : StreamKernels<R, NF, 2, false, true> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 11> : StreamKernels<R, NF, 3, true, true> {};
+// Variant 12: the tile-ELL iteration with direct, register-pipelined loads
+// and the deferred finish (two u' buffers of kTileRows + hmax entries); one
+// kernel per buffer parity.
+template <typename R, int NF, int MINB>
+struct DirectKernels : EllKernels<R, NF, 4> {
+    using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr int K = sizeof(FV<R, NF>) <= 8 ? 8 : 4;
+    static constexpr Fn iter = k_cgcg_iter_direct<R, NF, K, 0, MINB>;
+    static Fn iter_par(int par) { return par ? k_cgcg_iter_direct<R, NF, K, 1, MINB> : iter; }
+};
+template <typename R, int NF>
+struct CgKernels<R, NF, 12> : DirectKernels<R, NF, (sizeof(FV<R, NF>) <= 8 ? 3 : 2)> {};
+// Variants 14 and 15: direct row loads with the operator in a ring of 3
+// bulk-copy stages; registers for two or three resident blocks per SM.
+template <typename R, int NF, int S, int MINB>
+struct RingKernels : EllKernels<R, NF, 4> {
+    using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr Fn iter = k_cgcg_iter_ring<R, NF, S, 0, MINB>;
+    static Fn iter_par(int par) { return par ? k_cgcg_iter_ring<R, NF, S, 1, MINB> : iter; }
+    static size_t smem_iter(const StepArgs<R, NF>& a) { return ring_smem_bytes<R, NF>(a.emax, a.hmax, S); }
+};
+template <typename R, int NF>
+struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};
+template <typename R, int NF>
+struct CgKernels<R, NF, 15> : RingKernels<R, NF, 3, (sizeof(FV<R, NF>) <= 8 ? 3 : 2)> {};
+// Variant 13: the same with registers for two resident blocks per SM.
+template <typename R, int NF>
+struct CgKernels<R, NF, 13> : DirectKernels<R, NF, (sizeof(FV<R, NF>) <= 8 ? 2 : 1)> {};
 
 template <typename R, int NF, int WCH>
 struct Grids {
@@ -1012,6 +1702,9 @@ struct Grids {
         smem_iter = K::smem_iter(a);
         spmv = wave_grid(K::init, ceil_div(N, kBlock), smem_init);
         iter = wave_grid(K::iter, ceil_div(N, kBlock), smem_iter);
+        if (smem_iter > 48 * 1024 && K::iter_par(1) != K::iter)  // the other parity's kernel
+            FEA_CUDA_TRY(cudaFuncSetAttribute(K::iter_par(1), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem_iter));
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -1036,14 +1729,13 @@ struct LoopArgs {
 // Deferred-finish variants get node u the buffer parity u & 1 (kLoopUnroll
 // is even, so every pass starts at parity 0 as every solve does).
 static_assert(kLoopUnroll % 2 == 0, "loop passes keep the buffer parity");
-template <typename R, int NF>
-void add_iterations(cudaGraph_t body, void (*iter)(StepArgs<R, NF>), int grid, const StepArgs<R, NF>& a,
-                    size_t smem) {
+template <typename K, typename R, int NF>
+void add_iterations(cudaGraph_t body, int grid, const StepArgs<R, NF>& a, size_t smem) {
     cudaGraphNode_t prev = nullptr;
     for (int u = 0; u < kLoopUnroll; u++) {
         StepArgs<R, NF> au = a;
         au.par = a.defer ? (u & 1) : 0;
-        cudaGraphNode_t n = add_kernel(body, nullptr, iter, grid, kBlock, au, smem);
+        cudaGraphNode_t n = add_kernel(body, nullptr, K::iter_par(au.par), grid, kBlock, au, smem);
         if (prev) add_programmatic_edge(body, prev, n);
         prev = n;
     }
@@ -1071,11 +1763,11 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_iterations(body1, K::iter, g.iter, L.a1, g.smem_iter);
+    add_iterations<K>(body1, g.iter, L.a1, g.smem_iter);
     s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
+    add_iterations<K>(body2, g.iter, L.a2, g.smem_iter);
     if constexpr (EQ == EQ_WAVE_REF || EQ == EQ_WAVE_NEWMARK)
         s = add_kernel(step_body, s, k_post<R, NF, EQ>, g.stream, kBlock, L.a);
     add_kernel(step_body, s, k_stepctl<R, NF>, 1, 1, L.a);
@@ -1115,7 +1807,7 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
                     StepArgs<R, NF> aq = *la;
                     for (int q = 0; q < 2; q++) {
                         aq.par = q;
-                        K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(aq);
+                        K::iter_par(q)<<<g.iter, kBlock, g.smem_iter, st>>>(aq);
                         FEA_CHECK_LAUNCH();
                     }
                 } else {
@@ -1147,6 +1839,10 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     case 7: G ? build_graph_t<R, NF, EQ, 7>(*G, a, lf) : run_stream_t<R, NF, EQ, 7>(a, lf, st); break;
     case 10: G ? build_graph_t<R, NF, EQ, 10>(*G, a, lf) : run_stream_t<R, NF, EQ, 10>(a, lf, st); break;
     case 11: G ? build_graph_t<R, NF, EQ, 11>(*G, a, lf) : run_stream_t<R, NF, EQ, 11>(a, lf, st); break;
+    case 12: G ? build_graph_t<R, NF, EQ, 12>(*G, a, lf) : run_stream_t<R, NF, EQ, 12>(a, lf, st); break;
+    case 13: G ? build_graph_t<R, NF, EQ, 13>(*G, a, lf) : run_stream_t<R, NF, EQ, 13>(a, lf, st); break;
+    case 14: G ? build_graph_t<R, NF, EQ, 14>(*G, a, lf) : run_stream_t<R, NF, EQ, 14>(a, lf, st); break;
+    case 15: G ? build_graph_t<R, NF, EQ, 15>(*G, a, lf) : run_stream_t<R, NF, EQ, 15>(a, lf, st); break;
     case 4: G ? build_graph_t<R, NF, EQ, 4>(*G, a, lf) : run_stream_t<R, NF, EQ, 4>(a, lf, st); break;
     case 16: G ? build_graph_t<R, NF, EQ, 16>(*G, a, lf) : run_stream_t<R, NF, EQ, 16>(a, lf, st); break;
     default: G ? build_graph_t<R, NF, EQ, 8>(*G, a, lf) : run_stream_t<R, NF, EQ, 8>(a, lf, st); break;
@@ -1220,7 +1916,7 @@ void prepare_probe(const StepArgs<R, NF>& a, cudaStream_t st) {
 template <typename R, int NF, int WCH>
 void probe_t(const StepArgs<R, NF>& a, cudaStream_t st) {
     const Grids<R, NF, WCH> g(a);
-    CgKernels<R, NF, WCH>::iter<<<g.iter, kBlock, g.smem_iter, st>>>(a);
+    CgKernels<R, NF, WCH>::iter_par(a.par)<<<g.iter, kBlock, g.smem_iter, st>>>(a);
     FEA_CHECK_LAUNCH();
 }
 
@@ -1235,6 +1931,10 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     case 7: probe_t<R, NF, 7>(a, st); break;
     case 10: probe_t<R, NF, 10>(a, st); break;
     case 11: probe_t<R, NF, 11>(a, st); break;
+    case 12: probe_t<R, NF, 12>(a, st); break;
+    case 13: probe_t<R, NF, 13>(a, st); break;
+    case 14: probe_t<R, NF, 14>(a, st); break;
+    case 15: probe_t<R, NF, 15>(a, st); break;
     case 4: probe_t<R, NF, 4>(a, st); break;
     case 16: probe_t<R, NF, 16>(a, st); break;
     default: probe_t<R, NF, 8>(a, st); break;
@@ -1246,6 +1946,14 @@ template <typename R, int NF>
 size_t stream_stage_bytes(int emax, int hmax) {
     return StageLayout<R, NF>(emax, hmax).bytes;
 }
+template <typename R, int NF>
+size_t ring_smem_bytes(int emax, int hmax, int stages) {
+    return ring_bytes<R, NF>(emax, stages) + 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + hmax);
+}
+template size_t ring_smem_bytes<float, 1>(int, int, int);
+template size_t ring_smem_bytes<float, 2>(int, int, int);
+template size_t ring_smem_bytes<double, 1>(int, int, int);
+template size_t ring_smem_bytes<double, 2>(int, int, int);
 template size_t stream_stage_bytes<float, 1>(int, int);
 template size_t stream_stage_bytes<float, 2>(int, int);
 template size_t stream_stage_bytes<double, 1>(int, int);

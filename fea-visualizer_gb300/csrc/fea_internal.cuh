@@ -27,7 +27,9 @@ int launch_grid(int64_t n);
 void build_permuted(const Pattern& P, const int32_t* pos, const int32_t* inv, Pattern& Pc, int32_t* emap,
                     DeviceArena& keep, cudaStream_t st);
 void detect_boundary(const uint32_t* tri, int64_t T, int64_t V, uint8_t* ob, cudaStream_t st);
-bool check_triangles(const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st);
+// Bit 0: a triangle index >= V; bit 1: a non-finite vertex coordinate; bit 2:
+// a zero-area triangle (FP64 cross product of its edges is zero).  0: valid.
+int check_mesh(const float* xyz, const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st);
 int64_t build_idx_map(const uint8_t* ob, int64_t V, int bc, int32_t* idx, cudaStream_t st);
 void build_pattern(Pattern& P, DeviceArena& keep, const uint32_t* tri, int64_t T, const uint8_t* ob,
                    const int32_t* idx, int bc, int64_t N, cudaStream_t st);
@@ -46,6 +48,11 @@ struct TileEll {
     int32_t* halo_off = nullptr;   // [ntiles + 1]
     int32_t* halo_col = nullptr;   // sorted distinct out-of-tile columns per tile
     uint16_t* lcol = nullptr;      // [E] local column index
+    // [E] the same columns in pairs: slot sb + 32 m + lane of a slice that
+    // starts at entry sb holds the local columns of its row's entries 2m (low
+    // half) and 2m + 1 (high half) for m < ceil(width / 2); the slice's other
+    // slots are unused.  One 32-bit load then brings two columns.
+    uint32_t* lcol2 = nullptr;
     int32_t* emap = nullptr;       // [E] CSR slot of each entry, -1 for padding
     bool ok = false;
 };
@@ -161,6 +168,7 @@ struct StepArgs {
     // tile-ELL copy of A (the CG kernels' layout when ell.ok)
     const FV<R, NF>* As;
     const uint16_t* lcol;
+    const uint32_t* lcol2;  // column pairs (TileEll::lcol2)
     const int32_t* slice_off;
     const int32_t* halo_off;
     const int32_t* halo_col;
@@ -224,12 +232,16 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int lanes, cudaStream_t st);
 template <typename R, int NF>
 size_t stream_stage_bytes(int emax, int hmax);
 constexpr size_t kStreamSmemLimit = 220 * 1024;  // per block, below the 227 KB opt-in maximum
+// Dynamic shared memory of the ring iteration kernels (variants 14 and 15)
+// with `stages` operator stages.
+template <typename R, int NF>
+size_t ring_smem_bytes(int emax, int hmax, int stages);
 
 int max_grid_blocks();
 
 // CG variants whose iteration kernels finish the previous launch's iteration
 // at their start (deferred finish; see StepArgs::defer).
-constexpr bool is_deferred_variant(int l) { return l == 10 || l == 11; }
+constexpr bool is_deferred_variant(int l) { return l >= 10 && l <= 15; }
 
 // ---- adjoint of the explicit advection-diffusion step (adjoint.cu) ----------------
 // lam = M (u - t), *J = 1/2 (u - t).lam  (exact accumulators; one block-partial

@@ -16,6 +16,8 @@
 #include <vector>
 
 #include "fea_common.cuh"
+#include <algorithm>
+
 #include "fea_internal.cuh"
 
 namespace fea {
@@ -238,9 +240,29 @@ __global__ void k_idx_map(const uint8_t* ob, const int32_t* scan, int64_t V, int
         idx[v] = bc == FEA_NEUMANN ? (int32_t)v : (ob[v] ? -1 : scan[v]);
 }
 
-__global__ void k_check_tri(const uint32_t* tri, int64_t n, int64_t V, int32_t* bad) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        if ((int64_t)tri[i] >= V) atomicExch(bad, 1);
+// Mesh checks: bit 0 an index >= V, bit 1 a non-finite coordinate, bit 2 a
+// triangle whose edge vectors have a zero cross product in FP64 (zero area:
+// collinear or repeated corners; the element matrices would divide by it).
+__global__ void k_check_mesh(const float* xyz, const uint32_t* tri, int64_t T, int64_t V, int32_t* bad) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * V; i += stride)
+        if (!isfinite(xyz[i])) atomicOr(bad, 2);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < T; k += stride) {
+        const uint32_t a = tri[3 * k], b = tri[3 * k + 1], c = tri[3 * k + 2];
+        if ((int64_t)a >= V || (int64_t)b >= V || (int64_t)c >= V) {
+            atomicOr(bad, 1);
+            continue;
+        }
+        double e1[3], e2[3];
+        for (int d = 0; d < 3; d++) {
+            e1[d] = (double)xyz[3 * b + d] - (double)xyz[3 * a + d];
+            e2[d] = (double)xyz[3 * c + d] - (double)xyz[3 * a + d];
+        }
+        const double n0 = e1[1] * e2[2] - e1[2] * e2[1];
+        const double n1 = e1[2] * e2[0] - e1[0] * e2[2];
+        const double n2 = e1[0] * e2[1] - e1[1] * e2[0];
+        if (n0 == 0.0 && n1 == 0.0 && n2 == 0.0) atomicOr(bad, 4);
+    }
 }
 
 __global__ void k_find_diag(const int32_t* rp, const int32_t* col, int64_t N, int32_t* diag) {
@@ -329,16 +351,16 @@ void detect_boundary(const uint32_t* tri, int64_t T, int64_t V, uint8_t* ob, cud
     FEA_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
-bool check_triangles(const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st) {
+int check_mesh(const float* xyz, const uint32_t* tri, int64_t T, int64_t V, cudaStream_t st) {
     DeviceArena tmp;
     int32_t* bad = tmp.alloc<int32_t>(1);
     FEA_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
-    k_check_tri<<<grid_for(3 * T), kBlock, 0, st>>>(tri, 3 * T, V, bad);
+    k_check_mesh<<<grid_for(std::max(3 * V, T)), kBlock, 0, st>>>(xyz, tri, T, V, bad);
     FEA_CHECK_LAUNCH();
     int32_t h = 0;
     FEA_CUDA_TRY(cudaMemcpyAsync(&h, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     FEA_CUDA_TRY(cudaStreamSynchronize(st));
-    return h == 0;
+    return h;
 }
 
 // idx_map and the number of unknowns (FEMContext.cpp:46-48, 224-240).

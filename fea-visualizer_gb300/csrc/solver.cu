@@ -361,9 +361,16 @@ void build_context(fea_solver* s) {
         const size_t stage = s->precision == FEA_FP64 ? stream_stage_bytes<double, 2>(s->ell.emax, s->ell.hmax)
                                                       : stream_stage_bytes<float, 2>(s->ell.emax, s->ell.hmax);
         s->stream_stages = !s->ell.ok ? 0 : 3 * stage <= kStreamSmemLimit ? 3 : 2 * stage <= kStreamSmemLimit ? 2 : 0;
-        // default variant: the streamed deferred-finish kernel with as many
-        // stages as fit, else the tile-ELL kernel, else windowed CSR
-        s->lanes = !s->ell.ok ? 8 : s->stream_stages >= 3 ? 11 : s->stream_stages >= 2 ? 10 : 0;
+        // default variant: direct row loads with the operator ring (14) when
+        // its stages fit, else the streamed deferred-finish kernel with as
+        // many stages as fit, else the tile-ELL kernel, else windowed CSR
+        const size_t ring = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax, 3)
+                                                     : ring_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax, 3);
+        s->lanes = !s->ell.ok ? 8
+                   : ring <= kStreamSmemLimit ? 14
+                   : s->stream_stages >= 3    ? 11
+                   : s->stream_stages >= 2    ? 10
+                                              : 0;
     }
     s->Kloc = s->mat_mem.alloc<double>(9 * T);
     s->Mloc = s->mat_mem.alloc<double>(9 * T);
@@ -475,6 +482,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         if constexpr (NF == 1) a.As = (const FV<R, 1>*)(init_op ? s->S0 : s->S1);
         else a.As = (const FV<R, 2>*)s->S2;
         a.lcol = s->ell.lcol;
+        a.lcol2 = s->ell.lcol2;
         a.slice_off = s->ell.slice_off;
         a.halo_off = s->ell.halo_off;
         a.halo_col = s->ell.halo_col;
@@ -1300,9 +1308,11 @@ int fea_create(const float* vertices, int64_t V, const uint32_t* triangles, int6
     s->d_nodes = s->mesh_mem.alloc<float>(V);
     FEA_CUDA_TRY(cudaMemcpyAsync(s->xyz, vertices, sizeof(float) * 3 * V, cudaMemcpyHostToDevice, s->stream));
     FEA_CUDA_TRY(cudaMemcpyAsync(s->tri, triangles, sizeof(uint32_t) * 3 * T, cudaMemcpyHostToDevice, s->stream));
-    if (!check_triangles(s->tri, T, V, s->stream)) {
+    if (const int bad = check_mesh(s->xyz, s->tri, T, V, s->stream)) {
         fea_destroy(s);
-        return fail(FEA_ERR_BAD_MESH, "triangle index out of range");
+        return fail(FEA_ERR_BAD_MESH, (bad & 1)   ? "triangle index out of range"
+                                      : (bad & 2) ? "non-finite vertex coordinate"
+                                                  : "degenerate triangle (zero area)");
     }
     if (on_boundary) {
         FEA_CUDA_TRY(cudaMemcpyAsync(s->ob, on_boundary, V, cudaMemcpyHostToDevice, s->stream));
@@ -1724,9 +1734,15 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary) {
 static int variant_check(const fea_solver* s, int l) {
     const bool csr = l == 4 || l == 8 || l == 16;
     const int stages = (l == 2 || l == 6 || l == 10) ? 2 : (l == 3 || l == 7 || l == 11) ? 3 : 0;
-    if (!csr && l != 0 && l != 1 && stages == 0) return FEA_ERR_INVALID_ARGUMENT;
+    const int ring = (l == 14 || l == 15) ? 3 : 0;
+    if (!csr && l != 0 && l != 1 && l != 12 && l != 13 && stages == 0 && ring == 0) return FEA_ERR_INVALID_ARGUMENT;
     if (!csr && !s->ell.ok) return FEA_ERR_UNSUPPORTED;
     if (s->stream_stages < stages) return FEA_ERR_UNSUPPORTED;
+    if (ring) {
+        const size_t need = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax, ring)
+                                                     : ring_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax, ring);
+        if (need > kStreamSmemLimit) return FEA_ERR_UNSUPPORTED;
+    }
     return FEA_OK;
 }
 
@@ -1740,7 +1756,7 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[11] = {0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16};
+    const int cand[15] = {0, 1, 2, 3, 6, 7, 10, 11, 12, 13, 14, 15, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
@@ -1770,7 +1786,7 @@ int fea_set_cg_variant(fea_solver* s, int variant) {
     check_handle(s);
     switch (variant_check(s, variant)) {
     case FEA_ERR_INVALID_ARGUMENT:
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0, 1, 2, 3, 4, 6, 7, 8, 10, 11 or 16");
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0 to 4, 6 to 8, 10 to 16");
     case FEA_ERR_UNSUPPORTED:
         return fail(FEA_ERR_UNSUPPORTED, s->ell.ok ? "streamed tiles exceed the shared memory on this mesh"
                                                    : "tile-ELL layout unavailable on this mesh");

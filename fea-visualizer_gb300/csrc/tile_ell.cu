@@ -91,6 +91,17 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
             }
         }
     }
+    std::vector<uint32_t> lcol2(E, 0u);
+    for (int64_t s = 0; s < nslices; s++) {
+        const int64_t sb = slice_off[s];
+        const int32_t w = (slice_off[s + 1] - slice_off[s]) / 32;
+        for (int32_t m = 0; 2 * m < w; m++)
+            for (int lane = 0; lane < 32; lane++) {
+                const uint32_t lo = lcol[sb + 32 * (2 * m) + lane];
+                const uint32_t hi = 2 * m + 1 < w ? lcol[sb + 32 * (2 * m + 1) + lane] : lo;
+                lcol2[sb + 32 * m + lane] = lo | (hi << 16);
+            }
+    }
     int64_t emax = 0;
     for (int64_t t = 0; t < ntiles; t++)
         emax = std::max<int64_t>(emax, slice_off[(t + 1) * (kTileRows / 32)] - slice_off[t * (kTileRows / 32)]);
@@ -102,6 +113,7 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
     L.halo_off = keep.alloc<int32_t>(ntiles + 1);
     L.halo_col = keep.alloc<int32_t>(std::max<int64_t>(1, (int64_t)halo_col.size()));
     L.lcol = keep.alloc<uint16_t>(std::max<int64_t>(1, E));
+    L.lcol2 = keep.alloc<uint32_t>(std::max<int64_t>(1, E));
     L.emap = keep.alloc<int32_t>(std::max<int64_t>(1, E));
     FEA_CUDA_TRY(cudaMemcpyAsync(L.slice_off, slice_off.data(), sizeof(int32_t) * (nslices + 1),
                                  cudaMemcpyHostToDevice, st));
@@ -112,6 +124,7 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
                                      cudaMemcpyHostToDevice, st));
     if (E > 0) {
         FEA_CUDA_TRY(cudaMemcpyAsync(L.lcol, lcol.data(), sizeof(uint16_t) * E, cudaMemcpyHostToDevice, st));
+        FEA_CUDA_TRY(cudaMemcpyAsync(L.lcol2, lcol2.data(), sizeof(uint32_t) * E, cudaMemcpyHostToDevice, st));
         FEA_CUDA_TRY(cudaMemcpyAsync(L.emap, emap.data(), sizeof(int32_t) * E, cudaMemcpyHostToDevice, st));
     }
     FEA_CUDA_TRY(cudaStreamSynchronize(st));  // the host vectors go out of scope

@@ -81,6 +81,11 @@ class InstanceDesc(C.Structure):
 
 # every function of include/fea_gpu.h with its argument types
 _P = C.c_void_p
+
+# CG iteration kernel variants of fea_set_cg_variant, and those that finish
+# each iteration at the start of the next launch (deferred finish)
+CG_VARIANTS = (0, 1, 2, 3, 6, 7, 10, 11, 12, 13, 14, 15, 4, 8, 16)
+DEFERRED_VARIANTS = (10, 11, 12, 13, 14, 15)
 _I64 = C.c_int64
 SIGNATURES = {
     "fea_params_default": [C.POINTER(Params)],
@@ -264,8 +269,10 @@ class CUDASolver:
     def set_cg_variant(self, variant: int):
         """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 2, 3: tile-ELL streamed by bulk copies
         (2 or 3 stages); 6, 7: the same with two block barriers per tile; 10, 11: variants 2 and 7
-        with the deferred finish (each launch finishes the previous one's iteration); 4, 8, 16:
-        windowed CSR kernels."""
+        with the deferred finish (each launch finishes the previous one's iteration); 12, 13: tile-ELL
+        with direct loads pipelined one tile ahead, deferred finish (three or two blocks per SM);
+        14, 15: direct row loads with the operator in a ring of 3 bulk-copy stages, deferred
+        finish (two or three blocks per SM); 4, 8, 16: windowed CSR kernels.  `CG_VARIANTS` lists them all."""
         check(load().fea_set_cg_variant(self._h, int(variant)))
 
     def stream(self) -> int:

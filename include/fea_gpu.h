@@ -140,7 +140,13 @@ int fea_params_default(fea_params* out);
  * assemble_matrices (:57-64).  vertices: xyz float[3V]; triangles: uint32[3T];
  * on_boundary: uint8[V] or NULL to detect boundary points on the device as
  * Surface::init_from_obj does (Surface.cpp:104-122).  params may be NULL
- * (defaults).  Returns FEA_ERR_BAD_MESH for an empty mesh or an index >= V. */
+ * (defaults).  Returns FEA_ERR_BAD_MESH (nothing allocated, no kernel fault)
+ * for an empty mesh, a triangle index >= V, a non-finite coordinate, or a
+ * zero-area triangle (collinear or repeated corners): the reference builds
+ * NaN element matrices from such triangles (glm::normalize of a zero normal,
+ * FEMContext.cpp:76) and solves on; here they are refused up front.  A
+ * triangle listed twice is valid input: its entries are summed twice, as
+ * Eigen's setFromTriplets does, and its edges count twice for the boundary. */
 int fea_create(const float* vertices, int64_t num_vertices, const uint32_t* triangles,
                int64_t num_triangles, const uint8_t* on_boundary, int boundary_condition,
                int precision, const fea_params* params, fea_solver** out);

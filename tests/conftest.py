@@ -10,7 +10,12 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "fea-visualizer_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-REFERENCE_ASSETS = "/root/reference/assets/fem_meshes"
+# The reference checkout's mesh folder (assets/fem_meshes), when one is
+# present: only the tests that re-read the OBJ files need it.  The meshes
+# themselves travel as tests/golden/reference_meshes.npz.
+REFERENCE_ASSETS = os.environ.get("FEA_REFERENCE_ASSETS", "")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
 
 
 def pytest_configure(config):
@@ -18,7 +23,14 @@ def pytest_configure(config):
 
 
 def has_reference_assets():
-    return os.path.isdir(REFERENCE_ASSETS)
+    return bool(REFERENCE_ASSETS) and os.path.isdir(REFERENCE_ASSETS)
+
+
+def reference_meshes():
+    """The reference's icosphere.obj and tube.obj as committed fixtures:
+    name -> (xyz float32 [V, 3], tri uint32 [T, 3])."""
+    from make_golden import load_fixture
+    return load_fixture()
 
 
 @pytest.fixture(scope="session")
@@ -60,3 +72,14 @@ def oracle_step(oracle_mod, S, eq, dt, u, v, n, **kw):
     if eq == oracle_mod.WAVE and kw.get("wave_scheme", 0) == 1:
         a = S.newmark_init(p, u)
     return S.step(p, u, v, a, nsteps=n)
+
+
+def device_field(s, which):
+    """Unknown-indexed state field of a handle in its precision (float64 for
+    FP64 handles), read through the device API."""
+    import torch
+    dt = torch.float64 if s.precision == 1 else torch.float32
+    t = [torch.zeros(s.info.num_unknowns, dtype=dt, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    s.get_fields_device(t[0].data_ptr(), t[1].data_ptr())
+    return t[which].cpu().numpy().astype(np.float64)

@@ -1,12 +1,18 @@
-"""Generates tests/golden/reference_meshes.json from the reference's own mesh
-assets (assets/fem_meshes/icosphere.obj and tube.obj of the reference project).
+"""Generates the golden fixtures of the reference's own mesh assets
+(assets/fem_meshes/icosphere.obj and tube.obj of the reference project):
 
-    python tests/golden/make_golden.py /root/reference/assets/fem_meshes
+    python tests/golden/make_golden.py <reference>/assets/fem_meshes
+    FEA_REFERENCE_ASSETS=<reference>/assets/fem_meshes python tests/golden/make_golden.py
 
-The fixture holds counts, pattern checksums and a few oracle results per mesh;
-it pins the oracle when the reference checkout is present and documents the
-reference meshes' known sizes when it is not.  Quads of tube.obj are split as
-fans (0, k, k+1): tinyobjloader's split rule is not vendored with the reference.
+- reference_meshes.npz: the two meshes as the OBJ reader returns them
+  (float32 positions, triangles as uint16), so that the tests, on this machine
+  and on the GPU machine, run the reference's fixtures without the reference
+  checkout;
+- reference_meshes.json: the sha256 of each source OBJ file, counts, pattern
+  checksums and a few oracle results per mesh.
+
+Quads of tube.obj are split as fans (0, k, k+1): tinyobjloader's split rule
+is not vendored with the reference.
 """
 import hashlib
 import json
@@ -20,14 +26,15 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "fea-visualizer_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
+# mesh name -> boundary condition it is summarised with (tube: Dirichlet, 192 boundary points)
+MESHES = {"icosphere": 1, "tube": 0}
+
 
 def _sig(x):
     return float(f"{float(x):.10g}")
 
 
-def summarise(oracle, path, bc):
-    from fea_gb300 import meshgen as mg
-    xyz, tri = mg.read_obj(path)
+def summarise(oracle, xyz, tri, bc):
     S = oracle.System(xyz, tri, bc=bc)
     out = {
         "bc": bc, "V": int(S.V), "T": int(S.T), "num_boundary": int(S.num_boundary), "N": int(S.N),
@@ -46,17 +53,34 @@ def summarise(oracle, path, bc):
     return out
 
 
+def load_fixture():
+    """name -> (xyz float32 [V, 3], tri uint32 [T, 3]) from reference_meshes.npz."""
+    z = np.load(os.path.join(HERE, "reference_meshes.npz"))
+    return {n: (z[n + "_xyz"], z[n + "_tri"].astype(np.uint32)) for n in MESHES}
+
+
 def main(asset_dir):
     import oracle
+    from fea_gb300 import meshgen as mg
     oracle.build()
-    gold = {"source": "reference assets/fem_meshes", "meshes": {
-        "icosphere": summarise(oracle, os.path.join(asset_dir, "icosphere.obj"), oracle.NEUMANN),
-        "tube": summarise(oracle, os.path.join(asset_dir, "tube.obj"), oracle.DIRICHLET),
-    }}
+    arrays, gold = {}, {"source": "reference assets/fem_meshes", "meshes": {}}
+    for name, bc in MESHES.items():
+        path = os.path.join(asset_dir, name + ".obj")
+        with open(path, "rb") as fh:
+            digest = hashlib.sha256(fh.read()).hexdigest()
+        xyz, tri = mg.read_obj(path)
+        assert xyz.shape[0] < 65536
+        arrays[name + "_xyz"] = xyz.astype(np.float32)
+        arrays[name + "_tri"] = tri.astype(np.uint16)
+        gold["meshes"][name] = dict(summarise(oracle, xyz, tri, bc), obj_sha256=digest)
+    np.savez_compressed(os.path.join(HERE, "reference_meshes.npz"), **arrays)
     with open(os.path.join(HERE, "reference_meshes.json"), "w") as fh:
         json.dump(gold, fh, indent=1, sort_keys=True)
     print(json.dumps(gold, indent=1))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/assets/fem_meshes")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FEA_REFERENCE_ASSETS")
+    if not src:
+        sys.exit("usage: make_golden.py <reference>/assets/fem_meshes (or set FEA_REFERENCE_ASSETS)")
+    main(src)

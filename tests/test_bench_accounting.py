@@ -34,10 +34,12 @@ def test_textbook_comparison():
 
 
 def test_kernel_names():
-    names = {v: bench.cg_kernel_name(v) for v in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16)}
+    names = {v: bench.cg_kernel_name(v) for v in (0, 1, 2, 3, 6, 7, 10, 11, 12, 13, 14, 15, 4, 8, 16)}
     assert names[0] == names[1] == "k_cgcg_iter_ell"
     assert all(names[v] == "k_cgcg_iter_stream" for v in (2, 3, 6, 7))
     assert names[10] == names[11] == "k_cgcg_iter_stream (deferred finish)"
+    assert names[12] == names[13] == "k_cgcg_iter_direct"
+    assert names[14] == names[15] == "k_cgcg_iter_ring"
     assert all(names[v] == "k_cgcg_iter" for v in (4, 8, 16))
 
 

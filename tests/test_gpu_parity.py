@@ -8,7 +8,7 @@ FP64 values to 1e-13; one time step agrees with the FP64 oracle (solved to
 import numpy as np
 import pytest
 
-from conftest import oracle_step, rel_l2
+from conftest import device_field, oracle_step, rel_l2
 from fea_gb300 import meshgen as mg
 
 pytestmark = pytest.mark.gpu
@@ -82,14 +82,7 @@ def test_explicit_zeros_kept_on_device(fea, oracle_mod):
     assert np.array_equal(val == 0, S.K == 0) and np.sum(val == 0) > 0
 
 
-def _device_field(s, which):
-    """Unknown-indexed state field in the handle's precision (float64 for FP64)."""
-    import torch
-    dt = torch.float64 if s.precision == 1 else torch.float32
-    t = [torch.zeros(s.info.num_unknowns, dtype=dt, device="cuda") for _ in range(2)]
-    torch.cuda.synchronize()
-    s.get_fields_device(t[0].data_ptr(), t[1].data_ptr())
-    return t[which].cpu().numpy().astype(np.float64)
+_device_field = device_field
 
 
 _oracle_step = oracle_step
@@ -270,7 +263,7 @@ def test_step_determinism(fea):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("variant", [2, 4, 10, 11])
+@pytest.mark.parametrize("variant", [2, 4, 10, 11, 12, 13])
 def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
     """The step graph chains 8 iteration kernels per pass of each CG loop; the
     copies that run after a solve has stopped change nothing.  The same steps
@@ -296,7 +289,7 @@ def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
     (fg, ig, lg, lig), (fs, is_, ls, lis) = res["graph"], res["stream"]
     assert np.array_equal(fg[0], fs[0]) and np.array_equal(fg[1], fs[1])
     assert ig == is_ and lig == lis and ig > 0
-    if variant in (10, 11):
+    if variant in fea.DEFERRED_VARIANTS:
         assert is_ < ls <= is_ + 4 * 2 * 2  # 4 steps, 2 solve loops each, at most 2 launches past the last iteration
         assert ig < lg <= ig + 4 * 2 * 8
     else:
@@ -333,8 +326,8 @@ def test_deferred_finish_bit_identical(fea, pair, precision):
 def test_autotune_choice_is_valid(fea):
     xyz, tri = mg.jittered_grid(129, seed=1)
     s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION)
-    assert s.info.rows_per_warp_lanes in (10, 11)  # the streamed deferred-finish kernel is the default
-    assert s.autotune() in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16)
+    assert s.info.rows_per_warp_lanes in fea.DEFERRED_VARIANTS  # a deferred-finish kernel is the default
+    assert s.autotune() in fea.CG_VARIANTS
     with pytest.raises(fea.FeaError):
         s.set_cg_variant(5)
 
@@ -350,7 +343,7 @@ def test_cg_variants_agree(fea, oracle_mod, name, bc):
     S = oracle_mod.System(xyz, tri, bc=bc)
     p = None
     outs = []
-    for variant in (0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16):
+    for variant in fea.CG_VARIANTS:
         s = _solver(fea, xyz, tri, bc, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-7, **kw)
         s.set_cg_variant(variant)
         s.set_fields(u0, v0)
@@ -360,7 +353,7 @@ def test_cg_variants_agree(fea, oracle_mod, name, bc):
     uo, vo, *_ = oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
                              S.gather(v0), 2, Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate,
                              reaction_mode=1)
-    for variant, (ug, vg) in zip((0, 1, 2, 3, 6, 7, 10, 11, 4, 8, 16), outs):
+    for variant, (ug, vg) in zip(fea.CG_VARIANTS, outs):
         assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, variant
 
 

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import REFERENCE_ASSETS, has_reference_assets
+from conftest import REFERENCE_ASSETS, has_reference_assets, reference_meshes
 from fea_gb300 import meshgen as mg
 
 
@@ -62,7 +62,16 @@ def test_initial_fields():
     assert np.sum(v > 0.2) > 0 and np.mean(u) > 0.8
 
 
-@pytest.mark.skipif(not has_reference_assets(), reason="reference mesh assets not present")
+def test_reference_mesh_fixture():
+    m = reference_meshes()
+    xyz, tri = m["icosphere"]
+    assert xyz.shape == (10242, 3) and tri.shape == (20480, 3)
+    xyz, tri = m["tube"]
+    assert xyz.shape == (4704, 3) and tri.shape == (9216, 3)
+    assert mg.boundary_vertices(tri, xyz.shape[0]).sum() == 192
+
+
+@pytest.mark.skipif(not has_reference_assets(), reason="FEA_REFERENCE_ASSETS not set")
 def test_read_reference_obj():
     xyz, tri = mg.read_obj(REFERENCE_ASSETS + "/icosphere.obj")
     assert xyz.shape == (10242, 3) and tri.shape == (20480, 3)

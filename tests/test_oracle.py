@@ -15,7 +15,7 @@ import pytest
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-from conftest import REFERENCE_ASSETS, has_reference_assets, rel_l2
+from conftest import REFERENCE_ASSETS, has_reference_assets, reference_meshes, rel_l2
 from fea_gb300 import meshgen as mg
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -316,16 +316,33 @@ def test_adjoint_matches_finite_differences(oracle_mod):
         assert abs(fd - gD @ dD) < 1e-5 * max(abs(fd), 1e-8)
 
 
-@pytest.mark.skipif(not has_reference_assets(), reason="reference mesh assets not present")
 def test_reference_meshes_against_golden(oracle_mod):
-    """The oracle on the reference's own meshes reproduces the committed fixture."""
+    """The oracle on the reference's own meshes (committed fixture arrays)
+    reproduces the committed summaries."""
     with open(os.path.join(GOLDEN, "reference_meshes.json")) as fh:
         gold = json.load(fh)
-    sys.path.insert(0, GOLDEN)
     from make_golden import summarise
+    meshes = reference_meshes()
     for name, want in gold["meshes"].items():
-        got = summarise(oracle_mod, os.path.join(REFERENCE_ASSETS, name + ".obj"), want["bc"])
+        xyz, tri = meshes[name]
+        got = summarise(oracle_mod, xyz, tri, want["bc"])
+        want = {k: v for k, v in want.items() if k != "obj_sha256"}
         assert got == want, name
+
+
+@pytest.mark.skipif(not has_reference_assets(), reason="FEA_REFERENCE_ASSETS not set")
+def test_reference_fixture_matches_obj_files():
+    """The committed fixture arrays are the reference's OBJ files as read."""
+    import hashlib
+    with open(os.path.join(GOLDEN, "reference_meshes.json")) as fh:
+        gold = json.load(fh)
+    meshes = reference_meshes()
+    for name, want in gold["meshes"].items():
+        path = os.path.join(REFERENCE_ASSETS, name + ".obj")
+        with open(path, "rb") as fh:
+            assert hashlib.sha256(fh.read()).hexdigest() == want["obj_sha256"], name
+        xyz, tri = mg.read_obj(path)
+        assert np.array_equal(xyz, meshes[name][0]) and np.array_equal(tri, meshes[name][1]), name
 
 
 def test_golden_known_counts():
