@@ -112,10 +112,11 @@ class Clocks:
 
 
 # DRAM bytes (read + write) per in-loop launch of the CG iteration kernel, by
-# variant: the mean of six consecutive launches of the step loop of this
-# workload in one ncu capture without cache control
-# (profiles/k_cgcg_iter_stream_gray_scott_1024.md).
-IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6}
+# variant: the mean of consecutive steady launches of the step loop of this
+# workload in one ncu capture without cache control (the capture commands sit
+# with the kernels' profile summaries).  A variant without an entry reports
+# traffic null.
+IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6, 14: 103.9e6}
 
 
 def cg_kernel_name(variant):
@@ -126,7 +127,7 @@ def cg_kernel_name(variant):
         return "k_cgcg_iter_stream"
     if variant in (10, 11):
         return "k_cgcg_iter_stream (deferred finish)"
-    if variant in (12, 13):
+    if variant == 13:
         return "k_cgcg_iter_direct"
     if variant in (14, 15):
         return "k_cgcg_iter_ring"
@@ -437,20 +438,56 @@ def max_over_ranks(value, dist=None, device="cpu"):
     return float(t.item())
 
 
-def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads):
-    """The reference's Eigen-semantics CPU step (the oracle's FP32 port):
-    A = M/dt + D K rebuilt every step, zero initial guess, tol = FLT_EPSILON."""
+FLT_EPSILON = 1.1920928955078125e-07
+# the reference's CG set-up (CPUSolver.cpp:65: Eigen's default tolerance, zero guess)
+REF_CG = "jacobi-pcg, zero guess, |r| < FLT_EPSILON |b|, double dots, operator rebuilt every step"
+EQ_CG = f"jacobi-pcg, warm start, |r| < {CG_TOL:g} |b| (the GPU arm's setting), double dots"
+
+
+_CPU_SYSTEMS = {}
+
+
+def cpu_system(xyz, tri):
+    """The oracle's FP32 port of the reference's assembled system (cached per mesh)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    S = O.System(xyz, tri, bc=O.NEUMANN, dtype="float32")
+    key = (xyz.shape[0], tri.shape[0])
+    if key not in _CPU_SYSTEMS:
+        _CPU_SYSTEMS[key] = O.System(xyz, tri, bc=O.NEUMANN, dtype="float32")
+    return O, _CPU_SYSTEMS[key]
+
+
+def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads, tol=FLT_EPSILON, warm_start=0):
+    """The reference's Eigen-semantics CPU step (the oracle's FP32 port):
+    A = M/dt + D K rebuilt every step; by default a zero initial guess and
+    tol = FLT_EPSILON as Eigen's ConjugateGradient uses (CPUSolver.cpp:65).
+    Returns (steps/s, CG iterations, seconds, nnz)."""
+    O, S = cpu_system(xyz, tri)
     p = O.params(O.REACTION_DIFFUSION, 1.0, Du=2e-5, Dv=1e-5, F=0.037, k=0.06, reaction_mode=1,
-                 tol=1.1920928955078125e-07, warm_start=0, nthreads=nthreads)
+                 tol=tol, warm_start=warm_start, nthreads=nthreads)
     u, v = S.gather(u0), S.gather(v0)
-    u, v, *_ = S.step(p, u, v, nsteps=1)  # warm-up (page-in)
+    u, v, *_ = S.step(p, u, v, nsteps=1)  # warm-up (page-in; the warm start's first guess)
     t0 = time.perf_counter()
     u, v, _, it, _ = S.step(p, u, v, nsteps=nsteps)
     dt = time.perf_counter() - t0
-    return nsteps / dt, it, dt
+    return nsteps / dt, it, dt, int(S.nnz)
+
+
+def cpu_baselines(xyz, tri, u0, v0, steps_all, steps_one):
+    """The CPU figures beside the GPU arm: the reference's semantics on all
+    host cores and on one (the reference builds without OpenMP,
+    CMakeLists.txt:106), and the same step with the GPU arm's tolerance and
+    warm start on all cores (equal work), which splits the GPU/CPU ratio into
+    algorithm and hardware."""
+    nthreads = os.cpu_count() or 1
+    out = {}
+    for name, nt, n, tol, ws, cg in (("threads_all", nthreads, steps_all, FLT_EPSILON, 0, REF_CG),
+                                     ("threads_1", 1, steps_one, FLT_EPSILON, 0, REF_CG),
+                                     ("equal_work", nthreads, steps_all, CG_TOL, 1, EQ_CG)):
+        sps, it, dt, nnz = cpu_sample(xyz, tri, u0, v0, n, nt, tol, ws)
+        out[name] = {"value": sps, "unit": "steps/s", "cores": nt, "steps": n, "seconds": dt,
+                     "cg_iterations_per_step": it / n, "cg": cg}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -459,18 +496,18 @@ def run_reference(args, rank, world):
         return
     xyz, tri, u0, v0 = workload()
     nthreads = os.cpu_count() or 1
-    sps, _, _ = cpu_sample(xyz, tri, u0, v0, max(1, args.warmup), nthreads)  # warm-up steps
-    t0 = time.perf_counter()
-    sps, it, dt = cpu_sample(xyz, tri, u0, v0, args.steps, nthreads)
+    cpu_sample(xyz, tri, u0, v0, max(1, args.warmup), nthreads)  # warm-up steps
+    sps, it, dt, nnz = cpu_sample(xyz, tri, u0, v0, args.steps, nthreads)
     value = args.steps / dt
-    nnz = None
+    cfg = config(int(xyz.shape[0]), int(tri.shape[0]), nnz,
+                 {"parallelism": f"cpu, OpenMP {nthreads} threads", "cg": REF_CG,
+                  "cg_iterations_per_step": it / args.steps})
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(int(xyz.shape[0]), int(tri.shape[0]), nnz, {"parallelism": "cpu threads"}),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{args.steps} full steps of the workload, oracle FP32 port "
-                                       f"(Eigen semantics: zero guess, per-step operator build), OpenMP"},
+                             "sample": f"{args.steps} full steps of the workload, oracle FP32 port of the "
+                                       f"reference's CPU step ({REF_CG}), OpenMP {nthreads} threads"},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -481,7 +518,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the all-cores CPU baseline samples")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched sweep")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint inverse-problem timing")
@@ -617,12 +654,16 @@ def main():
     configs = None if args.no_configs else bench_configs(F)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        nthreads = os.cpu_count() or 1
-        cps, cit, cdt = cpu_sample(xyz, tri, u0, v0, args.cpu_steps, nthreads)
-        cpu = {"value": cps, "unit": "steps/s", "cores": nthreads, "kind": "port",
-               "sample": f"{args.cpu_steps} full steps of the same workload ({cdt:.1f} s), oracle FP32 port "
-                         f"with Eigen semantics (zero guess, per-step operator build, tol FLT_EPSILON), "
-                         f"{cit} CG iterations"}
+        runs = cpu_baselines(xyz, tri, u0, v0, args.cpu_steps, 1)
+        a = runs["threads_all"]
+        cpu = {"value": a["value"], "unit": "steps/s", "cores": a["cores"], "kind": "port",
+               "sample": f"{a['steps']} full steps of the same workload ({a['seconds']:.1f} s), oracle FP32 "
+                         f"port of the reference's CPU step ({REF_CG}), "
+                         f"{a['cg_iterations_per_step']:.0f} CG iterations per step",
+               **runs,
+               "split": {"gpu_vs_cpu_same_semantics": value / a["value"],
+                         "algorithm (reference semantics vs equal work, CPU)": runs["equal_work"]["value"] / a["value"],
+                         "hardware (GPU vs CPU, equal work)": value / runs["equal_work"]["value"]}}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,

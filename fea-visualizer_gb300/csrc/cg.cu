@@ -758,14 +758,14 @@ __device__ __forceinline__ T ld_keep(const T* p, uint64_t pol) {
 }
 
 // Totals of NV values over nb block partials p[k * stride + b]: warp k merges
-// value k (lane l takes b = l, l + 32, ... with four loads in flight, then a
+// value k (lane l takes b = l, l + 32, ... with 16 loads in flight, then a
 // shuffle tree), a fixed order; lane 0 of warp k leaves total k in sm[k].
 // Needs NV <= the block's warps; every thread calls it (no barrier inside).
 template <int NV, typename R>
 __device__ __forceinline__ void merge_partials_by_warp(const typename Acc<R>::Packed* p, int64_t stride, int nb,
                                                        typename Acc<R>::Packed* sm) {
     using P = typename Acc<R>::Packed;
-    constexpr int B = 4;
+    constexpr int B = 16;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (w >= NV) return;
     Acc<R> y;
@@ -1460,21 +1460,18 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
 }
 
 // After the first CG loop: zero right-hand sides give x = 0 (Eigen's
-// early exit), then one float-float true-residual pass r = b - A x.  Fields
-// whose true residual is still above the threshold restart CG from there.
-template <typename R, int NF, int LANES>
-__global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
-    CgState* cg = a.cg;
-    const int stop = cg->stop;
-    const int refine = a.run->refine && cg->iter < cg->max_iter && !stop;
-    int zero[NF];
-#pragma unroll
-    for (int f = 0; f < NF; f++) zero[f] = !stop && !(cg->bb[f] > 0.0);
-    Acc<R> dots[2 * NF];
+// early exit), then one true-residual pass r = b - A x.  Fields whose true
+// residual is still above the threshold restart CG from there.  The pass
+// accumulates in the handle's accumulators (float-float pairs for FP32
+// handles, about 48 significant bits) or, with RunState::refine == 2, in
+// FP64: A x, r and the norms r.r, r.z in double, r rounded once to R.
+template <typename A, typename R, int NF, int LANES>
+__device__ __forceinline__ void refine_rows(const StepArgs<R, NF>& a, bool refine, const int (&zero)[NF],
+                                            int parity, A (&dots)[2 * NF]) {
     RowMap<LANES> m;
     for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
         const int64_t row = base + m.grp;
-        Acc<R> ax[NF];
+        A ax[NF];
         if (refine && row < a.N) {
             const int32_t e1 = ldg(a.rp + row + 1);
             for (int32_t e = ldg(a.rp + row) + m.sub; e < e1; e += LANES) {
@@ -1506,31 +1503,68 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
                 FV<R, NF> rv, pv;
 #pragma unroll
                 for (int f = 0; f < NF; f++) {
-                    Acc<R> t;
+                    A t;
                     t.add(bv.v[f]);
                     t.sub(ax[f]);
-                    rv.v[f] = t.rounded();
+                    rv.v[f] = (R)t.rounded();
                     pv.v[f] = d.v[f] * rv.v[f];
                     dots[f].add_prod(rv.v[f], rv.v[f]);
                     dots[NF + f].add_prod(rv.v[f], pv.v[f]);
                 }
-                a.rb[a.defer ? 0 : (cg->iter & 1)][row] = rv;  // the restart's buffer parity
+                a.rb[parity][row] = rv;  // the restart's buffer parity
                 a.z[row] = pv;
             }
         }
     }
-    Acc<R> tot[2 * NF];
-    if (grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot) && threadIdx.x == 0) {
+}
+
+template <typename R, int NF, int LANES>
+__global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
+    CgState* cg = a.cg;
+    const int stop = cg->stop;
+    const int mode = a.run->refine;
+    const bool refine = mode && cg->iter < cg->max_iter && !stop;
+    const bool fp64 = sizeof(R) == 4 && mode == 2;
+    const int parity = a.defer ? 0 : (cg->iter & 1);
+    int zero[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) zero[f] = !stop && !(cg->bb[f] > 0.0);
+    double rr[NF], rz[NF];
+    bool last;
+    if (fp64) {
+        Acc<double> dots[2 * NF], tot[2 * NF];
+        refine_rows<Acc<double>, R, NF, LANES>(a, refine, zero, parity, dots);
+        last = grid_reduce<double, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            rr[f] = tot[f].value();
+            rz[f] = tot[NF + f].value();
+        }
+    } else {
+        Acc<R> dots[2 * NF], tot[2 * NF];
+        refine_rows<Acc<R>, R, NF, LANES>(a, refine, zero, parity, dots);
+        last = grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot);
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            rr[f] = tot[f].value();
+            rz[f] = tot[NF + f].value();
+            if (last && threadIdx.x == 0 && refine && !zero[f] && cg->bb[f] > 0.0 && rr[f] >= cg->thr[f])
+                set_gamma((volatile CgState*)cg, f, tot[NF + f]);  // the pair itself for FP32 handles
+        }
+    }
+    if (last && threadIdx.x == 0) {
         int any = 0;
 #pragma unroll
         for (int f = 0; f < NF; f++) {
             cg->active[f] = 0;
             cg->fresh[f] = 1;
             if (refine && !zero[f] && cg->bb[f] > 0.0) {
-                const double rr = tot[f].value();
-                cg->rr[f] = rr;
-                if (rr >= cg->thr[f]) {
-                    set_gamma((volatile CgState*)cg, f, tot[NF + f]);
+                cg->rr[f] = rr[f];
+                if (rr[f] >= cg->thr[f]) {
+                    if (fp64) {  // gamma = r.z from the FP64 sum (float-float copy for the iterations)
+                        cg->rz[f] = rz[f];
+                        if constexpr (sizeof(R) == 4) ff_store(cg->ffrz[f], ff_of(rz[f]));
+                    }
                     cg->active[f] = 1;
                     any = 1;
                 }
@@ -1672,10 +1706,8 @@ struct DirectKernels : EllKernels<R, NF, 4> {
     static constexpr Fn iter = k_cgcg_iter_direct<R, NF, K, 0, MINB>;
     static Fn iter_par(int par) { return par ? k_cgcg_iter_direct<R, NF, K, 1, MINB> : iter; }
 };
-template <typename R, int NF>
-struct CgKernels<R, NF, 12> : DirectKernels<R, NF, (sizeof(FV<R, NF>) <= 8 ? 3 : 2)> {};
-// Variants 14 and 15: direct row loads with the operator in a ring of 3
-// bulk-copy stages; registers for two or three resident blocks per SM.
+// Variants 14 and 15: direct row loads with the operator in a ring of 3 or 4
+// bulk-copy stages.
 template <typename R, int NF, int S, int MINB>
 struct RingKernels : EllKernels<R, NF, 4> {
     using Fn = void (*)(StepArgs<R, NF>);
@@ -1686,8 +1718,8 @@ struct RingKernels : EllKernels<R, NF, 4> {
 template <typename R, int NF>
 struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};
 template <typename R, int NF>
-struct CgKernels<R, NF, 15> : RingKernels<R, NF, 3, (sizeof(FV<R, NF>) <= 8 ? 3 : 2)> {};
-// Variant 13: the same with registers for two resident blocks per SM.
+struct CgKernels<R, NF, 15> : RingKernels<R, NF, 4, 2> {};
+// Variant 13: registers for two resident blocks per SM (FP32 pairs: no spills).
 template <typename R, int NF>
 struct CgKernels<R, NF, 13> : DirectKernels<R, NF, (sizeof(FV<R, NF>) <= 8 ? 2 : 1)> {};
 
@@ -1839,7 +1871,6 @@ void dispatch_variant(StepGraph* G, const StepArgs<R, NF>& a, int wch, LoopFlags
     case 7: G ? build_graph_t<R, NF, EQ, 7>(*G, a, lf) : run_stream_t<R, NF, EQ, 7>(a, lf, st); break;
     case 10: G ? build_graph_t<R, NF, EQ, 10>(*G, a, lf) : run_stream_t<R, NF, EQ, 10>(a, lf, st); break;
     case 11: G ? build_graph_t<R, NF, EQ, 11>(*G, a, lf) : run_stream_t<R, NF, EQ, 11>(a, lf, st); break;
-    case 12: G ? build_graph_t<R, NF, EQ, 12>(*G, a, lf) : run_stream_t<R, NF, EQ, 12>(a, lf, st); break;
     case 13: G ? build_graph_t<R, NF, EQ, 13>(*G, a, lf) : run_stream_t<R, NF, EQ, 13>(a, lf, st); break;
     case 14: G ? build_graph_t<R, NF, EQ, 14>(*G, a, lf) : run_stream_t<R, NF, EQ, 14>(a, lf, st); break;
     case 15: G ? build_graph_t<R, NF, EQ, 15>(*G, a, lf) : run_stream_t<R, NF, EQ, 15>(a, lf, st); break;
@@ -1931,7 +1962,6 @@ void launch_spmv_probe(const StepArgs<R, NF>& a, int wch, cudaStream_t st) {
     case 7: probe_t<R, NF, 7>(a, st); break;
     case 10: probe_t<R, NF, 10>(a, st); break;
     case 11: probe_t<R, NF, 11>(a, st); break;
-    case 12: probe_t<R, NF, 12>(a, st); break;
     case 13: probe_t<R, NF, 13>(a, st); break;
     case 14: probe_t<R, NF, 14>(a, st); break;
     case 15: probe_t<R, NF, 15>(a, st); break;

@@ -241,7 +241,7 @@ int max_grid_blocks();
 
 // CG variants whose iteration kernels finish the previous launch's iteration
 // at their start (deferred finish; see StepArgs::defer).
-constexpr bool is_deferred_variant(int l) { return l >= 10 && l <= 15; }
+constexpr bool is_deferred_variant(int l) { return l >= 10 && l <= 15 && l != 12; }
 
 // ---- adjoint of the explicit advection-diffusion step (adjoint.cu) ----------------
 // lam = M (u - t), *J = 1/2 (u - t).lam  (exact accumulators; one block-partial

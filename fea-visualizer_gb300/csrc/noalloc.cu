@@ -16,6 +16,12 @@
 // contents: each call clears the loop state before use, and calls that
 // overlap on the GPU (other streams, other host threads) race on it.
 //
+// Outcome: FEA_STATUS_* bits of the solve (breakdown, non-finite values, no
+// convergence within max_iterations); breakdown and non-finite values also
+// make the call return FEA_ERR_SOLVE, since x is then no solution.  The host
+// reads the loop condition once per kNaItersPerCheck iterations: the kernels
+// of iterations past the end return at once.
+//
 // Inner products and the initial residual accumulate in the solvers' exact
 // accumulators (float-float pairs in FP32), block and grid totals included.
 #include <cmath>
@@ -31,9 +37,12 @@ constexpr size_t kNaVecBytes = (size_t)16 << 20;
 constexpr size_t kNaHeadBytes = (size_t)64 << 10;
 constexpr int kNaMaxDevices = 64;
 
+constexpr int kNaItersPerCheck = 8;
+
 struct NaState {
     double bb, rr, rz, pq, thr, alpha, beta;
-    int active, iter, max_iter, cont, zero_rhs, breakdown;
+    int active, iter, max_iter, cont, zero_rhs;
+    unsigned int flags;  // FEA_STATUS_*
     unsigned int ticket[4];
 };
 constexpr size_t kNaPartOffset = 256;
@@ -102,8 +111,14 @@ __global__ void __launch_bounds__(kBlock) k_na_init(NaArgs<R> a, double tol, int
         st->thr = fmax(tol * tol * tot[0], tiny);
         st->iter = 0;
         st->max_iter = max_iter;
-        st->zero_rhs = !(tot[0] > 0.0);
-        st->active = !st->zero_rhs && tot[1] >= st->thr;
+        if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2])) {  // NaN or Inf in A, b or x
+            st->flags |= FEA_STATUS_NONFINITE;
+            st->zero_rhs = 0;
+            st->active = 0;
+        } else {
+            st->zero_rhs = !(tot[0] > 0.0);  // Eigen's early exit: x = 0
+            st->active = !st->zero_rhs && tot[1] >= st->thr;
+        }
         st->cont = st->active;
     }
 }
@@ -123,8 +138,8 @@ __global__ void __launch_bounds__(kBlock) k_na_spmv(NaArgs<R> a) {
         NaState* st = a.st;
         st->pq = tot[0];
         const double al = st->rz / tot[0];
-        if (!(tot[0] > 0.0) || !isfinite(al)) {
-            st->breakdown = 1;
+        if (!(tot[0] > 0.0) || !isfinite(al)) {  // p.Ap <= 0: A is not SPD (or non-finite)
+            st->flags |= isfinite(tot[0]) ? FEA_STATUS_BREAKDOWN : FEA_STATUS_BREAKDOWN | FEA_STATUS_NONFINITE;
             st->active = 0;
             st->cont = 0;
         } else {
@@ -150,14 +165,19 @@ __global__ void __launch_bounds__(kBlock) k_na_update(NaArgs<R> a) {
         NaState* st = a.st;
         st->iter += 1;
         st->rr = tot[1];
-        if (!(tot[1] >= st->thr)) {  // converged (or a NaN residual, flagged below)
-            st->breakdown |= !isfinite(tot[1]);
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+            st->flags |= FEA_STATUS_NONFINITE;
+            st->active = 0;
+            st->cont = 0;
+        } else if (tot[1] < st->thr) {  // converged
             st->active = 0;
             st->cont = 0;
         } else {
             st->beta = tot[0] / st->rz;
             st->rz = tot[0];
-            st->cont = st->iter < st->max_iter;
+            if (!isfinite(st->beta)) st->flags |= FEA_STATUS_BREAKDOWN;
+            st->cont = isfinite(st->beta) && st->iter < st->max_iter;
+            if (isfinite(st->beta) && !st->cont) st->flags |= FEA_STATUS_NOT_CONVERGED;
             st->active = st->cont;
         }
     }
@@ -201,7 +221,7 @@ int na_scratch(unsigned char** out) {
 
 template <typename R>
 int na_solve(int64_t n, const int32_t* rp, const int32_t* col, const void* val, const void* b, void* x,
-             double tol, int max_iter, cudaStream_t st, int* iterations, double* rel_res) {
+             double tol, int max_iter, cudaStream_t st, int* iterations, double* rel_res, unsigned int* flags) {
     unsigned char* base = nullptr;
     int rc = na_scratch(&base);
     if (rc != FEA_OK) return rc;
@@ -228,18 +248,20 @@ int na_solve(int64_t n, const int32_t* rp, const int32_t* col, const void* val, 
     cudaError_t e = cudaMemsetAsync(a.st, 0, sizeof(NaState), st);
     if (e != cudaSuccess) return fail(FEA_ERR_CUDA, cudaGetErrorString(e));
     k_na_init<R><<<grid, kBlock, 0, st>>>(a, tol, max_iter);
-    int it = 0;
-    for (;;) {
+    int64_t it = 0;
+    for (;;) {  // the loop condition is read once per kNaItersPerCheck iterations
         int cont = 0;
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(&cont, &a.st->cont, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return fail(FEA_ERR_CUDA, cudaGetErrorString(e));
         if (!cont || it > max_iter) break;
-        k_na_spmv<R><<<grid, kBlock, 0, st>>>(a);
-        k_na_update<R><<<grid, kBlock, 0, st>>>(a);
-        k_na_dir<R><<<grid, kBlock, 0, st>>>(a);
-        it++;
+        for (int k = 0; k < kNaItersPerCheck; k++) {  // iterations past the end return at once
+            k_na_spmv<R><<<grid, kBlock, 0, st>>>(a);
+            k_na_update<R><<<grid, kBlock, 0, st>>>(a);
+            k_na_dir<R><<<grid, kBlock, 0, st>>>(a);
+        }
+        it += kNaItersPerCheck;
     }
     k_na_zero<R><<<grid, kBlock, 0, st>>>(a);
     NaState h{};
@@ -248,7 +270,13 @@ int na_solve(int64_t n, const int32_t* rp, const int32_t* col, const void* val, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(FEA_ERR_CUDA, cudaGetErrorString(e));
     if (iterations) *iterations = h.iter;
-    if (rel_res) *rel_res = h.bb > 0.0 ? sqrt(h.rr / h.bb) : 0.0;
+    if (rel_res) *rel_res = h.bb > 0.0 && isfinite(h.rr) ? sqrt(h.rr / h.bb) : (h.flags ? NAN : 0.0);
+    if (flags) *flags = h.flags;
+    if (h.flags & (FEA_STATUS_BREAKDOWN | FEA_STATUS_NONFINITE)) {
+        set_error("solve failed: %s", (h.flags & FEA_STATUS_NONFINITE) ? "non-finite values in A, b, x or the iterates"
+                                                                     : "breakdown (p.Ap <= 0: the matrix is not SPD)");
+        return FEA_ERR_SOLVE;
+    }
     return FEA_OK;
 }
 
@@ -258,7 +286,7 @@ int na_solve(int64_t n, const int32_t* rp, const int32_t* col, const void* val, 
 extern "C" int fea_pcg_solve_csr_noalloc(int64_t n, const int32_t* row_ptr, const int32_t* col, const void* values,
                                          const void* b, void* x, int precision, double tolerance,
                                          int max_iterations, void* stream, int* iterations,
-                                         double* rel_residual) {
+                                         double* rel_residual, unsigned int* status_flags) {
     using namespace fea;
     if (precision != FEA_FP32 && precision != FEA_FP64) return fail(FEA_ERR_INVALID_ARGUMENT, "bad precision");
     const size_t rsz = precision == FEA_FP64 ? sizeof(double) : sizeof(float);
@@ -271,13 +299,14 @@ extern "C" int fea_pcg_solve_csr_noalloc(int64_t n, const int32_t* row_ptr, cons
     if (n == 0) {
         if (iterations) *iterations = 0;
         if (rel_residual) *rel_residual = 0.0;
+        if (status_flags) *status_flags = 0u;
         return FEA_OK;
     }
     if (!row_ptr || !col || !values || !b || !x) return fail(FEA_ERR_INVALID_ARGUMENT, "null array");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (precision == FEA_FP64)
         return na_solve<double>(n, row_ptr, col, values, b, x, tolerance, max_iterations, st, iterations,
-                                rel_residual);
-    return na_solve<float>(n, row_ptr, col, values, b, x, tolerance, max_iterations, st, iterations,
-                           rel_residual);
+                                rel_residual, status_flags);
+    return na_solve<float>(n, row_ptr, col, values, b, x, tolerance, max_iterations, st, iterations, rel_residual,
+                           status_flags);
 }

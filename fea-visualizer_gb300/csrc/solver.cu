@@ -1734,8 +1734,8 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary) {
 static int variant_check(const fea_solver* s, int l) {
     const bool csr = l == 4 || l == 8 || l == 16;
     const int stages = (l == 2 || l == 6 || l == 10) ? 2 : (l == 3 || l == 7 || l == 11) ? 3 : 0;
-    const int ring = (l == 14 || l == 15) ? 3 : 0;
-    if (!csr && l != 0 && l != 1 && l != 12 && l != 13 && stages == 0 && ring == 0) return FEA_ERR_INVALID_ARGUMENT;
+    const int ring = l == 14 ? 3 : l == 15 ? 4 : 0;
+    if (!csr && l != 0 && l != 1 && l != 13 && stages == 0 && ring == 0) return FEA_ERR_INVALID_ARGUMENT;
     if (!csr && !s->ell.ok) return FEA_ERR_UNSUPPORTED;
     if (s->stream_stages < stages) return FEA_ERR_UNSUPPORTED;
     if (ring) {
@@ -1756,7 +1756,7 @@ int fea_autotune(fea_solver* s) {
     cudaEvent_t e0, e1;
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
-    const int cand[15] = {0, 1, 2, 3, 6, 7, 10, 11, 12, 13, 14, 15, 4, 8, 16};
+    const int cand[14] = {0, 1, 2, 3, 6, 7, 10, 11, 13, 14, 15, 4, 8, 16};
     float best = 1e30f;
     int best_l = s->lanes;
     for (int l : cand) {
@@ -1786,7 +1786,7 @@ int fea_set_cg_variant(fea_solver* s, int variant) {
     check_handle(s);
     switch (variant_check(s, variant)) {
     case FEA_ERR_INVALID_ARGUMENT:
-        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0 to 4, 6 to 8, 10 to 16");
+        return fail(FEA_ERR_INVALID_ARGUMENT, "CG variant must be 0 to 4, 6 to 8, 10, 11 or 13 to 16");
     case FEA_ERR_UNSUPPORTED:
         return fail(FEA_ERR_UNSUPPORTED, s->ell.ok ? "streamed tiles exceed the shared memory on this mesh"
                                                    : "tile-ELL layout unavailable on this mesh");

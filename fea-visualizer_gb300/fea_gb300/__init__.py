@@ -8,4 +8,5 @@ from . import meshgen  # noqa: F401
 from .binding import (  # noqa: F401
     ADVECTION, ADVECTION_DIFFUSION, CG_VARIANTS, DEFERRED_VARIANTS, DIRICHLET, FP32, FP64, HEAT, MASS, NEUMANN,
     REACTION_DIFFUSION, STIFFNESS, WAVE, BatchSolver, CUDASolver, FeaError, Params, default_params, load,
+    triangulate_pslg,
 )

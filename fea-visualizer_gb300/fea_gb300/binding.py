@@ -26,7 +26,7 @@ MESH_OPEN, MESH_CLOSED, MESH_MIRRORED = 0, 1, 2
 
 ERRORS = {
     -1: "invalid argument", -2: "CUDA error", -3: "no CUDA device", -4: "bad mesh",
-    -5: "out of memory", -6: "bad call order", -7: "unsupported", -8: "too large",
+    -5: "out of memory", -6: "bad call order", -7: "unsupported", -8: "too large", -9: "solve failed",
 }
 
 
@@ -84,8 +84,8 @@ _P = C.c_void_p
 
 # CG iteration kernel variants of fea_set_cg_variant, and those that finish
 # each iteration at the start of the next launch (deferred finish)
-CG_VARIANTS = (0, 1, 2, 3, 6, 7, 10, 11, 12, 13, 14, 15, 4, 8, 16)
-DEFERRED_VARIANTS = (10, 11, 12, 13, 14, 15)
+CG_VARIANTS = (0, 1, 2, 3, 6, 7, 10, 11, 13, 14, 15, 4, 8, 16)
+DEFERRED_VARIANTS = (10, 11, 13, 14, 15)
 _I64 = C.c_int64
 SIGNATURES = {
     "fea_params_default": [C.POINTER(Params)],
@@ -131,7 +131,11 @@ SIGNATURES = {
     "fea_batch_get_status": [_P, _P, _P],
     "fea_batch_cg_variant": [_P, C.c_int, C.POINTER(C.c_int)],
     "fea_pcg_solve_csr_noalloc": [_I64, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int, _P,
-                                  C.POINTER(C.c_int), C.POINTER(C.c_double)],
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
+    "fea_triangulate_pslg": [_P, _I64, _P, _I64, _P, _I64, C.c_double, C.c_double, C.POINTER(C.c_void_p)],
+    "fea_pslg_mesh_sizes": [_P, C.POINTER(_I64), C.POINTER(_I64)],
+    "fea_pslg_mesh_copy": [_P, _P, _P, _P],
+    "fea_pslg_mesh_destroy": [_P],
 }
 
 _lib = None
@@ -269,10 +273,10 @@ class CUDASolver:
     def set_cg_variant(self, variant: int):
         """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 2, 3: tile-ELL streamed by bulk copies
         (2 or 3 stages); 6, 7: the same with two block barriers per tile; 10, 11: variants 2 and 7
-        with the deferred finish (each launch finishes the previous one's iteration); 12, 13: tile-ELL
-        with direct loads pipelined one tile ahead, deferred finish (three or two blocks per SM);
-        14, 15: direct row loads with the operator in a ring of 3 bulk-copy stages, deferred
-        finish (two or three blocks per SM); 4, 8, 16: windowed CSR kernels.  `CG_VARIANTS` lists them all."""
+        with the deferred finish (each launch finishes the previous one's iteration); 13: tile-ELL
+        with direct loads pipelined one tile ahead, deferred finish; 14, 15: direct row loads with
+        the operator in a ring of 3 or 4 bulk-copy stages, deferred finish; 4, 8, 16: windowed CSR
+        kernels.  `CG_VARIANTS` lists them all."""
         check(load().fea_set_cg_variant(self._h, int(variant)))
 
     def stream(self) -> int:
@@ -480,3 +484,27 @@ class BatchSolver:
             self.close()
         except Exception:
             pass
+
+
+def triangulate_pslg(points, segments, holes=None, max_area=0.005, min_angle=20.0):
+    """Quality triangulation of a PSLG on the XZ plane (fea_triangulate_pslg):
+    points (x, z) [P, 2], segments [S, 2] point indices, holes (x, z) [H, 2].
+    Returns (vertices float32 [V, 3] as (x, 0, z), triangles uint32 [T, 3],
+    on_boundary uint8 [V]), the inputs of CUDASolver (Surface::init_from_PSLG)."""
+    L = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
+    seg = np.ascontiguousarray(segments, dtype=np.int32).reshape(-1, 2)
+    hol = None if holes is None or len(holes) == 0 else np.ascontiguousarray(holes, dtype=np.float64).reshape(-1, 2)
+    h = C.c_void_p()
+    check(L.fea_triangulate_pslg(_ptr(pts), pts.shape[0], _ptr(seg), seg.shape[0], _ptr(hol),
+                                 0 if hol is None else hol.shape[0], float(max_area), float(min_angle), C.byref(h)))
+    try:
+        nv, nt = _I64(0), _I64(0)
+        check(L.fea_pslg_mesh_sizes(h, C.byref(nv), C.byref(nt)))
+        xyz = np.zeros((nv.value, 3), dtype=np.float32)
+        tri = np.zeros((nt.value, 3), dtype=np.uint32)
+        ob = np.zeros(nv.value, dtype=np.uint8)
+        check(L.fea_pslg_mesh_copy(h, _ptr(xyz), _ptr(tri), _ptr(ob)))
+    finally:
+        L.fea_pslg_mesh_destroy(h)
+    return xyz, tri, ob

@@ -42,6 +42,7 @@ extern "C" {
 #define FEA_ERR_STATE (-6)       /* call order violated (e.g. step before assemble) */
 #define FEA_ERR_UNSUPPORTED (-7)
 #define FEA_ERR_TOO_LARGE (-8)
+#define FEA_ERR_SOLVE (-9)       /* a solve broke down or met NaN/Inf (fea_pcg_solve_csr_noalloc) */
 
 /* ---- step status flags (fea_get_status) ---------------------------------- */
 #define FEA_STATUS_BLOWUP 1u       /* some u_i or v_i > 1e4 (CPUSolver.cpp:41-48) */
@@ -104,7 +105,13 @@ typedef struct {
                              for FP32 handles, 1e-10 for FP64 (Eigen's default is
                              the type's epsilon) */
     int cg_max_iterations; /* 0 -> 2N (Eigen's default) */
-    int cg_refine;         /* 1: one FP64 true-residual refinement pass per solve */
+    int cg_refine;         /* after each solve's CG loop, one true-residual pass
+                              r = b - A x (CG restarts from it when |r| is still
+                              above the tolerance): 1 accumulates it in the
+                              handle's accumulators (FP64 for FP64 handles,
+                              float-float pairs of about 48 significant bits
+                              for FP32 handles), 2 in FP64 for FP32 handles
+                              too, 0 skips it.  Default 1. */
 } fea_params;
 
 typedef struct {
@@ -226,17 +233,21 @@ int fea_get_idx_map(fea_solver* s, int32_t* idx_map, uint8_t* on_boundary);
  * next tile's first block barrier (two barriers per tile instead of three),
  * 10 and 11 = variants 2 and 7 whose iterations are finished by the next
  * launch (every block merges the block partials at its start) instead of
- * by the last block to end, 4 / 8 / 16 = warp-cooperative CSR with that many
- * entries per lane and window.  A new handle starts on variant 11 (10 when
- * only two stages fit in shared memory, 0 when none do, 8 without the
- * tile-ELL layout).  fea_autotune times one CG iteration of each candidate
- * on this mesh and keeps the fastest (fea_info.rows_per_warp_lanes); the
- * fields are left unchanged. */
+ * by the last block to end, 13 = tile-ELL with every load issued by the
+ * threads (operator entries into registers one tile ahead, rows half a tile
+ * ahead) and the deferred finish, 14 and 15 = variant 13 with the operator
+ * entries and columns moved by bulk copies into a ring of 3 or 4
+ * shared-memory stages, 4 / 8 / 16 = warp-cooperative CSR with that many
+ * entries per lane and window.  A new handle starts on variant 14 (11 when
+ * its ring does not fit in shared memory, 10 when only two streamed stages
+ * fit, 0 when none do, 8 without the tile-ELL layout).  fea_autotune times
+ * one CG iteration of each candidate on this mesh and keeps the fastest
+ * (fea_info.rows_per_warp_lanes); the fields are left unchanged. */
 int fea_autotune(fea_solver* s);
 /* Select a variant explicitly (FEA_ERR_INVALID_ARGUMENT for another value,
- * FEA_ERR_UNSUPPORTED for 0 to 3, 6, 7, 10 and 11 when the layout, or for
- * the streamed variants the shared memory of their stages, is unavailable
- * on this mesh). */
+ * FEA_ERR_UNSUPPORTED for the tile-ELL variants when the layout, or for the
+ * streamed and ring variants the shared memory of their stages, is
+ * unavailable on this mesh). */
 int fea_set_cg_variant(fea_solver* s, int variant);
 
 /* The CUDA stream (cudaStream_t) the handle runs on, for callers that order
@@ -384,12 +395,47 @@ int fea_batch_cg_variant(fea_batch* b, int set, int* variant);
  * The work vectors live in one static device array of 16 MiB + 64 KiB that
  * every GPU loading the library holds until exit, so n is limited to
  * 1,048,576 (FP32) or 524,288 (FP64); larger n returns FEA_ERR_TOO_LARGE.
- * The first call on a device looks up that array's device address; make it
- * before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race, so serialise them per device. */
+ * The first call on a device looks up that array's device address.  The
+ * call reads the loop condition back to the host (a copy and a stream
+ * synchronisation every 8 CG iterations), so it cannot be called while its
+ * stream is being captured into a graph.  Calls share the array: calls that
+ * overlap on the GPU race, so serialise them per device.
+ * Outcome: *status_flags (may be NULL) receives FEA_STATUS_* bits --
+ * FEA_STATUS_NOT_CONVERGED when max_iterations ran out above the tolerance
+ * (the call still returns FEA_OK; *rel_residual tells how far it got),
+ * FEA_STATUS_BREAKDOWN when p.Ap <= 0 (A is not SPD), FEA_STATUS_NONFINITE
+ * for NaN or Inf in A, b, x or the iterates.  The last two return
+ * FEA_ERR_SOLVE: x is then no solution.  A zero b gives x = 0 (Eigen's early
+ * exit), 0 iterations and FEA_OK. */
 int fea_pcg_solve_csr_noalloc(int64_t n, const int32_t* row_ptr, const int32_t* col, const void* values,
                               const void* b, void* x, int precision, double tolerance, int max_iterations,
-                              void* stream, int* iterations, double* rel_residual);
+                              void* stream, int* iterations, double* rel_residual, unsigned int* status_flags);
+
+/* ---- drawn domains: PSLG -> quality triangle mesh ----------------------------
+ * Replaces Surface::init_from_PSLG + Surface::perform_triangulation
+ * (src/Utils/Surface.cpp:25-49, 431-486), which call Triangle with the
+ * switches "Qeqpza<area>": a conforming quality mesh (minimum angle
+ * min_angle_deg, Triangle's default 20; max_area = PSLG::triangle_area,
+ * include/Utils/PSLG.hpp:29, default 0.005; 0 for no area bound) of the
+ * region enclosed by the segments, with the triangles around each hole point
+ * removed.  points: double[2 * num_points], the (x, z) coordinates on the XZ
+ * plane (Surface.cpp:28-31); segments: int32[2 * num_segments] point index
+ * pairs; holes: double[2 * num_holes] (x, z) or NULL.  Host code (no GPU).
+ * The result holds vertices (x, 0, z), triangles with the reference's
+ * reversed corner order (Surface.cpp:468) and on_boundary = 1 for vertices on
+ * a segment (Triangle's point markers, Surface.cpp:472-478), ready for
+ * fea_create.  FEA_ERR_BAD_MESH for an invalid PSLG (no triangle inside its
+ * segments -- Surface.cpp:40-41 throws -- crossing or duplicate input,
+ * indices out of range), FEA_ERR_TOO_LARGE when refinement would exceed its
+ * vertex budget. */
+typedef struct fea_pslg_mesh fea_pslg_mesh;
+int fea_triangulate_pslg(const double* points, int64_t num_points, const int32_t* segments, int64_t num_segments,
+                         const double* holes, int64_t num_holes, double max_area, double min_angle_deg,
+                         fea_pslg_mesh** out);
+int fea_pslg_mesh_sizes(const fea_pslg_mesh* m, int64_t* num_vertices, int64_t* num_triangles);
+/* vertices: float[3V], triangles: uint32[3T], on_boundary: uint8[V] (each may be NULL) */
+int fea_pslg_mesh_copy(const fea_pslg_mesh* m, float* vertices, uint32_t* triangles, uint8_t* on_boundary);
+int fea_pslg_mesh_destroy(fea_pslg_mesh* m);
 
 /* ---- misc ----------------------------------------------------------------- */
 const char* fea_last_error(void);

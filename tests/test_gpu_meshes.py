@@ -141,3 +141,30 @@ def test_duplicated_triangle(fea, oracle_mod, bc):
     s.advance_time(2)
     uo, *_ = oracle_step(oracle_mod, S, oracle_mod.HEAT, 0.01, S.gather(u0), np.zeros(S.N), 2, kappa=1.0)
     assert rel_l2(device_field(s, 0), uo) < 1e-9
+
+
+@pytest.mark.parametrize("bc", [0, 1])
+def test_pslg_mesh_steps(fea, oracle_mod, bc):
+    """A drawn domain (a square with a square hole, the reference's default
+    triangle area 0.005) triangulated by fea_triangulate_pslg goes through
+    fea_create with its boundary flags, as Surface::init_from_PSLG hands them
+    on (Surface.cpp:472-478), and steps to the oracle's result."""
+    sq = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], float)
+    hole = np.array([[0.4, 0.4], [0.6, 0.4], [0.6, 0.6], [0.4, 0.6]])
+    ring = lambda n, s: np.array([[s + i, s + (i + 1) % n] for i in range(n)])  # noqa: E731
+    xyz, tri, ob = fea.triangulate_pslg(np.vstack([sq, hole]), np.vstack([ring(4, 0), ring(4, 4)]), [[0.5, 0.5]],
+                                        max_area=0.005)
+    s = fea.CUDASolver(xyz, tri, boundary_condition=bc, precision=fea.FP64, on_boundary=ob,
+                       params=fea.default_params(equation=fea.HEAT, heat_time_step=0.01, heat_conductivity=0.5,
+                                                 cg_tolerance=1e-12))
+    S = oracle_mod.System(xyz, tri, bc=bc, on_boundary=ob)
+    assert s.info.num_boundary_points == int(ob.sum()) == S.num_boundary
+    rp, col, _, _ = s.matrix(fea.STIFFNESS)
+    np.testing.assert_array_equal(rp, S.row_ptr)
+    np.testing.assert_array_equal(col, S.col)
+    u0 = np.sin(np.pi * xyz[:, 0]) * np.sin(np.pi * xyz[:, 2]).astype(np.float32)
+    s.set_values(u0.astype(np.float32))
+    s.advance_time(3)
+    uo, *_ = oracle_step(oracle_mod, S, oracle_mod.HEAT, 0.01, S.gather(u0.astype(np.float32)), np.zeros(S.N), 3,
+                         kappa=0.5)
+    assert rel_l2(device_field(s, 0), uo) < 1e-9

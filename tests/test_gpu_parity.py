@@ -146,6 +146,33 @@ def test_gray_scott_per_step(fea, oracle_mod, mode):
     assert s.status().steps_done == 20
 
 
+@pytest.mark.parametrize("refine", [0, 1, 2])
+def test_refinement_modes(fea, oracle_mod, refine):
+    """cg_refine 0 (no true-residual pass), 1 (float-float for FP32 handles)
+    and 2 (FP64): Gray-Scott steps of an FP32 handle meet the same bar
+    against the FP64 oracle, and modes 1 and 2 agree closely."""
+    xyz, tri = mg.jittered_grid(65, seed=8)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=2, side=0.12)
+    kw = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+    out = {}
+    for mode in sorted({1, refine}):
+        s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-6,
+                    cg_refine=mode, **kw)
+        s.set_fields(u0, v0)
+        s.advance_time(5)
+        out[mode] = s.get_fields()
+        assert s.status().flags == 0
+        p = s.params
+    S = oracle_mod.System(xyz, tri, bc=1)
+    uo, vo, *_ = _oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
+                              S.gather(v0), 5, Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate,
+                              reaction_mode=1)
+    ug, vg = out[refine]
+    assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5
+    if refine != 1:
+        assert rel_l2(ug, out[1][0]) < 1e-5 and rel_l2(vg, out[1][1]) < 1e-5
+
+
 @pytest.mark.parametrize("scheme", [0, 1])
 def test_wave_steps(fea, oracle_mod, scheme):
     xyz, tri = mg.icosphere(4)
@@ -263,7 +290,7 @@ def test_step_determinism(fea):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("variant", [2, 4, 10, 11, 12, 13])
+@pytest.mark.parametrize("variant", [2, 4, 10, 11, 13, 14, 15])
 def test_unrolled_loop_matches_stream_launches(fea, monkeypatch, variant):
     """The step graph chains 8 iteration kernels per pass of each CG loop; the
     copies that run after a solve has stopped change nothing.  The same steps
