@@ -154,6 +154,9 @@ def iter_bytes(N, nnz, nfields=2):
 
 # Batched sweep: 256 Gray-Scott instances on icospheres of uneven size
 BATCH_N = 256
+# CG tolerance of the sweep: the loosest whose one step from the oracle's
+# state stays within rel-L2 1e-5 on every instance (tests/test_gpu_batch_sweep.py)
+BATCH_CG_TOL = 1e-6
 BATCH_LEVELS = (3, 4, 5, 6)
 BATCH_PARAMS = dict(time_step=0.5, Du=2e-4, Dv=1e-4)
 
@@ -368,38 +371,68 @@ def bench_gs_adjoint(F):
     return out
 
 
+def batch_iter_bytes(insts):
+    """Algorithmic bytes of one CG iteration of every instance of a batch:
+    iter_bytes of each instance's mesh (closed meshes: N = V, nnz = V + 2E)."""
+    import numpy as np
+    total = 0
+    for d in insts:
+        tri = np.asarray(d["triangles"], dtype=np.int64)
+        e = np.sort(np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]]), axis=1)
+        nedges = np.unique(e[:, 0] * (1 << 32) + e[:, 1]).size
+        V = d["vertices"].shape[0]
+        total += iter_bytes(V, V + 2 * nedges)
+    return total
+
+
 def bench_batched(F, steps, warmup, plain_steps):
     """The 256-instance sweep in one batch vs the plain loop of single-mesh
     handles (one after another, each advancing its own graph)."""
     import numpy as np
     insts, starts = batch_workload()
     t0 = time.perf_counter()
-    B = F.BatchSolver(insts, cg_tolerance=CG_TOL)
+    B = F.BatchSolver(insts, cg_tolerance=BATCH_CG_TOL)
     setup_s = time.perf_counter() - t0
     for i, (u, v) in enumerate(starts):
         B.set_fields(i, u, v)
     B.advance_time(warmup)
     B.synchronize()
+    it0, _ = B.counters()
     t0 = time.perf_counter()
     B.advance_time(steps)
     B.synchronize()
     batch_s = time.perf_counter() - t0
+    it1, _ = B.counters()
     flags, iters = B.status()
+    batch_variant = B.cg_variant
     handles = []
     for d in insts:
         p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=d["time_step"],
                              rd_Du=d["Du"], rd_Dv=d["Dv"], rd_feed_rate=d["feed_rate"],
-                             rd_kill_rate=d["kill_rate"], cg_tolerance=CG_TOL)
+                             rd_kill_rate=d["kill_rate"], cg_tolerance=BATCH_CG_TOL)
         handles.append(F.CUDASolver(d["vertices"], d["triangles"], boundary_condition=F.NEUMANN, params=p))
-    for h, (u, v) in zip(handles, starts):
-        h.set_fields(u, v)
-        h.advance_time(1)
-        h.synchronize()
-    t0 = time.perf_counter()
-    for h in handles:
-        h.advance_time(plain_steps)
-        h.synchronize()
-    plain_s = time.perf_counter() - t0
+    plain = {}
+    # the plain loop on the handles' default kernels, and on the batch's own kernel family
+    for name, var in (("default", None), ("same_family", batch_variant)):
+        for h, (u, v) in zip(handles, starts):
+            if var is not None:
+                h.set_cg_variant(var)
+            h.set_fields(u, v)
+            h.advance_time(1)
+            h.synchronize()
+        t0 = time.perf_counter()
+        for h in handles:
+            h.advance_time(plain_steps)
+            h.synchronize()
+        plain[name] = time.perf_counter() - t0
+    plain_s = plain["default"]
+    # roofline of the batched CG iteration kernel: one launch over every
+    # instance, back to back (each launch streams more than the L2)
+    it_ms = B.time_iteration(20)
+    it_bytes = batch_iter_bytes(insts)
+    peak, peak_kind = measured_peak_hbm()
+    # the whole sweep's effective rate: the iterations it ran, per second
+    sweep_bytes = float(np.sum((it1 - it0) * np.array([batch_iter_bytes([d]) for d in insts])))
     # accuracy of the batch against the plain handles: the same 5 steps from the start state
     for i, (h, (u, v)) in enumerate(zip(handles, starts)):
         h.set_fields(u, v)
@@ -414,12 +447,26 @@ def bench_batched(F, steps, warmup, plain_steps):
     nverts = sum(d["vertices"].shape[0] for d in insts)
     batch_rate = BATCH_N * steps / batch_s
     plain_rate = BATCH_N * plain_steps / plain_s
+    same_rate = BATCH_N * plain_steps / plain["same_family"]
     B.close()
+    achieved = it_bytes / (it_ms * 1e-3) / 1e9
     return {"workload": f"{BATCH_N} gray-scott instances, icospheres of levels {list(BATCH_LEVELS)} drawn "
-                        f"uniformly, F ~ U(0.01,0.06), k ~ U(0.045,0.07), Du 2e-4, Dv 1e-4, dt 0.5",
+                        f"uniformly, F ~ U(0.01,0.06), k ~ U(0.045,0.07), Du 2e-4, Dv 1e-4, dt 0.5, "
+                        f"CG |r| < {BATCH_CG_TOL:g} |b|",
             "vertices": nverts, "steps": steps, "instance_steps_per_s": batch_rate,
             "sweep_steps_per_s": steps / batch_s, "plain_instance_steps_per_s": plain_rate,
             "plain_steps_timed": plain_steps, "speedup_vs_plain": batch_rate / plain_rate,
+            "plain_same_family_instance_steps_per_s": same_rate, "speedup_vs_plain_same_family": batch_rate / same_rate,
+            "cg_variant": batch_variant,
+            "cg_iterations_per_sweep_step_mean_instance": float(np.mean(it1 - it0)) / steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "algorithmic_bytes_per_batched_iteration": it_bytes, "ms_per_batched_iteration": it_ms,
+                         "how": "fea_batch_time_iteration: the iteration kernel over every instance, fields masked, "
+                                "20 launches back to back (CUDA events); bytes: iter_bytes of each instance's mesh",
+                         "peak_source": peak_kind,
+                         "sweep_effective_GBps": sweep_bytes / batch_s / 1e9,
+                         "sweep_effective_how": "algorithmic bytes of the CG iterations the timed sweep ran, over "
+                                                "its wall time (right-hand sides, refinement and launches included)"},
             "max_rel_l2_vs_plain_after_5_steps": err, "setup_s": setup_s,
             "status_flags_or": int(np.bitwise_or.reduce(flags)),
             "max_iterations_last_solve": int(iters.max()), "min_iterations_last_solve": int(iters.min()),
@@ -643,6 +690,19 @@ def main():
     e2e = world * args.steps / e2e_s
 
     flags = s.status().flags
+    # the cost of the FP64 true-residual pass (cg_refine = 2) against the
+    # default float-float pass: the same steps from the same state, device-timed
+    refine_ms = {}
+    for mode in (1, 2):
+        q = F.binding.Params.from_buffer_copy(p)
+        q.cg_refine = mode
+        s.set_params(q)
+        s.set_fields(start_u, start_v)
+        s.advance_time(1)  # graph instantiation
+        s.set_fields(start_u, start_v)
+        ms, its = _timed_steps(s, args.steps)
+        refine_ms[mode] = (ms / args.steps, its / args.steps)
+    s.set_params(p)
     # the roofline's launch duration: one CG iteration as the step loop runs it
     iter_ms, pinned_iters = in_loop_iteration_ms(F, s, p, start_u, start_v, stream)
     achieved = bytes_spmv / (iter_ms * 1e-3) / 1e9
@@ -690,6 +750,10 @@ def main():
                          "peak_source": peak_kind, "variant": lanes,
                          "ms_per_launch_isolated_by_variant": variant_ms},
             "cpu_baseline": cpu,
+            "refinement": {"float_float_ms_per_step": refine_ms[1][0], "fp64_ms_per_step": refine_ms[2][0],
+                           "float_float_cg_iterations_per_step": refine_ms[1][1],
+                           "fp64_cg_iterations_per_step": refine_ms[2][1],
+                           "how": "cg_refine 1 and 2, the same steps from the warm-up state, no L2 flush"},
             "batched": batched,
             "adjoint": adjoint,
             "gray_scott_adjoint": gs_adjoint,

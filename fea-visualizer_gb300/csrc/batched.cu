@@ -186,6 +186,22 @@ __device__ __forceinline__ bool batch_stopped(const BArgs<R>& a) {
     return true;
 }
 
+// Timing probe of an iteration kernel: every tile iterates with its fields
+// masked, so x and p are written back unchanged and only CG scratch (which
+// the next step recomputes) changes; the instances' state is left alone.
+template <typename R>
+__device__ __forceinline__ void probe_mask(PhaseCtl<R, 2>& c) {
+#pragma unroll
+    for (int f = 0; f < 2; f++) {
+        c.act[f] = 0;
+        c.fresh[f] = false;
+        c.alpha[f] = 0;
+        c.beta[f] = 0;
+    }
+    c.need_old = true;
+    c.any = false;
+}
+
 // Right-hand side b = M (x/dt + f(x)) of every unfrozen instance, initial
 // residual r = b - A x (warm start), z = D^-1 r, and the set-up scalars;
 // instances whose state entering the step is unstable are frozen.
@@ -329,20 +345,21 @@ __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) kb_iter(BArgs<R> a
         const int i = a.tile_inst[tile];
         PhaseCtl<R, 2> c;
         c.set(iter, (const volatile BInst*)(a.inst + i));
-        if (!c.any) continue;
+        if (a.probe) probe_mask(c);
+        if (!c.any && !a.probe) continue;
         Acc<R> dots[kNV];  // gamma', delta', |r'|^2
         cgcg_tile<R, 2, WCH>(v, c, (int64_t)tile * kTile, a.N, sm[wib], ut, dots);
         Acc<R> blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
-        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
             volatile BInst* s = a.inst + i;
             if (finish_cgcg<R, 2>(s, &a.inst[i].flags, c.act, tot))
                 atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
         }
     }
     grid_launch_dependents();
-    phase_end(a, kIterNext);
+    if (!a.probe) phase_end(a, kIterNext);
 }
 
 // The same two kernels on the tile-ELL layout of the stacked matrix (the
@@ -417,21 +434,22 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
         const int i = a.tile_inst[tile];
         PhaseCtl<R, 2> c;
         c.set(iter, (const volatile BInst*)(a.inst + i));
-        if (!c.any) continue;
+        if (a.probe) probe_mask(c);
+        if (!c.any && !a.probe) continue;
         Acc<R> dots[kNV];
         cgcg_tile_ell<R, 2, KPRE>(v, e, c, tile, ell_ref(e, tile, a.ntiles), a.N, ut + buf * stride, dots);
         buf ^= 1;
         Acc<R> blk[kNV], tot[kNV];
         block_totals<kNV>(dots, red, blk);
         const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
-        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0) {
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && threadIdx.x == 0 && !a.probe) {
             volatile BInst* s = a.inst + i;
             if (finish_cgcg<R, 2>(s, &a.inst[i].flags, c.act, tot))
                 atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
         }
     }
     grid_launch_dependents();
-    phase_end(a, kIterNext);
+    if (!a.probe) phase_end(a, kIterNext);
 }
 
 // After the first solve loop: zero right-hand sides give x = 0, then one
@@ -864,6 +882,29 @@ void batch_probe(fea_batch* B, int var) {
     }
 }
 
+template <typename R, int V>
+void batch_iter_probe_t(fea_batch* B, const BArgs<R>& a) {
+    const BGrids<R, V> g(B);
+    BKernels<R, V>::iter<<<g.iter, kBlock, g.smem, B->stream>>>(a);
+    FEA_CHECK_LAUNCH();
+}
+
+// One iteration kernel of the batch's variant over every tile, fields masked
+// (probe_mask): the timing probe of fea_batch_time_iteration.
+template <typename R>
+void batch_iter_probe(fea_batch* B) {
+    BArgs<R> a = make_bargs<R>(B);
+    a.probe = 1;
+    a.use_graph = 0;
+    a.cont = &B->flags->probe;
+    switch (B->wch) {
+    case 0: batch_iter_probe_t<R, 0>(B, a); break;
+    case 1: batch_iter_probe_t<R, 1>(B, a); break;
+    case 4: batch_iter_probe_t<R, 4>(B, a); break;
+    default: batch_iter_probe_t<R, 8>(B, a); break;
+    }
+}
+
 // Pick the CG kernel variant by timing the set-up SpMV of each candidate.
 template <typename R>
 void autotune_batch(fea_batch* B) {
@@ -1205,6 +1246,68 @@ int fea_batch_cg_variant(fea_batch* B, int set, int* variant) {
     if (v != 0 && v != 1 && v != 4 && v != 8) return fail(FEA_ERR_INVALID_ARGUMENT, "batch CG variant must be 0, 1, 4 or 8");
     if (v <= 1 && !B->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable for this batch");
     B->wch = v;
+    BATCH_API_END
+}
+
+int fea_batch_set_cg(fea_batch* B, double cg_tolerance, int cg_max_iterations) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    if (!(cg_tolerance >= 0.0)) return fail(FEA_ERR_INVALID_ARGUMENT, "bad CG tolerance");
+    const int n = B->ninst;
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    std::vector<BInst> h(n);
+    std::vector<int32_t> t0(n + 1);
+    BCtl c{};
+    FEA_CUDA_TRY(cudaMemcpy(h.data(), B->inst, sizeof(BInst) * n, cudaMemcpyDeviceToHost));
+    FEA_CUDA_TRY(cudaMemcpy(t0.data(), B->inst_tile, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost));
+    FEA_CUDA_TRY(cudaMemcpy(&c, B->ctl, sizeof(BCtl), cudaMemcpyDeviceToHost));
+    B->tol = cg_tolerance > 0.0 ? cg_tolerance : (B->precision == FEA_FP64 ? 1e-10 : 1.1920928955078125e-07);
+    B->max_iter_cfg = cg_max_iterations;
+    for (int i = 0; i < n; i++) {  // default limit: twice the instance's rows (its tiles, padding included)
+        const int64_t lim = cg_max_iterations > 0 ? cg_max_iterations : 2 * (int64_t)(t0[i + 1] - t0[i]) * kTile;
+        h[i].max_iter = (int)std::min<int64_t>(std::max<int64_t>(lim, 1), 0x7fffffff);
+    }
+    c.tol = B->tol;
+    FEA_CUDA_TRY(cudaMemcpy(B->inst, h.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice));
+    FEA_CUDA_TRY(cudaMemcpy(B->ctl, &c, sizeof(BCtl), cudaMemcpyHostToDevice));
+    BATCH_API_END
+}
+
+int fea_batch_time_iteration(fea_batch* B, int reps, double* ms_per_launch) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    if (reps <= 0 || !ms_per_launch) return fail(FEA_ERR_INVALID_ARGUMENT, "bad arguments");
+    cudaEvent_t e0, e1;
+    FEA_CUDA_TRY(cudaEventCreate(&e0));
+    FEA_CUDA_TRY(cudaEventCreate(&e1));
+    auto launch = [&]() {
+        if (B->precision == FEA_FP64) batch_iter_probe<double>(B);
+        else batch_iter_probe<float>(B);
+    };
+    launch();  // warm-up
+    FEA_CUDA_TRY(cudaEventRecord(e0, B->stream));
+    for (int r = 0; r < reps; r++) launch();
+    FEA_CUDA_TRY(cudaEventRecord(e1, B->stream));
+    FEA_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    FEA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_launch = ms / reps;
+    BATCH_API_END
+}
+
+int fea_batch_get_counters(fea_batch* B, int64_t* total_iterations, int64_t* steps_done) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    const int n = B->ninst;
+    std::vector<BInst> h(n);
+    FEA_CUDA_TRY(cudaMemcpyAsync(h.data(), B->inst, sizeof(BInst) * n, cudaMemcpyDeviceToHost, B->stream));
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    for (int i = 0; i < n; i++) {
+        if (total_iterations) total_iterations[i] = h[i].total_iters;
+        if (steps_done) steps_done[i] = h[i].steps_done;
+    }
     BATCH_API_END
 }
 

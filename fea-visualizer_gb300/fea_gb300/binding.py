@@ -129,6 +129,9 @@ SIGNATURES = {
     "fea_batch_advance_time": [_P, _I64],
     "fea_batch_synchronize": [_P],
     "fea_batch_get_status": [_P, _P, _P],
+    "fea_batch_set_cg": [_P, C.c_double, C.c_int],
+    "fea_batch_get_counters": [_P, _P, _P],
+    "fea_batch_time_iteration": [_P, C.c_int, C.POINTER(C.c_double)],
     "fea_batch_cg_variant": [_P, C.c_int, C.POINTER(C.c_int)],
     "fea_pcg_solve_csr_noalloc": [_I64, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int, _P,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
@@ -466,6 +469,23 @@ class BatchSolver:
         """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 4, 8: windowed CSR kernels."""
         v = C.c_int(int(variant))
         check(load().fea_batch_cg_variant(self._h, 1, C.byref(v)))
+
+    def set_cg(self, tolerance: float, max_iterations: int = 0):
+        """New CG stopping rule of every instance (fea_batch_set_cg)."""
+        check(load().fea_batch_set_cg(self._h, float(tolerance), int(max_iterations)))
+
+    def time_iteration(self, reps: int = 10) -> float:
+        """ms per CG iteration launch over every instance (fea_batch_time_iteration)."""
+        ms = C.c_double(0)
+        check(load().fea_batch_time_iteration(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def counters(self):
+        """(total CG iterations int64[n], steps done int64[n]) since creation."""
+        it = np.zeros(self.num_instances, dtype=np.int64)
+        st = np.zeros(self.num_instances, dtype=np.int64)
+        check(load().fea_batch_get_counters(self._h, _ptr(it), _ptr(st)))
+        return it, st
 
     def status(self):
         """(flags uint32[n], iterations int32[n, 2] of the last solve)."""

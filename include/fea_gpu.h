@@ -374,6 +374,18 @@ int fea_batch_advance_time(fea_batch* b, int64_t nsteps);
 int fea_batch_synchronize(fea_batch* b);
 /* flags: uint32[num_instances]; iterations: int32[2*num_instances] (last solve) */
 int fea_batch_get_status(fea_batch* b, uint32_t* flags, int32_t* iterations);
+/* No reference counterpart.  New CG stopping rule of every instance:
+ * tolerance (0 -> FLT_EPSILON, 1e-10 for FP64) and iteration limit (0 ->
+ * twice the instance's rows, whole tiles). */
+int fea_batch_set_cg(fea_batch* b, double cg_tolerance, int cg_max_iterations);
+/* No reference counterpart.  Per instance, int64[num_instances] each (NULL to
+ * skip): CG iterations and steps since the batch was created. */
+int fea_batch_get_counters(fea_batch* b, int64_t* total_iterations, int64_t* steps_done);
+/* No reference counterpart.  Device time of one CG iteration kernel of the
+ * batch's variant over every instance (fields masked: x and the instances'
+ * state are unchanged; only CG scratch that the next step recomputes is
+ * written), averaged over reps back-to-back launches after one warm-up. */
+int fea_batch_time_iteration(fea_batch* b, int reps, double* ms_per_launch);
 /* CG kernel variant of the batch: 0 / 1 tile-ELL (8 / 4 entries prefetched;
  * FEA_ERR_UNSUPPORTED when the layout is unavailable), 4 / 8 windowed CSR.
  * fea_batch_create picks the fastest by timing; *variant receives the
