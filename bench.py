@@ -36,6 +36,9 @@ PARAMS = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_k
 # against the FP64 oracle stays below 1e-5 with margin (about 2.5e-6, set by the
 # FP32 matrix values; tests/test_gpu_fullsize.py checks it on this workload)
 CG_TOL = 1e-5
+# the solves' start: 1 = 2 x_n - x_(n-1) from the last two steps (0: the
+# previous solution)
+CG_GUESS = 1
 METRIC = "Gray-Scott 1M-vert steps/s at rel-L2<=1e-5, batched vs plain; CG SpMV HBM GB/s"
 
 
@@ -116,7 +119,7 @@ class Clocks:
 # workload in one ncu capture without cache control (the capture commands sit
 # with the kernels' profile summaries).  A variant without an entry reports
 # traffic null.
-IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6, 14: 103.9e6}
+IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6, 14: 91.2e6}
 
 
 def cg_kernel_name(variant):
@@ -488,7 +491,8 @@ def max_over_ranks(value, dist=None, device="cpu"):
 FLT_EPSILON = 1.1920928955078125e-07
 # the reference's CG set-up (CPUSolver.cpp:65: Eigen's default tolerance, zero guess)
 REF_CG = "jacobi-pcg, zero guess, |r| < FLT_EPSILON |b|, double dots, operator rebuilt every step"
-EQ_CG = f"jacobi-pcg, warm start, |r| < {CG_TOL:g} |b| (the GPU arm's setting), double dots"
+EQ_CG = f"jacobi-pcg, |r| < {CG_TOL:g} |b| (the GPU arm's setting), double dots"
+GUESS_LABEL = {0: "previous solution", 1: "2 x_n - x_(n-1) (extrapolated)"}
 
 
 _CPU_SYSTEMS = {}
@@ -504,34 +508,47 @@ def cpu_system(xyz, tri):
     return O, _CPU_SYSTEMS[key]
 
 
-def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads, tol=FLT_EPSILON, warm_start=0):
+def cpu_sample(xyz, tri, u0, v0, nsteps, nthreads, tol=FLT_EPSILON, warm_start=0, prev=None):
     """The reference's Eigen-semantics CPU step (the oracle's FP32 port):
     A = M/dt + D K rebuilt every step; by default a zero initial guess and
     tol = FLT_EPSILON as Eigen's ConjugateGradient uses (CPUSolver.cpp:65).
-    Returns (steps/s, CG iterations, seconds, nnz)."""
+    Without `prev` the timed steps follow one untimed step from (u0, v0);
+    with prev (the state one step before u0, v0) they start at (u0, v0)
+    itself, the first one extrapolated from prev (warm_start 2), after an
+    untimed step from the same state.  Returns (steps/s, CG iterations,
+    seconds, nnz)."""
     O, S = cpu_system(xyz, tri)
     p = O.params(O.REACTION_DIFFUSION, 1.0, Du=2e-5, Dv=1e-5, F=0.037, k=0.06, reaction_mode=1,
                  tol=tol, warm_start=warm_start, nthreads=nthreads)
     u, v = S.gather(u0), S.gather(v0)
-    u, v, *_ = S.step(p, u, v, nsteps=1)  # warm-up (page-in; the warm start's first guess)
+    pv = None if prev is None else (S.gather(prev[0]), S.gather(prev[1]))
+    u1, v1, *_ = S.step(p, u, v, nsteps=1, prev=pv)  # warm-up (page-in)
+    if prev is None:
+        u, v = u1, v1  # the warm start's first guess
     t0 = time.perf_counter()
-    u, v, _, it, _ = S.step(p, u, v, nsteps=nsteps)
+    u, v, _, it, _ = S.step(p, u, v, nsteps=nsteps, prev=pv)
     dt = time.perf_counter() - t0
     return nsteps / dt, it, dt, int(S.nnz)
 
 
-def cpu_baselines(xyz, tri, u0, v0, steps_all, steps_one):
+def cpu_baselines(xyz, tri, u0, v0, steps_all, steps_one, guess, eq_state):
     """The CPU figures beside the GPU arm: the reference's semantics on all
     host cores and on one (the reference builds without OpenMP,
     CMakeLists.txt:106), and the same step with the GPU arm's tolerance and
-    warm start on all cores (equal work), which splits the GPU/CPU ratio into
-    algorithm and hardware."""
+    initial guess on all cores (equal work), which splits the GPU/CPU ratio
+    into algorithm and hardware.  The equal-work sample runs the GPU arm's
+    timed steps themselves: from the state where its timed region starts,
+    eq_state = (u, v, u_prev, v_prev), four times as many steps as the other
+    samples (they are cheaper)."""
     nthreads = os.cpu_count() or 1
     out = {}
-    for name, nt, n, tol, ws, cg in (("threads_all", nthreads, steps_all, FLT_EPSILON, 0, REF_CG),
-                                     ("threads_1", 1, steps_one, FLT_EPSILON, 0, REF_CG),
-                                     ("equal_work", nthreads, steps_all, CG_TOL, 1, EQ_CG)):
-        sps, it, dt, nnz = cpu_sample(xyz, tri, u0, v0, n, nt, tol, ws)
+    eu, ev, pu, pv = eq_state
+    for name, nt, n, tol, ws, cg, start, prev in (
+            ("threads_all", nthreads, steps_all, FLT_EPSILON, 0, REF_CG, (u0, v0), None),
+            ("threads_1", 1, steps_one, FLT_EPSILON, 0, REF_CG, (u0, v0), None),
+            ("equal_work", nthreads, 4 * steps_all, CG_TOL, 1 + guess, f"{EQ_CG}, start: {GUESS_LABEL[guess]}",
+             (eu, ev), (pu, pv) if guess == 1 else None)):
+        sps, it, dt, nnz = cpu_sample(xyz, tri, start[0], start[1], n, nt, tol, ws, prev)
         out[name] = {"value": sps, "unit": "steps/s", "cores": nt, "steps": n, "seconds": dt,
                      "cg_iterations_per_step": it / n, "cg": cg}
     return out
@@ -574,6 +591,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--cg-variant", type=int, default=None,
                     help="CG kernel variant instead of the autotuned one (profiling captures)")
+    ap.add_argument("--initial-guess", type=int, default=CG_GUESS,
+                    help="cg_initial_guess: 0 previous solution, 1 extrapolated from the last two steps")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="vertices per side (other sizes are for profiling captures, not bench lines)")
     args = ap.parse_args()
@@ -597,7 +616,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     xyz, tri, u0, v0 = workload()
-    p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=CG_TOL, **PARAMS)
+    p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=CG_TOL,
+                         cg_initial_guess=args.initial_guess, **PARAMS)
     s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=F.FP32, params=p)
     lanes = s.autotune()
     if args.cg_variant is not None:
@@ -611,7 +631,9 @@ def main():
 
     # warm-up; the timed step sequences below all start from this state, so
     # they run the same steps (the CG iteration count changes as the pattern evolves)
-    s.advance_time(args.warmup)
+    s.advance_time(args.warmup - 1)
+    prev_u, prev_v = s.get_fields()  # the state one step before the timed region (unchanged history)
+    s.advance_time(1)
     s.synchronize()
     st0 = s.status()
     start_u, start_v = s.get_fields()
@@ -714,7 +736,8 @@ def main():
     configs = None if args.no_configs else bench_configs(F)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        runs = cpu_baselines(xyz, tri, u0, v0, args.cpu_steps, 1)
+        runs = cpu_baselines(xyz, tri, u0, v0, args.cpu_steps, 1, args.initial_guess,
+                             (start_u, start_v, prev_u, prev_v))
         a = runs["threads_all"]
         cpu = {"value": a["value"], "unit": "steps/s", "cores": a["cores"], "kind": "port",
                "sample": f"{a['steps']} full steps of the same workload ({a['seconds']:.1f} s), oracle FP32 "
@@ -731,11 +754,16 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config(int(V), int(tri.shape[0]), int(nnz),
                              {"parallelism": "replicas" if world > 1 else "single gpu", "cg_variant": lanes,
+                              "cg": f"jacobi-pcg, |r| < {CG_TOL:g} |b|, start: {GUESS_LABEL[args.initial_guess]}, "
+                                    "float-float dots and scalars",
                               "cg_iterations_per_step": iters / args.steps,
                               "one_launch_ms_per_step": one_launch_ms / args.steps}),
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": 4 * V},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": IN_LOOP_TRAFFIC.get(lanes),
+                         "frac_algorithmic": achieved / peak,
+                         "frac_dram": (IN_LOOP_TRAFFIC[lanes] / (iter_ms * 1e-3) / 1e9 / peak
+                                       if lanes in IN_LOOP_TRAFFIC else None),
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, in-loop launches, "
                                            "--cache-control none" if lanes in IN_LOOP_TRAFFIC else
                                            "no capture of this variant",

@@ -28,6 +28,8 @@
 #include <vector>
 
 #include "cg_device.cuh"
+#include "ring.cuh"
+#include "tma.cuh"
 
 namespace fea {
 namespace {
@@ -102,6 +104,17 @@ struct BArgs {
     const int32_t* halo_off;
     const int32_t* halo_col;
     int hmax;
+    // ring kernel (variant 14): the layout it streams (the tile-ELL copy
+    // without diagonal entries; the diagonal term A_ii u'_i is the row's new
+    // residual r'_i, as u' = D^-1 r'), its largest tile
+    const FV<R, 2>* As_od;
+    const uint16_t* lcol_od;
+    const int32_t* slice_off_od;
+    int emax;                  // stored entries of the largest tile of the streamed layout
+    int tcap;                  // tile-list capacity of a block
+    const int32_t* inst_grp;   // [ninst + 1] first group slot of each instance
+    double* gpart;             // [groups * kNV] group partials
+    int32_t* act_pos;          // [ninst + 1] active-tile table (build_active_table); null: not kept
     cudaGraphConditionalHandle cond;
     int* cont;
     int use_graph;
@@ -137,9 +150,57 @@ __device__ bool inst_commit(const Acc<R> (&blk)[NV], double* part, int tile, int
 
 enum { kIterKeep = 0, kIterNext = 1, kIterReset = 2 };
 
+// Sum of v over the block, in every thread, and in `before` the sum over the
+// threads below this one; wsum: kBlock / 32 ints.
+__device__ __forceinline__ int block_sum_int(int v, int* wsum, int& before) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[wib] = incl;
+    __syncthreads();
+    int tot = 0;
+    before = incl - v;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; w++) {
+        const int s = wsum[w];
+        tot += s;
+        if (w < wib) before += s;
+    }
+    __syncthreads();  // wsum is reused
+    return tot;
+}
+
+// The active-tile table of the ring kernel (act_pos): instance i's tiles
+// start at act_pos[i] in the sequence of the active instances' tiles laid end
+// to end; act_pos[ninst] is the total.  Built by the last block of a phase,
+// when no block of the phase reads it any more and before the next phase can.
+template <typename R>
+__device__ void build_active_table(const BArgs<R>& a) {
+    __shared__ int wsum[kBlock / 32];
+    int base = 0;
+    for (int i0 = 0; i0 < a.ninst; i0 += kBlock) {
+        const int i = i0 + threadIdx.x;
+        int nt = 0;
+        if (i < a.ninst) {
+            const volatile BInst* s = a.inst + i;
+            if (s->active[0] || s->active[1]) nt = a.inst_tile[i + 1] - a.inst_tile[i];
+        }
+        int before;
+        const int tot = block_sum_int(nt, wsum, before);
+        if (i < a.ninst) a.act_pos[i] = base + before;
+        base += tot;
+    }
+    if (threadIdx.x == 0) a.act_pos[a.ninst] = base;
+}
+
 // End of a phase: the block that finishes last publishes whether any
 // (instance, field) solve is still active, resets the phase counter, moves the
-// iteration counter and sets the loop condition.
+// iteration counter and sets the loop condition; with the ring kernel it also
+// builds the next phase's active-tile table.
 template <typename R>
 __device__ void phase_end(const BArgs<R>& a, int iter_mode) {
     __shared__ bool lastb;
@@ -158,6 +219,10 @@ __device__ void phase_end(const BArgs<R>& a, int iter_mode) {
         if (iter_mode == kIterNext) c->iter = c->iter + 1;
         if (iter_mode == kIterReset) c->iter = 0;
         signal_loop(a, n > 0);
+    }
+    if (lastb && a.act_pos) {
+        __threadfence();
+        build_active_table(a);
     }
 }
 
@@ -452,6 +517,350 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
     if (!a.probe) phase_end(a, kIterNext);
 }
 
+// ---- variant 14: the operator streamed by a bulk-copy ring ----------------------
+//
+// The single-mesh ring kernel's tile pipeline over the batch's tiles: thread
+// 0 moves each tile's operator entries and 16-bit local columns with
+// cp.async.bulk into a ring of S shared-memory stages, S - 1 tiles ahead of
+// the product; the threads load their rows' r, w, s, D^-1, x, p and their
+// halo slot's operands one tile ahead; one block barrier per tile orders the
+// staged u'.
+//
+// Work.  Each instance's tiles are cut into groups of kGroupTiles consecutive
+// tiles (an instance's last group may be shorter).  At the start of a launch
+// every block reads every instance's activity, lays the active instances'
+// tiles end to end, and takes the groups that start in its equal share of
+// that sequence, so the blocks get equal work however many instances have
+// converged.  The threads accumulate a group's inner products over its
+// tiles; at the group's last tile the block reduces them into the group's
+// partials, and the block that completes an instance's last group sums the
+// instance's group partials in group order and advances its CG scalars.  The
+// groups are fixed per instance, so an instance's results depend neither on
+// the other instances nor on the schedule.
+constexpr int kGroupTiles = 8;
+
+// An active instance with groups in the block's share.
+struct BRingInst {
+    int inst, nt, t0, g0, ng;  // instance, tiles, first tile, first group slot, groups
+    int u0, u1;                // its groups in the share
+};
+
+// Dynamic shared memory of kb_iter_ring: the ring, the two u' buffers, then
+// the block's instances, their phase controls and its tile list (tile, index
+// of its instance in the block's list, group slot), each for up to tcap tiles.
+template <typename R>
+struct BRingLayout {
+    size_t ubuf, ov, ctl, tl, tq, tg, total;
+    __host__ __device__ BRingLayout(int emax, int hmax, int tcap, int stages) {
+        auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
+        ubuf = al((size_t)stages * RingStage(emax, sizeof(FV<R, 2>)).bytes);
+        ov = al(ubuf + 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + hmax));
+        ctl = al(ov + sizeof(BRingInst) * (size_t)tcap);
+        tl = al(ctl + sizeof(PhaseCtl<R, 2>) * (size_t)tcap);
+        tq = al(tl + sizeof(int32_t) * (size_t)tcap);
+        tg = al(tq + sizeof(int32_t) * (size_t)tcap);
+        total = al(tg + sizeof(int32_t) * (size_t)tcap);
+    }
+};
+
+template <typename R, int S>
+__global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
+    using V = FV<R, 2>;
+    static_assert(S >= 2 && S <= 8, "ring depth");
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
+    __shared__ __align__(8) uint64_t bars[S];
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
+    __shared__ int s_nov, s_ntl;
+    const BRingLayout<R> Lay(a.emax, a.hmax, a.tcap, S);
+    const RingStage L(a.emax, sizeof(V));
+    const bool od = a.As_od != nullptr;  // the streamed layout lacks the diagonal entries
+    const V* const Aop = od ? a.As_od : a.As;
+    const uint16_t* const lop = od ? a.lcol_od : a.lcol;
+    const int32_t* const soff = od ? a.slice_off_od : a.slice_off;
+    unsigned char* const ring = dyn_smem;
+    V* const ubuf = reinterpret_cast<V*>(dyn_smem + Lay.ubuf);
+    BRingInst* const ov = reinterpret_cast<BRingInst*>(dyn_smem + Lay.ov);
+    PhaseCtl<R, 2>* const ovc = reinterpret_cast<PhaseCtl<R, 2>*>(dyn_smem + Lay.ctl);
+    int32_t* const tl = reinterpret_cast<int32_t*>(dyn_smem + Lay.tl);
+    int32_t* const tq = reinterpret_cast<int32_t*>(dyn_smem + Lay.tq);
+    int32_t* const tg = reinterpret_cast<int32_t*>(dyn_smem + Lay.tg);
+    const int ustride = kTileRows + a.hmax;
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
+    const int ntiles = a.ntiles, tcap = a.tcap;
+    if (t == 0) {
+        for (int b = 0; b < S; b++) mbar_init(&bars[b], 1);
+        mbar_fence_init();
+        s_nov = 0;
+    }
+    grid_dependency_wait();
+    if (batch_stopped(a)) return;
+    const int iter = iter_of(a), par = iter & 1;
+    // the active instances' tiles laid end to end (the table the previous
+    // phase's last block built; every instance in a probe); this block's share
+    // [lo, hi) and the instances with a group starting in it
+    const int32_t* pos_of = a.probe ? a.inst_tile : a.act_pos;
+    const int T = pos_of[a.ninst];
+    const int lo = (int)((int64_t)T * blockIdx.x / gridDim.x);
+    const int hi = (int)((int64_t)T * (blockIdx.x + 1) / gridDim.x);
+    for (int i = t; i < a.ninst; i += kBlock) {
+        const int pos = pos_of[i], nt = pos_of[i + 1] - pos;
+        if (nt > 0 && pos + nt > lo && pos < hi) {
+            const int ng = (nt + kGroupTiles - 1) / kGroupTiles;
+            const int u0 = lo > pos ? (lo - pos + kGroupTiles - 1) / kGroupTiles : 0;
+            const int u1 = min(ng, (hi - pos + kGroupTiles - 1) / kGroupTiles);
+            if (u0 < u1) {
+                PhaseCtl<R, 2> c;
+                c.set(iter, (const volatile BInst*)(a.inst + i));
+                if (a.probe) probe_mask(c);
+                const int q = atomicAdd(&s_nov, 1);
+                if (q < tcap) {
+                    ov[q] = BRingInst{i, nt, a.inst_tile[i], a.inst_grp[i], ng, u0, u1};
+                    ovc[q] = c;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (t == 0) {  // the block's tile list
+        const int nov = min(s_nov, tcap);
+        int k = 0;
+        for (int q = 0; q < nov; q++) {
+            const BRingInst o = ov[q];
+            for (int u = o.u0; u < o.u1; u++) {
+                const int x1 = min((u + 1) * kGroupTiles, o.nt);
+                for (int x = u * kGroupTiles; x < x1; x++, k++)
+                    if (k < tcap) {
+                        tl[k] = o.t0 + x;
+                        tq[k] = q;
+                        tg[k] = o.g0 + u;
+                    }
+            }
+        }
+        s_ntl = k;
+        if (k > tcap || s_nov > tcap) {  // the host sizes tcap for the largest share: not reached
+            atomicOr(&a.inst[0].flags, FEA_STATUS_BREAKDOWN);
+            s_ntl = 0;
+        }
+    }
+    __syncthreads();
+    const int ntl = s_ntl;
+    auto tile_at = [&](int k) { return k < ntl ? tl[k] : ntiles; };
+    auto halo_head = [&](int tile, int32_t& h0, int32_t& cnt) {
+        h0 = cnt = 0;
+        if (tile < ntiles) {
+            h0 = a.halo_off[tile];
+            cnt = a.halo_off[tile + 1] - h0;
+        }
+    };
+    auto slice_ref = [&](int tile, int32_t& sb, int32_t& sw) {
+        sb = sw = 0;
+        if (tile < ntiles) {
+            const int sl = tile * (kTileRows / 32) + wib;
+            const int32_t s0 = soff[sl];
+            sb = s0 - soff[tile * (kTileRows / 32)];
+            sw = (soff[sl + 1] - s0) >> 5;
+        }
+    };
+    auto tile_range = [&](int tile, int32_t& e0, int32_t& e1) {
+        e0 = e1 = 0;
+        if (tile < ntiles) {
+            e0 = soff[tile * (kTileRows / 32)];
+            e1 = soff[(tile + 1) * (kTileRows / 32)];
+        }
+    };
+    auto stage_of = [&](int b) { return ring + (size_t)b * L.bytes; };
+    auto issue = [&](int b, int32_t e0, int32_t e1) {
+        uint64_t* bar = &bars[b];
+        const uint32_t n = (uint32_t)(e1 - e0);  // a multiple of 32 entries
+        if (n == 0) {
+            mbar_arrive(bar);
+            return;
+        }
+        mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
+        const uint64_t pol = l2_evict_first_policy();
+        bulk_g2s_hint(stage_of(b) + L.A, Aop + e0, n * (uint32_t)sizeof(V), bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.L, lop + e0, 2 * n, bar, pol);
+    };
+    uint32_t armed = 0;  // thread 0: bit b set while stage b has copies in flight
+    int32_t re0 = 0, re1 = 0;
+    if (t == 0) {
+        for (int b = 0; b < S && b < ntl; b++) {
+            int32_t e0, e1;
+            tile_range(tl[b], e0, e1);
+            issue(b, e0, e1);
+            armed |= 1u << b;
+        }
+        tile_range(tile_at(S), re0, re1);
+    }
+    int32_t sb, sw, sbn, swn;
+    slice_ref(tile_at(0), sb, sw);
+    slice_ref(tile_at(1), sbn, swn);
+    int32_t h0c, hcc, h0n, hcn, hh0, hhc;
+    halo_head(tile_at(0), h0c, hcc);
+    halo_head(tile_at(1), h0n, hcn);
+    halo_head(tile_at(2), hh0, hhc);
+    const int32_t fcol = j < hcc ? a.halo_col[h0c + j] : -1;
+    int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
+    CgVecs<R, 2> v;
+    v.rp = a.rp;
+    v.col = a.col;
+    v.A = a.A;
+    v.dinv = a.dinv;
+    v.x = a.x;
+    v.p = a.p;
+    v.r0 = a.rb[par];
+    v.w0 = a.wb[par];
+    v.s0 = a.sb[par];
+    v.r1 = a.rb[par ^ 1];
+    v.w1 = a.wb[par ^ 1];
+    v.s1 = a.sb[par ^ 1];
+    V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
+    {
+        const uint64_t pol_keep = l2_evict_last_policy();
+        if (ntl > 0) {
+            const int row = tl[0] * kTileRows + t;
+            cr = ld_keep(v.r0 + row, pol_keep);
+            cw = ld_keep(v.w0 + row, pol_keep);
+            cs = ld_keep(v.s0 + row, pol_keep);
+            cd = ld_keep(v.dinv + row, pol_keep);
+            cx = ld_keep(v.x + row, pol_keep);
+            cp = ld_keep(v.p + row, pol_keep);
+        }
+        if (fcol >= 0) {
+            hr = ld_keep(v.r0 + fcol, pol_keep);
+            hw = ld_keep(v.w0 + fcol, pol_keep);
+            hs = ld_keep(v.s0 + fcol, pol_keep);
+            hd = ld_keep(v.dinv + fcol, pol_keep);
+        }
+    }
+    PhaseCtl<R, 2> c;
+    int cq = -1;
+    Acc<R> dots[kNV];
+    uint32_t phases = 0u;  // bit b: parity of stage b's next phase
+    int bad_inst = -1;     // instance of a tile whose stage wait expired
+    int buf = 0, b = 0;
+    for (int k = 0; k < ntl; k++) {
+        const int tile = tl[k], q = tq[k];
+        if (q != cq) {
+            c = ovc[q];
+            cq = q;
+        }
+        V* ut = ubuf + buf * ustride;
+        const int row = tile * kTileRows + t;
+        V un, wn;  // wn: the product's start, the diagonal term in the diagonal-free layout
+#pragma unroll
+        for (int f = 0; f < 2; f++) un.v[f] = wn.v[f] = 0;
+        if (row < a.N) {
+            V sn, rn;
+            cg_advance(c, cr, cw, c.need_old ? cs : cw, cd, sn, rn, un);
+            if (od) wn = rn;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                if (c.act[f]) {
+                    const R ui = cd.v[f] * cr.v[f];
+                    cp.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], cp.v[f], ui);
+                    cx.v[f] = fmar(c.alpha[f], cp.v[f], cx.v[f]);
+                }
+                dots[f].add_prod(rn.v[f], un.v[f]);
+                dots[4 + f].add_prod(rn.v[f], rn.v[f]);
+            }
+            v.x[row] = cx;
+            v.p[row] = cp;
+            v.r1[row] = rn;
+            v.s1[row] = sn;
+        }
+        ut[t] = un;
+        const uint64_t pol_keep = l2_evict_last_policy();
+        const int nt = tile_at(k + 1);
+        if (nt < ntiles) {
+            const int nrow = nt * kTileRows + t;
+            cr = ld_keep(v.r0 + nrow, pol_keep);
+            cw = ld_keep(v.w0 + nrow, pol_keep);
+            cs = ld_keep(v.s0 + nrow, pol_keep);
+            cd = ld_keep(v.dinv + nrow, pol_keep);
+            cx = ld_keep(v.x + nrow, pol_keep);
+            cp = ld_keep(v.p + nrow, pol_keep);
+        }
+        if (j < hcc) {
+            V sn, rn, u2;
+            cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
+            ut[kTileRows + j] = u2;
+        }
+        if (hcoln >= 0) {
+            hr = ld_keep(v.r0 + hcoln, pol_keep);
+            hw = ld_keep(v.w0 + hcoln, pol_keep);
+            hs = ld_keep(v.s0 + hcoln, pol_keep);
+            hd = ld_keep(v.dinv + hcoln, pol_keep);
+        }
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock)
+            ut[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0c + h]);
+        __syncthreads();
+        if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
+            const int bp = b == 0 ? S - 1 : b - 1;
+            if (k + S - 1 < ntl) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(bp, re0, re1);
+                armed |= 1u << bp;
+            }
+            tile_range(tile_at(k + S), re0, re1);
+        }
+        h0c = h0n;
+        hcc = hcn;
+        hcoln = j < hhc ? a.halo_col[hh0 + j] : -1;
+        h0n = hh0;
+        hcn = hhc;
+        halo_head(tile_at(k + 3), hh0, hhc);
+        int32_t sb2, sw2;
+        slice_ref(tile_at(k + 2), sb2, sw2);
+        // the product from the stage
+        const bool got = mbar_wait(&bars[b], (phases >> b) & 1u);
+        phases ^= 1u << b;
+        if (!got) bad_inst = ov[q].inst;
+        if (t == 0 && got) armed &= ~(1u << b);
+        const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+#pragma unroll 4
+        for (int kk = 0; kk < sw; kk++) {
+            const V av = As[32 * kk];
+            const V g = ut[Ls[32 * kk]];
+#pragma unroll
+            for (int f = 0; f < 2; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
+        }
+        if (row < a.N) {
+            v.w1[row] = wn;
+#pragma unroll
+            for (int f = 0; f < 2; f++) dots[2 + f].add_prod(wn.v[f], un.v[f]);
+        }
+        sb = sbn;
+        sw = swn;
+        sbn = sb2;
+        swn = sw2;
+        buf ^= 1;
+        b = b + 1 == S ? 0 : b + 1;
+        if (k + 1 == ntl || tg[k + 1] != tg[k]) {  // the group's last tile: its partials
+            const BRingInst o = ov[q];
+            Acc<R> blk[kNV], tot[kNV];
+            block_totals<kNV>(dots, red, blk);
+            if (inst_commit<kNV>(blk, a.gpart, tg[k], o.g0, o.ng, a.iticket + o.inst, red, tot) && t == 0 &&
+                !a.probe) {
+                volatile BInst* s = a.inst + o.inst;
+                if (finish_cgcg<R, 2>(s, &a.inst[o.inst].flags, c.act, tot))
+                    atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
+            }
+#pragma unroll
+            for (int f = 0; f < kNV; f++) dots[f] = Acc<R>();
+        }
+    }
+    grid_launch_dependents();
+    if (__syncthreads_or(bad_inst >= 0)) {
+        if (bad_inst >= 0) atomicOr(&a.inst[bad_inst].flags, FEA_STATUS_BREAKDOWN);
+        if (t == 0)
+            for (int q2 = 0; q2 < S; q2++)  // copies still in flight land before the block leaves
+                if (armed & (1u << q2)) mbar_wait(&bars[q2], (phases >> q2) & 1u);
+    }
+    if (!a.probe) phase_end(a, kIterNext);
+}
+
 // After the first solve loop: zero right-hand sides give x = 0, then one
 // float-float true-residual pass r = b - A x; fields still above their
 // threshold restart CG from there.
@@ -645,9 +1054,12 @@ struct fea_batch {
     int precision = FEA_FP32;
     int ninst = 0, ntiles = 0;
     int64_t N = 0, nnz = 0;
-    int wch = 8;  // CG kernel variant (autotuned): 0/1 tile-ELL (8/4 entries prefetched), 4/8 CSR window
+    int wch = 8;  // CG kernel variant (autotuned): 0/1 tile-ELL (8/4 entries prefetched), 4/8 CSR window,
+                  // 14 tile-ELL with the operator streamed by a bulk-copy ring
     TileEll ell;  // tile-ELL layout of the stacked matrix
     void* As = nullptr;
+    TileEll ell_od;  // the same without diagonal entries (ring variant)
+    void* As_od = nullptr;
     std::vector<int64_t> V, node_off;
     DeviceArena mem;
     int32_t *rp = nullptr, *col = nullptr, *tile_inst = nullptr, *inst_tile = nullptr, *node_map = nullptr;
@@ -658,6 +1070,10 @@ struct fea_batch {
     BCtl* ctl = nullptr;
     double* part = nullptr;
     unsigned int* iticket = nullptr;
+    int ngroups = 0;               // groups of kGroupTiles tiles (variant 14)
+    int32_t* inst_grp = nullptr;   // [ninst + 1] first group of each instance
+    double* gpart = nullptr;       // [ngroups * kNV]
+    int32_t* act_pos = nullptr;    // [ninst + 1] active-tile table
     BFlags* flags = nullptr;
     float* staging = nullptr;  // node-sized staging buffer (largest instance)
     double tol = 0.0;
@@ -705,7 +1121,17 @@ BArgs<R> make_bargs(fea_batch* B) {
         a.halo_off = B->ell.halo_off;
         a.halo_col = B->ell.halo_col;
         a.hmax = B->ell.hmax;
+        a.emax = B->ell.emax;
+        if (B->ell_od.ok) {
+            a.As_od = (const FV<R, 2>*)B->As_od;
+            a.lcol_od = B->ell_od.lcol;
+            a.slice_off_od = B->ell_od.slice_off;
+            a.emax = B->ell_od.emax;
+        }
     }
+    a.inst_grp = B->inst_grp;
+    a.gpart = B->gpart;
+    a.act_pos = B->wch == 14 ? B->act_pos : nullptr;
     return a;
 }
 
@@ -721,7 +1147,8 @@ struct BLoop {
 };
 
 // The CG kernels of a variant: 4 and 8 the windowed CSR kernels, 0 and 1 the
-// tile-ELL kernels with 8 or 4 entries prefetched.
+// tile-ELL kernels with 8 or 4 entries prefetched, 14 the tile-ELL ring kernel
+// (its set-up product is variant 1's).
 template <typename R, int V>
 struct BKernels {
     static constexpr void (*init)(BArgs<R>) = kb_init<R, V>;
@@ -738,19 +1165,63 @@ template <typename R>
 struct BKernels<R, 0> : BEllKernels<R, 8> {};
 template <typename R>
 struct BKernels<R, 1> : BEllKernels<R, 4> {};
+constexpr int kBatchRingStages = 3;
+template <typename R>
+struct BKernels<R, 14> : BEllKernels<R, 4> {
+    static constexpr void (*iter)(BArgs<R>) = kb_iter_ring<R, kBatchRingStages>;
+};
+
+// Tile-list capacity of a ring-kernel block for a grid of `grid` blocks: a
+// block's share is at most ceil(tiles / grid) tiles, and its last group may
+// reach kGroupTiles - 1 tiles beyond it.
+int ring_tcap(const fea_batch* B, int64_t grid) {
+    return (int)(ceil_div(B->ntiles, std::max<int64_t>(grid, 1)) + kGroupTiles);
+}
+
+// Entries of the largest tile the ring kernel streams.
+int ring_emax(const fea_batch* B) { return B->ell_od.ok ? B->ell_od.emax : B->ell.emax; }
+
+template <typename R>
+size_t ring_smem(const fea_batch* B, int tcap) {
+    return BRingLayout<R>(ring_emax(B), B->ell.hmax, tcap, kBatchRingStages).total;
+}
+
+// Whether the ring kernel fits: the tile-ELL layout exists and a block's
+// shared memory is within the opt-in limit for the largest tile list a grid
+// can give it (a grid of min(SMs, groups) blocks).
+template <typename R>
+bool ring_fits(const fea_batch* B) {
+    if (!B->ell.ok || ring_emax(B) <= 0) return false;
+    int dev = 0, lim = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return false;
+    const int64_t g = std::max<int64_t>(1, std::min<int64_t>(num_sms(), B->ngroups));
+    return ring_smem<R>(B, ring_tcap(B, g)) + 2048 <= (size_t)lim;
+}
 
 template <typename R, int V>
 struct BGrids {
     using K = BKernels<R, V>;
-    int rhs, init, iter, stream;
-    size_t smem;
+    int rhs, init, iter, stream, tcap = 0;
+    size_t smem_init, smem_iter;
     explicit BGrids(const fea_batch* B) {
-        smem = K::smem(B);
+        smem_init = smem_iter = K::smem(B);
         rhs = wave_grid(kb_rhs<R>, B->ntiles);
-        init = wave_grid(K::init, B->ntiles, smem);
-        iter = wave_grid(K::iter, B->ntiles, smem);
+        init = wave_grid(K::init, B->ntiles, smem_init);
+        if constexpr (V == 14) {
+            // the grid from the capacity of one block per SM, then the capacity
+            // of that grid (never larger, so the occupancy holds)
+            iter = wave_grid(K::iter, std::max(B->ngroups, 1), ring_smem<R>(B, ring_tcap(B, num_sms())));
+            tcap = ring_tcap(B, iter);
+            smem_iter = ring_smem<R>(B, tcap);  // larger when fewer groups than SMs shrink the grid
+            ensure_dyn_smem(K::iter, smem_iter);
+        } else {
+            iter = wave_grid(K::iter, B->ntiles, smem_iter);
+        }
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(B->N, kBlock)));
     }
+    void apply(BArgs<R>& a) const { a.tcap = tcap; }
 };
 
 // The iteration kernels of a loop pass, chained by programmatic edges.
@@ -770,6 +1241,7 @@ template <typename R, int WCH>
 void build_batch_graph_t(fea_batch* B) {
     BLoop<R> L(make_bargs<R>(B), B->flags, 1);
     const BGrids<R, WCH> g(B);
+    for (BArgs<R>* x : {&L.a, &L.a1, &L.a2}) g.apply(*x);
     using K = BKernels<R, WCH>;
     StepGraph& G = B->graph;
     cudaGraph_t top;
@@ -783,14 +1255,14 @@ void build_batch_graph_t(fea_batch* B) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, kb_rhs<R>, g.rhs, kBlock, L.a1);
-    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem);
+    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
-    add_batch_iterations(body1, K::iter, g.iter, L.a1, g.smem);
+    add_batch_iterations(body1, K::iter, g.iter, L.a1, g.smem_iter);
     s = add_kernel(step_body, s, kb_refine<R>, g.rhs, kBlock, L.a2);
-    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem);
+    s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
-    add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem);
+    add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
     add_kernel(step_body, s, kb_stepctl<R>, 1, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
     G.lanes = WCH;
@@ -809,6 +1281,7 @@ template <typename R, int WCH>
 void run_batch_stream_t(fea_batch* B) {
     BLoop<R> L(make_bargs<R>(B), B->flags, 0);
     const BGrids<R, WCH> g(B);
+    for (BArgs<R>* x : {&L.a, &L.a1, &L.a2}) g.apply(*x);
     using K = BKernels<R, WCH>;
     cudaStream_t st = B->stream;
     kb_start<R><<<1, 1, 0, st>>>(L.a);
@@ -822,10 +1295,10 @@ void run_batch_stream_t(fea_batch* B) {
                 kb_refine<R><<<g.rhs, kBlock, 0, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
-            K::init<<<g.init, kBlock, g.smem, st>>>(la);
+            K::init<<<g.init, kBlock, g.smem_init, st>>>(la);
             FEA_CHECK_LAUNCH();
             while (read_int(la.cont, st)) {
-                K::iter<<<g.iter, kBlock, g.smem, st>>>(la);
+                K::iter<<<g.iter, kBlock, g.smem_iter, st>>>(la);
                 FEA_CHECK_LAUNCH();
             }
         }
@@ -843,6 +1316,7 @@ void run_batch(fea_batch* B) {
         case 0: run_batch_stream_t<R, 0>(B); break;
         case 1: run_batch_stream_t<R, 1>(B); break;
         case 4: run_batch_stream_t<R, 4>(B); break;
+        case 14: run_batch_stream_t<R, 14>(B); break;
         default: run_batch_stream_t<R, 8>(B); break;
         }
         return;
@@ -853,6 +1327,7 @@ void run_batch(fea_batch* B) {
         case 0: build_batch_graph_t<R, 0>(B); break;
         case 1: build_batch_graph_t<R, 1>(B); break;
         case 4: build_batch_graph_t<R, 4>(B); break;
+        case 14: build_batch_graph_t<R, 14>(B); break;
         default: build_batch_graph_t<R, 8>(B); break;
         }
     }
@@ -860,52 +1335,41 @@ void run_batch(fea_batch* B) {
 }
 
 template <typename R, int V>
-void batch_probe_t(fea_batch* B, const BArgs<R>& a) {
+void batch_iter_probe_t(fea_batch* B, BArgs<R> a) {
     const BGrids<R, V> g(B);
-    BKernels<R, V>::init<<<g.init, kBlock, g.smem, B->stream>>>(a);
+    g.apply(a);
+    BKernels<R, V>::iter<<<g.iter, kBlock, g.smem_iter, B->stream>>>(a);
     FEA_CHECK_LAUNCH();
 }
 
-// One set-up SpMV (w = A z over every tile) of the given variant: the
-// autotuning probe.  It writes only CG scratch that every solve recomputes.
+// One iteration kernel of variant `var` over every tile, fields masked
+// (probe_mask): x and p are written back unchanged and only CG scratch, which
+// every solve recomputes, changes.  The timing probe of autotuning and of
+// fea_batch_time_iteration.
 template <typename R>
-void batch_probe(fea_batch* B, int var) {
+void batch_iter_probe(fea_batch* B, int var) {
     BArgs<R> a = make_bargs<R>(B);
     a.probe = 1;
     a.use_graph = 0;
     a.cont = &B->flags->probe;
     switch (var) {
-    case 0: batch_probe_t<R, 0>(B, a); break;
-    case 1: batch_probe_t<R, 1>(B, a); break;
-    case 4: batch_probe_t<R, 4>(B, a); break;
-    default: batch_probe_t<R, 8>(B, a); break;
-    }
-}
-
-template <typename R, int V>
-void batch_iter_probe_t(fea_batch* B, const BArgs<R>& a) {
-    const BGrids<R, V> g(B);
-    BKernels<R, V>::iter<<<g.iter, kBlock, g.smem, B->stream>>>(a);
-    FEA_CHECK_LAUNCH();
-}
-
-// One iteration kernel of the batch's variant over every tile, fields masked
-// (probe_mask): the timing probe of fea_batch_time_iteration.
-template <typename R>
-void batch_iter_probe(fea_batch* B) {
-    BArgs<R> a = make_bargs<R>(B);
-    a.probe = 1;
-    a.use_graph = 0;
-    a.cont = &B->flags->probe;
-    switch (B->wch) {
     case 0: batch_iter_probe_t<R, 0>(B, a); break;
     case 1: batch_iter_probe_t<R, 1>(B, a); break;
     case 4: batch_iter_probe_t<R, 4>(B, a); break;
+    case 14: batch_iter_probe_t<R, 14>(B, a); break;
     default: batch_iter_probe_t<R, 8>(B, a); break;
     }
 }
 
-// Pick the CG kernel variant by timing the set-up SpMV of each candidate.
+// Whether variant v can run on this batch.
+template <typename R>
+bool batch_variant_ok(const fea_batch* B, int v) {
+    if (v == 0 || v == 1) return B->ell.ok;
+    if (v == 14) return ring_fits<R>(B);
+    return v == 4 || v == 8;
+}
+
+// Pick the CG kernel variant by timing one iteration kernel of each candidate.
 template <typename R>
 void autotune_batch(fea_batch* B) {
     cudaEvent_t e0, e1;
@@ -913,11 +1377,11 @@ void autotune_batch(fea_batch* B) {
     FEA_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     int pick = 8;
-    for (int w : {0, 1, 4, 8}) {
-        if (w <= 1 && !B->ell.ok) continue;
+    for (int w : {0, 1, 4, 8, 14}) {
+        if (!batch_variant_ok<R>(B, w)) continue;
         for (int rep = 0; rep < 13; rep++) {
             if (rep == 3) FEA_CUDA_TRY(cudaEventRecord(e0, B->stream));
-            batch_probe<R>(B, w);
+            batch_iter_probe<R>(B, w);
         }
         FEA_CUDA_TRY(cudaEventRecord(e1, B->stream));
         FEA_CUDA_TRY(cudaEventSynchronize(e1));
@@ -1049,6 +1513,12 @@ void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
     B->ctl = B->mem.alloc<BCtl>(1);
     B->part = B->mem.alloc<double>(tiles * kNV);
     B->iticket = B->mem.alloc<unsigned int>(n);
+    std::vector<int32_t> grp0(n + 1);  // groups of kGroupTiles tiles per instance (ring kernel)
+    for (int i = 0; i < n; i++) grp0[i + 1] = grp0[i] + (int32_t)ceil_div(tile0[i + 1] - tile0[i], kGroupTiles);
+    B->ngroups = grp0[n];
+    B->inst_grp = B->mem.alloc<int32_t>(n + 1);
+    B->gpart = B->mem.alloc<double>((int64_t)B->ngroups * kNV);
+    B->act_pos = B->mem.alloc<int32_t>(n + 1);
     B->flags = B->mem.alloc<BFlags>(1);
     B->staging = B->mem.alloc<float>(vmax);
     const size_t fv = sizeof(FV<R, 2>);
@@ -1059,6 +1529,9 @@ void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
     FEA_CUDA_TRY(cudaMemsetAsync(B->iticket, 0, sizeof(unsigned int) * n, st));
     FEA_CUDA_TRY(cudaMemsetAsync(B->flags, 0, sizeof(BFlags), st));
     FEA_CUDA_TRY(cudaMemsetAsync(B->part, 0, sizeof(double) * tiles * kNV, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->gpart, 0, sizeof(double) * (size_t)B->ngroups * kNV, st));
+    FEA_CUDA_TRY(cudaMemsetAsync(B->act_pos, 0, sizeof(int32_t) * (n + 1), st));
+    FEA_CUDA_TRY(cudaMemcpyAsync(B->inst_grp, grp0.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
     FEA_CUDA_TRY(cudaMemcpyAsync(B->tile_inst, tinst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, st));
     FEA_CUDA_TRY(cudaMemcpyAsync(B->inst_tile, tile0.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
     std::vector<BPrm> hp(n);
@@ -1094,6 +1567,10 @@ void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
         if (build_tile_ell(hrp, hcol, Nr, sizeof(FV<R, 2>), kEllSmemBudget, B->ell, B->mem, st)) {
             B->As = B->mem.alloc<FV<R, 2>>(B->ell.E);
             fill_tile_ell<R, 2>(B->ell, (const FV<R, 2>*)B->A, (FV<R, 2>*)B->As, st);
+            if (build_tile_ell(hrp, hcol, Nr, sizeof(FV<R, 2>), kEllSmemBudget, B->ell_od, B->mem, st, true)) {
+                B->As_od = B->mem.alloc<FV<R, 2>>(B->ell_od.E);
+                fill_tile_ell<R, 2>(B->ell_od, (const FV<R, 2>*)B->A, (FV<R, 2>*)B->As_od, st);
+            }
         }
     }
     autotune_batch<R>(B);
@@ -1243,8 +1720,13 @@ int fea_batch_cg_variant(fea_batch* B, int set, int* variant) {
         return FEA_OK;
     }
     const int v = *variant;
-    if (v != 0 && v != 1 && v != 4 && v != 8) return fail(FEA_ERR_INVALID_ARGUMENT, "batch CG variant must be 0, 1, 4 or 8");
-    if (v <= 1 && !B->ell.ok) return fail(FEA_ERR_UNSUPPORTED, "tile-ELL layout unavailable for this batch");
+    if (v != 0 && v != 1 && v != 4 && v != 8 && v != 14)
+        return fail(FEA_ERR_INVALID_ARGUMENT, "batch CG variant must be 0, 1, 4, 8 or 14");
+    const bool ok = B->precision == FEA_FP64 ? batch_variant_ok<double>(B, v) : batch_variant_ok<float>(B, v);
+    if (!ok) {
+        set_error("batch CG variant %d unavailable: no tile-ELL layout, or its shared memory does not fit", v);
+        return FEA_ERR_UNSUPPORTED;
+    }
     B->wch = v;
     BATCH_API_END
 }
@@ -1281,8 +1763,8 @@ int fea_batch_time_iteration(fea_batch* B, int reps, double* ms_per_launch) {
     FEA_CUDA_TRY(cudaEventCreate(&e0));
     FEA_CUDA_TRY(cudaEventCreate(&e1));
     auto launch = [&]() {
-        if (B->precision == FEA_FP64) batch_iter_probe<double>(B);
-        else batch_iter_probe<float>(B);
+        if (B->precision == FEA_FP64) batch_iter_probe<double>(B, B->wch);
+        else batch_iter_probe<float>(B, B->wch);
     };
     launch();  // warm-up
     FEA_CUDA_TRY(cudaEventRecord(e0, B->stream));

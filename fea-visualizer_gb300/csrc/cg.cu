@@ -21,6 +21,7 @@
 #include <cmath>
 
 #include "cg_device.cuh"
+#include "ring.cuh"
 #include "tma.cuh"
 
 namespace fea {
@@ -80,12 +81,28 @@ struct RowMap {
 // updates, and the SpMV recomputes u' at each gathered column from the old r,
 // w and s there (so r, w and s alternate between two buffers).
 
+// The set-up of a step's first solve (Gray-Scott with the guess buffers):
+// the state becomes x_(n-1) and the start k_rhs formed becomes x (the two are
+// equal without the extrapolation); a skipped step keeps both.  Every later
+// step may then extrapolate.
+template <typename R, int NF>
+__device__ __forceinline__ void move_guess(const StepArgs<R, NF>& a) {
+    if (((const volatile CgState*)a.cg)->stop) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.N; i += (int64_t)gridDim.x * blockDim.x) {
+        const FV<R, NF> x = a.x[i];
+        a.xprev[i] = x;
+        a.x[i] = a.xg[i];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.run->prev_valid = 1;
+}
+
 // Set-up of a solve: w0 = A z (z = D^-1 r0 from k_rhs / k_refine), delta0 =
 // z.w0 and alpha0 = r0.z / delta0.
 template <typename R, int NF, int WCH>
 __global__ void __launch_bounds__(kBlock, (WCH <= 4 ? 6 : 4)) k_cgcg_init(StepArgs<R, NF> a) {
     __shared__ FV<R, NF> sm[kBlock / 32][32 * WCH];
     __shared__ typename Acc<R>::Packed red[32 * NF];
+    if (a.guess_init && a.xg) move_guess(a);
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
@@ -179,6 +196,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_init_ell(StepArgs<R, NF> a) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     FV<R, NF>* ut = reinterpret_cast<FV<R, NF>*>(dyn_smem);
     __shared__ typename Acc<R>::Packed red[32 * NF];
+    if (a.guess_init && a.xg) move_guess(a);
     PhaseCtl<R, NF> c;
     c.load(a.cg);
     if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
@@ -324,9 +342,6 @@ __device__ void stage_rows(unsigned char* S, const StageLayout<R, NF>& L, const 
     for (int k = 0; k < 6; k++) bulk_g2s_hint(S + L.V + (size_t)k * nV, src[k], nV, bar, vpol);
 }
 
-// Thread t's halo slot: slots are dealt round-robin over the warps, so every
-// warp stages about the same share of a tile's halo.
-__device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
 
 // The per-tile references (entry ranges, slice offsets, halo lists) are loaded
 // ahead of use in a software pipeline, so that no load waits on another
@@ -683,7 +698,7 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
     }
 }
 
-// ---- variant 12: tile-ELL with direct loads, pipelined one tile ahead -------------
+// ---- variant 13: tile-ELL with direct loads, pipelined one tile ahead -------------
 //
 // Each warp multiplies its 32-row slice of a tile from registers.  The
 // slice's operator entries and 16-bit local columns go straight from global
@@ -701,61 +716,6 @@ __global__ void __launch_bounds__(kBlock) k_cgcg_iter_stream(StepArgs<R, NF> a) 
 // each value to one warp: at the start, warp k merges value k of every
 // block's partials; at the end, value k of the block's threads.
 
-// Loads of data read once per iteration (the operator entries and columns):
-// no L1 allocation, first out of the L2 (policy from l2_evict_first_policy).
-template <typename T>
-__device__ __forceinline__ T ld_once(const T* p, uint64_t pol) {
-    T o;
-    if constexpr (sizeof(T) == 4) {
-        uint32_t x;
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(x) : "l"(p), "l"(pol));
-        memcpy(&o, &x, 4);
-    } else if constexpr (sizeof(T) == 8) {
-        uint2 x;
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
-            : "=r"(x.x), "=r"(x.y)
-            : "l"(p), "l"(pol));
-        memcpy(&o, &x, 8);
-    } else {
-        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
-        uint4 x;
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
-            : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w)
-            : "l"(p), "l"(pol));
-        memcpy(&o, &x, 16);
-    }
-    return o;
-}
-__device__ __forceinline__ uint32_t ld_once_u16(const uint16_t* p, uint64_t pol) {
-    unsigned short x;
-    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(x) : "l"(p), "l"(pol));
-    return x;
-}
-// Loads of the iteration's vectors, which the next iteration reads again:
-// kept in the L2 ahead of the operator (l2_evict_last_policy).
-template <typename T>
-__device__ __forceinline__ T ld_keep(const T* p, uint64_t pol) {
-    T o;
-    if constexpr (sizeof(T) == 4) {
-        uint32_t x;
-        asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(x) : "l"(p), "l"(pol));
-        memcpy(&o, &x, 4);
-    } else if constexpr (sizeof(T) == 8) {
-        uint2 x;
-        asm volatile("ld.global.nc.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;"
-                     : "=r"(x.x), "=r"(x.y)
-                     : "l"(p), "l"(pol));
-        memcpy(&o, &x, 8);
-    } else {
-        static_assert(sizeof(T) == 16, "4, 8 or 16 bytes");
-        uint4 x;
-        asm volatile("ld.global.nc.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
-                     : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w)
-                     : "l"(p), "l"(pol));
-        memcpy(&o, &x, 16);
-    }
-    return o;
-}
 
 // Totals of NV values over nb block partials p[k * stride + b]: warp k merges
 // value k (lane l takes b = l, l + 32, ... with 16 loads in flight, then a
@@ -1080,26 +1040,6 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_direct(StepArgs<R, N
 // end of the launch, after thread 0 has waited (bounded) for the copies it
 // issued.
 
-// One stage of the ring: a tile's operator entries, then its local columns.
-struct RingStage {
-    size_t A, L, bytes;
-    __host__ __device__ RingStage(int emax, size_t fv) {
-        auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
-        A = 0;
-        L = al(fv * (size_t)emax);
-        bytes = al(L + 2 * (size_t)emax);
-    }
-};
-
-// Dynamic shared memory of the ring kernels: the ring (which the end-of-launch
-// reduction reuses once every copy has landed), then the two u' buffers.
-template <typename R, int NF>
-__host__ __device__ size_t ring_bytes(int emax, int stages) {
-    const size_t ring = (size_t)stages * RingStage(emax, sizeof(FV<R, NF>)).bytes;
-    const size_t red = (size_t)3 * NF * kBlock * sizeof(typename Acc<R>::Packed);
-    return (ring > red ? ring : red + 127) & ~(size_t)127;
-}
-
 template <typename R, int NF, int S, int PAR, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF> a) {
     using V = FV<R, NF>;
@@ -1107,14 +1047,22 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
     constexpr int NV = 3 * NF;
     static_assert(NV <= kBlock / 32, "one warp per reduced value");
     static_assert(S >= 2 && S <= 8, "ring depth");
-    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
     __shared__ P mred[NV];
     __shared__ __align__(8) uint64_t bars[S];
     __shared__ CgState st;
     __shared__ unsigned int sflags;
-    const RingStage L(a.emax, sizeof(V));
+    // the streamed layout: without the diagonal entries when it was built
+    // (the diagonal term A_ii u'_i is then the row's new residual r'_i, as
+    // u' = D^-1 r'), else the full one
+    const bool od = a.As_od != nullptr;
+    const V* const Aop = od ? a.As_od : a.As;
+    const uint16_t* const lop = od ? a.lcol_od : a.lcol;
+    const int32_t* const soff = od ? a.slice_off_od : a.slice_off;
+    const int emx = od ? a.emax_od : a.emax;
+    const RingStage L(emx, sizeof(V));
     unsigned char* const ring = dyn_smem;
-    V* const ubuf = reinterpret_cast<V*>(dyn_smem + ring_bytes<R, NF>(a.emax, S));
+    V* const ubuf = reinterpret_cast<V*>(dyn_smem + ring_bytes<R, NF>(emx, S));
     const int ustride = kTileRows + a.hmax;
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
@@ -1130,16 +1078,16 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
         sb = sw = 0;
         if (tile < ntiles) {
             const int sl = tile * (kTileRows / 32) + wib;
-            const int32_t s0 = a.slice_off[sl];
-            sb = s0 - a.slice_off[tile * (kTileRows / 32)];
-            sw = (a.slice_off[sl + 1] - s0) >> 5;
+            const int32_t s0 = soff[sl];
+            sb = s0 - soff[tile * (kTileRows / 32)];
+            sw = (soff[sl + 1] - s0) >> 5;
         }
     };
     auto tile_range = [&](int tile, int32_t& e0, int32_t& e1) {
         e0 = e1 = 0;
         if (tile < ntiles) {
-            e0 = a.slice_off[tile * (kTileRows / 32)];
-            e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
+            e0 = soff[tile * (kTileRows / 32)];
+            e1 = soff[(tile + 1) * (kTileRows / 32)];
         }
     };
     auto stage_of = [&](int b) { return ring + (size_t)b * L.bytes; };
@@ -1153,8 +1101,8 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
         }
         mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
         const uint64_t pol = l2_evict_first_policy();
-        bulk_g2s_hint(stage_of(b) + L.A, a.As + e0, n * (uint32_t)sizeof(V), bar, pol);
-        bulk_g2s_hint(stage_of(b) + L.L, a.lcol + e0, 2 * n, bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.A, Aop + e0, n * (uint32_t)sizeof(V), bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.L, lop + e0, 2 * n, bar, pol);
     };
     // Before the dependency wait, only what no earlier kernel writes: the
     // stages' barriers, the first S tiles' operator copies, the references.
@@ -1231,12 +1179,13 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
     for (int tile = t0; tile < ntiles; tile += G, k++) {
         V* ut = ubuf + buf * ustride;
         const int row = tile * kTileRows + t;
-        V un;
+        V un, wn;  // wn: the product's start, the diagonal term in the diagonal-free layout
 #pragma unroll
-        for (int f = 0; f < NF; f++) un.v[f] = 0;
+        for (int f = 0; f < NF; f++) un.v[f] = wn.v[f] = 0;
         if (row < a.N) {
             V sn, rn;
             cg_advance(c, cr, cw, c.need_old ? cs : cw, cd, sn, rn, un);
+            if (od) wn = rn;
 #pragma unroll
             for (int f = 0; f < NF; f++) {
                 if (c.act[f]) {
@@ -1303,9 +1252,6 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
         if (t == 0 && got) armed &= ~(1u << b);
         const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
         const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
-        V wn;
-#pragma unroll
-        for (int f = 0; f < NF; f++) wn.v[f] = 0;
 #pragma unroll 4
         for (int kk = 0; kk < sw; kk++) {
             const V av = As[32 * kk];
@@ -1347,6 +1293,20 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
     const R dt = (R)P.dt;
     Acc<R> dots[3 * NF];  // |b|^2, |r|^2, r.z per field
     unsigned int flags = 0;
+    // Gray-Scott: the solve starts from x0 = 2 x_n - x_(n-1) (one rounding;
+    // 2 x is exact) when the extrapolation is on and x_(n-1) is the previous
+    // step's state; b still comes from x_n
+    constexpr bool kGS = EQ == EQ_GS_REF || EQ == EQ_GS_CONSISTENT;
+    const bool extrap = kGS && a.xprev != nullptr && a.run->guess == 1 && a.run->prev_valid != 0;
+    auto guess_at = [&](const FV<R, NF>& xn, int64_t i) {
+        FV<R, NF> g = xn;
+        if (extrap) {
+            const FV<R, NF> xp = a.xprev[i];
+#pragma unroll
+            for (int f = 0; f < NF; f++) g.v[f] = fmar((R)2, xn.v[f], -xp.v[f]);
+        }
+        return g;
+    };
     RowMap<LANES> m;
     for (int64_t base = m.warp * m.RPW; base < a.N; base += m.nwarps * m.RPW) {
         const int64_t row = base + m.grp;
@@ -1357,6 +1317,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                 const int32_t c = ldg(a.col + e);
                 const FV<R, NF> av = ldfv(a.A + e);
                 const FV<R, NF> xc = a.x[c];
+                const FV<R, NF> x0c = kGS ? guess_at(xc, c) : xc;  // the solve's start at column c
                 const R me = ldg(a.M + e);
                 if constexpr (EQ == EQ_HEAT) {
                     bs[0].add_prod(div_rn(me, dt), xc.v[0]);
@@ -1386,7 +1347,7 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
                     bs[NF - 1].add_prod(me, wv);
                 }
 #pragma unroll
-                for (int f = 0; f < NF; f++) ax[f].add_prod(av.v[f], xc.v[f]);
+                for (int f = 0; f < NF; f++) ax[f].add_prod(av.v[f], x0c.v[f]);
             }
         }
 #pragma unroll
@@ -1398,6 +1359,8 @@ __global__ void __launch_bounds__(kBlock) k_rhs(StepArgs<R, NF> a) {
             }
         if (m.sub == 0 && row < a.N) {
             const FV<R, NF> xr = a.x[row];
+            if constexpr (kGS)
+                if (a.xg) a.xg[row] = guess_at(xr, row);  // the set-up kernel makes it x
             if constexpr (EQ == EQ_GS_REF) {  // nodal reaction, CPUSolver.cpp:134,137
                 const R u = xr.v[0], v = xr.v[NF - 1];
                 const R uvv = u * (v * v);
@@ -1713,7 +1676,9 @@ struct RingKernels : EllKernels<R, NF, 4> {
     using Fn = void (*)(StepArgs<R, NF>);
     static constexpr Fn iter = k_cgcg_iter_ring<R, NF, S, 0, MINB>;
     static Fn iter_par(int par) { return par ? k_cgcg_iter_ring<R, NF, S, 1, MINB> : iter; }
-    static size_t smem_iter(const StepArgs<R, NF>& a) { return ring_smem_bytes<R, NF>(a.emax, a.hmax, S); }
+    static size_t smem_iter(const StepArgs<R, NF>& a) {
+        return ring_smem_bytes<R, NF>(a.As_od ? a.emax_od : a.emax, a.hmax, S);
+    }
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};
@@ -1734,9 +1699,7 @@ struct Grids {
         smem_iter = K::smem_iter(a);
         spmv = wave_grid(K::init, ceil_div(N, kBlock), smem_init);
         iter = wave_grid(K::iter, ceil_div(N, kBlock), smem_iter);
-        if (smem_iter > 48 * 1024 && K::iter_par(1) != K::iter)  // the other parity's kernel
-            FEA_CUDA_TRY(cudaFuncSetAttribute(K::iter_par(1), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem_iter));
+        if (K::iter_par(1) != K::iter) ensure_dyn_smem(K::iter_par(1), smem_iter);  // the other parity's kernel
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
     }
@@ -1749,6 +1712,7 @@ struct LoopArgs {
     StepArgs<R, NF> a, a1, a2;
     LoopArgs(const StepArgs<R, NF>& base, LoopFlags* lf, int use_graph) : a(base), a1(base), a2(base) {
         a.use_graph = a1.use_graph = a2.use_graph = use_graph;
+        a1.guess_init = 1;  // the set-up of a step's first solve takes the right-hand side's guess
         a.cont = &lf->step;
         a1.cont = &lf->cg1;
         a2.cont = &lf->cg2;

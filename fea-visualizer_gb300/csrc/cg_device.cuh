@@ -851,13 +851,25 @@ cudaGraphNode_t add_while(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphCondition
     return n;
 }
 
+// Opts `kernel` in to `smem` bytes of dynamic shared memory when that is above
+// its current limit.  The limit is a property of the function, shared by
+// every handle, so it only ever grows: a graph instantiated for a larger
+// handle stays launchable after a smaller one is set up.
+template <typename K>
+void ensure_dyn_smem(K kernel, size_t smem) {
+    if (smem <= 48 * 1024) return;
+    cudaFuncAttributes fa{};
+    FEA_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < smem)
+        FEA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+}
+
 // Grid of one wave: SMs x resident blocks of this kernel (from the occupancy
 // calculator, with `smem` bytes of dynamic shared memory, opted in above the
 // default 48 KB), capped by the work and by the partial-sum stride.
 template <typename K>
 int wave_grid(K kernel, int64_t work_blocks, size_t smem = 0) {
-    if (smem > 48 * 1024)
-        FEA_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_dyn_smem(kernel, smem);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;

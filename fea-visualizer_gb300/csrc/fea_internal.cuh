@@ -59,8 +59,10 @@ struct TileEll {
 // From host copies of a solver-order CSR pattern.  Returns false (L.ok false)
 // when a tile's halo does not fit the 16-bit indices or `smem_budget` bytes of
 // shared memory at fv_bytes per operand.
+// skip_diag: each row's diagonal entry is left out (a kernel that adds the
+// diagonal term from the row's own values reads the rest); no lcol2.
 bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& col, int64_t N, size_t fv_bytes,
-                    size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st);
+                    size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st, bool skip_diag = false);
 // As[k] = A[emap[k]] (0 for padding): the layout's copy of operator values.
 template <typename R, int NF>
 void fill_tile_ell(const TileEll& L, const FV<R, NF>* A, FV<R, NF>* As, cudaStream_t st);
@@ -136,6 +138,8 @@ struct RunState {
     double tol;
     int max_iter;
     int refine;
+    int guess;       // Gray-Scott: 1 starts each step's CG from 2 x_n - x_(n-1)
+    int prev_valid;  // x_(n-1) of the extrapolation is the previous step's state
 };
 
 // Everything a step-loop kernel needs, passed by value.
@@ -165,6 +169,12 @@ struct StepArgs {
     R* ut;                  // Newmark predictors
     R* vt;
     const FV<R, NF>* rhs;   // EQ_GIVEN: right-hand side [N]
+    // Gray-Scott initial-guess extrapolation (nullptr otherwise): the
+    // previous step's state and the guess k_rhs formed; the set-up kernel
+    // of a step's first solve (guess_init) moves x to xprev and the guess to x.
+    FV<R, NF>* xprev;
+    FV<R, NF>* xg;
+    int guess_init;
     // tile-ELL copy of A (the CG kernels' layout when ell.ok)
     const FV<R, NF>* As;
     const uint16_t* lcol;
@@ -173,6 +183,14 @@ struct StepArgs {
     const int32_t* halo_off;
     const int32_t* halo_col;
     int hmax, emax;
+    // The same layout without the diagonal entries (ring kernels, when built):
+    // the iteration adds the diagonal term A_ii u'_i = r'_i from the row's
+    // own residual (u' = D^-1 r'), so the operator stream carries one entry
+    // less per row.  Same halo lists.  Null: the full layout above.
+    const FV<R, NF>* As_od;
+    const uint16_t* lcol_od;
+    const int32_t* slice_off_od;
+    int emax_od;
     const StepParams* prm;
     CgState* cg;
     // Deferred-finish variants: the state is double-buffered (cg and cg_alt),

@@ -40,12 +40,27 @@ int num_sms() {
 namespace {
 
 // ---- node <-> unknown maps (CPUSolver.cpp:13-37) --------------------------------
+// Stores a state value; a store that changes its bits clears *prev_valid (the
+// extrapolated initial guess needs the state the loop itself produced, so a
+// field written back unchanged between frames keeps the history).
+template <typename R>
+__device__ __forceinline__ void store_state(R* dst, R val, int* prev_valid) {
+    if (prev_valid) {
+        const R old = *dst;
+        bool same;
+        if constexpr (sizeof(R) == 8) same = __double_as_longlong(old) == __double_as_longlong(val);
+        else same = __float_as_uint(old) == __float_as_uint(val);
+        if (!same) *prev_valid = 0;
+    }
+    *dst = val;
+}
+
 template <typename R>
 __global__ void k_gather_nodes(const float* __restrict__ vals, const int32_t* __restrict__ idx, int64_t V, R* out,
-                               int stride, int off) {
+                               int stride, int off, int* prev_valid) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < V; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t k = idx[i];
-        if (k >= 0) out[(int64_t)k * stride + off] = (R)vals[i];
+        if (k >= 0) store_state(out + (int64_t)k * stride + off, (R)vals[i], prev_valid);
     }
 }
 
@@ -77,9 +92,9 @@ __global__ void k_deinterleave(const R* __restrict__ uv, int64_t N, R* u, R* v) 
 // Caller-order unknown u <-> solver-order index pos[u].
 template <typename R>
 __global__ void k_copy_to_state(const R* __restrict__ in, const int32_t* __restrict__ pos, int64_t N, R* out,
-                                int stride, int off) {
+                                int stride, int off, int* prev_valid) {
     for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < N; u += (int64_t)gridDim.x * blockDim.x)
-        out[(int64_t)pos[u] * stride + off] = in[u];
+        store_state(out + (int64_t)pos[u] * stride + off, in[u], prev_valid);
 }
 
 template <typename R>
@@ -136,6 +151,7 @@ struct Fields {
     void *A0 = nullptr, *d0 = nullptr;  // Newmark start-up operator (M)
     // two fields
     void *A2 = nullptr, *d2 = nullptr, *b2 = nullptr, *r2 = nullptr, *z2 = nullptr, *p2 = nullptr, *q2 = nullptr;
+    void *xprev2 = nullptr, *xg2 = nullptr;  // Gray-Scott: previous state, extrapolated guess
 };
 
 }  // namespace fea
@@ -174,6 +190,8 @@ struct fea_solver {
     TileEll ell;                    // the CG kernels' layout of Pc (tile_ell.cu)
     int stream_stages = 0;          // stages of the streamed iteration that fit in shared memory (0, 2 or 3)
     void *S1 = nullptr, *S0 = nullptr, *S2 = nullptr;          // tile-ELL copies of A1, A0, A2
+    TileEll ell_od;                                            // the layout without diagonal entries (ring kernels)
+    void *S1d = nullptr, *S0d = nullptr, *S2d = nullptr;       // its copies of A1, A0, A2
     std::vector<float> h_xyz;       // host copy of the points (ordering keys)
     uint8_t* adv_present = nullptr;
     Fields F;
@@ -203,6 +221,10 @@ namespace fea {
 namespace {
 
 size_t rsize(const fea_solver* s) { return s->precision == FEA_FP64 ? 8 : 4; }
+
+// Entries of the largest tile the ring kernels stream (the diagonal-free
+// layout when it was built).
+int ring_emax(const fea_solver* s) { return s->ell_od.ok ? s->ell_od.emax : s->ell.emax; }
 
 int64_t pad_tiles(int64_t n) { return ceil_div(n, kTileRows) * kTileRows; }
 
@@ -336,8 +358,10 @@ void build_context(fea_solver* s) {
     s->P = Pattern{};
     s->Pc = Pattern{};
     s->ell = TileEll{};
+    s->ell_od = TileEll{};
     s->stream_stages = 0;
     s->S1 = s->S0 = s->S2 = nullptr;
+    s->S1d = s->S0d = s->S2d = nullptr;
     s->F = Fields{};
     cudaStream_t st = s->stream;
     s->idx = s->mat_mem.alloc<int32_t>(s->V);
@@ -356,6 +380,11 @@ void build_context(fea_solver* s) {
             s->S1 = ralloc(s->mat_mem, s, s->ell.E);
             s->S0 = ralloc(s->mat_mem, s, s->ell.E);
             s->S2 = ralloc(s->mat_mem, s, 2 * s->ell.E);
+            if (build_tile_ell(rp, col, N, 2 * rsize(s), kEllSmemBudget, s->ell_od, s->mat_mem, st, true)) {
+                s->S1d = ralloc(s->mat_mem, s, s->ell_od.E);
+                s->S0d = ralloc(s->mat_mem, s, s->ell_od.E);
+                s->S2d = ralloc(s->mat_mem, s, 2 * s->ell_od.E);
+            }
         }
         // both field counts fit when the two-field stages do
         const size_t stage = s->precision == FEA_FP64 ? stream_stage_bytes<double, 2>(s->ell.emax, s->ell.hmax)
@@ -364,8 +393,9 @@ void build_context(fea_solver* s) {
         // default variant: direct row loads with the operator ring (14) when
         // its stages fit, else the streamed deferred-finish kernel with as
         // many stages as fit, else the tile-ELL kernel, else windowed CSR
-        const size_t ring = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax, 3)
-                                                     : ring_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax, 3);
+        const int remax = ring_emax(s);
+        const size_t ring = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(remax, s->ell.hmax, 3)
+                                                     : ring_smem_bytes<float, 2>(remax, s->ell.hmax, 3);
         s->lanes = !s->ell.ok ? 8
                    : ring <= kStreamSmemLimit ? 14
                    : s->stream_stages >= 3    ? 11
@@ -419,12 +449,14 @@ void build_context(fea_solver* s) {
     F.z2 = ralloc(s->mat_mem, s, 2 * Nt);
     F.p2 = ralloc(s->mat_mem, s, 4 * Np);
     F.q2 = ralloc(s->mat_mem, s, 2 * Nt);
+    F.xprev2 = ralloc(s->mat_mem, s, 2 * Nt);
+    F.xg2 = ralloc(s->mat_mem, s, 2 * Nt);
     // every vector starts at zero (the direction buffers are read with weight
     // beta = 0 only after a write, but a zero start keeps them finite)
     const std::pair<void*, int64_t> zeroed[] = {
         {F.u, Nt}, {F.v, Nt}, {F.a, Nt}, {F.ut, Nt}, {F.vt, Nt}, {F.uv, 2 * Nt}, {F.d1, Nt}, {F.b1, Nt},
         {F.r1, 6 * Np}, {F.z1, Nt}, {F.p1, 2 * Np}, {F.q1, Nt}, {F.d0, Nt}, {F.d2, 2 * Nt}, {F.b2, 2 * Nt},
-        {F.r2, 12 * Np}, {F.z2, 2 * Nt}, {F.p2, 4 * Np}, {F.q2, 2 * Nt}};
+        {F.r2, 12 * Np}, {F.z2, 2 * Nt}, {F.p2, 4 * Np}, {F.q2, 2 * Nt}, {F.xprev2, 2 * Nt}, {F.xg2, 2 * Nt}};
     for (const auto& zv : zeroed)
         FEA_CUDA_TRY(cudaMemsetAsync(zv.first, 0, rsize(s) * (size_t)(zv.second > 0 ? zv.second : 1), st));
     F.interleaved = false;
@@ -488,6 +520,13 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.halo_col = s->ell.halo_col;
         a.hmax = s->ell.hmax;
         a.emax = s->ell.emax;
+        if (s->ell_od.ok) {
+            if constexpr (NF == 1) a.As_od = (const FV<R, 1>*)(init_op ? s->S0d : s->S1d);
+            else a.As_od = (const FV<R, 2>*)s->S2d;
+            a.lcol_od = s->ell_od.lcol;
+            a.slice_off_od = s->ell_od.slice_off;
+            a.emax_od = s->ell_od.emax;
+        }
     }
     a.prm = s->d_prm;
     a.cg = s->d_cg + 1;
@@ -506,6 +545,10 @@ void set_x(fea_solver* s, StepArgs<R, NF>& a, int kind) {
     Fields& F = s->F;
     if constexpr (NF == 2) {
         a.x = (FV<R, 2>*)F.uv;
+        if (kind == EQ_GS_REF || kind == EQ_GS_CONSISTENT) {  // the initial-guess extrapolation's buffers
+            a.xprev = (FV<R, 2>*)F.xprev2;
+            a.xg = (FV<R, 2>*)F.xg2;
+        }
     } else {
         if (kind == EQ_WAVE_REF) a.x = (FV<R, 1>*)F.v;
         else if (kind == EQ_WAVE_NEWMARK || kind == EQ_NEWMARK_INIT) a.x = (FV<R, 1>*)F.a;
@@ -534,6 +577,8 @@ void upload_params(fea_solver* s) {
     r.tol = tol;
     r.max_iter = p.cg_max_iterations > 0 ? p.cg_max_iterations : (int)(2 * s->N > 0x7fffffff ? 0x7fffffff : 2 * s->N);
     r.refine = p.cg_refine;
+    if (r.guess != p.cg_initial_guess) r.prev_valid = 0;  // a new rule starts from the warm start
+    r.guess = p.cg_initial_guess;
     FEA_CUDA_TRY(cudaMemcpyAsync(s->d_run, &r, sizeof(r), cudaMemcpyHostToDevice, s->stream));
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
 }
@@ -551,6 +596,7 @@ void update_operator(fea_solver* s, int kind) {
         combine_operator<R, 2>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->F.d2,
                                s->stream);
         fill_tile_ell<R, 2>(s->ell, (const FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->S2, s->stream);
+        fill_tile_ell<R, 2>(s->ell_od, (const FV<R, 2>*)s->F.A2, (FV<R, 2>*)s->S2d, s->stream);
     } else {
         OpCoef<1> c{};
         c.f[0] = {dt, 0.0, 1.0, 0.0};
@@ -574,12 +620,39 @@ void update_operator(fea_solver* s, int kind) {
             combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, m, (FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->F.d0,
                                    s->stream);
             fill_tile_ell<R, 1>(s->ell, (const FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->S0, s->stream);
+            fill_tile_ell<R, 1>(s->ell_od, (const FV<R, 1>*)s->F.A0, (FV<R, 1>*)s->S0d, s->stream);
         }
         combine_operator<R, 1>(s->Pc, s->emap, s->M64, s->K64, s->Adv64, c, (FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->F.d1,
                                s->stream);
         fill_tile_ell<R, 1>(s->ell, (const FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->S1, s->stream);
+        fill_tile_ell<R, 1>(s->ell_od, (const FV<R, 1>*)s->F.A1, (FV<R, 1>*)s->S1d, s->stream);
     }
 }
+
+// Fields changed from outside the step loop: the next step starts its solves
+// from the previous solution (the initial-guess extrapolation needs two steps
+// of the loop's own history).
+void invalidate_guess(fea_solver* s) {
+    if (s->d_run) FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->prev_valid, 0, sizeof(int), s->stream));
+}
+
+// Forces the previous-solution start while it lives (the adjoints recompute
+// forward states from checkpoints and must reproduce them exactly), then
+// restores the handle's rule.
+struct GuessOff {
+    fea_solver* s;
+    explicit GuessOff(fea_solver* h) : s(h) {
+        const int zero = 0;
+        FEA_CUDA_TRY(cudaMemcpyAsync(&s->d_run->guess, &zero, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    }
+    ~GuessOff() {
+        const int g = s->prm.cg_initial_guess;
+        cudaMemcpyAsync(&s->d_run->guess, &g, sizeof(int), cudaMemcpyHostToDevice, s->stream);
+        cudaMemsetAsync(&s->d_run->prev_valid, 0, sizeof(int), s->stream);
+        cudaStreamSynchronize(s->stream);
+    }
+};
 
 template <typename R>
 void ensure_layout(fea_solver* s, bool interleaved) {
@@ -593,6 +666,7 @@ void ensure_layout(fea_solver* s, bool interleaved) {
     else
         k_deinterleave<R><<<launch_grid(F.N), kBlock, 0, s->stream>>>((R*)F.uv, F.N, (R*)F.u, (R*)F.v);
     FEA_CHECK_LAUNCH();
+    invalidate_guess(s);
     F.interleaved = interleaved;
 }
 
@@ -654,11 +728,12 @@ void set_node_field(fea_solver* s, const float* host, int which /*0 u, 1 v*/) {
     float* d = s->d_nodes;
     FEA_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(float) * s->V, cudaMemcpyHostToDevice, s->stream));
     Fields& F = s->F;
+    int* pv = s->d_run ? &s->d_run->prev_valid : nullptr;
     if (F.interleaved)
-        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx_c, s->V, (R*)F.uv, 2, which);
+        k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx_c, s->V, (R*)F.uv, 2, which, pv);
     else
         k_gather_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>(d, s->idx_c, s->V,
-                                                                        (R*)(which ? F.v : F.u), 1, 0);
+                                                                        (R*)(which ? F.v : F.u), 1, 0, pv);
     FEA_CHECK_LAUNCH();
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
 }
@@ -684,9 +759,10 @@ void copy_field_device(fea_solver* s, const void* src, void* dst, int which, boo
     if (N == 0) return;
     R* state = F.interleaved ? (R*)F.uv : (R*)(which ? F.v : F.u);
     const int st = F.interleaved ? 2 : 1, off = F.interleaved ? which : 0;
-    if (to_state)
-        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, s->stream>>>((const R*)src, s->pos, N, state, st, off);
-    else
+    if (to_state) {
+        int* pv = s->d_run ? &s->d_run->prev_valid : nullptr;
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, s->stream>>>((const R*)src, s->pos, N, state, st, off, pv);
+    } else
         k_copy_from_state<R><<<launch_grid(N), kBlock, 0, s->stream>>>(state, s->pos, N, (R*)dst, st, off);
     FEA_CHECK_LAUNCH();
 }
@@ -832,6 +908,7 @@ double adjoint_gs_core(fea_solver* s, const FV<R, 2>* x0, const FV<R, 2>* t, int
         set_error("the Gray-Scott adjoint needs equation FEA_REACTION_DIFFUSION with reaction_mode 1");
         throw Error{FEA_ERR_STATE};
     }
+    const GuessOff guess_off(s);  // recomputed forward states must equal the forward sweep's
     cudaStream_t st = s->stream;
     const int64_t N = s->N;
     const size_t xb = sizeof(FV<R, 2>) * (size_t)N;
@@ -912,7 +989,7 @@ void adjoint_gs_host(fea_solver* s, const float* u0, const float* v0, const floa
         if (!in.first) continue;
         FEA_CUDA_TRY(cudaMemcpyAsync(s->d_nodes, in.first, sizeof(float) * V, cudaMemcpyHostToDevice, st));
         k_gather_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(s->d_nodes, s->idx_c, V, in.second.first, 2,
-                                                              in.second.second);
+                                                              in.second.second, nullptr);
         FEA_CHECK_LAUNCH();
     }
     const bool grads = gu || gv || gparams;
@@ -949,7 +1026,7 @@ void adjoint_gs_device(fea_solver* s, const void* u0, const void* v0, const void
         for (const auto& in : ins) {
             if (!in.first) continue;
             k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)in.first, s->pos, N, in.second.first, 2,
-                                                                   in.second.second);
+                                                                   in.second.second, nullptr);
             FEA_CHECK_LAUNCH();
         }
     const bool grads = gu || gv || gparams;
@@ -980,7 +1057,7 @@ void adjoint_host(fea_solver* s, const float* u0, const float* target, int64_t n
     const std::pair<const float*, R*> ins[2] = {{u0, u0s}, {target, ts}};
     for (const auto& in : ins) {
         FEA_CUDA_TRY(cudaMemcpyAsync(s->d_nodes, in.first, sizeof(float) * V, cudaMemcpyHostToDevice, st));
-        k_gather_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(s->d_nodes, s->idx_c, V, in.second, 1, 0);
+        k_gather_nodes<R><<<launch_grid(V), kBlock, 0, st>>>(s->d_nodes, s->idx_c, V, in.second, 1, 0, nullptr);
         FEA_CHECK_LAUNCH();
     }
     const bool grads = grad_u0 || grad_D;
@@ -1011,8 +1088,8 @@ void adjoint_device(fea_solver* s, const void* u0, const void* target, int64_t n
     R* lam = tmp.alloc<R>(N);
     double* gD = tmp.alloc<double>(T);
     if (N > 0) {
-        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)u0, s->pos, N, u0s, 1, 0);
-        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)target, s->pos, N, ts, 1, 0);
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)u0, s->pos, N, u0s, 1, 0, nullptr);
+        k_copy_to_state<R><<<launch_grid(N), kBlock, 0, st>>>((const R*)target, s->pos, N, ts, 1, 0, nullptr);
         FEA_CHECK_LAUNCH();
     }
     const bool grads = grad_u0 || grad_D;
@@ -1276,6 +1353,7 @@ int fea_params_default(fea_params* o) {
     o->cg_tolerance = 0.0;
     o->cg_max_iterations = 0;
     o->cg_refine = 1;
+    o->cg_initial_guess = 0;
     return FEA_OK;
 }
 
@@ -1560,6 +1638,7 @@ int fea_clear_values(fea_solver* s) {
     FEA_CUDA_TRY(cudaMemsetAsync(F.uv, 0, 2 * n, s->stream));
     FEA_CUDA_TRY(cudaMemsetAsync(&s->d_run->flags, 0, sizeof(unsigned int), s->stream));
     s->acc_valid = false;
+    invalidate_guess(s);
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
     API_END
 }
@@ -1739,8 +1818,8 @@ static int variant_check(const fea_solver* s, int l) {
     if (!csr && !s->ell.ok) return FEA_ERR_UNSUPPORTED;
     if (s->stream_stages < stages) return FEA_ERR_UNSUPPORTED;
     if (ring) {
-        const size_t need = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(s->ell.emax, s->ell.hmax, ring)
-                                                     : ring_smem_bytes<float, 2>(s->ell.emax, s->ell.hmax, ring);
+        const size_t need = s->precision == FEA_FP64 ? ring_smem_bytes<double, 2>(ring_emax(s), s->ell.hmax, ring)
+                                                     : ring_smem_bytes<float, 2>(ring_emax(s), s->ell.hmax, ring);
         if (need > kStreamSmemLimit) return FEA_ERR_UNSUPPORTED;
     }
     return FEA_OK;

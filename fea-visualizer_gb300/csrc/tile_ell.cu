@@ -10,7 +10,8 @@
 // CG kernels place the vector they multiply for the tile's rows and its halo
 // in shared memory, so every gathered operand is a shared-memory load.
 // Entries keep their CSR order within a row (same summation order), and
-// padding entries hold 0 with the row's own local index.
+// padding entries hold 0 with the row's own local index.  The diagonal-free
+// variant of the layout leaves each row's diagonal entry out.
 #include <algorithm>
 #include <vector>
 
@@ -35,15 +36,23 @@ __global__ void k_fill_tile_ell(int64_t E, const int32_t* __restrict__ emap, con
 }  // namespace
 
 bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& col, int64_t N, size_t fv_bytes,
-                    size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st) {
+                    size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st, bool skip_diag) {
     L = TileEll{};
     if (N <= 0) return false;
     const int64_t ntiles = ceil_div(N, kTileRows), nslices = ntiles * (kTileRows / 32);
     std::vector<int32_t> slice_off(nslices + 1, 0), halo_off(ntiles + 1, 0), halo_col;
+    // the stored entries of row r, in CSR order: rows[r] .. rows[r + 1] of `ents`
+    std::vector<int32_t> rows(N + 1, 0), ents;
+    ents.reserve(rp[N]);
+    for (int64_t r = 0; r < N; r++) {
+        for (int32_t e = rp[r]; e < rp[r + 1]; e++)
+            if (!skip_diag || col[e] != r) ents.push_back(e);
+        rows[r + 1] = (int32_t)ents.size();
+    }
     int64_t E = 0;
     for (int64_t s = 0; s < nslices; s++) {
         int32_t w = 0;
-        for (int64_t r = s * 32; r < std::min<int64_t>(N, s * 32 + 32); r++) w = std::max(w, rp[r + 1] - rp[r]);
+        for (int64_t r = s * 32; r < std::min<int64_t>(N, s * 32 + 32); r++) w = std::max(w, rows[r + 1] - rows[r]);
         slice_off[s] = (int32_t)E;
         E += 32 * (int64_t)w;
         if (E >= (int64_t)INT32_MAX) return false;
@@ -74,11 +83,11 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
         const int32_t* he = halo_col.data() + halo_off[t + 1];
         for (int lane = 0; lane < 32; lane++) {
             const int64_t r = s * 32 + lane;
-            const int32_t len = r < N ? rp[r + 1] - rp[r] : 0;
+            const int32_t len = r < N ? rows[r + 1] - rows[r] : 0;
             for (int32_t k = 0; k < w; k++) {
                 const int64_t at = slice_off[s] + 32 * (int64_t)k + lane;
                 if (k < len) {
-                    const int32_t e = rp[r] + k, c = col[e];
+                    const int32_t e = ents[rows[r] + k], c = col[e];
                     int64_t lc;
                     if (c >= t0 && c < t0 + kTileRows && c < N) lc = c - t0;
                     else lc = kTileRows + (std::lower_bound(hb, he, c) - hb);
@@ -91,8 +100,8 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
             }
         }
     }
-    std::vector<uint32_t> lcol2(E, 0u);
-    for (int64_t s = 0; s < nslices; s++) {
+    std::vector<uint32_t> lcol2(skip_diag ? 0 : E, 0u);
+    for (int64_t s = 0; s < (skip_diag ? 0 : nslices); s++) {
         const int64_t sb = slice_off[s];
         const int32_t w = (slice_off[s + 1] - slice_off[s]) / 32;
         for (int32_t m = 0; 2 * m < w; m++)
@@ -113,7 +122,7 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
     L.halo_off = keep.alloc<int32_t>(ntiles + 1);
     L.halo_col = keep.alloc<int32_t>(std::max<int64_t>(1, (int64_t)halo_col.size()));
     L.lcol = keep.alloc<uint16_t>(std::max<int64_t>(1, E));
-    L.lcol2 = keep.alloc<uint32_t>(std::max<int64_t>(1, E));
+    if (!skip_diag) L.lcol2 = keep.alloc<uint32_t>(std::max<int64_t>(1, E));
     L.emap = keep.alloc<int32_t>(std::max<int64_t>(1, E));
     FEA_CUDA_TRY(cudaMemcpyAsync(L.slice_off, slice_off.data(), sizeof(int32_t) * (nslices + 1),
                                  cudaMemcpyHostToDevice, st));
@@ -124,7 +133,8 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
                                      cudaMemcpyHostToDevice, st));
     if (E > 0) {
         FEA_CUDA_TRY(cudaMemcpyAsync(L.lcol, lcol.data(), sizeof(uint16_t) * E, cudaMemcpyHostToDevice, st));
-        FEA_CUDA_TRY(cudaMemcpyAsync(L.lcol2, lcol2.data(), sizeof(uint32_t) * E, cudaMemcpyHostToDevice, st));
+        if (!skip_diag)
+            FEA_CUDA_TRY(cudaMemcpyAsync(L.lcol2, lcol2.data(), sizeof(uint32_t) * E, cudaMemcpyHostToDevice, st));
         FEA_CUDA_TRY(cudaMemcpyAsync(L.emap, emap.data(), sizeof(int32_t) * E, cudaMemcpyHostToDevice, st));
     }
     FEA_CUDA_TRY(cudaStreamSynchronize(st));  // the host vectors go out of scope

@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("newmark_beta", C.c_double), ("newmark_gamma", C.c_double),
         ("advection_scheme", C.c_int), ("advection_sign", C.c_float), ("velocity_mode", C.c_int),
         ("cg_tolerance", C.c_double), ("cg_max_iterations", C.c_int), ("cg_refine", C.c_int),
+        ("cg_initial_guess", C.c_int),
     ]
 
 

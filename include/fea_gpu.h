@@ -112,6 +112,14 @@ typedef struct {
                               float-float pairs of about 48 significant bits
                               for FP32 handles), 2 in FP64 for FP32 handles
                               too, 0 skips it.  Default 1. */
+    int cg_initial_guess;  /* Gray-Scott: the CG start of each step's solves.
+                              0: the previous solution (warm start; the
+                              reference's Eigen solve starts from zero,
+                              CPUSolver.cpp:140-142); 1: the linear
+                              extrapolation 2 x_n - x_(n-1) of the last two
+                              steps (the previous solution after fields were
+                              set or on a handle's first step).  The stopping
+                              rule is the same.  Default 0. */
 } fea_params;
 
 typedef struct {
@@ -386,10 +394,13 @@ int fea_batch_get_counters(fea_batch* b, int64_t* total_iterations, int64_t* ste
  * state are unchanged; only CG scratch that the next step recomputes is
  * written), averaged over reps back-to-back launches after one warm-up. */
 int fea_batch_time_iteration(fea_batch* b, int reps, double* ms_per_launch);
-/* CG kernel variant of the batch: 0 / 1 tile-ELL (8 / 4 entries prefetched;
- * FEA_ERR_UNSUPPORTED when the layout is unavailable), 4 / 8 windowed CSR.
- * fea_batch_create picks the fastest by timing; *variant receives the
- * current one when `set` is 0. */
+/* CG kernel variant of the batch: 0 / 1 tile-ELL (8 / 4 entries prefetched),
+ * 4 / 8 windowed CSR, 14 tile-ELL with the operator streamed through a ring
+ * of shared-memory stages by bulk copies, the work shared out evenly over the
+ * blocks in groups of 8 tiles of an instance.  FEA_ERR_UNSUPPORTED when a
+ * variant's layout or shared memory does not fit the batch.
+ * fea_batch_create picks the fastest by timing one iteration of each;
+ * *variant receives the current one when `set` is 0. */
 int fea_batch_cg_variant(fea_batch* b, int set, int* variant);
 
 /* ---- solve without device allocation ---------------------------------------

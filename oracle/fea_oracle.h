@@ -78,8 +78,13 @@ typedef struct {
     int k_scaled;       /* 1: K already carries the diffusivity (per-element D) */
     double tol;         /* CG relative tolerance */
     int max_iter;       /* <= 0: 2N (Eigen default) */
-    int warm_start;     /* 0: zero guess (Eigen solve()), 1: previous field */
+    int warm_start;     /* 0: zero guess (Eigen solve()), 1: previous field,
+                           2 (Gray-Scott): 2 x_n - x_(n-1) from the call's own
+                           previous step; on its first step from prev_u/prev_v
+                           when given, else the previous field */
     int nthreads;       /* OpenMP threads for SpMV/dots (1 = serial, deterministic) */
+    const void* prev_u; /* warm_start 2: the state one step before u, v (R[N]) or NULL */
+    const void* prev_v;
 } fo_params;
 
 #define FO_DECL(R, S) \

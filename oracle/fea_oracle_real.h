@@ -259,7 +259,14 @@ int64_t FN(fo_step)(int64_t N, const int32_t* rp, const int32_t* col, const R* M
     R* w2 = (R*)malloc(sizeof(R) * (size_t)N);
     R* x1 = (R*)malloc(sizeof(R) * (size_t)N);
     R* x2 = (R*)malloc(sizeof(R) * (size_t)N);
+    R* up = (R*)malloc(sizeof(R) * (size_t)N);  /* the previous step's state (warm_start 2) */
+    R* vp = (R*)malloc(sizeof(R) * (size_t)N);
     int zg = prm->warm_start ? 0 : 1;
+    int have_prev = prm->warm_start == 2 && prm->prev_u && prm->prev_v;
+    if (have_prev) {
+        memcpy(up, prm->prev_u, sizeof(R) * (size_t)N);
+        memcpy(vp, prm->prev_v, sizeof(R) * (size_t)N);
+    }
     double rr;
     int64_t total = 0;
     R kap = (R)prm->kappa;
@@ -342,8 +349,17 @@ int64_t FN(fo_step)(int64_t N, const int32_t* rp, const int32_t* col, const R* M
                 FN(spmv_mt)(N, rp, col, M, w1, b1, nt);
                 FN(spmv_mt)(N, rp, col, M, w2, b2, nt);
             }
-            memcpy(x1, u, sizeof(R) * (size_t)N);
-            memcpy(x2, v, sizeof(R) * (size_t)N);
+            if (prm->warm_start == 2 && (s > 0 || have_prev)) {  /* extrapolated start, as the GPU's cg_initial_guess 1 */
+                for (int64_t i = 0; i < N; i++) {
+                    x1[i] = (R)2 * u[i] - up[i];
+                    x2[i] = (R)2 * v[i] - vp[i];
+                }
+            } else {
+                memcpy(x1, u, sizeof(R) * (size_t)N);
+                memcpy(x2, v, sizeof(R) * (size_t)N);
+            }
+            memcpy(up, u, sizeof(R) * (size_t)N);
+            memcpy(vp, v, sizeof(R) * (size_t)N);
             total += FN(fo_pcg)(N, rp, col, A1, b1, x1, prm->tol, prm->max_iter, zg, nt, &rr);
             total += FN(fo_pcg)(N, rp, col, A2, b2, x2, prm->tol, prm->max_iter, zg, nt, &rr);
             memcpy(u, x1, sizeof(R) * (size_t)N);
@@ -361,6 +377,8 @@ int64_t FN(fo_step)(int64_t N, const int32_t* rp, const int32_t* col, const R* M
     free(w2);
     free(x1);
     free(x2);
+    free(up);
+    free(vp);
     if (iters) *iters += total;
     return FN(fo_instability)(N, u, v);
 }

@@ -33,7 +33,7 @@ class Params(C.Structure):
         ("beta", C.c_double), ("gamma", C.c_double),
         ("adv_scheme", C.c_int), ("adv_sign", C.c_double), ("k_scaled", C.c_int),
         ("tol", C.c_double), ("max_iter", C.c_int), ("warm_start", C.c_int),
-        ("nthreads", C.c_int),
+        ("nthreads", C.c_int), ("prev_u", C.c_void_p), ("prev_v", C.c_void_p),
     ]
 
 
@@ -236,15 +236,25 @@ class System:
         out[m] = np.asarray(vec)[self.idx[m]]
         return out
 
-    def step(self, params: Params, u, v, a=None, nsteps=1):
-        """advance_time x nsteps on unknown-indexed fields (copies returned)."""
+    def step(self, params: Params, u, v, a=None, nsteps=1, prev=None):
+        """advance_time x nsteps on unknown-indexed fields (copies returned).
+        prev: (u, v) one step before u, v, for the first step's extrapolated
+        start (warm_start 2)."""
         u = _c(u, self.dtype).copy()
         v = _c(v, self.dtype).copy()
         a = np.zeros(self.N, dtype=self.dtype) if a is None else _c(a, self.dtype).copy()
         it = C.c_int64(0)
-        flags = getattr(lib(), f"fo_step_{_suffix(self.dtype)}")(
-            self.N, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.M), _ptr(self.K), _ptr(self.Adv),
-            C.byref(params), _ptr(u), _ptr(v), _ptr(a), int(nsteps), C.byref(it))
+        pu = pv = None
+        if prev is not None:
+            pu, pv = _c(prev[0], self.dtype), _c(prev[1], self.dtype)
+        params.prev_u = None if pu is None else pu.ctypes.data
+        params.prev_v = None if pv is None else pv.ctypes.data
+        try:
+            flags = getattr(lib(), f"fo_step_{_suffix(self.dtype)}")(
+                self.N, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.M), _ptr(self.K), _ptr(self.Adv),
+                C.byref(params), _ptr(u), _ptr(v), _ptr(a), int(nsteps), C.byref(it))
+        finally:
+            params.prev_u = params.prev_v = None
         return u, v, a, int(it.value), int(flags)
 
     def newmark_init(self, params: Params, u):

@@ -100,12 +100,13 @@ def test_batched_matches_single_mesh_handles(fea):
         assert abs(int(iters[i, 1]) - st.last_iterations[1]) <= 1
 
 
-def test_batched_repeatable_and_masked(fea):
+@pytest.mark.parametrize("variant", [0, 14])
+def test_batched_repeatable_and_masked(fea, variant):
     insts = _instances()
     runs = []
     for _ in range(2):
         B = fea.BatchSolver(insts, cg_tolerance=1e-6)
-        B.set_cg_variant(0)  # bit-for-bit comparisons need the same kernels
+        B.set_cg_variant(variant)  # bit-for-bit comparisons need the same kernels
         for i, d in enumerate(insts):
             B.set_fields(i, *_start(d, 7 + i))
         B.advance_time(5)
@@ -118,13 +119,14 @@ def test_batched_repeatable_and_masked(fea):
         np.testing.assert_array_equal(a, b)
 
 
-def test_blowup_freezes_only_its_instance(fea):
+@pytest.mark.parametrize("variant", [0, 14])
+def test_blowup_freezes_only_its_instance(fea, variant):
     insts = _instances()
     starts = [_start(d, 30 + i) for i, d in enumerate(insts)]
     ref = fea.BatchSolver(insts, cg_tolerance=1e-6)
     bad = fea.BatchSolver(insts, cg_tolerance=1e-6)
-    ref.set_cg_variant(0)
-    bad.set_cg_variant(0)
+    ref.set_cg_variant(variant)
+    bad.set_cg_variant(variant)
     for i, (u, v) in enumerate(starts):
         ref.set_fields(i, u, v)
         if i == 1:
@@ -145,7 +147,7 @@ def test_blowup_freezes_only_its_instance(fea):
             np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 4, 8])
+@pytest.mark.parametrize("variant", [0, 1, 4, 8, 14])
 def test_batched_variants_match_oracle(fea, oracle_mod, variant):
     insts = _instances()
     B = fea.BatchSolver(insts, cg_tolerance=1e-7)
@@ -172,3 +174,46 @@ def test_batch_arguments(fea):
         B.advance_time(-1)
     with pytest.raises(fea.FeaError):
         B.set_cg_variant(2)
+
+
+@pytest.mark.parametrize("variant", [0, 14])
+def test_instance_independent_of_batch(fea, variant):
+    """An instance's results do not depend on the other instances: each
+    instance stepped alone in a batch of one matches its fields in the full
+    batch bit for bit (its partial sums are grouped by its own tiles only)."""
+    insts = _instances()
+    B = fea.BatchSolver(insts, cg_tolerance=1e-6)
+    B.set_cg_variant(variant)
+    for i, d in enumerate(insts):
+        B.set_fields(i, *_start(d, 60 + i))
+    B.advance_time(3)
+    for i, d in enumerate(insts):
+        one = fea.BatchSolver([d], cg_tolerance=1e-6)
+        one.set_cg_variant(variant)
+        one.set_fields(0, *_start(d, 60 + i))
+        one.advance_time(3)
+        for a, b in zip(B.get_fields(i), one.get_fields(0)):
+            np.testing.assert_array_equal(a, b)
+        one.close()
+
+
+@pytest.mark.parametrize("variant", [0, 14])
+def test_batch_timing_probe_leaves_state(fea, variant):
+    """fea_batch_time_iteration runs the iteration kernel over every instance
+    with the fields masked: the steps that follow match an unprobed batch bit
+    for bit."""
+    insts = _instances()
+    out = []
+    for probe in (False, True):
+        B = fea.BatchSolver(insts, cg_tolerance=1e-6)
+        B.set_cg_variant(variant)
+        for i, d in enumerate(insts):
+            B.set_fields(i, *_start(d, 40 + i))
+        B.advance_time(2)
+        if probe:
+            assert B.time_iteration(3) > 0
+        B.advance_time(3)
+        out.append([B.get_fields(i) for i in range(len(insts))])
+        B.close()
+    for (ua, va), (ub, vb) in zip(*out):
+        assert np.array_equal(ua, ub) and np.array_equal(va, vb)

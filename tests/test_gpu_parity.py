@@ -173,6 +173,114 @@ def test_refinement_modes(fea, oracle_mod, refine):
         assert rel_l2(ug, out[1][0]) < 1e-5 and rel_l2(vg, out[1][1]) < 1e-5
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_extrapolated_initial_guess(fea, oracle_mod, precision):
+    """cg_initial_guess 1 starts each step's solves from 2 x_n - x_(n-1):
+    the steps still meet the bar against the FP64 oracle, with fewer CG
+    iterations than the previous-solution start; fields set from outside
+    with new values restart the history (the first step after them takes
+    the warm start; the FP64 handle's round trip through float32 changes
+    them, the FP32 handle's does not)."""
+    xyz, tri = mg.jittered_grid(65, seed=8)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=2, side=0.12)
+    kw = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+    tol, bar = (1e-6, 1e-5) if precision == 0 else (1e-12, 1e-8)  # nine steps of drift
+    res = {}
+    for guess in (0, 1):
+        s = _solver(fea, xyz, tri, 1, precision=precision, equation=fea.REACTION_DIFFUSION, reaction_mode=1,
+                    cg_tolerance=tol, cg_initial_guess=guess, **kw)
+        s.set_fields(u0, v0)
+        s.advance_time(3)
+        s.set_fields(*s.get_fields())
+        s.advance_time(9)
+        st = s.status()
+        assert st.flags == 0
+        res[guess] = (s.get_fields(), st.total_iterations, _device_field(s, 0), _device_field(s, 1))
+        p = s.params
+    S = oracle_mod.System(xyz, tri, bc=1)
+    okw = dict(Du=p.rd_Du, Dv=p.rd_Dv, F=p.rd_feed_rate, k=p.rd_kill_rate, reaction_mode=1)
+    u3, v3, *_ = _oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, S.gather(u0),
+                              S.gather(v0), 3, **okw)
+    u3, v3 = S.gather(S.scatter(u3).astype(np.float32)), S.gather(S.scatter(v3).astype(np.float32))
+    uo, vo, *_ = _oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, p.rd_time_step, u3, v3, 9, **okw)
+    for guess in (0, 1):
+        (ug, vg), _, ud, vd = res[guess]
+        assert rel_l2(ud, uo) < bar and rel_l2(vd, vo) < bar, guess
+    assert res[1][1] < res[0][1]  # fewer CG iterations
+    print(f"iterations over 12 steps: previous solution {res[0][1]}, extrapolated {res[1][1]}")
+
+
+def test_unchanged_fields_keep_history(fea):
+    """A frame loop that writes the displayed field back unchanged
+    (set_values after get_values, CPUSolver.cpp:130,144) keeps the
+    extrapolation's history: the trajectory is bit-identical to the one
+    without the round trips.  A field written with a changed value restarts
+    it: the result is bit-identical to a fresh handle started from the
+    changed state."""
+    xyz, tri = mg.jittered_grid(49, seed=4)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=3, side=0.15)
+    kw = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+
+    def handle():
+        s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-5,
+                    cg_initial_guess=1, **kw)
+        s.set_fields(u0, v0)
+        return s
+
+    def run(s, n, round_trip):
+        for _ in range(n):
+            if round_trip:
+                s.set_values(s.get_values())
+                s.set_fields(*s.get_fields())
+            s.advance_time(1)
+
+    a = handle()
+    run(a, 6, False)
+    b = handle()
+    run(b, 6, True)
+    assert a.status().total_iterations == b.status().total_iterations
+    for f in (0, 1):
+        assert np.array_equal(_device_field(a, f), _device_field(b, f))
+    # a changed value: same as a fresh start from the changed state
+    c = handle()
+    run(c, 3, False)
+    u3, v3 = c.get_fields()
+    u3[len(u3) // 2] += 1e-3
+    c.set_fields(u3, v3)
+    it0 = c.status().total_iterations
+    run(c, 3, False)
+    d = handle()
+    d.set_fields(u3, v3)
+    run(d, 3, False)
+    assert c.status().total_iterations - it0 == d.status().total_iterations
+    for f in (0, 1):
+        assert np.array_equal(_device_field(c, f), _device_field(d, f))
+
+
+def test_extrapolation_matches_oracle_start(fea, oracle_mod):
+    """The oracle's extrapolated start (warm_start 2) solves the same systems:
+    with a loose tolerance both take the same route, so FP64 GPU and FP64
+    oracle agree far below the tolerance-limited error."""
+    xyz, tri = mg.jittered_grid(33, seed=3)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=1, side=0.2)
+    kw = dict(rd_time_step=1.0, rd_Du=2e-4, rd_Dv=1e-4, rd_feed_rate=0.04, rd_kill_rate=0.06)
+    s = _solver(fea, xyz, tri, 1, precision=1, equation=fea.REACTION_DIFFUSION, reaction_mode=1,
+                cg_tolerance=1e-4, cg_initial_guess=1, cg_refine=0, **kw)
+    s.set_fields(u0, v0)
+    s.advance_time(6)
+    p = s.params
+    S = oracle_mod.System(xyz, tri, bc=1)
+    f32 = lambda x: float(np.float32(x))  # noqa: E731
+    po = oracle_mod.params(oracle_mod.REACTION_DIFFUSION, f32(p.rd_time_step), Du=f32(p.rd_Du), Dv=f32(p.rd_Dv),
+                           F=f32(p.rd_feed_rate), k=f32(p.rd_kill_rate), reaction_mode=1, tol=1e-4, warm_start=2)
+    uo, vo, *_ = S.step(po, S.gather(u0), S.gather(v0), nsteps=6)
+    po.warm_start = 1
+    uw, vw, *_ = S.step(po, S.gather(u0), S.gather(v0), nsteps=6)
+    e_extrap = max(rel_l2(_device_field(s, 0), uo), rel_l2(_device_field(s, 1), vo))
+    e_warm = max(rel_l2(_device_field(s, 0), uw), rel_l2(_device_field(s, 1), vw))
+    assert e_extrap < 1e-9 < e_warm  # the GPU followed the extrapolated route, not the warm one
+
+
 @pytest.mark.parametrize("scheme", [0, 1])
 def test_wave_steps(fea, oracle_mod, scheme):
     xyz, tri = mg.icosphere(4)

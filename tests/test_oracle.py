@@ -390,3 +390,21 @@ def test_gray_scott_adjoint_matches_finite_differences(oracle_mod):
     J_u_only = S.adjoint_gray_scott(p, u0, v0, tu, None, nsteps, ck)[0]
     J_v_only = S.adjoint_gray_scott(p, u0, v0, None, tv, nsteps, ck)[0]
     assert abs(J_u_only + J_v_only - J) <= 1e-12 * J
+
+
+def test_extrapolated_start_from_given_previous_state(oracle_mod):
+    """warm_start 2 with prev: a one-step call from (u1, v1) with prev (u0, v0)
+    takes the same route as the second step of a two-step call from (u0, v0)."""
+    O = oracle_mod
+    xyz, tri = mg.jittered_grid(17, seed=2)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=4, side=0.3)
+    S = O.System(xyz, tri, bc=O.NEUMANN)
+    p = O.params(O.REACTION_DIFFUSION, 1.0, Du=2e-4, Dv=1e-4, F=0.04, k=0.06, reaction_mode=1, tol=1e-5,
+                 warm_start=2)
+    u, v = S.gather(u0), S.gather(v0)
+    u2, v2, _, it2, _ = S.step(p, u, v, nsteps=2)
+    u1, v1, _, it1, _ = S.step(p, u, v, nsteps=1)
+    ue, ve, _, ite, _ = S.step(p, u1, v1, nsteps=1, prev=(u, v))
+    assert np.array_equal(ue, u2) and np.array_equal(ve, v2) and it1 + ite == it2
+    uw, vw, *_ = S.step(p, u1, v1, nsteps=1)  # no prev: the previous-field start
+    assert not np.array_equal(uw, u2)
