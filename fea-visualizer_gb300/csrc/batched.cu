@@ -96,8 +96,10 @@ struct BArgs {
     double* part;           // [ntiles * kNV] tile partials
     unsigned int* iticket;  // [ninst] tiles finished per instance in this phase
     int probe;              // timing probe: every tile, no state update
-    // tile-ELL copy of A (variants 0 and 1)
+    // tile-ELL copies of A (variants 0 and 1, the staged right-hand side and
+    // refinement) and of M (the staged right-hand side)
     const FV<R, 2>* As;
+    const R* Ms;
     const uint16_t* lcol;
     const uint32_t* lcol2;  // column pairs (TileEll::lcol2)
     const int32_t* slice_off;
@@ -861,6 +863,199 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
     if (!a.probe) phase_end(a, kIterNext);
 }
 
+// ---- right-hand side and refinement on the tile-ELL layout ------------------------
+//
+// kb_rhs and kb_refine multiply by the whole operator once per step.  These
+// forms stage the tile's x (and for the right-hand side the nodal reaction
+// w(x), evaluated once per unknown instead of once per stored entry) for the
+// tile's rows and its halo in shared memory, then each warp reads its 32-row
+// slice of the tile-ELL copies of A and M with coalesced loads and gathers
+// from shared memory.  Entries keep their CSR order within a row and padding
+// entries hold 0, so the sums and their rounding are those of the CSR forms.
+
+// x of the tile's rows and halo in g[0 .. kTileRows + halo); with `react`,
+// the nodal reaction w(x) in gw[] too.  Every thread of the block calls it;
+// a barrier follows in the caller.
+template <typename R, typename F>
+__device__ __forceinline__ void stage_tile_x(const BArgs<R>& a, int tile, FV<R, 2>* gx, FV<R, 2>* gw, F react) {
+    const int t = threadIdx.x;
+    const FV<R, 2> xr = a.x[(int64_t)tile * kTileRows + t];
+    gx[t] = xr;
+    if (gw) gw[t] = react(xr);
+    const int32_t h0 = a.halo_off[tile], hn = a.halo_off[tile + 1] - h0;
+    for (int h = t; h < hn; h += kBlock) {
+        const FV<R, 2> xc = a.x[a.halo_col[h0 + h]];
+        gx[kTileRows + h] = xc;
+        if (gw) gw[kTileRows + h] = react(xc);
+    }
+}
+
+// Right-hand side b = M w(x) and r0 = b - A x (warm start), z = D^-1 r0 and
+// the set-up scalars of every unfrozen instance, as kb_rhs.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_rhs_ell(BArgs<R> a) {
+    using V = FV<R, 2>;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    V* const gx = reinterpret_cast<V*>(dyn_smem);
+    V* const gw = gx + (kTileRows + a.hmax);
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        BInst* s = a.inst + i;
+        if (((const volatile BInst*)s)->stop) continue;
+        const BPrm P = a.prm[i];
+        const R dt = (R)P.dt, Fr = (R)P.F, Kr = (R)P.k;
+        auto react = [&](const V& x) {  // CPUSolver.cpp:134,137 with the mass weight
+            const R u = x.v[0], v = x.v[1];
+            const R uvv = u * (v * v);
+            V w;
+            w.v[0] = u / dt - uvv + Fr * ((R)1 - u);
+            w.v[1] = v / dt + uvv - (Fr + Kr) * v;
+            return w;
+        };
+        stage_tile_x(a, tile, gx, gw, react);
+        const int sl = tile * (kTileRows / 32) + wib;
+        const int32_t sb = a.slice_off[sl], sw = (a.slice_off[sl + 1] - sb) >> 5;
+        __syncthreads();
+        Acc<R> bs[2], ax[2];
+#pragma unroll 4
+        for (int32_t k = 0; k < sw; k++) {
+            const int32_t e = sb + 32 * k + lane;
+            const V av = ldv(a.As + e, false);
+            const R me = ldg(a.Ms + e);
+            const int l = a.lcol[e];
+            const V w = gw[l], x = gx[l];
+            bs[0].add_prod(me, w.v[0]);
+            bs[1].add_prod(me, w.v[1]);
+            ax[0].add_prod(av.v[0], x.v[0]);
+            ax[1].add_prod(av.v[1], x.v[1]);
+        }
+        const int64_t row = (int64_t)tile * kTileRows + t;
+        const V xr = gx[t];
+        const unsigned int flags = check_value(xr.v[0]) | check_value(xr.v[1]);
+        const V d = ldv(a.dinv + row, false);
+        Acc<R> dots[kNV];  // |b|^2, |r|^2, r.z per field
+        V bv, rv, zv;
+#pragma unroll
+        for (int f = 0; f < 2; f++) {
+            bv.v[f] = bs[f].rounded();
+            bs[f].sub(ax[f]);
+            rv.v[f] = bs[f].rounded();
+            zv.v[f] = d.v[f] * rv.v[f];
+            dots[f].add_prod(bv.v[f], bv.v[f]);
+            dots[2 + f].add_prod(rv.v[f], rv.v[f]);
+            dots[4 + f].add_prod(rv.v[f], zv.v[f]);
+        }
+        a.b[row] = bv;
+        a.rb[0][row] = rv;  // the solve starts at iteration 0 (parity 0)
+        a.z[row] = zv;
+        raise_inst(s, flags);
+        Acc<R> blk[kNV], tot[kNV];
+        block_totals<kNV>(dots, red, blk);  // its barriers also free gx, gw for the next tile
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<kNV>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && t == 0) {
+            volatile BInst* vs = s;
+            const int stop = (atomicOr(&s->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
+            const double tol = a.ctl->tol;
+            vs->stop = stop;
+            vs->iter = 0;
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) nact += start_solve<R>(vs, f, stop, tol, tot[f], tot[2 + f], tot[4 + f]);
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterReset);
+}
+
+// The refinement pass of kb_refine on the tile-ELL layout: zero right-hand
+// sides give x = 0, then the float-float true residual r = b - A x; fields
+// still above their threshold restart CG from there.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_refine_ell(BArgs<R> a) {
+    using V = FV<R, 2>;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    V* const gx = reinterpret_cast<V*>(dyn_smem);
+    __shared__ typename Acc<R>::Packed red[32 * kNV];
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5;
+    const int par = iter_of(a) & 1;
+    const int refine_on = a.ctl->refine;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int i = a.tile_inst[tile];
+        const volatile BInst* s = a.inst + i;
+        const int stop = s->stop;
+        const int refine = refine_on && s->iter < s->max_iter && !stop;
+        int zero[2];
+#pragma unroll
+        for (int f = 0; f < 2; f++) zero[f] = !stop && !(s->bb[f] > 0.0);
+        if (!refine && !zero[0] && !zero[1]) continue;
+        const int64_t row = (int64_t)tile * kTileRows + t;
+        Acc<R> ax[2];
+        if (refine) {  // uniform over the block (one instance per tile)
+            stage_tile_x(a, tile, gx, (V*)nullptr, [](const V& x) { return x; });
+            const int sl = tile * (kTileRows / 32) + wib;
+            const int32_t sb = a.slice_off[sl], sw = (a.slice_off[sl + 1] - sb) >> 5;
+            __syncthreads();
+#pragma unroll 4
+            for (int32_t k = 0; k < sw; k++) {
+                const int32_t e = sb + 32 * k + lane;
+                const V av = ldv(a.As + e, false);
+                const V x = gx[a.lcol[e]];
+#pragma unroll
+                for (int f = 0; f < 2; f++) ax[f].add_prod(av.v[f], x.v[f]);
+            }
+        }
+        Acc<R> dots[4];  // |r|^2, r.z per field
+        if (zero[0] || zero[1]) {
+            V xr = a.x[row];
+#pragma unroll
+            for (int f = 0; f < 2; f++)
+                if (zero[f]) xr.v[f] = 0;
+            a.x[row] = xr;
+        }
+        if (refine) {
+            const V bv = a.b[row], d = ldv(a.dinv + row, false);
+            V rv, zv;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                Acc<R> tr;
+                tr.add(bv.v[f]);
+                tr.sub(ax[f]);
+                rv.v[f] = tr.rounded();
+                zv.v[f] = d.v[f] * rv.v[f];
+                dots[f].add_prod(rv.v[f], rv.v[f]);
+                dots[2 + f].add_prod(rv.v[f], zv.v[f]);
+            }
+            a.rb[par][row] = rv;  // the restart continues the iteration parity
+            a.z[row] = zv;
+        }
+        Acc<R> blk[4], tot[4];
+        block_totals<4>(dots, red, blk);  // its barriers also free gx for the next tile
+        const int t0 = a.inst_tile[i], nt = a.inst_tile[i + 1] - t0;
+        if (inst_commit<4>(blk, a.part, tile, t0, nt, a.iticket + i, red, tot) && t == 0) {
+            volatile BInst* w = a.inst + i;
+            int nact = 0;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                w->active[f] = 0;
+                w->fresh[f] = 1;
+                if (refine && !zero[f] && w->bb[f] > 0.0) {
+                    const double rr = tot[f].value();
+                    w->rr[f] = rr;
+                    if (rr >= w->thr[f]) {
+                        set_gamma(w, f, tot[2 + f]);
+                        w->active[f] = 1;
+                        nact++;
+                    }
+                }
+            }
+            if (nact) atomicAdd(&a.ctl->n_next, nact);
+        }
+    }
+    phase_end(a, kIterKeep);
+}
+
 // After the first solve loop: zero right-hand sides give x = 0, then one
 // float-float true-residual pass r = b - A x; fields still above their
 // threshold restart CG from there.
@@ -1058,6 +1253,7 @@ struct fea_batch {
                   // 14 tile-ELL with the operator streamed by a bulk-copy ring
     TileEll ell;  // tile-ELL layout of the stacked matrix
     void* As = nullptr;
+    void* Ms = nullptr;  // its copy of M
     TileEll ell_od;  // the same without diagonal entries (ring variant)
     void* As_od = nullptr;
     std::vector<int64_t> V, node_off;
@@ -1115,6 +1311,7 @@ BArgs<R> make_bargs(fea_batch* B) {
     a.iticket = B->iticket;
     if (B->ell.ok) {
         a.As = (const FV<R, 2>*)B->As;
+        a.Ms = (const R*)B->Ms;
         a.lcol = B->ell.lcol;
         a.lcol2 = B->ell.lcol2;
         a.slice_off = B->ell.slice_off;
@@ -1203,11 +1400,19 @@ bool ring_fits(const fea_batch* B) {
 template <typename R, int V>
 struct BGrids {
     using K = BKernels<R, V>;
+    using Fn = void (*)(BArgs<R>);
     int rhs, init, iter, stream, tcap = 0;
-    size_t smem_init, smem_iter;
+    size_t smem_init, smem_iter, smem_rhs = 0;
+    Fn rhs_k = kb_rhs<R>, refine_k = kb_refine<R>;  // the staged tile-ELL forms when the layout exists
     explicit BGrids(const fea_batch* B) {
         smem_init = smem_iter = K::smem(B);
-        rhs = wave_grid(kb_rhs<R>, B->ntiles);
+        if (B->ell.ok) {
+            rhs_k = kb_rhs_ell<R>;
+            refine_k = kb_refine_ell<R>;
+            smem_rhs = 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + B->ell.hmax);
+            ensure_dyn_smem(refine_k, smem_rhs);
+        }
+        rhs = wave_grid(rhs_k, B->ntiles, smem_rhs);
         init = wave_grid(K::init, B->ntiles, smem_init);
         if constexpr (V == 14) {
             // the grid from the capacity of one block per SM, then the capacity
@@ -1254,12 +1459,12 @@ void build_batch_graph_t(fea_batch* B) {
     add_kernel(top, n, kb_final_check<R>, g.stream, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
-    cudaGraphNode_t s = add_kernel(step_body, nullptr, kb_rhs<R>, g.rhs, kBlock, L.a1);
+    cudaGraphNode_t s = add_kernel(step_body, nullptr, g.rhs_k, g.rhs, kBlock, L.a1, g.smem_rhs);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
     add_batch_iterations(body1, K::iter, g.iter, L.a1, g.smem_iter);
-    s = add_kernel(step_body, s, kb_refine<R>, g.rhs, kBlock, L.a2);
+    s = add_kernel(step_body, s, g.refine_k, g.rhs, kBlock, L.a2, g.smem_rhs);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
     add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
@@ -1287,12 +1492,12 @@ void run_batch_stream_t(fea_batch* B) {
     kb_start<R><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_int(&B->flags->step, st)) {
-        kb_rhs<R><<<g.rhs, kBlock, 0, st>>>(L.a1);
+        g.rhs_k<<<g.rhs, kBlock, g.smem_rhs, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
         for (int loop = 0; loop < 2; loop++) {
             const BArgs<R>& la = loop ? L.a2 : L.a1;
             if (loop) {
-                kb_refine<R><<<g.rhs, kBlock, 0, st>>>(L.a2);
+                g.refine_k<<<g.rhs, kBlock, g.smem_rhs, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
             K::init<<<g.init, kBlock, g.smem_init, st>>>(la);
@@ -1567,6 +1772,8 @@ void create_batch(fea_batch* B, const fea_instance_desc* inst, int n) {
         if (build_tile_ell(hrp, hcol, Nr, sizeof(FV<R, 2>), kEllSmemBudget, B->ell, B->mem, st)) {
             B->As = B->mem.alloc<FV<R, 2>>(B->ell.E);
             fill_tile_ell<R, 2>(B->ell, (const FV<R, 2>*)B->A, (FV<R, 2>*)B->As, st);
+            B->Ms = B->mem.alloc<R>(B->ell.E);
+            fill_tile_ell<R, 1>(B->ell, (const FV<R, 1>*)B->M, (FV<R, 1>*)B->Ms, st);
             if (build_tile_ell(hrp, hcol, Nr, sizeof(FV<R, 2>), kEllSmemBudget, B->ell_od, B->mem, st, true)) {
                 B->As_od = B->mem.alloc<FV<R, 2>>(B->ell_od.E);
                 fill_tile_ell<R, 2>(B->ell_od, (const FV<R, 2>*)B->A, (FV<R, 2>*)B->As_od, st);

@@ -45,7 +45,7 @@ def test_kernel_names():
 
 # the variants that a new handle starts on, or that the autotuner has picked,
 # on this workload
-PICKED_ON_WORKLOAD = (10, 11, 14)
+PICKED_ON_WORKLOAD = (14, 15)
 
 
 def test_traffic_figures_cover_default_variants():
