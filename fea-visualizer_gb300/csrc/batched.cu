@@ -112,7 +112,7 @@ struct BArgs {
     const FV<R, 2>* As_od;
     const uint16_t* lcol_od;
     const int32_t* slice_off_od;
-    int emax;                  // stored entries of the largest tile of the streamed layout
+    int emax, emax_od;         // stored entries of the largest tile of each layout
     int tcap;                  // tile-list capacity of a block
     const int32_t* inst_grp;   // [ninst + 1] first group slot of each instance
     double* gpart;             // [groups * kNV] group partials
@@ -519,74 +519,137 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
     if (!a.probe) phase_end(a, kIterNext);
 }
 
-// ---- variant 14: the operator streamed by a bulk-copy ring ----------------------
+// ---- variant 14: the ring pipeline -------------------------------------------------
 //
 // The single-mesh ring kernel's tile pipeline over the batch's tiles: thread
 // 0 moves each tile's operator entries and 16-bit local columns with
 // cp.async.bulk into a ring of S shared-memory stages, S - 1 tiles ahead of
-// the product; the threads load their rows' r, w, s, D^-1, x, p and their
-// halo slot's operands one tile ahead; one block barrier per tile orders the
-// staged u'.
+// the product; the threads load their rows' values and their halo slot's
+// operands one tile ahead; one block barrier per tile orders the staged
+// vector.  The CG iteration, the right-hand side, the set-up product and the
+// refinement all run on it (kb_ring's phases).
 //
 // Work.  Each instance's tiles are cut into groups of kGroupTiles consecutive
 // tiles (an instance's last group may be shorter).  At the start of a launch
-// every block reads every instance's activity, lays the active instances'
-// tiles end to end, and takes the groups that start in its equal share of
-// that sequence, so the blocks get equal work however many instances have
+// every block lays the instances' tiles end to end (for the iteration only
+// the active instances', from the table the previous phase's last block
+// built) and takes the groups that start in its equal share of that
+// sequence, so the blocks get equal work however many instances have
 // converged.  The threads accumulate a group's inner products over its
 // tiles; at the group's last tile the block reduces them into the group's
 // partials, and the block that completes an instance's last group sums the
-// instance's group partials in group order and advances its CG scalars.  The
+// instance's group partials in group order and advances its state.  The
 // groups are fixed per instance, so an instance's results depend neither on
 // the other instances nor on the schedule.
 constexpr int kGroupTiles = 8;
 
-// An active instance with groups in the block's share.
+// Phases of a batched solve that run on the ring pipeline: the CG iteration,
+// the right-hand side with the initial residual, the set-up product of a
+// solve, and the true-residual refinement.
+enum { kPhIter = 0, kPhRhs = 1, kPhInit = 2, kPhRefine = 3 };
+
+// An instance with groups in the block's share.
 struct BRingInst {
     int inst, nt, t0, g0, ng;  // instance, tiles, first tile, first group slot, groups
     int u0, u1;                // its groups in the share
 };
 
-// Dynamic shared memory of kb_iter_ring: the ring, the two u' buffers, then
-// the block's instances, their phase controls and its tile list (tile, index
-// of its instance in the block's list, group slot), each for up to tcap tiles.
+// What a phase needs of such an instance, read at the start of the launch:
+// the CG phase control (iteration, set-up), the step's parameters (right-hand
+// side), the refinement's decisions.
+template <typename R>
+struct BRingCtl {
+    PhaseCtl<R, 2> c;
+    R dt, F, k;
+    int refine, zero[2];
+};
+
+// One stage of the ring: a tile's operator entries, its entries of M (the
+// right-hand side), then its local columns.
+struct BStage {
+    size_t A, M, L, bytes;
+    __host__ __device__ BStage(int emax, size_t fv, size_t mv) {
+        auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
+        A = 0;
+        M = al(fv * (size_t)emax);
+        L = al(M + mv * (size_t)emax);
+        bytes = al(L + 2 * (size_t)emax);
+    }
+};
+
+// Dynamic shared memory of kb_ring: the ring, two staging buffers (u' of the
+// tile and its halo; x and the nodal reaction for the right-hand side), then
+// the block's instances, their controls and its tile list (tile, index of its
+// instance in the block's list, group slot), each for up to tcap tiles.
 template <typename R>
 struct BRingLayout {
     size_t ubuf, ov, ctl, tl, tq, tg, total;
-    __host__ __device__ BRingLayout(int emax, int hmax, int tcap, int stages) {
+    __host__ __device__ BRingLayout(int emax, int hmax, int tcap, int stages, int ph) {
         auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
-        ubuf = al((size_t)stages * RingStage(emax, sizeof(FV<R, 2>)).bytes);
-        ov = al(ubuf + 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + hmax));
+        const size_t mv = ph == kPhRhs ? sizeof(R) : 0;
+        ubuf = al((size_t)stages * BStage(emax, sizeof(FV<R, 2>), mv).bytes);
+        const size_t per = (size_t)(ph == kPhRhs ? 2 : 1) * sizeof(FV<R, 2>) * (size_t)(kTileRows + hmax);
+        ov = al(ubuf + 2 * per);
         ctl = al(ov + sizeof(BRingInst) * (size_t)tcap);
-        tl = al(ctl + sizeof(PhaseCtl<R, 2>) * (size_t)tcap);
+        tl = al(ctl + sizeof(BRingCtl<R>) * (size_t)tcap);
         tq = al(tl + sizeof(int32_t) * (size_t)tcap);
         tg = al(tq + sizeof(int32_t) * (size_t)tcap);
         total = al(tg + sizeof(int32_t) * (size_t)tcap);
     }
 };
 
-template <typename R, int S>
-__global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
+// The nodal reaction of the mass-weighted Gray-Scott right-hand side,
+// b = M w(x) (CPUSolver.cpp:134,137 with the mass weight).
+template <typename R>
+__device__ __forceinline__ FV<R, 2> gs_reaction(const FV<R, 2>& x, R dt, R F, R k) {
+    const R u = x.v[0], v = x.v[1];
+    const R uvv = u * (v * v);
+    FV<R, 2> w;
+    w.v[0] = u / dt - uvv + F * ((R)1 - u);
+    w.v[1] = v / dt + uvv - (F + k) * v;
+    return w;
+}
+
+// One phase over every participating instance on the ring pipeline.  The
+// iteration streams the diagonal-free layout when it exists; the other phases
+// stream the full one (the right-hand side also M's entries).  Per phase:
+//   iteration   rows r, w, s, D^-1, x, p; stages u'; w' = A u'; finish_cgcg
+//   rhs         rows x, D^-1; stages x and w(x); b = M w(x), r0 = b - A x
+//               in float-float; start_solve (every unfrozen instance)
+//   init        rows z; stages z; w0 = A z; finish_spmv (active instances)
+//   refine      rows x, b, D^-1; stages x; r = b - A x in float-float;
+//               the restart decision (instances to refine or to zero)
+// The iteration shares out the active instances' tiles (the table its
+// previous phase built); the others share out every instance's tiles and
+// skip the groups of instances that do not take part, whose state no commit
+// of the phase changes before those groups are read.
+template <typename R, int S, int PH>
+__global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
     using V = FV<R, 2>;
+    using Ctl = BRingCtl<R>;
     static_assert(S >= 2 && S <= 8, "ring depth");
+    constexpr bool kIt = PH == kPhIter, kRhs = PH == kPhRhs, kIni = PH == kPhInit, kRef = PH == kPhRefine;
+    constexpr int NVP = kIni ? 2 : kRef ? 4 : kNV;  // partials per group
     extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
     __shared__ __align__(8) uint64_t bars[S];
     __shared__ typename Acc<R>::Packed red[32 * kNV];
     __shared__ int s_nov, s_ntl;
-    const BRingLayout<R> Lay(a.emax, a.hmax, a.tcap, S);
-    const RingStage L(a.emax, sizeof(V));
-    const bool od = a.As_od != nullptr;  // the streamed layout lacks the diagonal entries
+    const bool od = kIt && a.As_od != nullptr;  // the streamed layout lacks the diagonal entries
     const V* const Aop = od ? a.As_od : a.As;
     const uint16_t* const lop = od ? a.lcol_od : a.lcol;
     const int32_t* const soff = od ? a.slice_off_od : a.slice_off;
+    const int emx = od ? a.emax_od : a.emax;
+    const BRingLayout<R> Lay(emx, a.hmax, a.tcap, S, PH);
+    const BStage L(emx, sizeof(V), kRhs ? sizeof(R) : 0);
     unsigned char* const ring = dyn_smem;
     V* const ubuf = reinterpret_cast<V*>(dyn_smem + Lay.ubuf);
     BRingInst* const ov = reinterpret_cast<BRingInst*>(dyn_smem + Lay.ov);
-    PhaseCtl<R, 2>* const ovc = reinterpret_cast<PhaseCtl<R, 2>*>(dyn_smem + Lay.ctl);
+    Ctl* const ovc = reinterpret_cast<Ctl*>(dyn_smem + Lay.ctl);
     int32_t* const tl = reinterpret_cast<int32_t*>(dyn_smem + Lay.tl);
     int32_t* const tq = reinterpret_cast<int32_t*>(dyn_smem + Lay.tq);
     int32_t* const tg = reinterpret_cast<int32_t*>(dyn_smem + Lay.tg);
-    const int ustride = kTileRows + a.hmax;
+    const int hstride = kTileRows + a.hmax;             // one staged vector: the tile's rows, then its halo
+    const int bstride = (kRhs ? 2 : 1) * hstride;       // one staging buffer
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int ntiles = a.ntiles, tcap = a.tcap;
     if (t == 0) {
@@ -595,12 +658,15 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
         s_nov = 0;
     }
     grid_dependency_wait();
-    if (batch_stopped(a)) return;
+    if constexpr (kIt)
+        if (batch_stopped(a)) return;
     const int iter = iter_of(a), par = iter & 1;
-    // the active instances' tiles laid end to end (the table the previous
-    // phase's last block built; every instance in a probe); this block's share
-    // [lo, hi) and the instances with a group starting in it
-    const int32_t* pos_of = a.probe ? a.inst_tile : a.act_pos;
+    const int refine_on = kRef ? a.ctl->refine : 0;
+    // the tiles laid end to end (the active instances' for the iteration, from
+    // the table the previous phase's last block built; every instance's
+    // otherwise); this block's share [lo, hi) and the taking part instances
+    // with a group starting in it
+    const int32_t* pos_of = (kIt && !a.probe) ? a.act_pos : a.inst_tile;
     const int T = pos_of[a.ninst];
     const int lo = (int)((int64_t)T * blockIdx.x / gridDim.x);
     const int hi = (int)((int64_t)T * (blockIdx.x + 1) / gridDim.x);
@@ -611,13 +677,32 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
             const int u0 = lo > pos ? (lo - pos + kGroupTiles - 1) / kGroupTiles : 0;
             const int u1 = min(ng, (hi - pos + kGroupTiles - 1) / kGroupTiles);
             if (u0 < u1) {
-                PhaseCtl<R, 2> c;
-                c.set(iter, (const volatile BInst*)(a.inst + i));
-                if (a.probe) probe_mask(c);
-                const int q = atomicAdd(&s_nov, 1);
-                if (q < tcap) {
-                    ov[q] = BRingInst{i, nt, a.inst_tile[i], a.inst_grp[i], ng, u0, u1};
-                    ovc[q] = c;
+                const volatile BInst* s = a.inst + i;
+                Ctl cc;
+                bool take = true;
+                if constexpr (kIt || kIni) {
+                    cc.c.set(iter, s);
+                    if (a.probe) probe_mask(cc.c);
+                    if constexpr (kIni) take = cc.c.any;
+                } else if constexpr (kRhs) {
+                    take = !s->stop;
+                    const BPrm P = a.prm[i];
+                    cc.dt = (R)P.dt;
+                    cc.F = (R)P.F;
+                    cc.k = (R)P.k;
+                } else {
+                    const int stop = s->stop;
+                    cc.refine = refine_on && s->iter < s->max_iter && !stop;
+#pragma unroll
+                    for (int f = 0; f < 2; f++) cc.zero[f] = !stop && !(s->bb[f] > 0.0);
+                    take = cc.refine || cc.zero[0] || cc.zero[1];
+                }
+                if (take) {
+                    const int q = atomicAdd(&s_nov, 1);
+                    if (q < tcap) {
+                        ov[q] = BRingInst{i, nt, a.inst_tile[i], a.inst_grp[i], ng, u0, u1};
+                        ovc[q] = cc;
+                    }
                 }
             }
         }
@@ -678,9 +763,10 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
             mbar_arrive(bar);
             return;
         }
-        mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
+        mbar_arrive_expect_tx(bar, n * (uint32_t)(sizeof(V) + (kRhs ? sizeof(R) : 0) + 2));
         const uint64_t pol = l2_evict_first_policy();
         bulk_g2s_hint(stage_of(b) + L.A, Aop + e0, n * (uint32_t)sizeof(V), bar, pol);
+        if constexpr (kRhs) bulk_g2s_hint(stage_of(b) + L.M, a.Ms + e0, n * (uint32_t)sizeof(R), bar, pol);
         bulk_g2s_hint(stage_of(b) + L.L, lop + e0, 2 * n, bar, pol);
     };
     uint32_t armed = 0;  // thread 0: bit b set while stage b has copies in flight
@@ -716,43 +802,58 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
     v.r1 = a.rb[par ^ 1];
     v.w1 = a.wb[par ^ 1];
     v.s1 = a.sb[par ^ 1];
-    V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
-    {
+    // the halo slot's staged vector: z (set-up) or x (right-hand side, refinement)
+    const V* const hsrc = kIni ? a.z : a.x;
+    // row values of the next tile: iteration r, w, s, D^-1, x, p; right-hand
+    // side x, D^-1; set-up z (in cx); refinement x, b (in cw), D^-1
+    auto load_rows = [&](int tile, V& cr, V& cw, V& cs, V& cd, V& cx, V& cp) {
         const uint64_t pol_keep = l2_evict_last_policy();
-        if (ntl > 0) {
-            const int row = tl[0] * kTileRows + t;
+        const int row = tile * kTileRows + t;  // every vector holds whole tiles
+        if constexpr (kIt) {
             cr = ld_keep(v.r0 + row, pol_keep);
             cw = ld_keep(v.w0 + row, pol_keep);
             cs = ld_keep(v.s0 + row, pol_keep);
-            cd = ld_keep(v.dinv + row, pol_keep);
-            cx = ld_keep(v.x + row, pol_keep);
             cp = ld_keep(v.p + row, pol_keep);
         }
-        if (fcol >= 0) {
-            hr = ld_keep(v.r0 + fcol, pol_keep);
-            hw = ld_keep(v.w0 + fcol, pol_keep);
-            hs = ld_keep(v.s0 + fcol, pol_keep);
-            hd = ld_keep(v.dinv + fcol, pol_keep);
+        if constexpr (kRef) cw = ld_keep(a.b + row, pol_keep);
+        if constexpr (!kIni) cd = ld_keep(v.dinv + row, pol_keep);
+        cx = ld_keep((kIni ? a.z : v.x) + row, pol_keep);
+    };
+    auto load_halo = [&](int32_t col, V& hr, V& hw, V& hs, V& hd) {
+        const uint64_t pol_keep = l2_evict_last_policy();
+        if constexpr (kIt) {
+            hr = ld_keep(v.r0 + col, pol_keep);
+            hw = ld_keep(v.w0 + col, pol_keep);
+            hs = ld_keep(v.s0 + col, pol_keep);
+            hd = ld_keep(v.dinv + col, pol_keep);
+        } else {
+            hr = ld_keep(hsrc + col, pol_keep);
         }
-    }
-    PhaseCtl<R, 2> c;
+    };
+    V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
+    if (ntl > 0) load_rows(tl[0], cr, cw, cs, cd, cx, cp);
+    if (fcol >= 0) load_halo(fcol, hr, hw, hs, hd);
+    Ctl cc;
     int cq = -1;
-    Acc<R> dots[kNV];
-    uint32_t phases = 0u;  // bit b: parity of stage b's next phase
-    int bad_inst = -1;     // instance of a tile whose stage wait expired
+    Acc<R> dots[NVP];
+    unsigned int flags = 0;  // right-hand side: the instability test of the group's rows
+    uint32_t phases = 0u;    // bit b: parity of stage b's next phase
+    int bad_inst = -1;       // instance of a tile whose stage wait expired
     int buf = 0, b = 0;
     for (int k = 0; k < ntl; k++) {
         const int tile = tl[k], q = tq[k];
         if (q != cq) {
-            c = ovc[q];
+            cc = ovc[q];
             cq = q;
         }
-        V* ut = ubuf + buf * ustride;
+        const PhaseCtl<R, 2>& c = cc.c;
+        V* const ut = ubuf + buf * bstride;  // staged: u', z or x
+        V* const uw = ut + hstride;          // right-hand side: the nodal reaction
         const int row = tile * kTileRows + t;
-        V un, wn;  // wn: the product's start, the diagonal term in the diagonal-free layout
+        V un, wn;  // iteration: u' and the product's start (the diagonal term in the diagonal-free layout)
 #pragma unroll
         for (int f = 0; f < 2; f++) un.v[f] = wn.v[f] = 0;
-        if (row < a.N) {
+        if constexpr (kIt) {
             V sn, rn;
             cg_advance(c, cr, cw, c.need_old ? cs : cw, cd, sn, rn, un);
             if (od) wn = rn;
@@ -770,32 +871,39 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
             v.p[row] = cp;
             v.r1[row] = rn;
             v.s1[row] = sn;
+            ut[t] = un;
+        } else {
+            ut[t] = cx;
+            if constexpr (kRhs) {
+                uw[t] = gs_reaction(cx, cc.dt, cc.F, cc.k);
+                flags |= check_value(cx.v[0]) | check_value(cx.v[1]);
+            }
         }
-        ut[t] = un;
-        const uint64_t pol_keep = l2_evict_last_policy();
+        // the tile's own values this thread keeps past the loads of the next tile
+        const V xr = cx, dr = cd, br = cw;
         const int nt = tile_at(k + 1);
-        if (nt < ntiles) {
-            const int nrow = nt * kTileRows + t;
-            cr = ld_keep(v.r0 + nrow, pol_keep);
-            cw = ld_keep(v.w0 + nrow, pol_keep);
-            cs = ld_keep(v.s0 + nrow, pol_keep);
-            cd = ld_keep(v.dinv + nrow, pol_keep);
-            cx = ld_keep(v.x + nrow, pol_keep);
-            cp = ld_keep(v.p + nrow, pol_keep);
-        }
+        if (nt < ntiles) load_rows(nt, cr, cw, cs, cd, cx, cp);
         if (j < hcc) {
-            V sn, rn, u2;
-            cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
-            ut[kTileRows + j] = u2;
+            if constexpr (kIt) {
+                V sn, rn, u2;
+                cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
+                ut[kTileRows + j] = u2;
+            } else {
+                ut[kTileRows + j] = hr;
+                if constexpr (kRhs) uw[kTileRows + j] = gs_reaction(hr, cc.dt, cc.F, cc.k);
+            }
         }
-        if (hcoln >= 0) {
-            hr = ld_keep(v.r0 + hcoln, pol_keep);
-            hw = ld_keep(v.w0 + hcoln, pol_keep);
-            hs = ld_keep(v.s0 + hcoln, pol_keep);
-            hd = ld_keep(v.dinv + hcoln, pol_keep);
+        if (hcoln >= 0) load_halo(hcoln, hr, hw, hs, hd);
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock) {
+            const int32_t col = a.halo_col[h0c + h];
+            if constexpr (kIt) {
+                ut[kTileRows + h] = cg_u_at(v, c, col);
+            } else {
+                const V g = hsrc[col];
+                ut[kTileRows + h] = g;
+                if constexpr (kRhs) uw[kTileRows + h] = gs_reaction(g, cc.dt, cc.F, cc.k);
+            }
         }
-        for (int32_t h = kBlock + t; h < hcc; h += kBlock)
-            ut[kTileRows + h] = cg_u_at(v, c, a.halo_col[h0c + h]);
         __syncthreads();
         if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
             const int bp = b == 0 ? S - 1 : b - 1;
@@ -821,17 +929,84 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
         if (t == 0 && got) armed &= ~(1u << b);
         const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
         const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+        if constexpr (kIt || kIni) {
 #pragma unroll 4
-        for (int kk = 0; kk < sw; kk++) {
-            const V av = As[32 * kk];
-            const V g = ut[Ls[32 * kk]];
+            for (int kk = 0; kk < sw; kk++) {
+                const V av = As[32 * kk];
+                const V g = ut[Ls[32 * kk]];
 #pragma unroll
-            for (int f = 0; f < 2; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
-        }
-        if (row < a.N) {
-            v.w1[row] = wn;
+                for (int f = 0; f < 2; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
+            }
+            if constexpr (kIt) {
+                v.w1[row] = wn;
 #pragma unroll
-            for (int f = 0; f < 2; f++) dots[2 + f].add_prod(wn.v[f], un.v[f]);
+                for (int f = 0; f < 2; f++) dots[2 + f].add_prod(wn.v[f], un.v[f]);
+            } else {
+                a.wb[par][row] = wn;
+#pragma unroll
+                for (int f = 0; f < 2; f++) dots[f].add_prod(xr.v[f], wn.v[f]);  // z.w0
+            }
+        } else if constexpr (kRhs) {
+            const R* Ms = reinterpret_cast<const R*>(stage_of(b) + L.M) + sb + lane;
+            Acc<R> bs[2], ax[2];
+#pragma unroll 4
+            for (int kk = 0; kk < sw; kk++) {
+                const V av = As[32 * kk];
+                const R me = Ms[32 * kk];
+                const int l = Ls[32 * kk];
+                const V w = uw[l], x = ut[l];
+                bs[0].add_prod(me, w.v[0]);
+                bs[1].add_prod(me, w.v[1]);
+                ax[0].add_prod(av.v[0], x.v[0]);
+                ax[1].add_prod(av.v[1], x.v[1]);
+            }
+            V bv, rv, zv;
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                bv.v[f] = bs[f].rounded();
+                bs[f].sub(ax[f]);
+                rv.v[f] = bs[f].rounded();
+                zv.v[f] = dr.v[f] * rv.v[f];
+                dots[f].add_prod(bv.v[f], bv.v[f]);
+                dots[2 + f].add_prod(rv.v[f], rv.v[f]);
+                dots[4 + f].add_prod(rv.v[f], zv.v[f]);
+            }
+            a.b[row] = bv;
+            a.rb[0][row] = rv;  // the solve starts at iteration 0 (parity 0)
+            a.z[row] = zv;
+        } else {  // refinement
+            Acc<R> ax[2];
+            if (cc.refine) {
+#pragma unroll 4
+                for (int kk = 0; kk < sw; kk++) {
+                    const V av = As[32 * kk];
+                    const V x = ut[Ls[32 * kk]];
+#pragma unroll
+                    for (int f = 0; f < 2; f++) ax[f].add_prod(av.v[f], x.v[f]);
+                }
+            }
+            if (cc.zero[0] || cc.zero[1]) {  // only zero fields change: their products go unused
+                V xz = xr;
+#pragma unroll
+                for (int f = 0; f < 2; f++)
+                    if (cc.zero[f]) xz.v[f] = 0;
+                a.x[row] = xz;
+            }
+            if (cc.refine) {
+                V rv, zv;
+#pragma unroll
+                for (int f = 0; f < 2; f++) {
+                    Acc<R> tr;
+                    tr.add(br.v[f]);
+                    tr.sub(ax[f]);
+                    rv.v[f] = tr.rounded();
+                    zv.v[f] = dr.v[f] * rv.v[f];
+                    dots[f].add_prod(rv.v[f], rv.v[f]);
+                    dots[2 + f].add_prod(rv.v[f], zv.v[f]);
+                }
+                a.rb[par][row] = rv;  // the restart continues the iteration parity
+                a.z[row] = zv;
+            }
         }
         sb = sbn;
         sw = swn;
@@ -841,16 +1016,59 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
         b = b + 1 == S ? 0 : b + 1;
         if (k + 1 == ntl || tg[k + 1] != tg[k]) {  // the group's last tile: its partials
             const BRingInst o = ov[q];
-            Acc<R> blk[kNV], tot[kNV];
-            block_totals<kNV>(dots, red, blk);
-            if (inst_commit<kNV>(blk, a.gpart, tg[k], o.g0, o.ng, a.iticket + o.inst, red, tot) && t == 0 &&
+            BInst* const s = a.inst + o.inst;
+            if constexpr (kRhs) {
+                raise_inst(s, flags);
+                flags = 0;
+            }
+            Acc<R> blk[NVP], tot[NVP];
+            block_totals<NVP>(dots, red, blk);
+            if (inst_commit<NVP>(blk, a.gpart, tg[k], o.g0, o.ng, a.iticket + o.inst, red, tot) && t == 0 &&
                 !a.probe) {
-                volatile BInst* s = a.inst + o.inst;
-                if (finish_cgcg<R, 2>(s, &a.inst[o.inst].flags, c.act, tot))
-                    atomicAdd(&a.ctl->n_next, s->active[0] + s->active[1]);
+                volatile BInst* vs = s;
+                if constexpr (kIt) {
+                    if (finish_cgcg<R, 2>(vs, &s->flags, c.act, tot))
+                        atomicAdd(&a.ctl->n_next, vs->active[0] + vs->active[1]);
+                } else if constexpr (kRhs) {
+                    const int stop = (atomicOr(&s->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
+                    const double tol = a.ctl->tol;
+                    vs->stop = stop;
+                    vs->iter = 0;
+                    int nact = 0;
+#pragma unroll
+                    for (int f = 0; f < 2; f++)
+                        nact += start_solve<R>(vs, f, stop, tol, tot[f], tot[2 + f], tot[4 + f]);
+                    if (nact) atomicAdd(&a.ctl->n_next, nact);
+                } else if constexpr (kIni) {
+                    finish_spmv<R, 2>(vs, &s->flags, c.act, tot);
+                    int nact = 0;
+#pragma unroll
+                    for (int f = 0; f < 2; f++) {
+                        vs->fresh[f] = 1;  // the first iteration takes p = u, s = w
+                        nact += vs->active[f];
+                    }
+                    if (nact) atomicAdd(&a.ctl->n_next, nact);
+                } else {
+                    int nact = 0;
+#pragma unroll
+                    for (int f = 0; f < 2; f++) {
+                        vs->active[f] = 0;
+                        vs->fresh[f] = 1;
+                        if (cc.refine && !cc.zero[f] && vs->bb[f] > 0.0) {
+                            const double rr = tot[f].value();
+                            vs->rr[f] = rr;
+                            if (rr >= vs->thr[f]) {
+                                set_gamma(vs, f, tot[2 + f]);
+                                vs->active[f] = 1;
+                                nact++;
+                            }
+                        }
+                    }
+                    if (nact) atomicAdd(&a.ctl->n_next, nact);
+                }
             }
 #pragma unroll
-            for (int f = 0; f < kNV; f++) dots[f] = Acc<R>();
+            for (int f = 0; f < NVP; f++) dots[f] = Acc<R>();
         }
     }
     grid_launch_dependents();
@@ -860,7 +1078,11 @@ __global__ void __launch_bounds__(kBlock, 2) kb_iter_ring(BArgs<R> a) {
             for (int q2 = 0; q2 < S; q2++)  // copies still in flight land before the block leaves
                 if (armed & (1u << q2)) mbar_wait(&bars[q2], (phases >> q2) & 1u);
     }
-    if (!a.probe) phase_end(a, kIterNext);
+    if constexpr (kIt) {
+        if (!a.probe) phase_end(a, kIterNext);
+    } else {
+        phase_end(a, kRhs ? kIterReset : kIterKeep);
+    }
 }
 
 // ---- right-hand side and refinement on the tile-ELL layout ------------------------
@@ -1323,7 +1545,7 @@ BArgs<R> make_bargs(fea_batch* B) {
             a.As_od = (const FV<R, 2>*)B->As_od;
             a.lcol_od = B->ell_od.lcol;
             a.slice_off_od = B->ell_od.slice_off;
-            a.emax = B->ell_od.emax;
+            a.emax_od = B->ell_od.emax;
         }
     }
     a.inst_grp = B->inst_grp;
@@ -1365,7 +1587,8 @@ struct BKernels<R, 1> : BEllKernels<R, 4> {};
 constexpr int kBatchRingStages = 3;
 template <typename R>
 struct BKernels<R, 14> : BEllKernels<R, 4> {
-    static constexpr void (*iter)(BArgs<R>) = kb_iter_ring<R, kBatchRingStages>;
+    static constexpr void (*init)(BArgs<R>) = kb_ring<R, kBatchRingStages, kPhInit>;
+    static constexpr void (*iter)(BArgs<R>) = kb_ring<R, kBatchRingStages, kPhIter>;
 };
 
 // Tile-list capacity of a ring-kernel block for a grid of `grid` blocks: a
@@ -1375,12 +1598,21 @@ int ring_tcap(const fea_batch* B, int64_t grid) {
     return (int)(ceil_div(B->ntiles, std::max<int64_t>(grid, 1)) + kGroupTiles);
 }
 
-// Entries of the largest tile the ring kernel streams.
-int ring_emax(const fea_batch* B) { return B->ell_od.ok ? B->ell_od.emax : B->ell.emax; }
+// Entries of the largest tile a ring phase streams (the iteration streams
+// the diagonal-free layout when it exists).
+int ring_emax(const fea_batch* B, int ph) { return ph == kPhIter && B->ell_od.ok ? B->ell_od.emax : B->ell.emax; }
 
 template <typename R>
-size_t ring_smem(const fea_batch* B, int tcap) {
-    return BRingLayout<R>(ring_emax(B), B->ell.hmax, tcap, kBatchRingStages).total;
+size_t ring_smem(const fea_batch* B, int tcap, int ph) {
+    return BRingLayout<R>(ring_emax(B, ph), B->ell.hmax, tcap, kBatchRingStages, ph).total;
+}
+
+// The largest of the phases' shared memory.
+template <typename R>
+size_t ring_smem_max(const fea_batch* B, int tcap) {
+    size_t m = 0;
+    for (int ph : {kPhIter, kPhRhs, kPhInit, kPhRefine}) m = std::max(m, ring_smem<R>(B, tcap, ph));
+    return m;
 }
 
 // Whether the ring kernel fits: the tile-ELL layout exists and a block's
@@ -1388,13 +1620,13 @@ size_t ring_smem(const fea_batch* B, int tcap) {
 // can give it (a grid of min(SMs, groups) blocks).
 template <typename R>
 bool ring_fits(const fea_batch* B) {
-    if (!B->ell.ok || ring_emax(B) <= 0) return false;
+    if (!B->ell.ok || B->ell.emax <= 0) return false;
     int dev = 0, lim = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
         return false;
     const int64_t g = std::max<int64_t>(1, std::min<int64_t>(num_sms(), B->ngroups));
-    return ring_smem<R>(B, ring_tcap(B, g)) + 2048 <= (size_t)lim;
+    return ring_smem_max<R>(B, ring_tcap(B, g)) + 2048 <= (size_t)lim;
 }
 
 template <typename R, int V>
@@ -1402,26 +1634,45 @@ struct BGrids {
     using K = BKernels<R, V>;
     using Fn = void (*)(BArgs<R>);
     int rhs, init, iter, stream, tcap = 0;
-    size_t smem_init, smem_iter, smem_rhs = 0;
+    size_t smem_init, smem_iter, smem_rhs = 0, smem_refine = 0;
     Fn rhs_k = kb_rhs<R>, refine_k = kb_refine<R>;  // the staged tile-ELL forms when the layout exists
     explicit BGrids(const fea_batch* B) {
         smem_init = smem_iter = K::smem(B);
-        if (B->ell.ok) {
-            rhs_k = kb_rhs_ell<R>;
-            refine_k = kb_refine_ell<R>;
-            smem_rhs = 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + B->ell.hmax);
-            ensure_dyn_smem(refine_k, smem_rhs);
-        }
-        rhs = wave_grid(rhs_k, B->ntiles, smem_rhs);
-        init = wave_grid(K::init, B->ntiles, smem_init);
         if constexpr (V == 14) {
-            // the grid from the capacity of one block per SM, then the capacity
-            // of that grid (never larger, so the occupancy holds)
-            iter = wave_grid(K::iter, std::max(B->ngroups, 1), ring_smem<R>(B, ring_tcap(B, num_sms())));
-            tcap = ring_tcap(B, iter);
-            smem_iter = ring_smem<R>(B, tcap);  // larger when fewer groups than SMs shrink the grid
-            ensure_dyn_smem(K::iter, smem_iter);
+            // Every phase on the ring pipeline, at one grid: the smallest of
+            // the phases' one-wave grids at the tile-list capacity of one
+            // block per SM; then the capacity of that grid (never larger, so
+            // the occupancy holds; larger when fewer groups than SMs shrink
+            // the grid) and each phase's shared memory for it.
+            const Fn ks[4] = {K::iter, kb_ring<R, kBatchRingStages, kPhRhs>, K::init,
+                              kb_ring<R, kBatchRingStages, kPhRefine>};
+            const int phs[4] = {kPhIter, kPhRhs, kPhInit, kPhRefine};
+            const int tcap0 = ring_tcap(B, num_sms());
+            int g = INT32_MAX;
+            for (int p = 0; p < 4; p++)
+                g = std::min(g, wave_grid(ks[p], std::max(B->ngroups, 1), ring_smem<R>(B, tcap0, phs[p])));
+            tcap = ring_tcap(B, g);
+            size_t sm[4];
+            for (int p = 0; p < 4; p++) {
+                sm[p] = ring_smem<R>(B, tcap, phs[p]);
+                ensure_dyn_smem(ks[p], sm[p]);
+            }
+            rhs_k = ks[1];
+            refine_k = ks[3];
+            smem_iter = sm[0];
+            smem_rhs = sm[1];
+            smem_init = sm[2];
+            smem_refine = sm[3];
+            rhs = init = iter = g;
         } else {
+            if (B->ell.ok) {
+                rhs_k = kb_rhs_ell<R>;
+                refine_k = kb_refine_ell<R>;
+                smem_rhs = smem_refine = 2 * sizeof(FV<R, 2>) * (size_t)(kTileRows + B->ell.hmax);
+                ensure_dyn_smem(refine_k, smem_refine);
+            }
+            rhs = wave_grid(rhs_k, B->ntiles, smem_rhs);
+            init = wave_grid(K::init, B->ntiles, smem_init);
             iter = wave_grid(K::iter, B->ntiles, smem_iter);
         }
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(B->N, kBlock)));
@@ -1464,7 +1715,7 @@ void build_batch_graph_t(fea_batch* B) {
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
     add_batch_iterations(body1, K::iter, g.iter, L.a1, g.smem_iter);
-    s = add_kernel(step_body, s, g.refine_k, g.rhs, kBlock, L.a2, g.smem_rhs);
+    s = add_kernel(step_body, s, g.refine_k, g.rhs, kBlock, L.a2, g.smem_refine);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
     add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
@@ -1497,7 +1748,7 @@ void run_batch_stream_t(fea_batch* B) {
         for (int loop = 0; loop < 2; loop++) {
             const BArgs<R>& la = loop ? L.a2 : L.a1;
             if (loop) {
-                g.refine_k<<<g.rhs, kBlock, g.smem_rhs, st>>>(L.a2);
+                g.refine_k<<<g.rhs, kBlock, g.smem_refine, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
             K::init<<<g.init, kBlock, g.smem_init, st>>>(la);
