@@ -27,11 +27,15 @@ pytestmark = pytest.mark.gpu
 STATES = os.path.join(GOLDEN, "_states")
 PER_STEP = (5, 25, 55, 100, 250, 500, 1000, 1500, 2000)
 # rel-L2 drift bounds of the GPU run from the initial state, per horizon
-# (u and v): the measured drift (v: 1.3e-5, 1.8e-5, 2.4e-5 after 25, 55 and
-# 100 steps at the bench's tolerance; 2.1e-5 after 100 steps at tolerances
-# down to 1e-7, so FP32 rounding, not the CG tolerance, sets it) with a
-# margin of about 2.5x
-DRIFT_BOUND = {25: 3e-5, 55: 5e-5, 100: 6e-5}
+# (u and v), with the bench's tolerance and extrapolated start.  Measured on
+# a GB300 (u / v): 2.7e-6 / 1.7e-5 after 25 steps, 4.4e-6 / 2.3e-5 after 55,
+# 7.4e-6 / 4.0e-5 after 100, 3.9e-5 / 1.2e-4 after 250, 7.6e-5 / 1.8e-4
+# after 500, 2.4e-4 / 4.7e-4 after 1,000, 6.5e-4 / 1.2e-3 after 1,500 and
+# 7.6e-4 / 1.4e-3 after 2,000.  The per-step error stays near 1e-6 (FP32
+# operator values: the drift after 100 steps is the same at CG tolerances
+# down to 1e-7), and the unstable pattern amplifies it.  Bounds: about 2.5x
+# the measured drift.
+DRIFT_BOUND = {25: 5e-5, 55: 6e-5, 100: 1e-4, 250: 3e-4, 500: 5e-4, 1000: 1.2e-3, 1500: 3e-3, 2000: 3.5e-3}
 
 
 def _state(k):
