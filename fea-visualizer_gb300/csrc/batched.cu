@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "cg_device.cuh"
@@ -835,7 +836,14 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
     if (fcol >= 0) load_halo(fcol, hr, hw, hs, hd);
     Ctl cc;
     int cq = -1;
-    Acc<R> dots[NVP];
+    // the iteration sums its rows' inner products per thread in R (fused
+    // multiply-adds over at most a group's tiles), the other phases in the
+    // handle's accumulators; the block and instance totals use the latter
+    using DA = std::conditional_t<kIt, R, Acc<R>>;
+    DA dots[NVP];
+    if constexpr (kIt)
+#pragma unroll
+        for (int f = 0; f < NVP; f++) dots[f] = 0;
     unsigned int flags = 0;  // right-hand side: the instability test of the group's rows
     uint32_t phases = 0u;    // bit b: parity of stage b's next phase
     int bad_inst = -1;       // instance of a tile whose stage wait expired
@@ -864,8 +872,8 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
                     cp.v[f] = c.fresh[f] ? ui : fmar(c.beta[f], cp.v[f], ui);
                     cx.v[f] = fmar(c.alpha[f], cp.v[f], cx.v[f]);
                 }
-                dots[f].add_prod(rn.v[f], un.v[f]);
-                dots[4 + f].add_prod(rn.v[f], rn.v[f]);
+                dots[f] = fmar(rn.v[f], un.v[f], dots[f]);
+                dots[4 + f] = fmar(rn.v[f], rn.v[f], dots[4 + f]);
             }
             v.x[row] = cx;
             v.p[row] = cp;
@@ -940,7 +948,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             if constexpr (kIt) {
                 v.w1[row] = wn;
 #pragma unroll
-                for (int f = 0; f < 2; f++) dots[2 + f].add_prod(wn.v[f], un.v[f]);
+                for (int f = 0; f < 2; f++) dots[2 + f] = fmar(wn.v[f], un.v[f], dots[2 + f]);
             } else {
                 a.wb[par][row] = wn;
 #pragma unroll
@@ -1021,8 +1029,13 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
                 raise_inst(s, flags);
                 flags = 0;
             }
-            Acc<R> blk[NVP], tot[NVP];
-            block_totals<NVP>(dots, red, blk);
+            Acc<R> blk[NVP], tot[NVP], acc[NVP];
+#pragma unroll
+            for (int f = 0; f < NVP; f++) {
+                if constexpr (kIt) acc[f].add(dots[f]);
+                else acc[f] = dots[f];
+            }
+            block_totals<NVP>(acc, red, blk);
             if (inst_commit<NVP>(blk, a.gpart, tg[k], o.g0, o.ng, a.iticket + o.inst, red, tot) && t == 0 &&
                 !a.probe) {
                 volatile BInst* vs = s;
@@ -1068,7 +1081,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
                 }
             }
 #pragma unroll
-            for (int f = 0; f < NVP; f++) dots[f] = Acc<R>();
+            for (int f = 0; f < NVP; f++) dots[f] = DA();
         }
     }
     grid_launch_dependents();

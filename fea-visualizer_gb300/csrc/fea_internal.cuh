@@ -191,6 +191,7 @@ struct StepArgs {
     const uint16_t* lcol_od;
     const int32_t* slice_off_od;
     int emax_od;
+    const R* Ms;  // tile-ELL copy of M (the staged Gray-Scott right-hand side), or null
     const StepParams* prm;
     CgState* cg;
     // Deferred-finish variants: the state is double-buffered (cg and cg_alt),

@@ -190,6 +190,7 @@ struct fea_solver {
     TileEll ell;                    // the CG kernels' layout of Pc (tile_ell.cu)
     int stream_stages = 0;          // stages of the streamed iteration that fit in shared memory (0, 2 or 3)
     void *S1 = nullptr, *S0 = nullptr, *S2 = nullptr;          // tile-ELL copies of A1, A0, A2
+    void* Ms_ell = nullptr;                                    // tile-ELL copy of M
     TileEll ell_od;                                            // the layout without diagonal entries (ring kernels)
     void *S1d = nullptr, *S0d = nullptr, *S2d = nullptr;       // its copies of A1, A0, A2
     std::vector<float> h_xyz;       // host copy of the points (ordering keys)
@@ -271,10 +272,12 @@ void assemble(fea_solver* s) {
         round_copy<float>(s->K64, s->emap, s->P.nnz, (float*)s->Kc, s->stream);
         round_copy<float>(s->M64, s->emap, s->P.nnz, (float*)s->Mc, s->stream);
         round_copy<float>(s->Adv64, s->emap, s->P.nnz, (float*)s->Advc, s->stream);
+        fill_tile_ell<float, 1>(s->ell, (const FV<float, 1>*)s->Mc, (FV<float, 1>*)s->Ms_ell, s->stream);
     } else {
         round_copy<double>(s->K64, s->emap, s->P.nnz, (double*)s->Kc, s->stream);
         round_copy<double>(s->M64, s->emap, s->P.nnz, (double*)s->Mc, s->stream);
         round_copy<double>(s->Adv64, s->emap, s->P.nnz, (double*)s->Advc, s->stream);
+        fill_tile_ell<double, 1>(s->ell, (const FV<double, 1>*)s->Mc, (FV<double, 1>*)s->Ms_ell, s->stream);
     }
     memcpy(s->cur_vel, s->prm.advdiff_velocity, sizeof(s->cur_vel));
     s->cur_vel_mode = s->prm.velocity_mode;
@@ -362,6 +365,7 @@ void build_context(fea_solver* s) {
     s->stream_stages = 0;
     s->S1 = s->S0 = s->S2 = nullptr;
     s->S1d = s->S0d = s->S2d = nullptr;
+    s->Ms_ell = nullptr;
     s->F = Fields{};
     cudaStream_t st = s->stream;
     s->idx = s->mat_mem.alloc<int32_t>(s->V);
@@ -380,6 +384,7 @@ void build_context(fea_solver* s) {
             s->S1 = ralloc(s->mat_mem, s, s->ell.E);
             s->S0 = ralloc(s->mat_mem, s, s->ell.E);
             s->S2 = ralloc(s->mat_mem, s, 2 * s->ell.E);
+            s->Ms_ell = ralloc(s->mat_mem, s, s->ell.E);
             if (build_tile_ell(rp, col, N, 2 * rsize(s), kEllSmemBudget, s->ell_od, s->mat_mem, st, true)) {
                 s->S1d = ralloc(s->mat_mem, s, s->ell_od.E);
                 s->S0d = ralloc(s->mat_mem, s, s->ell_od.E);
@@ -520,6 +525,7 @@ StepArgs<R, NF> make_args(fea_solver* s, bool init_op) {
         a.halo_col = s->ell.halo_col;
         a.hmax = s->ell.hmax;
         a.emax = s->ell.emax;
+        a.Ms = (const R*)s->Ms_ell;
         if (s->ell_od.ok) {
             if constexpr (NF == 1) a.As_od = (const FV<R, 1>*)(init_op ? s->S0d : s->S1d);
             else a.As_od = (const FV<R, 2>*)s->S2d;

@@ -19,9 +19,15 @@ from conftest import oracle_step, rel_l2
 pytestmark = pytest.mark.gpu
 
 HORIZON = 1000
-# rel-L2 bound of batch vs single handles after HORIZON steps (the measured
-# worst instance with a margin)
-HORIZON_BOUND = 1e-3
+# rel-L2 bound of batch vs single handles after HORIZON steps.  Both solve
+# every step to the same tolerance, but their CG iterations sum the rows'
+# inner products in per-thread groups of different rows (a batch group of at
+# most 8 tiles; a single handle's block share), so alpha and beta differ in
+# their last bits, and unstable patterns amplify that over the horizon.
+# Measured on a GB300: median 1.3e-6, 95th percentile 1.6e-5, worst 1.2e-3,
+# the order of the FP32 drift against the FP64 oracle (1.4e-3 after 2,000
+# steps on the 1M-vertex workload).  Bound: about 4x the worst.
+HORIZON_BOUND = 5e-3
 
 
 @pytest.fixture(scope="module")
