@@ -119,7 +119,7 @@ class Clocks:
 # workload in one ncu capture without cache control (the capture commands sit
 # with the kernels' profile summaries).  A variant without an entry reports
 # traffic null.
-IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6, 14: 91.2e6, 15: 91.4e6}
+IN_LOOP_TRAFFIC = {10: 104.1e6, 11: 106.9e6, 14: 91.7e6, 15: 91.4e6}
 
 
 def cg_kernel_name(variant):

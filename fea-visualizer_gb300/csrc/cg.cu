@@ -1259,30 +1259,14 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
         phases ^= 1u << b;
         bad |= !got;
         if (t == 0 && got) armed &= ~(1u << b);
-        if (od) {  // entries in lane pairs: two values and two columns per load
-            const VPair<V>* Ap = reinterpret_cast<const VPair<V>*>(stage_of(b) + L.A) + (sb >> 1) + lane;
-            const uint32_t* Lp = reinterpret_cast<const uint32_t*>(stage_of(b) + L.L) + (sb >> 1) + lane;
-#pragma unroll 2
-            for (int m = 0; m < (sw >> 1); m++) {
-                const VPair<V> ap = Ap[32 * m];
-                const uint32_t lp = Lp[32 * m];
-                const V g0 = ut[lp & 0xffffu], g1 = ut[lp >> 16];
-#pragma unroll
-                for (int f = 0; f < NF; f++) {
-                    wn.v[f] = fmar(ap.a.v[f], g0.v[f], wn.v[f]);
-                    wn.v[f] = fmar(ap.b.v[f], g1.v[f], wn.v[f]);
-                }
-            }
-        } else {
-            const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
-            const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+        const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
 #pragma unroll 4
-            for (int kk = 0; kk < sw; kk++) {
-                const V av = As[32 * kk];
-                const V g = ut[Ls[32 * kk]];
+        for (int kk = 0; kk < sw; kk++) {
+            const V av = As[32 * kk];
+            const V g = ut[Ls[32 * kk]];
 #pragma unroll
-                for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
-            }
+            for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
         }
         if (row < a.N) {
             v.w1[row] = wn;

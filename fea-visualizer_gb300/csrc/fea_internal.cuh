@@ -60,9 +60,7 @@ struct TileEll {
 // when a tile's halo does not fit the 16-bit indices or `smem_budget` bytes of
 // shared memory at fv_bytes per operand.
 // skip_diag: each row's diagonal entry is left out (a kernel that adds the
-// diagonal term from the row's own values reads the rest), each lane's
-// entries are stored in adjacent pairs (entry k of the slice's row `lane` at
-// slice_off + 64 (k / 2) + 2 lane + k % 2, even widths); no lcol2.
+// diagonal term from the row's own values reads the rest); no lcol2.
 bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& col, int64_t N, size_t fv_bytes,
                     size_t smem_budget, TileEll& L, DeviceArena& keep, cudaStream_t st, bool skip_diag = false);
 // As[k] = A[emap[k]] (0 for padding): the layout's copy of operator values.

@@ -72,13 +72,6 @@ __device__ __forceinline__ T ld_keep(const T* p, uint64_t pol) {
 // warp stages about the same share of a tile's halo.
 __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
 
-// Two adjacent operator entries of a lane in the paired (diagonal-free)
-// layout: one 16-byte load for FV<float, 2>.
-template <typename V>
-struct alignas(2 * sizeof(V)) VPair {
-    V a, b;
-};
-
 // One stage of the ring: a tile's operator entries, then its local columns.
 struct RingStage {
     size_t A, L, bytes;

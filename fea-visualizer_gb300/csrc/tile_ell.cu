@@ -11,10 +11,7 @@
 // in shared memory, so every gathered operand is a shared-memory load.
 // Entries keep their CSR order within a row (same summation order), and
 // padding entries hold 0 with the row's own local index.  The diagonal-free
-// variant of the layout leaves each row's diagonal entry out and stores each
-// row's entries in pairs: entry k of the slice's row `lane` at slice_off[s] +
-// 64 (k / 2) + 2 lane + k % 2, the width rounded up to even, so one 16-byte
-// load brings a lane two values and one 32-bit load their two columns.
+// variant of the layout leaves each row's diagonal entry out.
 #include <algorithm>
 #include <vector>
 
@@ -56,7 +53,6 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
     for (int64_t s = 0; s < nslices; s++) {
         int32_t w = 0;
         for (int64_t r = s * 32; r < std::min<int64_t>(N, s * 32 + 32); r++) w = std::max(w, rows[r + 1] - rows[r]);
-        if (skip_diag) w = (w + 1) & ~1;
         slice_off[s] = (int32_t)E;
         E += 32 * (int64_t)w;
         if (E >= (int64_t)INT32_MAX) return false;
@@ -89,8 +85,7 @@ bool build_tile_ell(const std::vector<int32_t>& rp, const std::vector<int32_t>& 
             const int64_t r = s * 32 + lane;
             const int32_t len = r < N ? rows[r + 1] - rows[r] : 0;
             for (int32_t k = 0; k < w; k++) {
-                const int64_t at = slice_off[s] + (skip_diag ? 64 * (int64_t)(k >> 1) + 2 * lane + (k & 1)
-                                                             : 32 * (int64_t)k + lane);
+                const int64_t at = slice_off[s] + 32 * (int64_t)k + lane;
                 if (k < len) {
                     const int32_t e = ents[rows[r] + k], c = col[e];
                     int64_t lc;

@@ -117,9 +117,11 @@ typedef struct {
                               reference's Eigen solve starts from zero,
                               CPUSolver.cpp:140-142); 1: the linear
                               extrapolation 2 x_n - x_(n-1) of the last two
-                              steps (the previous solution after fields were
-                              set or on a handle's first step).  The stopping
-                              rule is the same.  Default 0. */
+                              steps (the previous solution on a handle's
+                              first step and after fields are set to values
+                              that differ from the state; writing back the
+                              values just read keeps the history).  The
+                              stopping rule is the same.  Default 0. */
 } fea_params;
 
 typedef struct {
@@ -131,7 +133,7 @@ typedef struct {
     int64_t max_row_nonzeros;    /* FEMContext::compute_max_row_nonzeros (:207-219) */
     int precision;               /* FEA_FP32 / FEA_FP64 */
     int boundary_condition;
-    int rows_per_warp_lanes;     /* CG kernel variant (fea_autotune): 0 tile-ELL, else CSR window */
+    int rows_per_warp_lanes;     /* CG kernel variant (fea_set_cg_variant, fea_autotune) */
     int64_t device_bytes;        /* device memory held by the handle */
 } fea_info;
 
