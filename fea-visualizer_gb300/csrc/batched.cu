@@ -679,7 +679,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             const int u1 = min(ng, (hi - pos + kGroupTiles - 1) / kGroupTiles);
             if (u0 < u1) {
                 const volatile BInst* s = a.inst + i;
-                Ctl cc;
+                Ctl cc{};  // the members this phase does not set stay zero
                 bool take = true;
                 if constexpr (kIt || kIni) {
                     cc.c.set(iter, s);
@@ -834,7 +834,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
     V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
     if (ntl > 0) load_rows(tl[0], cr, cw, cs, cd, cx, cp);
     if (fcol >= 0) load_halo(fcol, hr, hw, hs, hd);
-    Ctl cc;
+    Ctl cc{};
     int cq = -1;
     // the iteration sums its rows' inner products per thread in R (fused
     // multiply-adds over at most a group's tiles), the other phases in the
