@@ -396,6 +396,7 @@ def bench_batched(F, steps, warmup, plain_steps):
     t0 = time.perf_counter()
     B = F.BatchSolver(insts, cg_tolerance=BATCH_CG_TOL)
     setup_s = time.perf_counter() - t0
+    B.set_initial_guess(CG_GUESS)  # the solves' start, as on the single-mesh handles
     for i, (u, v) in enumerate(starts):
         B.set_fields(i, u, v)
     B.advance_time(warmup)
@@ -412,7 +413,7 @@ def bench_batched(F, steps, warmup, plain_steps):
     for d in insts:
         p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=d["time_step"],
                              rd_Du=d["Du"], rd_Dv=d["Dv"], rd_feed_rate=d["feed_rate"],
-                             rd_kill_rate=d["kill_rate"], cg_tolerance=BATCH_CG_TOL)
+                             rd_kill_rate=d["kill_rate"], cg_tolerance=BATCH_CG_TOL, cg_initial_guess=CG_GUESS)
         handles.append(F.CUDASolver(d["vertices"], d["triangles"], boundary_condition=F.NEUMANN, params=p))
     plain = {}
     # the plain loop on the handles' default kernels, and on the batch's own kernel family
@@ -460,7 +461,7 @@ def bench_batched(F, steps, warmup, plain_steps):
             "sweep_steps_per_s": steps / batch_s, "plain_instance_steps_per_s": plain_rate,
             "plain_steps_timed": plain_steps, "speedup_vs_plain": batch_rate / plain_rate,
             "plain_same_family_instance_steps_per_s": same_rate, "speedup_vs_plain_same_family": batch_rate / same_rate,
-            "cg_variant": batch_variant,
+            "cg_variant": batch_variant, "initial_guess": GUESS_LABEL[CG_GUESS],
             "cg_iterations_per_sweep_step_mean_instance": float(np.mean(it1 - it0)) / steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "algorithmic_bytes_per_batched_iteration": it_bytes, "ms_per_batched_iteration": it_ms,

@@ -56,6 +56,7 @@ struct BInst {
     int last_iters[2];
     double last_rel[2];
     long long steps_done, total_iters;
+    int prev_valid;  // xprev holds the state one step before x (the extrapolated start)
 };
 
 // Loop state shared by the instances.
@@ -118,6 +119,10 @@ struct BArgs {
     const int32_t* inst_grp;   // [ninst + 1] first group slot of each instance
     double* gpart;             // [groups * kNV] group partials
     int32_t* act_pos;          // [ninst + 1] active-tile table (build_active_table); null: not kept
+    // Extrapolated initial guess (variant 14; null otherwise): the state one
+    // step back and the start 2 x_n - x_(n-1) the right-hand side formed.
+    FV<R, 2>* xprev;
+    FV<R, 2>* xg;
     cudaGraphConditionalHandle cond;
     int* cont;
     int use_graph;
@@ -520,6 +525,30 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
     if (!a.probe) phase_end(a, kIterNext);
 }
 
+// After the right-hand side, with the extrapolated start: every unfrozen
+// instance's state moves to xprev and the start 2 x_n - x_(n-1) the
+// right-hand side formed (x_n itself where the instance had no history)
+// becomes x, the start of its solves; its history is then valid.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kb_guess_move(BArgs<R> a) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.N; r += stride) {
+        const int i = a.tile_inst[r / kTile];
+        if (((const volatile BInst*)(a.inst + i))->stop) continue;
+        a.xprev[r] = a.x[r];
+        a.x[r] = a.xg[r];
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.ninst; i += stride)
+        if (!((const volatile BInst*)(a.inst + i))->stop) a.inst[i].prev_valid = 1;
+}
+
+// Histories of the extrapolated start cleared (instance `only`, or all when
+// it is negative).
+__global__ void kb_clear_history(BInst* inst, int n, int only) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (only < 0 || i == only) inst[i].prev_valid = 0;
+}
+
 // ---- variant 14: the ring pipeline -------------------------------------------------
 //
 // The single-mesh ring kernel's tile pipeline over the batch's tiles: thread
@@ -563,6 +592,7 @@ struct BRingCtl {
     PhaseCtl<R, 2> c;
     R dt, F, k;
     int refine, zero[2];
+    int extrap;  // right-hand side: the solve starts from 2 x_n - x_(n-1)
 };
 
 // One stage of the ring: a tile's operator entries, its entries of M (the
@@ -687,6 +717,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
                     if constexpr (kIni) take = cc.c.any;
                 } else if constexpr (kRhs) {
                     take = !s->stop;
+                    cc.extrap = a.xg != nullptr && s->prev_valid != 0;
                     const BPrm P = a.prm[i];
                     cc.dt = (R)P.dt;
                     cc.F = (R)P.F;
@@ -806,7 +837,9 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
     // the halo slot's staged vector: z (set-up) or x (right-hand side, refinement)
     const V* const hsrc = kIni ? a.z : a.x;
     // row values of the next tile: iteration r, w, s, D^-1, x, p; right-hand
-    // side x, D^-1; set-up z (in cx); refinement x, b (in cw), D^-1
+    // side x, D^-1 and, with the extrapolated start, x_(n-1) (in cr); set-up z
+    // (in cx); refinement x, b (in cw), D^-1
+    const bool xp_on = kRhs && a.xg != nullptr;
     auto load_rows = [&](int tile, V& cr, V& cw, V& cs, V& cd, V& cx, V& cp) {
         const uint64_t pol_keep = l2_evict_last_policy();
         const int row = tile * kTileRows + t;  // every vector holds whole tiles
@@ -816,6 +849,8 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             cs = ld_keep(v.s0 + row, pol_keep);
             cp = ld_keep(v.p + row, pol_keep);
         }
+        if constexpr (kRhs)
+            if (xp_on) cr = ld_keep(a.xprev + row, pol_keep);
         if constexpr (kRef) cw = ld_keep(a.b + row, pol_keep);
         if constexpr (!kIni) cd = ld_keep(v.dinv + row, pol_keep);
         cx = ld_keep((kIni ? a.z : v.x) + row, pol_keep);
@@ -829,7 +864,18 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             hd = ld_keep(v.dinv + col, pol_keep);
         } else {
             hr = ld_keep(hsrc + col, pol_keep);
+            if constexpr (kRhs)
+                if (xp_on) hw = ld_keep(a.xprev + col, pol_keep);
         }
+    };
+    // the solve's start at an unknown: 2 x_n - x_(n-1) (one rounding; 2 x is
+    // exact) with the extrapolated start, else x_n
+    auto start_at = [&](const V& xn, const V& xp, bool extrap) {
+        V g = xn;
+        if (extrap)
+#pragma unroll
+            for (int f = 0; f < 2; f++) g.v[f] = fmar((R)2, xn.v[f], -xp.v[f]);
+        return g;
     };
     V cr, cw, cs, cd, cx, cp, hr, hw, hs, hd;
     if (ntl > 0) load_rows(tl[0], cr, cw, cs, cd, cx, cp);
@@ -859,6 +905,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
         V* const uw = ut + hstride;          // right-hand side: the nodal reaction
         const int row = tile * kTileRows + t;
         V un, wn;  // iteration: u' and the product's start (the diagonal term in the diagonal-free layout)
+        V x0r = cx;  // right-hand side: the solve's start at this row
 #pragma unroll
         for (int f = 0; f < 2; f++) un.v[f] = wn.v[f] = 0;
         if constexpr (kIt) {
@@ -880,12 +927,13 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             v.r1[row] = rn;
             v.s1[row] = sn;
             ut[t] = un;
+        } else if constexpr (kRhs) {
+            x0r = start_at(cx, cr, cc.extrap);
+            ut[t] = x0r;                                 // A x0 with the solve's start
+            uw[t] = gs_reaction(cx, cc.dt, cc.F, cc.k);  // b from x_n
+            flags |= check_value(cx.v[0]) | check_value(cx.v[1]);
         } else {
             ut[t] = cx;
-            if constexpr (kRhs) {
-                uw[t] = gs_reaction(cx, cc.dt, cc.F, cc.k);
-                flags |= check_value(cx.v[0]) | check_value(cx.v[1]);
-            }
         }
         // the tile's own values this thread keeps past the loads of the next tile
         const V xr = cx, dr = cd, br = cw;
@@ -896,9 +944,11 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
                 V sn, rn, u2;
                 cg_advance(c, hr, hw, c.need_old ? hs : hw, hd, sn, rn, u2);
                 ut[kTileRows + j] = u2;
+            } else if constexpr (kRhs) {
+                ut[kTileRows + j] = start_at(hr, hw, cc.extrap);
+                uw[kTileRows + j] = gs_reaction(hr, cc.dt, cc.F, cc.k);
             } else {
                 ut[kTileRows + j] = hr;
-                if constexpr (kRhs) uw[kTileRows + j] = gs_reaction(hr, cc.dt, cc.F, cc.k);
             }
         }
         if (hcoln >= 0) load_halo(hcoln, hr, hw, hs, hd);
@@ -906,10 +956,12 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             const int32_t col = a.halo_col[h0c + h];
             if constexpr (kIt) {
                 ut[kTileRows + h] = cg_u_at(v, c, col);
-            } else {
+            } else if constexpr (kRhs) {
                 const V g = hsrc[col];
-                ut[kTileRows + h] = g;
-                if constexpr (kRhs) uw[kTileRows + h] = gs_reaction(g, cc.dt, cc.F, cc.k);
+                ut[kTileRows + h] = start_at(g, xp_on ? a.xprev[col] : g, cc.extrap);
+                uw[kTileRows + h] = gs_reaction(g, cc.dt, cc.F, cc.k);
+            } else {
+                ut[kTileRows + h] = hsrc[col];
             }
         }
         __syncthreads();
@@ -982,6 +1034,7 @@ __global__ void __launch_bounds__(kBlock, 2) kb_ring(BArgs<R> a) {
             a.b[row] = bv;
             a.rb[0][row] = rv;  // the solve starts at iteration 0 (parity 0)
             a.z[row] = zv;
+            if (xp_on) a.xg[row] = x0r;  // kb_guess_move makes it x
         } else {  // refinement
             Acc<R> ax[2];
             if (cc.refine) {
@@ -1507,6 +1560,8 @@ struct fea_batch {
     int32_t* act_pos = nullptr;    // [ninst + 1] active-tile table
     BFlags* flags = nullptr;
     float* staging = nullptr;  // node-sized staging buffer (largest instance)
+    int guess_rule = 0;        // start of the solves: 0 x_n, 1 2 x_n - x_(n-1) (variant 14)
+    void *xprev = nullptr, *xg = nullptr;  // [N] x_(n-1) and the next start (allocated with rule 1)
     double tol = 0.0;
     int max_iter_cfg = 0;
     bool stream_mode = false;
@@ -1564,8 +1619,15 @@ BArgs<R> make_bargs(fea_batch* B) {
     a.inst_grp = B->inst_grp;
     a.gpart = B->gpart;
     a.act_pos = B->wch == 14 ? B->act_pos : nullptr;
+    if (B->guess_rule == 1 && B->wch == 14 && B->xprev) {
+        a.xprev = (FV<R, 2>*)B->xprev;
+        a.xg = (FV<R, 2>*)B->xg;
+    }
     return a;
 }
+
+// Graph identity: the variant and whether the extrapolated start is on.
+int graph_key(const fea_batch* B) { return B->wch + (B->guess_rule == 1 && B->wch == 14 ? 1000 : 0); }
 
 template <typename R>
 struct BLoop {
@@ -1724,6 +1786,7 @@ void build_batch_graph_t(fea_batch* B) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, g.rhs_k, g.rhs, kBlock, L.a1, g.smem_rhs);
+    if (L.a1.xg) s = add_kernel(step_body, s, kb_guess_move<R>, g.stream, kBlock, L.a1);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
@@ -1734,7 +1797,7 @@ void build_batch_graph_t(fea_batch* B) {
     add_batch_iterations(body2, K::iter, g.iter, L.a2, g.smem_iter);
     add_kernel(step_body, s, kb_stepctl<R>, 1, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphInstantiate(&G.exec, top, 0));
-    G.lanes = WCH;
+    G.lanes = graph_key(B);
 }
 
 int read_int(const int* d, cudaStream_t st) {
@@ -1758,6 +1821,10 @@ void run_batch_stream_t(fea_batch* B) {
     while (read_int(&B->flags->step, st)) {
         g.rhs_k<<<g.rhs, kBlock, g.smem_rhs, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
+        if (L.a1.xg) {
+            kb_guess_move<R><<<g.stream, kBlock, 0, st>>>(L.a1);
+            FEA_CHECK_LAUNCH();
+        }
         for (int loop = 0; loop < 2; loop++) {
             const BArgs<R>& la = loop ? L.a2 : L.a1;
             if (loop) {
@@ -1790,7 +1857,7 @@ void run_batch(fea_batch* B) {
         }
         return;
     }
-    if (!B->graph.exec || B->graph.lanes != B->wch) {
+    if (!B->graph.exec || B->graph.lanes != graph_key(B)) {
         B->graph.destroy();
         switch (B->wch) {
         case 0: build_batch_graph_t<R, 0>(B); break;
@@ -2135,6 +2202,8 @@ int fea_batch_set_fields(fea_batch* B, int instance, const float* u, const float
             kb_gather<float><<<launch_grid(V), kBlock, 0, B->stream>>>(B->staging, map, V, (FV<float, 2>*)B->x, f);
         FEA_CHECK_LAUNCH();
     }
+    kb_clear_history<<<1, kBlock, 0, B->stream>>>(B->inst, B->ninst, instance);  // a new state has no history
+    FEA_CHECK_LAUNCH();
     FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
     BATCH_API_END
 }
@@ -2198,7 +2267,32 @@ int fea_batch_cg_variant(fea_batch* B, int set, int* variant) {
         set_error("batch CG variant %d unavailable: no tile-ELL layout, or its shared memory does not fit", v);
         return FEA_ERR_UNSUPPORTED;
     }
+    if (v != B->wch) {  // the histories of the extrapolated start are kept by variant 14 only
+        kb_clear_history<<<launch_grid(B->ninst), kBlock, 0, B->stream>>>(B->inst, B->ninst, -1);
+        FEA_CHECK_LAUNCH();
+    }
     B->wch = v;
+    BATCH_API_END
+}
+
+int fea_batch_set_initial_guess(fea_batch* B, int rule) {
+    BATCH_API_BEGIN
+    check_batch(B);
+    if (rule != 0 && rule != 1) return fail(FEA_ERR_INVALID_ARGUMENT, "initial guess rule must be 0 or 1");
+    if (rule == B->guess_rule) return FEA_OK;
+    if (rule == 1 && !B->xprev) {
+        const size_t nb = (B->precision == FEA_FP64 ? sizeof(FV<double, 2>) : sizeof(FV<float, 2>)) * (size_t)B->N;
+        void* xp = B->mem.alloc<char>((int64_t)nb);
+        void* xg = B->mem.alloc<char>((int64_t)nb);
+        FEA_CUDA_TRY(cudaMemsetAsync(xp, 0, nb, B->stream));
+        FEA_CUDA_TRY(cudaMemsetAsync(xg, 0, nb, B->stream));
+        B->xprev = xp;
+        B->xg = xg;
+    }
+    kb_clear_history<<<launch_grid(B->ninst), kBlock, 0, B->stream>>>(B->inst, B->ninst, -1);
+    FEA_CHECK_LAUNCH();
+    FEA_CUDA_TRY(cudaStreamSynchronize(B->stream));
+    B->guess_rule = rule;
     BATCH_API_END
 }
 

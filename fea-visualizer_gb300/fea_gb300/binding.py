@@ -134,6 +134,7 @@ SIGNATURES = {
     "fea_batch_get_counters": [_P, _P, _P],
     "fea_batch_time_iteration": [_P, C.c_int, C.POINTER(C.c_double)],
     "fea_batch_cg_variant": [_P, C.c_int, C.POINTER(C.c_int)],
+    "fea_batch_set_initial_guess": [_P, C.c_int],
     "fea_pcg_solve_csr_noalloc": [_I64, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int, _P,
                                   C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
     "fea_triangulate_pslg": [_P, _I64, _P, _I64, _P, _I64, C.c_double, C.c_double, C.POINTER(C.c_void_p)],
@@ -467,13 +468,19 @@ class BatchSolver:
         return v.value
 
     def set_cg_variant(self, variant: int):
-        """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 4, 8: windowed CSR kernels."""
+        """0, 1: tile-ELL kernels (8 or 4 entries prefetched); 4, 8: windowed CSR kernels;
+        14: tile-ELL with the operator streamed through a bulk-copy ring."""
         v = C.c_int(int(variant))
         check(load().fea_batch_cg_variant(self._h, 1, C.byref(v)))
 
     def set_cg(self, tolerance: float, max_iterations: int = 0):
         """New CG stopping rule of every instance (fea_batch_set_cg)."""
         check(load().fea_batch_set_cg(self._h, float(tolerance), int(max_iterations)))
+
+    def set_initial_guess(self, rule: int):
+        """Start of the solves: 0 the state x_n, 1 the extrapolated 2 x_n - x_(n-1)
+        (variant 14; fea_batch_set_initial_guess)."""
+        check(load().fea_batch_set_initial_guess(self._h, int(rule)))
 
     def time_iteration(self, reps: int = 10) -> float:
         """ms per CG iteration launch over every instance (fea_batch_time_iteration)."""

@@ -404,6 +404,14 @@ int fea_batch_time_iteration(fea_batch* b, int reps, double* ms_per_launch);
  * fea_batch_create picks the fastest by timing one iteration of each;
  * *variant receives the current one when `set` is 0. */
 int fea_batch_cg_variant(fea_batch* b, int set, int* variant);
+/* No reference counterpart.  Start of every instance's solves: rule 0 its
+ * state x_n (the default); rule 1 the extrapolated state 2 x_n - x_(n-1)
+ * once the instance has stepped since its fields were last set (the
+ * single-mesh cg_initial_guess 1).  Rule 1 takes effect with CG variant 14;
+ * the other variants start from x_n.  Setting a rule, a new variant or an
+ * instance's fields clears the histories it concerns.  Rule 1 allocates two
+ * more state-sized vectors on first use. */
+int fea_batch_set_initial_guess(fea_batch* b, int rule);
 
 /* ---- solve without device allocation ---------------------------------------
  * No counterpart in the reference.  Solves A x = b with Jacobi-preconditioned

@@ -174,6 +174,8 @@ def test_batch_arguments(fea):
         B.advance_time(-1)
     with pytest.raises(fea.FeaError):
         B.set_cg_variant(2)
+    with pytest.raises(fea.FeaError):
+        B.set_initial_guess(2)
 
 
 @pytest.mark.parametrize("variant", [0, 14])
@@ -217,3 +219,113 @@ def test_batch_timing_probe_leaves_state(fea, variant):
         B.close()
     for (ua, va), (ub, vb) in zip(*out):
         assert np.array_equal(ua, ub) and np.array_equal(va, vb)
+
+
+def _extrapolating_batch(fea, insts, seed, tol=1e-6):
+    B = fea.BatchSolver(insts, cg_tolerance=tol)
+    B.set_cg_variant(14)
+    B.set_initial_guess(1)
+    for i, d in enumerate(insts):
+        B.set_fields(i, *_start(d, seed + i))
+    return B
+
+
+def test_extrapolated_start_matches_single_mesh_handles(fea):
+    """Rule 1 (solves started from 2 x_n - x_(n-1)) against single-mesh
+    handles with cg_initial_guess 1: the same states to 1e-5 over ten steps
+    and iteration counts within 2.  Against the rule-0 batch, whose solves
+    start elsewhere and so stop at other points within the tolerance (1e-6
+    per solve), the states agree to 5e-5 and rule 1 takes fewer iterations."""
+    insts = _instances()
+    B = _extrapolating_batch(fea, insts, 300)
+    B0 = fea.BatchSolver(insts, cg_tolerance=1e-6)
+    B0.set_cg_variant(14)
+    singles = []
+    for i, d in enumerate(insts):
+        u0, v0 = _start(d, 300 + i)
+        B0.set_fields(i, u0, v0)
+        p = fea.default_params(equation=fea.REACTION_DIFFUSION, reaction_mode=1, rd_time_step=d["time_step"],
+                               rd_Du=d["Du"], rd_Dv=d["Dv"], rd_feed_rate=d["feed_rate"],
+                               rd_kill_rate=d["kill_rate"], cg_tolerance=1e-6, cg_initial_guess=1)
+        s = fea.CUDASolver(d["vertices"], d["triangles"], boundary_condition=d["boundary_condition"], params=p)
+        s.set_fields(u0, v0)
+        singles.append(s)
+    B.advance_time(10)
+    B0.advance_time(10)
+    for s in singles:
+        s.advance_time(10)
+    _, iters = B.status()
+    for i, s in enumerate(singles):
+        ub, vb = B.get_fields(i)
+        us, vs = s.get_fields()
+        assert rel_l2(ub, us) < 1e-5 and rel_l2(vb, vs) < 1e-5, i
+        u0b, v0b = B0.get_fields(i)
+        assert rel_l2(ub, u0b) < 5e-5 and rel_l2(vb, v0b) < 5e-5, i
+        st = s.status()
+        assert abs(int(iters[i, 0]) - st.last_iterations[0]) <= 2, (i, iters[i], st.last_iterations)
+        assert abs(int(iters[i, 1]) - st.last_iterations[1]) <= 2, (i, iters[i], st.last_iterations)
+    it1, steps1 = B.counters()
+    it0, steps0 = B0.counters()
+    assert np.all(steps1 == 10) and np.all(steps0 == 10)
+    assert it1.sum() < it0.sum(), (it1, it0)
+
+
+def test_extrapolated_start_matches_oracle(fea, oracle_mod):
+    """Rule 1 over three steps against the FP64 oracle (solved to 1e-14):
+    the start only changes where CG begins, not what it converges to."""
+    insts = _instances()
+    B = _extrapolating_batch(fea, insts, 320, tol=1e-7)
+    B.advance_time(3)
+    for i, d in enumerate(insts):
+        S = oracle_mod.System(d["vertices"], d["triangles"], bc=d["boundary_condition"])
+        u0, v0 = _start(d, 320 + i)
+        uo, vo, *_ = oracle_step(oracle_mod, S, oracle_mod.REACTION_DIFFUSION, d["time_step"],
+                                 S.gather(u0.astype(np.float32)), S.gather(v0.astype(np.float32)), 3, **_okw(d))
+        ug, vg = B.get_fields(i)
+        assert rel_l2(ug, S.scatter(uo)) < 1e-5 and rel_l2(vg, S.scatter(vo)) < 1e-5, i
+
+
+def test_extrapolated_start_histories(fea):
+    """Histories are per instance: new fields for one instance restart its
+    history (its next step starts from x_n, bit-identical to a fresh batch),
+    and an instance stepped alone matches the full batch bit for bit."""
+    insts = _instances()
+    B = _extrapolating_batch(fea, insts, 340)
+    B.advance_time(3)
+    u5, v5 = _start(insts[2], 999)
+    B.set_fields(2, u5, v5)
+    B.advance_time(2)
+    one = fea.BatchSolver([insts[2]], cg_tolerance=1e-6)
+    one.set_cg_variant(14)
+    one.set_initial_guess(1)
+    one.set_fields(0, u5, v5)
+    one.advance_time(2)
+    for a, b in zip(B.get_fields(2), one.get_fields(0)):
+        np.testing.assert_array_equal(a, b)
+    one.close()
+    for i in (0, 4):
+        one = _extrapolating_batch(fea, [insts[i]], 340 + i)
+        one.advance_time(5)
+        for a, b in zip(B.get_fields(i), one.get_fields(0)):
+            np.testing.assert_array_equal(a, b)
+        one.close()
+
+
+def test_extrapolated_start_rule_switch(fea):
+    """Switching rule 1 off returns to the x_n start: a batch stepped with
+    rule 1, switched to rule 0, steps bit-identically to a rule-0 batch
+    given the same state."""
+    insts = _instances()[:3]
+    B = _extrapolating_batch(fea, insts, 360)
+    B.advance_time(3)
+    states = [B.get_fields(i) for i in range(len(insts))]
+    B.set_initial_guess(0)
+    B.advance_time(2)
+    R = fea.BatchSolver(insts, cg_tolerance=1e-6)
+    R.set_cg_variant(14)
+    for i, (u, v) in enumerate(states):
+        R.set_fields(i, u, v)
+    R.advance_time(2)
+    for i in range(len(insts)):
+        for a, b in zip(B.get_fields(i), R.get_fields(i)):
+            np.testing.assert_array_equal(a, b)
