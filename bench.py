@@ -577,6 +577,56 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_probe(kind, cg_variant=None):
+    """Small fixed runs for profiler captures (no JSON line).
+
+    batch-iteration: the 256-instance batch is created (its autotuner times one
+      iteration of each variant), started, stepped twice, and
+      fea_batch_time_iteration runs 5 launches;
+    batch-step: the batch with the extrapolated start, 6 steps, then one step
+      inside the NVTX range "capture";
+    step: the 1024 x 1024 handle, 25 steps, then one step inside "capture"."""
+    import torch
+    import fea_gb300 as F
+    if kind == "step":
+        xyz, tri, u0, v0 = workload()
+        p = F.default_params(equation=F.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=CG_TOL,
+                             cg_initial_guess=CG_GUESS, **PARAMS)
+        s = F.CUDASolver(xyz, tri, boundary_condition=F.NEUMANN, precision=F.FP32, params=p)
+        if cg_variant is not None:
+            s.set_cg_variant(cg_variant)
+        s.set_fields(u0, v0)
+        s.advance_time(25)
+        s.synchronize()
+        torch.cuda.nvtx.range_push("capture")
+        s.advance_time(1)
+        s.synchronize()
+        torch.cuda.nvtx.range_pop()
+        st = s.status()
+        print("iterations per field", list(st.last_iterations), "flags", st.flags)
+        return
+    insts, starts = batch_workload()
+    B = F.BatchSolver(insts, cg_tolerance=BATCH_CG_TOL)
+    if cg_variant is not None:
+        B.set_cg_variant(cg_variant)
+    if kind == "batch-step":
+        B.set_initial_guess(CG_GUESS)
+    for i, (u, w) in enumerate(starts):
+        B.set_fields(i, u, w)
+    if kind == "batch-iteration":
+        B.advance_time(2)
+        print("variant", B.cg_variant, "ms per iteration launch", B.time_iteration(5))
+        return
+    B.advance_time(6)
+    B.synchronize()
+    torch.cuda.nvtx.range_push("capture")
+    B.advance_time(1)
+    B.synchronize()
+    torch.cuda.nvtx.range_pop()
+    _, it = B.status()
+    print("variant", B.cg_variant, "iterations of the last solve: max", int(it.max()), "mean", float(it.mean()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -596,7 +646,11 @@ def main():
                     help="cg_initial_guess: 0 previous solution, 1 extrapolated from the last two steps")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="vertices per side (other sizes are for profiling captures, not bench lines)")
+    ap.add_argument("--probe", choices=["step", "batch-step", "batch-iteration"], default=None,
+                    help="a small fixed run for profiler captures instead of the bench (no JSON line)")
     args = ap.parse_args()
+    if args.probe:
+        return run_probe(args.probe, args.cg_variant)
     args.warmup = max(args.warmup, 3)
     globals()["GRID_N"] = args.grid
 
