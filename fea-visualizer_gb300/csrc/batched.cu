@@ -531,15 +531,17 @@ __global__ void __launch_bounds__(kBlock) kb_iter_ell(BArgs<R> a) {
 // becomes x, the start of its solves; its history is then valid.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) kb_guess_move(BArgs<R> a) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.N; r += stride) {
-        const int i = a.tile_inst[r / kTile];
-        if (((const volatile BInst*)(a.inst + i))->stop) continue;
-        a.xprev[r] = a.x[r];
-        a.x[r] = a.xg[r];
+    // one tile per block pass, one row per thread; an instance's stop flag is
+    // fixed while this kernel runs (no other kernel runs beside it)
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        if (a.inst[a.tile_inst[tile]].stop) continue;
+        const int64_t r = (int64_t)tile * kTile + threadIdx.x;
+        const FV<R, 2> xn = a.x[r], x0 = a.xg[r];
+        a.xprev[r] = xn;
+        a.x[r] = x0;
     }
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.ninst; i += stride)
-        if (!((const volatile BInst*)(a.inst + i))->stop) a.inst[i].prev_valid = 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.ninst; i += gridDim.x * blockDim.x)
+        if (!a.inst[i].stop) a.inst[i].prev_valid = 1;
 }
 
 // Histories of the extrapolated start cleared (instance `only`, or all when
@@ -1626,6 +1628,9 @@ BArgs<R> make_bargs(fea_batch* B) {
     return a;
 }
 
+// Blocks of kb_guess_move: one per tile, up to 16 passes' worth per SM.
+int move_grid(const fea_batch* B) { return std::max(1, std::min(B->ntiles, 16 * num_sms())); }
+
 // Graph identity: the variant and whether the extrapolated start is on.
 int graph_key(const fea_batch* B) { return B->wch + (B->guess_rule == 1 && B->wch == 14 ? 1000 : 0); }
 
@@ -1786,7 +1791,7 @@ void build_batch_graph_t(fea_batch* B) {
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
     cudaGraphNode_t s = add_kernel(step_body, nullptr, g.rhs_k, g.rhs, kBlock, L.a1, g.smem_rhs);
-    if (L.a1.xg) s = add_kernel(step_body, s, kb_guess_move<R>, g.stream, kBlock, L.a1);
+    if (L.a1.xg) s = add_kernel(step_body, s, kb_guess_move<R>, move_grid(B), kBlock, L.a1);
     s = add_kernel(step_body, s, K::init, g.init, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
@@ -1822,7 +1827,7 @@ void run_batch_stream_t(fea_batch* B) {
         g.rhs_k<<<g.rhs, kBlock, g.smem_rhs, st>>>(L.a1);
         FEA_CHECK_LAUNCH();
         if (L.a1.xg) {
-            kb_guess_move<R><<<g.stream, kBlock, 0, st>>>(L.a1);
+            kb_guess_move<R><<<move_grid(B), kBlock, 0, st>>>(L.a1);
             FEA_CHECK_LAUNCH();
         }
         for (int loop = 0; loop < 2; loop++) {

@@ -727,12 +727,28 @@ void check_handle(const fea_solver* s) {
     FEA_CUDA_TRY(cudaSetDevice(s->device));
 }
 
-// Host fields travel through the handle's node-sized staging buffer; the
-// copy is a DMA transfer when the caller's buffer is page-locked.
+// The device alias of a page-locked host buffer, or nullptr for pageable
+// memory.  Page-locked host memory is mapped into the device's address space
+// (unified addressing), so the node gather and scatter kernels read and write
+// it directly over the host link, in one pass and without the staging copy.
+const void* mapped_alias(const void* host) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        (void)cudaGetLastError();  // an unknown pointer is pageable memory
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Host fields travel through the handle's node-sized staging buffer, or are
+// read and written in place when the caller's buffer is page-locked.
 template <typename R>
 void set_node_field(fea_solver* s, const float* host, int which /*0 u, 1 v*/) {
-    float* d = s->d_nodes;
-    FEA_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(float) * s->V, cudaMemcpyHostToDevice, s->stream));
+    const float* d = static_cast<const float*>(mapped_alias(host));
+    if (!d) {
+        FEA_CUDA_TRY(cudaMemcpyAsync(s->d_nodes, host, sizeof(float) * s->V, cudaMemcpyHostToDevice, s->stream));
+        d = s->d_nodes;
+    }
     Fields& F = s->F;
     int* pv = s->d_run ? &s->d_run->prev_valid : nullptr;
     if (F.interleaved)
@@ -746,7 +762,8 @@ void set_node_field(fea_solver* s, const float* host, int which /*0 u, 1 v*/) {
 
 template <typename R>
 void get_node_field(fea_solver* s, float* host, int which) {
-    float* d = s->d_nodes;
+    float* mapped = static_cast<float*>(const_cast<void*>(mapped_alias(host)));
+    float* d = mapped ? mapped : s->d_nodes;
     Fields& F = s->F;
     if (F.interleaved)
         k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)F.uv, s->idx_c, s->V, d, 2, which);
@@ -754,7 +771,8 @@ void get_node_field(fea_solver* s, float* host, int which) {
         k_scatter_nodes<R><<<launch_grid(s->V), kBlock, 0, s->stream>>>((R*)(which ? F.v : F.u), s->idx_c, s->V, d,
                                                                          1, 0);
     FEA_CHECK_LAUNCH();
-    FEA_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(float) * s->V, cudaMemcpyDeviceToHost, s->stream));
+    if (!mapped)
+        FEA_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(float) * s->V, cudaMemcpyDeviceToHost, s->stream));
     FEA_CUDA_TRY(cudaStreamSynchronize(s->stream));
 }
 

@@ -502,3 +502,46 @@ def test_boundary_condition_switch(fea, oracle_mod):
     assert s.info.num_unknowns == S.N
     rp, col, _, _ = s.matrix(fea.MASS)
     np.testing.assert_array_equal(col, S.col)
+
+
+def test_page_locked_host_buffers(fea):
+    """Page-locked host buffers are read and written in place by the node
+    gather and scatter kernels (no staging copy).  Through set_values /
+    get_values and set_fields / get_fields they give the same bits as
+    pageable arrays, and a frame loop that writes the displayed field back
+    from a page-locked buffer keeps the extrapolation's history."""
+    import ctypes as C
+    import torch
+    xyz, tri = mg.jittered_grid(65, seed=6)
+    u0, v0 = mg.gray_scott_patches(xyz, seed=5, side=0.15)
+    kw = dict(rd_time_step=1.0, rd_Du=2e-5, rd_Dv=1e-5, rd_feed_rate=0.037, rd_kill_rate=0.06)
+    lib = fea.load()
+    V = xyz.shape[0]
+    pinned = [torch.empty(V, dtype=torch.float32).pin_memory() for _ in range(2)]
+    hu, hv = (t.numpy() for t in pinned)
+    ptr = [C.c_void_p(a.ctypes.data) for a in (hu, hv)]
+
+    def handle():
+        s = _solver(fea, xyz, tri, 1, equation=fea.REACTION_DIFFUSION, reaction_mode=1, cg_tolerance=1e-5,
+                    cg_initial_guess=1, **kw)
+        return s
+
+    a = handle()
+    a.set_fields(u0, v0)
+    b = handle()
+    hu[:], hv[:] = u0, v0
+    fea.binding.check(lib.fea_set_fields(b._h, ptr[0], ptr[1]))
+    for f in (0, 1):
+        assert np.array_equal(_device_field(a, f), _device_field(b, f))
+    for _ in range(5):
+        a.set_values(a.get_values())
+        a.advance_time(1)
+        fea.binding.check(lib.fea_get_values(b._h, ptr[1]))
+        fea.binding.check(lib.fea_set_values(b._h, ptr[1]))
+        fea.binding.check(lib.fea_advance_time(b._h, 1))
+    assert a.status().total_iterations == b.status().total_iterations
+    fea.binding.check(lib.fea_get_fields(b._h, ptr[0], ptr[1]))
+    ua, va = a.get_fields()
+    assert np.array_equal(ua, hu) and np.array_equal(va, hv)
+    fea.binding.check(lib.fea_get_values(b._h, ptr[0]))
+    assert np.array_equal(a.get_values(), hu)
