@@ -1296,6 +1296,187 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
     store_block_partials<R, NV>(a, q, acc, reinterpret_cast<P*>(ring));
 }
 
+// Set-up of a solve for variants 14 and 15: w0 = A z, delta0 = z.w0 and
+// alpha0 = r0.z / delta0, bit for bit as k_cgcg_init_ell computes them (the
+// full tile-ELL layout, each row's entries summed in CSR order from 0).  The
+// operator is streamed through a ring of bulk-copy stages as in the
+// iteration; z of each tile's rows and halo is loaded directly one tile
+// ahead and staged once.  (Starting from the residual on the diagonal-free
+// layout, as the iteration does, changes w0's rounding and cost about two
+// CG iterations per step on the 1M-vertex workload.)
+template <typename R, int NF, int S>
+__global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a) {
+    using V = FV<R, NF>;
+    static_assert(S >= 2 && S <= 8, "ring depth");
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
+    __shared__ typename Acc<R>::Packed red[32 * NF];
+    __shared__ __align__(8) uint64_t bars[S];
+    if (a.guess_init && a.xg) move_guess(a);
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
+        if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+        return;
+    }
+    const V* const Aop = a.As;
+    const uint16_t* const lop = a.lcol;
+    const int32_t* const soff = a.slice_off;
+    const RingStage L(a.emax, sizeof(V));
+    unsigned char* const ring = dyn_smem;
+    V* const ubuf = reinterpret_cast<V*>(dyn_smem + ring_bytes<R, NF>(a.emax, S));
+    const int ustride = kTileRows + a.hmax;
+    const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
+    const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
+    const V* const z = a.z;
+    V* const w = a.wb[a.defer ? 0 : c.par];
+    auto halo_head = [&](int tile, int32_t& h0, int32_t& cnt) {
+        h0 = cnt = 0;
+        if (tile < ntiles) {
+            h0 = a.halo_off[tile];
+            cnt = a.halo_off[tile + 1] - h0;
+        }
+    };
+    auto slice_ref = [&](int tile, int32_t& sb, int32_t& sw) {
+        sb = sw = 0;
+        if (tile < ntiles) {
+            const int sl = tile * (kTileRows / 32) + wib;
+            const int32_t s0 = soff[sl];
+            sb = s0 - soff[tile * (kTileRows / 32)];
+            sw = (soff[sl + 1] - s0) >> 5;
+        }
+    };
+    auto tile_range = [&](int tile, int32_t& e0, int32_t& e1) {
+        e0 = e1 = 0;
+        if (tile < ntiles) {
+            e0 = soff[tile * (kTileRows / 32)];
+            e1 = soff[(tile + 1) * (kTileRows / 32)];
+        }
+    };
+    auto stage_of = [&](int b) { return ring + (size_t)b * L.bytes; };
+    auto issue = [&](int b, int32_t e0, int32_t e1) {  // thread 0
+        uint64_t* bar = &bars[b];
+        const uint32_t n = (uint32_t)(e1 - e0);  // a multiple of 32 entries
+        if (n == 0) {
+            mbar_arrive(bar);
+            return;
+        }
+        mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
+        const uint64_t pol = l2_evict_first_policy();
+        bulk_g2s_hint(stage_of(b) + L.A, Aop + e0, n * (uint32_t)sizeof(V), bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.L, lop + e0, 2 * n, bar, pol);
+    };
+    uint32_t armed = 0;        // thread 0: bit b set while stage b has copies in flight
+    int32_t re0 = 0, re1 = 0;  // thread 0: entry range of the next refill
+    if (t == 0) {
+        for (int b = 0; b < S; b++) mbar_init(&bars[b], 1);
+        mbar_fence_init();
+        for (int b = 0; b < S; b++) {
+            if (t0 + b * G < ntiles) {
+                int32_t e0, e1;
+                tile_range(t0 + b * G, e0, e1);
+                issue(b, e0, e1);
+                armed |= 1u << b;
+            }
+        }
+        tile_range(t0 + S * G, re0, re1);
+    }
+    __syncthreads();  // the barriers are initialised before any thread waits on them
+    int32_t sb, sw, sbn, swn;
+    slice_ref(t0, sb, sw);
+    slice_ref(t0 + G, sbn, swn);
+    int32_t h0c, hcc, h0n, hcn, hh0, hhc;
+    halo_head(t0, h0c, hcc);
+    halo_head(t0 + G, h0n, hcn);
+    halo_head(t0 + 2 * G, hh0, hhc);
+    int32_t hcol = j < hcc ? a.halo_col[h0c + j] : -1;
+    int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
+    const uint64_t pol_keep = l2_evict_last_policy();
+    V cz, hz;
+    if (t0 < ntiles) cz = ld_keep(z + t0 * kTileRows + t, pol_keep);  // every vector holds whole tiles
+    if (hcol >= 0) hz = ld_keep(z + hcol, pol_keep);
+    Acc<R> dot[NF];
+    uint32_t phases = 0u;  // bit b: parity of stage b's next phase
+    bool bad = false;      // a stage wait expired
+    int buf = 0, b = 0, k = 0;
+    for (int tile = t0; tile < ntiles; tile += G, k++) {
+        V* ut = ubuf + buf * ustride;
+        const int row = tile * kTileRows + t;
+        const V zr = cz;
+        V wn;
+#pragma unroll
+        for (int f = 0; f < NF; f++) wn.v[f] = 0;
+        ut[t] = zr;
+        if (j < hcc) ut[kTileRows + j] = hz;
+        const int nt = tile + G;
+        if (nt < ntiles) cz = ld_keep(z + nt * kTileRows + t, pol_keep);
+        if (hcoln >= 0) hz = ld_keep(z + hcoln, pol_keep);
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock) ut[kTileRows + h] = z[a.halo_col[h0c + h]];
+        __syncthreads();
+        if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
+            const int bp = b == 0 ? S - 1 : b - 1;
+            const int target = tile + (S - 1) * G;
+            if (target < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(bp, re0, re1);
+                armed |= 1u << bp;
+            }
+            tile_range(target + G, re0, re1);
+        }
+        h0c = h0n;
+        hcc = hcn;
+        hcoln = j < hhc ? a.halo_col[hh0 + j] : -1;
+        h0n = hh0;
+        hcn = hhc;
+        halo_head(tile + 3 * G, hh0, hhc);
+        int32_t sb2, sw2;
+        slice_ref(tile + 2 * G, sb2, sw2);
+        const bool got = mbar_wait(&bars[b], (phases >> b) & 1u);
+        phases ^= 1u << b;
+        bad |= !got;
+        if (t == 0 && got) armed &= ~(1u << b);
+        const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
+        const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+#pragma unroll 4
+        for (int kk = 0; kk < sw; kk++) {
+            const V av = As[32 * kk];
+            const V g = ut[Ls[32 * kk]];
+#pragma unroll
+            for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
+        }
+        if (row < a.N) {
+            w[row] = wn;
+#pragma unroll
+            for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wn.v[f]);
+        }
+        sb = sbn;
+        sw = swn;
+        sbn = sb2;
+        swn = sw2;
+        buf ^= 1;
+        b = b + 1 == S ? 0 : b + 1;
+    }
+    if (__syncthreads_or(bad)) {
+        if (t == 0) {
+            atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+            for (int q2 = 0; q2 < S; q2++)  // copies still in flight land before the block leaves
+                if (armed & (1u << q2)) mbar_wait(&bars[q2], (phases >> q2) & 1u);
+        }
+    }
+    Acc<R> blk[NF], tot[NF];
+    block_totals<NF>(dot, red, blk);
+    if (grid_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
+        volatile CgState* cg = a.cg;
+        finish_spmv<R, NF>(cg, &a.run->flags, c.act, tot);
+        int any = 0;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            cg->fresh[f] = 1;
+            any |= cg->active[f];
+        }
+        signal_loop(a, any != 0);
+    }
+}
+
 // Fused right-hand side + initial residual r = b - A x0 (warm start x0 = the
 // previous solution), z = D^-1 r, p = z, and the CG set-up scalars.  Also the
 // has_numerical_instability test of the state entering the step.
@@ -1793,13 +1974,15 @@ struct DirectKernels : EllKernels<R, NF, 4> {
 // Variants 14 and 15: direct row loads with the operator in a ring of 3 or 4
 // bulk-copy stages.
 template <typename R, int NF, int S, int MINB>
-struct RingKernels : EllKernels<R, NF, 4> {
+struct RingKernels {
     using Fn = void (*)(StepArgs<R, NF>);
+    static constexpr Fn init = k_cgcg_init_ring<R, NF, S>;
     static constexpr Fn iter = k_cgcg_iter_ring<R, NF, S, 0, MINB>;
     static Fn iter_par(int par) { return par ? k_cgcg_iter_ring<R, NF, S, 1, MINB> : iter; }
     static size_t smem_iter(const StepArgs<R, NF>& a) {
         return ring_smem_bytes<R, NF>(a.As_od ? a.emax_od : a.emax, a.hmax, S);
     }
+    static size_t smem_init(const StepArgs<R, NF>& a) { return ring_smem_bytes<R, NF>(a.emax, a.hmax, S); }
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};

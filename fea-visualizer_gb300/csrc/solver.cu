@@ -225,7 +225,9 @@ size_t rsize(const fea_solver* s) { return s->precision == FEA_FP64 ? 8 : 4; }
 
 // Entries of the largest tile the ring kernels stream (the diagonal-free
 // layout when it was built).
-int ring_emax(const fea_solver* s) { return s->ell_od.ok ? s->ell_od.emax : s->ell.emax; }
+// The widest tile of the ring kernels' layouts: the set-up product streams
+// the full layout, the iteration the one without the diagonal.
+int ring_emax(const fea_solver* s) { return s->ell.emax; }
 
 int64_t pad_tiles(int64_t n) { return ceil_div(n, kTileRows) * kTileRows; }
 
