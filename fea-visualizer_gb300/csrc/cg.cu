@@ -1296,39 +1296,26 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
     store_block_partials<R, NV>(a, q, acc, reinterpret_cast<P*>(ring));
 }
 
-// Set-up of a solve for variants 14 and 15: w0 = A z, delta0 = z.w0 and
-// alpha0 = r0.z / delta0, bit for bit as k_cgcg_init_ell computes them (the
-// full tile-ELL layout, each row's entries summed in CSR order from 0).  The
-// operator is streamed through a ring of bulk-copy stages as in the
-// iteration; z of each tile's rows and halo is loaded directly one tile
-// ahead and staged once.  (Starting from the residual on the diagonal-free
-// layout, as the iteration does, changes w0's rounding and cost about two
-// CG iterations per step on the 1M-vertex workload.)
-template <typename R, int NF, int S>
-__global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a) {
+// The tile loop of the ring set-up and refinement kernels (variants 14 and
+// 15): the full tile-ELL layout streamed through S bulk-copy stages, the
+// block's tiles strided by the grid.  Per tile, thread t stages vec of its
+// row and of its halo slot, loaded directly one tile ahead, once; after the
+// block barrier each thread sums its row's entries against the staged values
+// in CSR order (Sum::add from a value-initialised Sum; padding entries hold
+// 0) and row_done(row, own value, extra, sum) finishes the row, with `extra`
+// fetched by load_extra(row) one tile ahead.  Returns false when a stage
+// wait expired; the copies in flight have landed by then.  smem holds the
+// ring (ring_bytes) and two staging buffers of kTileRows + hmax values.
+template <typename R, int NF, int S, typename Sum, typename LoadExtra, typename RowDone>
+__device__ bool ring_product_tiles(const StepArgs<R, NF>& a, const FV<R, NF>* __restrict__ vec, unsigned char* smem,
+                                   uint64_t* bars, LoadExtra load_extra, RowDone row_done) {
     using V = FV<R, NF>;
     static_assert(S >= 2 && S <= 8, "ring depth");
-    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
-    __shared__ typename Acc<R>::Packed red[32 * NF];
-    __shared__ __align__(8) uint64_t bars[S];
-    if (a.guess_init && a.xg) move_guess(a);
-    PhaseCtl<R, NF> c;
-    c.load(a.cg);
-    if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
-        if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
-        return;
-    }
-    const V* const Aop = a.As;
-    const uint16_t* const lop = a.lcol;
-    const int32_t* const soff = a.slice_off;
     const RingStage L(a.emax, sizeof(V));
-    unsigned char* const ring = dyn_smem;
-    V* const ubuf = reinterpret_cast<V*>(dyn_smem + ring_bytes<R, NF>(a.emax, S));
+    V* const ubuf = reinterpret_cast<V*>(smem + ring_bytes<R, NF>(a.emax, S));
     const int ustride = kTileRows + a.hmax;
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
-    const V* const z = a.z;
-    V* const w = a.wb[a.defer ? 0 : c.par];
     auto halo_head = [&](int tile, int32_t& h0, int32_t& cnt) {
         h0 = cnt = 0;
         if (tile < ntiles) {
@@ -1340,19 +1327,19 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
         sb = sw = 0;
         if (tile < ntiles) {
             const int sl = tile * (kTileRows / 32) + wib;
-            const int32_t s0 = soff[sl];
-            sb = s0 - soff[tile * (kTileRows / 32)];
-            sw = (soff[sl + 1] - s0) >> 5;
+            const int32_t s0 = a.slice_off[sl];
+            sb = s0 - a.slice_off[tile * (kTileRows / 32)];
+            sw = (a.slice_off[sl + 1] - s0) >> 5;
         }
     };
     auto tile_range = [&](int tile, int32_t& e0, int32_t& e1) {
         e0 = e1 = 0;
         if (tile < ntiles) {
-            e0 = soff[tile * (kTileRows / 32)];
-            e1 = soff[(tile + 1) * (kTileRows / 32)];
+            e0 = a.slice_off[tile * (kTileRows / 32)];
+            e1 = a.slice_off[(tile + 1) * (kTileRows / 32)];
         }
     };
-    auto stage_of = [&](int b) { return ring + (size_t)b * L.bytes; };
+    auto stage_of = [&](int b) { return smem + (size_t)b * L.bytes; };
     auto issue = [&](int b, int32_t e0, int32_t e1) {  // thread 0
         uint64_t* bar = &bars[b];
         const uint32_t n = (uint32_t)(e1 - e0);  // a multiple of 32 entries
@@ -1362,8 +1349,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
         }
         mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
         const uint64_t pol = l2_evict_first_policy();
-        bulk_g2s_hint(stage_of(b) + L.A, Aop + e0, n * (uint32_t)sizeof(V), bar, pol);
-        bulk_g2s_hint(stage_of(b) + L.L, lop + e0, 2 * n, bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.A, a.As + e0, n * (uint32_t)sizeof(V), bar, pol);
+        bulk_g2s_hint(stage_of(b) + L.L, a.lcol + e0, 2 * n, bar, pol);
     };
     uint32_t armed = 0;        // thread 0: bit b set while stage b has copies in flight
     int32_t re0 = 0, re1 = 0;  // thread 0: entry range of the next refill
@@ -1388,29 +1375,35 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
     halo_head(t0, h0c, hcc);
     halo_head(t0 + G, h0n, hcn);
     halo_head(t0 + 2 * G, hh0, hhc);
-    int32_t hcol = j < hcc ? a.halo_col[h0c + j] : -1;
+    const int32_t hcol = j < hcc ? a.halo_col[h0c + j] : -1;
     int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
     const uint64_t pol_keep = l2_evict_last_policy();
-    V cz, hz;
-    if (t0 < ntiles) cz = ld_keep(z + t0 * kTileRows + t, pol_keep);  // every vector holds whole tiles
-    if (hcol >= 0) hz = ld_keep(z + hcol, pol_keep);
-    Acc<R> dot[NF];
+    V cv{}, hv{};
+    decltype(load_extra(0)) ce{};
+    if (t0 < ntiles) {
+        const int row = t0 * kTileRows + t;  // every vector holds whole tiles
+        cv = ld_keep(vec + row, pol_keep);
+        ce = load_extra(row);
+    }
+    if (hcol >= 0) hv = ld_keep(vec + hcol, pol_keep);
     uint32_t phases = 0u;  // bit b: parity of stage b's next phase
     bool bad = false;      // a stage wait expired
     int buf = 0, b = 0, k = 0;
     for (int tile = t0; tile < ntiles; tile += G, k++) {
         V* ut = ubuf + buf * ustride;
         const int row = tile * kTileRows + t;
-        const V zr = cz;
-        V wn;
-#pragma unroll
-        for (int f = 0; f < NF; f++) wn.v[f] = 0;
-        ut[t] = zr;
-        if (j < hcc) ut[kTileRows + j] = hz;
+        const V vr = cv;
+        const auto er = ce;
+        ut[t] = vr;
+        if (j < hcc) ut[kTileRows + j] = hv;
         const int nt = tile + G;
-        if (nt < ntiles) cz = ld_keep(z + nt * kTileRows + t, pol_keep);
-        if (hcoln >= 0) hz = ld_keep(z + hcoln, pol_keep);
-        for (int32_t h = kBlock + t; h < hcc; h += kBlock) ut[kTileRows + h] = z[a.halo_col[h0c + h]];
+        if (nt < ntiles) {
+            const int nrow = nt * kTileRows + t;
+            cv = ld_keep(vec + nrow, pol_keep);
+            ce = load_extra(nrow);
+        }
+        if (hcoln >= 0) hv = ld_keep(vec + hcoln, pol_keep);
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock) ut[kTileRows + h] = vec[a.halo_col[h0c + h]];
         __syncthreads();
         if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
             const int bp = b == 0 ? S - 1 : b - 1;
@@ -1436,18 +1429,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
         if (t == 0 && got) armed &= ~(1u << b);
         const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
         const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
+        Sum sum{};
 #pragma unroll 4
-        for (int kk = 0; kk < sw; kk++) {
-            const V av = As[32 * kk];
-            const V g = ut[Ls[32 * kk]];
-#pragma unroll
-            for (int f = 0; f < NF; f++) wn.v[f] = fmar(av.v[f], g.v[f], wn.v[f]);
-        }
-        if (row < a.N) {
-            w[row] = wn;
-#pragma unroll
-            for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], wn.v[f]);
-        }
+        for (int kk = 0; kk < sw; kk++) sum.add(As[32 * kk], ut[Ls[32 * kk]]);
+        if (row < a.N) row_done(row, vr, er, sum);
         sb = sbn;
         sw = swn;
         sbn = sb2;
@@ -1456,12 +1441,56 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
         b = b + 1 == S ? 0 : b + 1;
     }
     if (__syncthreads_or(bad)) {
-        if (t == 0) {
-            atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+        if (t == 0)
             for (int q2 = 0; q2 < S; q2++)  // copies still in flight land before the block leaves
                 if (armed & (1u << q2)) mbar_wait(&bars[q2], (phases >> q2) & 1u);
-        }
+        return false;
     }
+    return true;
+}
+
+// Row sums of the ring set-up product: R with fused multiply-adds, as the
+// tile-ELL product (EllRow::finish) sums them.
+template <typename R, int NF>
+struct FmaRowSum {
+    FV<R, NF> w{};
+    __device__ __forceinline__ void add(const FV<R, NF>& av, const FV<R, NF>& g) {
+#pragma unroll
+        for (int f = 0; f < NF; f++) w.v[f] = fmar(av.v[f], g.v[f], w.v[f]);
+    }
+};
+struct NoExtra {};
+
+// Set-up of a solve for variants 14 and 15: w0 = A z, delta0 = z.w0 and
+// alpha0 = r0.z / delta0, bit for bit as k_cgcg_init_ell computes them (the
+// full tile-ELL layout, each row's entries summed in CSR order from 0), with
+// the operator streamed through a ring of bulk-copy stages as in the
+// iteration (ring_product_tiles).  (Starting from the residual on the
+// diagonal-free layout, as the iteration does, changes w0's rounding and
+// cost about two CG iterations per step on the 1M-vertex workload.)
+template <typename R, int NF, int S>
+__global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a) {
+    using V = FV<R, NF>;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
+    __shared__ typename Acc<R>::Packed red[32 * NF];
+    __shared__ __align__(8) uint64_t bars[S];
+    if (a.guess_init && a.xg) move_guess(a);
+    PhaseCtl<R, NF> c;
+    c.load(a.cg);
+    if (!c.any) {  // no field iterates (every solve converged or stopped): no product to set up
+        if (blockIdx.x == 0 && threadIdx.x == 0) signal_loop(a, false);
+        return;
+    }
+    V* const w = a.wb[a.defer ? 0 : c.par];
+    Acc<R> dot[NF];
+    const bool ok = ring_product_tiles<R, NF, S, FmaRowSum<R, NF>>(
+        a, a.z, dyn_smem, bars, [](int) { return NoExtra{}; },
+        [&](int row, const V& zr, const NoExtra&, const FmaRowSum<R, NF>& sum) {
+            w[row] = sum.w;
+#pragma unroll
+            for (int f = 0; f < NF; f++) dot[f].add_prod(zr.v[f], sum.w.v[f]);
+        });
+    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
     Acc<R> blk[NF], tot[NF];
     block_totals<NF>(dot, red, blk);
     if (grid_commit<NF>(blk, a.part, a.part_stride, a.tickets + 0, red, tot) && threadIdx.x == 0) {
@@ -1783,8 +1812,78 @@ __device__ __forceinline__ void refine_rows(const StepArgs<R, NF>& a, bool refin
     }
 }
 
-template <typename R, int NF, int LANES>
+// Row sums of the ring refinement: the handle's accumulators (float-float
+// pairs for FP32 handles, or FP64), in CSR order as refine_rows sums them.
+template <typename A, typename R, int NF>
+struct AccRowSum {
+    A ax[NF];
+    __device__ __forceinline__ void add(const FV<R, NF>& av, const FV<R, NF>& g) {
+#pragma unroll
+        for (int f = 0; f < NF; f++) ax[f].add_prod(av.v[f], g.v[f]);
+    }
+};
+
+// refine_rows on the ring layout of variants 14 and 15: the same sums in the
+// same order (padding entries add exact zeros), so r, z and the norms are
+// bit-identical; x of each tile and its halo is staged once and the operator
+// streamed through bulk-copy stages (ring_product_tiles).
+template <typename A, typename R, int NF, int S>
+__device__ __forceinline__ void refine_rows_ring(const StepArgs<R, NF>& a, bool refine, const int (&zero)[NF],
+                                                 int parity, A (&dots)[2 * NF], unsigned char* smem,
+                                                 uint64_t* bars) {
+    using V = FV<R, NF>;
+    bool zany = false;
+#pragma unroll
+    for (int f = 0; f < NF; f++) zany |= zero[f] != 0;
+    auto zeroed = [&](V x) {
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            if (zero[f]) x.v[f] = 0;
+        return x;
+    };
+    if (!refine) {  // no products: only the zero fields' unknowns are set to 0
+        if (zany)
+            for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < a.N;
+                 row += (int64_t)gridDim.x * blockDim.x)
+                a.x[row] = zeroed(a.x[row]);
+        return;
+    }
+    struct Extra {
+        V b, d;
+    };
+    // x is staged before this kernel zeroes a field: only zero fields change,
+    // and their residuals go unused
+    const bool ok = ring_product_tiles<R, NF, S, AccRowSum<A, R, NF>>(
+        a, a.x, smem, bars,
+        [&](int row) {
+            const uint64_t pol = l2_evict_last_policy();
+            return Extra{ld_keep(a.b + row, pol), ld_keep(a.dinv + row, pol)};
+        },
+        [&](int row, const V& xr, const Extra& e, const AccRowSum<A, R, NF>& sum) {
+            if (zany) a.x[row] = zeroed(xr);
+            V rv, pv;
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                A t;
+                t.add(e.b.v[f]);
+                t.sub(sum.ax[f]);
+                rv.v[f] = (R)t.rounded();
+                pv.v[f] = e.d.v[f] * rv.v[f];
+                dots[f].add_prod(rv.v[f], rv.v[f]);
+                dots[NF + f].add_prod(rv.v[f], pv.v[f]);
+            }
+            a.rb[parity][row] = rv;  // the restart's buffer parity
+            a.z[row] = pv;
+        });
+    if (!ok && threadIdx.x == 0) atomicOr(&a.run->flags, FEA_STATUS_BREAKDOWN);
+}
+
+// The true-residual pass; S > 0: on the ring layout of variants 14 and 15
+// (dynamic shared memory ring_smem_bytes(emax, hmax, S)).
+template <typename R, int NF, int LANES, int S = 0>
 __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ __align__(8) uint64_t bars[S > 0 ? S : 1];
     CgState* cg = a.cg;
     const int stop = cg->stop;
     const int mode = a.run->refine;
@@ -1798,7 +1897,8 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
     bool last;
     if (fp64) {
         Acc<double> dots[2 * NF], tot[2 * NF];
-        refine_rows<Acc<double>, R, NF, LANES>(a, refine, zero, parity, dots);
+        if constexpr (S > 0) refine_rows_ring<Acc<double>, R, NF, S>(a, refine, zero, parity, dots, dyn_smem, bars);
+        else refine_rows<Acc<double>, R, NF, LANES>(a, refine, zero, parity, dots);
         last = grid_reduce<double, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot);
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -1807,7 +1907,8 @@ __global__ void __launch_bounds__(kBlock) k_refine(StepArgs<R, NF> a) {
         }
     } else {
         Acc<R> dots[2 * NF], tot[2 * NF];
-        refine_rows<Acc<R>, R, NF, LANES>(a, refine, zero, parity, dots);
+        if constexpr (S > 0) refine_rows_ring<Acc<R>, R, NF, S>(a, refine, zero, parity, dots, dyn_smem, bars);
+        else refine_rows<Acc<R>, R, NF, LANES>(a, refine, zero, parity, dots);
         last = grid_reduce<R, 2 * NF>(dots, a.part, a.part_stride, a.tickets + 3, tot);
 #pragma unroll
         for (int f = 0; f < NF; f++) {
@@ -1918,6 +2019,7 @@ struct CgKernels {
     static Fn iter_par(int) { return iter; }
     static size_t smem_init(const StepArgs<R, NF>&) { return 0; }
     static size_t smem_iter(const StepArgs<R, NF>&) { return 0; }
+    static constexpr int kRefineStages = 0;  // the true-residual pass on CSR rows
 };
 // Variants 0 and 1: the tile-ELL kernels with 8 or 4 entries per row
 // prefetched into registers; two staging buffers of kTileRows + hmax entries.
@@ -1931,6 +2033,7 @@ struct EllKernels {
         return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
     }
     static size_t smem_iter(const StepArgs<R, NF>& a) { return smem_init(a); }
+    static constexpr int kRefineStages = 0;
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
@@ -1983,6 +2086,7 @@ struct RingKernels {
         return ring_smem_bytes<R, NF>(a.As_od ? a.emax_od : a.emax, a.hmax, S);
     }
     static size_t smem_init(const StepArgs<R, NF>& a) { return ring_smem_bytes<R, NF>(a.emax, a.hmax, S); }
+    static constexpr int kRefineStages = S;  // the true-residual pass on the ring too
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};
@@ -2015,8 +2119,10 @@ struct RhsKernel {
 template <typename R, int NF, int WCH>
 struct Grids {
     using K = CgKernels<R, NF, WCH>;
-    int spmv, iter, rhs, stream;
-    size_t smem_init, smem_iter;
+    using Fn = void (*)(StepArgs<R, NF>);
+    int spmv, iter, rhs, stream, refine;
+    size_t smem_init, smem_iter, smem_refine = 0;
+    Fn refine_k = k_refine<R, NF, kRowLanes, K::kRefineStages>;
     explicit Grids(const StepArgs<R, NF>& a) {
         const int64_t N = a.N;
         smem_init = K::smem_init(a);
@@ -2026,6 +2132,11 @@ struct Grids {
         if (K::iter_par(1) != K::iter) ensure_dyn_smem(K::iter_par(1), smem_iter);  // the other parity's kernel
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
+        refine = rhs;
+        if constexpr (K::kRefineStages > 0) {
+            smem_refine = ring_smem_bytes<R, NF>(a.emax, a.hmax, K::kRefineStages);
+            refine = wave_grid(refine_k, ceil_div(N, kTileRows), smem_refine);
+        }
     }
 };
 
@@ -2085,7 +2196,7 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     cudaGraph_t body1, body2;
     s = add_while(step_body, s, L.a1.cond, &body1);
     add_iterations<K>(body1, g.iter, L.a1, g.smem_iter);
-    s = add_kernel(step_body, s, k_refine<R, NF, kRowLanes>, g.rhs, kBlock, L.a2);
+    s = add_kernel(step_body, s, g.refine_k, g.refine, kBlock, L.a2, g.smem_refine);
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a2, g.smem_init);
     s = add_while(step_body, s, L.a2.cond, &body2);
     add_iterations<K>(body2, g.iter, L.a2, g.smem_iter);
@@ -2119,7 +2230,7 @@ void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
         FEA_CHECK_LAUNCH();
         for (const StepArgs<R, NF>* la : {&L.a1, &L.a2}) {
             if (la == &L.a2) {
-                k_refine<R, NF, kRowLanes><<<g.rhs, kBlock, 0, st>>>(L.a2);
+                g.refine_k<<<g.refine, kBlock, g.smem_refine, st>>>(L.a2);
                 FEA_CHECK_LAUNCH();
             }
             K::init<<<g.spmv, kBlock, g.smem_init, st>>>(*la);
