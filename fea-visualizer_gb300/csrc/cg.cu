@@ -1296,23 +1296,29 @@ __global__ void __launch_bounds__(kBlock, MINB) k_cgcg_iter_ring(StepArgs<R, NF>
     store_block_partials<R, NV>(a, q, acc, reinterpret_cast<P*>(ring));
 }
 
-// The tile loop of the ring set-up and refinement kernels (variants 14 and
-// 15): the full tile-ELL layout streamed through S bulk-copy stages, the
-// block's tiles strided by the grid.  Per tile, thread t stages vec of its
-// row and of its halo slot, loaded directly one tile ahead, once; after the
-// block barrier each thread sums its row's entries against the staged values
-// in CSR order (Sum::add from a value-initialised Sum; padding entries hold
-// 0) and row_done(row, own value, extra, sum) finishes the row, with `extra`
-// fetched by load_extra(row) one tile ahead.  Returns false when a stage
-// wait expired; the copies in flight have landed by then.  smem holds the
-// ring (ring_bytes) and two staging buffers of kTileRows + hmax values.
-template <typename R, int NF, int S, typename Sum, typename LoadExtra, typename RowDone>
-__device__ bool ring_product_tiles(const StepArgs<R, NF>& a, const FV<R, NF>* __restrict__ vec, unsigned char* smem,
-                                   uint64_t* bars, LoadExtra load_extra, RowDone row_done) {
+// The tile loop of the ring kernels that run once per solve or step
+// (variants 14 and 15): the full tile-ELL layout (with kM, also the mass
+// matrix's copy) streamed through S bulk-copy stages, the block's tiles
+// strided by the grid.  Per tile, thread t loads load_raw(index, policy) of
+// its row and of its halo slot one tile ahead and stages make(raw) once;
+// after the block barrier each thread sums its row's entries against the
+// staged values in CSR order (Sum::add from a value-initialised Sum; padding
+// entries hold 0) and row_done(row, raw, extra, sum) finishes the row, with
+// `extra` fetched by load_extra(row, policy) one tile ahead.  Returns false
+// when a stage wait expired; the copies in flight have landed by then.  smem
+// holds the ring (ring_bytes) and two staging buffers of kTileRows + hmax
+// staged values.
+template <typename R, int NF, int S, typename Sum, bool kM, typename LoadRaw, typename Make, typename LoadExtra,
+          typename RowDone>
+__device__ bool ring_product_tiles(const StepArgs<R, NF>& a, unsigned char* smem, uint64_t* bars, LoadRaw load_raw,
+                                   Make make, LoadExtra load_extra, RowDone row_done) {
     using V = FV<R, NF>;
+    using Raw = decltype(load_raw(0, uint64_t{}));
+    using Gv = decltype(make(Raw{}));
     static_assert(S >= 2 && S <= 8, "ring depth");
-    const RingStage L(a.emax, sizeof(V));
-    V* const ubuf = reinterpret_cast<V*>(smem + ring_bytes<R, NF>(a.emax, S));
+    constexpr size_t mv = kM ? sizeof(R) : 0;
+    const RingStage L(a.emax, sizeof(V), mv);
+    Gv* const ubuf = reinterpret_cast<Gv*>(smem + ring_bytes<R, NF>(a.emax, S, mv));
     const int ustride = kTileRows + a.hmax;
     const int t = threadIdx.x, lane = t & 31, wib = t >> 5, j = halo_slot(t);
     const int ntiles = (int)ceil_div(a.N, kTileRows), G = (int)gridDim.x, t0 = (int)blockIdx.x;
@@ -1347,9 +1353,10 @@ __device__ bool ring_product_tiles(const StepArgs<R, NF>& a, const FV<R, NF>* __
             mbar_arrive(bar);
             return;
         }
-        mbar_arrive_expect_tx(bar, n * (uint32_t)sizeof(V) + 2 * n);
+        mbar_arrive_expect_tx(bar, n * (uint32_t)(sizeof(V) + mv + 2));
         const uint64_t pol = l2_evict_first_policy();
         bulk_g2s_hint(stage_of(b) + L.A, a.As + e0, n * (uint32_t)sizeof(V), bar, pol);
+        if constexpr (kM) bulk_g2s_hint(stage_of(b) + L.M, a.Ms + e0, n * (uint32_t)mv, bar, pol);
         bulk_g2s_hint(stage_of(b) + L.L, a.lcol + e0, 2 * n, bar, pol);
     };
     uint32_t armed = 0;        // thread 0: bit b set while stage b has copies in flight
@@ -1378,32 +1385,32 @@ __device__ bool ring_product_tiles(const StepArgs<R, NF>& a, const FV<R, NF>* __
     const int32_t hcol = j < hcc ? a.halo_col[h0c + j] : -1;
     int32_t hcoln = j < hcn ? a.halo_col[h0n + j] : -1;
     const uint64_t pol_keep = l2_evict_last_policy();
-    V cv{}, hv{};
-    decltype(load_extra(0)) ce{};
+    Raw cv{}, hv{};
+    decltype(load_extra(0, uint64_t{})) ce{};
     if (t0 < ntiles) {
         const int row = t0 * kTileRows + t;  // every vector holds whole tiles
-        cv = ld_keep(vec + row, pol_keep);
-        ce = load_extra(row);
+        cv = load_raw(row, pol_keep);
+        ce = load_extra(row, pol_keep);
     }
-    if (hcol >= 0) hv = ld_keep(vec + hcol, pol_keep);
+    if (hcol >= 0) hv = load_raw(hcol, pol_keep);
     uint32_t phases = 0u;  // bit b: parity of stage b's next phase
     bool bad = false;      // a stage wait expired
     int buf = 0, b = 0, k = 0;
     for (int tile = t0; tile < ntiles; tile += G, k++) {
-        V* ut = ubuf + buf * ustride;
+        Gv* ut = ubuf + buf * ustride;
         const int row = tile * kTileRows + t;
-        const V vr = cv;
+        const Raw vr = cv;
         const auto er = ce;
-        ut[t] = vr;
-        if (j < hcc) ut[kTileRows + j] = hv;
+        ut[t] = make(vr);
+        if (j < hcc) ut[kTileRows + j] = make(hv);
         const int nt = tile + G;
         if (nt < ntiles) {
             const int nrow = nt * kTileRows + t;
-            cv = ld_keep(vec + nrow, pol_keep);
-            ce = load_extra(nrow);
+            cv = load_raw(nrow, pol_keep);
+            ce = load_extra(nrow, pol_keep);
         }
-        if (hcoln >= 0) hv = ld_keep(vec + hcoln, pol_keep);
-        for (int32_t h = kBlock + t; h < hcc; h += kBlock) ut[kTileRows + h] = vec[a.halo_col[h0c + h]];
+        if (hcoln >= 0) hv = load_raw(hcoln, pol_keep);
+        for (int32_t h = kBlock + t; h < hcc; h += kBlock) ut[kTileRows + h] = make(load_raw(a.halo_col[h0c + h], pol_keep));
         __syncthreads();
         if (t == 0 && k > 0) {  // refill the previous tile's stage, S - 1 tiles ahead
             const int bp = b == 0 ? S - 1 : b - 1;
@@ -1430,8 +1437,14 @@ __device__ bool ring_product_tiles(const StepArgs<R, NF>& a, const FV<R, NF>* __
         const V* As = reinterpret_cast<const V*>(stage_of(b) + L.A) + sb + lane;
         const uint16_t* Ls = reinterpret_cast<const uint16_t*>(stage_of(b) + L.L) + sb + lane;
         Sum sum{};
+        if constexpr (kM) {
+            const R* Ms = reinterpret_cast<const R*>(stage_of(b) + L.M) + sb + lane;
 #pragma unroll 4
-        for (int kk = 0; kk < sw; kk++) sum.add(As[32 * kk], ut[Ls[32 * kk]]);
+            for (int kk = 0; kk < sw; kk++) sum.add(As[32 * kk], Ms[32 * kk], ut[Ls[32 * kk]]);
+        } else {
+#pragma unroll 4
+            for (int kk = 0; kk < sw; kk++) sum.add(As[32 * kk], ut[Ls[32 * kk]]);
+        }
         if (row < a.N) row_done(row, vr, er, sum);
         sb = sbn;
         sw = swn;
@@ -1483,8 +1496,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cgcg_init_ring(StepArgs<R, NF> a)
     }
     V* const w = a.wb[a.defer ? 0 : c.par];
     Acc<R> dot[NF];
-    const bool ok = ring_product_tiles<R, NF, S, FmaRowSum<R, NF>>(
-        a, a.z, dyn_smem, bars, [](int) { return NoExtra{}; },
+    const bool ok = ring_product_tiles<R, NF, S, FmaRowSum<R, NF>, false>(
+        a, dyn_smem, bars, [&](int i, uint64_t pol) { return ld_keep(a.z + i, pol); }, [](const V& g) { return g; },
+        [](int, uint64_t) { return NoExtra{}; },
         [&](int row, const V& zr, const NoExtra&, const FmaRowSum<R, NF>& sum) {
             w[row] = sum.w;
 #pragma unroll
@@ -1753,6 +1767,115 @@ __global__ void __launch_bounds__(kBlock) k_rhs_gs_ell(StepArgs<R, NF> a) {
     }
 }
 
+// Staged values and row sums of the ring Gray-Scott right-hand side.
+template <typename R, int NF>
+struct GsRaw {
+    FV<R, NF> x, xp;  // the state and, for the extrapolated start, the state one step before
+};
+template <typename R, int NF>
+struct GsStaged {
+    FV<R, NF> w, x0;  // the nodal reaction w(x) and the solve's start
+};
+template <typename R, int NF>
+struct GsRowSum {
+    Acc<R> bs[NF], ax[NF];
+    __device__ __forceinline__ void add(const FV<R, NF>& av, R me, const GsStaged<R, NF>& g) {
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            bs[f].add_prod(me, g.w.v[f]);
+            ax[f].add_prod(av.v[f], g.x0.v[f]);
+        }
+    }
+};
+
+// k_rhs_gs_ell on the ring of variants 14 and 15: the nodal reaction and the
+// solve's start of each tile's rows and halo are staged once, A and the mass
+// matrix's tile-ELL copy stream through the bulk-copy stages
+// (ring_product_tiles), and each row sums the same products in the same
+// order, so b, r0, z and the set-up sums are bit-identical.
+template <typename R, int NF, int S>
+__global__ void __launch_bounds__(kBlock, 2) k_rhs_gs_ring(StepArgs<R, NF> a) {
+    static_assert(NF == 2, "the paired Gray-Scott solve");
+    using V = FV<R, NF>;
+    using Raw = GsRaw<R, NF>;
+    using Gv = GsStaged<R, NF>;
+    extern __shared__ __align__(16) unsigned char dyn_smem[];  // bulk copies need 16-byte destinations
+    __shared__ __align__(8) uint64_t bars[S];
+    const StepParams P = *a.prm;
+    const R dt = (R)P.dt, Fr = (R)P.F, Kr = (R)P.k;
+    const bool extrap = a.xprev != nullptr && a.run->guess == 1 && a.run->prev_valid != 0;
+    auto start = [&](const Raw& r) {
+        V g = r.x;
+        if (extrap)
+#pragma unroll
+            for (int f = 0; f < NF; f++) g.v[f] = fmar((R)2, r.x.v[f], -r.xp.v[f]);
+        return g;
+    };
+    auto react = [&](const V& x) {
+        const R u = x.v[0], v = x.v[1];
+        const R uvv = u * (v * v);
+        V w;
+        w.v[0] = u / dt - uvv + Fr * ((R)1 - u);
+        w.v[1] = v / dt + uvv - (Fr + Kr) * v;
+        return w;
+    };
+    Acc<R> dots[3 * NF];  // |b|^2, |r|^2, r.z per field
+    unsigned int flags = 0;
+    const bool ok = ring_product_tiles<R, NF, S, GsRowSum<R, NF>, true>(
+        a, dyn_smem, bars,
+        [&](int i, uint64_t pol) {
+            Raw r;
+            r.x = ld_keep(a.x + i, pol);
+            r.xp = extrap ? ld_keep(a.xprev + i, pol) : r.x;
+            return r;
+        },
+        [&](const Raw& r) { return Gv{react(r.x), start(r)}; },
+        [&](int row, uint64_t pol) { return ld_keep(a.dinv + row, pol); },
+        [&](int row, const Raw& xr, const V& d, GsRowSum<R, NF> sum) {
+            if (a.xg) a.xg[row] = start(xr);  // the set-up kernel makes it x
+#pragma unroll
+            for (int f = 0; f < NF; f++) flags |= check_value(xr.x.v[f]);
+            V bv, rv, pv;
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                bv.v[f] = sum.bs[f].rounded();
+                sum.bs[f].sub(sum.ax[f]);
+                rv.v[f] = sum.bs[f].rounded();
+                pv.v[f] = d.v[f] * rv.v[f];
+                dots[f].add_prod(bv.v[f], bv.v[f]);
+                dots[NF + f].add_prod(rv.v[f], rv.v[f]);
+                dots[2 * NF + f].add_prod(rv.v[f], pv.v[f]);
+            }
+            a.b[row] = bv;
+            a.rb[0][row] = rv;  // iteration 0 reads parity 0
+            a.z[row] = pv;
+        });
+    if (!ok) flags |= FEA_STATUS_BREAKDOWN;
+    raise_flags(a.run, flags);
+    Acc<R> tot[3 * NF];
+    if (grid_reduce<R, 3 * NF>(dots, a.part, a.part_stride, a.tickets + 2, tot) && threadIdx.x == 0) {
+        CgState* cg = a.cg;
+        RunState* run = a.run;
+        const int stop = (atomicOr(&run->flags, 0u) & (FEA_STATUS_BLOWUP | FEA_STATUS_NONFINITE)) != 0;
+        cg->stop = stop;
+        cg->iter = 0;
+        cg->max_iter = run->max_iter;
+        int any = 0;
+#pragma unroll
+        for (int f = 0; f < NF; f++)
+            any |= start_solve<R>((volatile CgState*)cg, f, stop, run->tol, tot[f], tot[NF + f], tot[2 * NF + f]);
+        cg->pending = 0;
+        signal_loop(a, any != 0);
+    }
+}
+
+// Dynamic shared memory of k_rhs_gs_ring: the ring with the mass entries and
+// two staging buffers of kTileRows + hmax (reaction, start) pairs.
+template <typename R, int NF>
+size_t rhs_ring_smem_bytes(int emax, int hmax, int stages) {
+    return ring_bytes<R, NF>(emax, stages, sizeof(R)) + 2 * sizeof(GsStaged<R, NF>) * (size_t)(kTileRows + hmax);
+}
+
 // After the first CG loop: zero right-hand sides give x = 0 (Eigen's
 // early exit), then one true-residual pass r = b - A x.  Fields whose true
 // residual is still above the threshold restart CG from there.  The pass
@@ -1853,12 +1976,9 @@ __device__ __forceinline__ void refine_rows_ring(const StepArgs<R, NF>& a, bool 
     };
     // x is staged before this kernel zeroes a field: only zero fields change,
     // and their residuals go unused
-    const bool ok = ring_product_tiles<R, NF, S, AccRowSum<A, R, NF>>(
-        a, a.x, smem, bars,
-        [&](int row) {
-            const uint64_t pol = l2_evict_last_policy();
-            return Extra{ld_keep(a.b + row, pol), ld_keep(a.dinv + row, pol)};
-        },
+    const bool ok = ring_product_tiles<R, NF, S, AccRowSum<A, R, NF>, false>(
+        a, smem, bars, [&](int i, uint64_t pol) { return ld_keep(a.x + i, pol); }, [](const V& g) { return g; },
+        [&](int row, uint64_t pol) { return Extra{ld_keep(a.b + row, pol), ld_keep(a.dinv + row, pol)}; },
         [&](int row, const V& xr, const Extra& e, const AccRowSum<A, R, NF>& sum) {
             if (zany) a.x[row] = zeroed(xr);
             V rv, pv;
@@ -2019,7 +2139,7 @@ struct CgKernels {
     static Fn iter_par(int) { return iter; }
     static size_t smem_init(const StepArgs<R, NF>&) { return 0; }
     static size_t smem_iter(const StepArgs<R, NF>&) { return 0; }
-    static constexpr int kRefineStages = 0;  // the true-residual pass on CSR rows
+    static constexpr int kPassStages = 0;  // ring stages of the once-per-step passes (0: CSR / tile-ELL forms)
 };
 // Variants 0 and 1: the tile-ELL kernels with 8 or 4 entries per row
 // prefetched into registers; two staging buffers of kTileRows + hmax entries.
@@ -2033,7 +2153,7 @@ struct EllKernels {
         return 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
     }
     static size_t smem_iter(const StepArgs<R, NF>& a) { return smem_init(a); }
-    static constexpr int kRefineStages = 0;
+    static constexpr int kPassStages = 0;
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 0> : EllKernels<R, NF, 8> {};
@@ -2086,7 +2206,7 @@ struct RingKernels {
         return ring_smem_bytes<R, NF>(a.As_od ? a.emax_od : a.emax, a.hmax, S);
     }
     static size_t smem_init(const StepArgs<R, NF>& a) { return ring_smem_bytes<R, NF>(a.emax, a.hmax, S); }
-    static constexpr int kRefineStages = S;  // the true-residual pass on the ring too
+    static constexpr int kPassStages = S;  // right-hand side and true-residual pass on the ring too
 };
 template <typename R, int NF>
 struct CgKernels<R, NF, 14> : RingKernels<R, NF, 3, 2> {};
@@ -2096,20 +2216,28 @@ struct CgKernels<R, NF, 15> : RingKernels<R, NF, 4, 2> {};
 template <typename R, int NF>
 struct CgKernels<R, NF, 13> : DirectKernels<R, NF, (sizeof(FV<R, NF>) <= 8 ? 2 : 1)> {};
 
-// The right-hand side kernel of an equation: the staged tile-ELL form for
-// the mass-weighted Gray-Scott step when the layout exists, else k_rhs.
+// The right-hand side kernel of an equation: for the mass-weighted
+// Gray-Scott step on the tile-ELL layout, the ring form when the variant's
+// once-per-step passes run on the ring (ring_stages 3 or 4) and its shared
+// memory fits, else the staged tile-ELL form; otherwise k_rhs.
 template <typename R, int NF, int EQ>
 struct RhsKernel {
     using Fn = void (*)(StepArgs<R, NF>);
     Fn fn = k_rhs<R, NF, EQ, kRowLanes>;
     int grid = 0;
     size_t smem = 0;
-    explicit RhsKernel(const StepArgs<R, NF>& a) {
+    explicit RhsKernel(const StepArgs<R, NF>& a, int ring_stages = 0) {
         grid = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(a.N, (kBlock / kRowLanes))));
         if constexpr (EQ == EQ_GS_CONSISTENT && NF == 2) {
             if (a.Ms && a.As) {
-                fn = k_rhs_gs_ell<R, NF>;
-                smem = 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
+                const size_t ring = ring_stages ? rhs_ring_smem_bytes<R, NF>(a.emax, a.hmax, ring_stages) : 0;
+                if (ring_stages && ring <= kStreamSmemLimit) {
+                    fn = ring_stages == 4 ? k_rhs_gs_ring<R, NF, 4> : k_rhs_gs_ring<R, NF, 3>;
+                    smem = ring;
+                } else {
+                    fn = k_rhs_gs_ell<R, NF>;
+                    smem = 2 * sizeof(FV<R, NF>) * (size_t)(kTileRows + a.hmax);
+                }
                 grid = wave_grid(fn, ceil_div(a.N, kTileRows), smem);
             }
         }
@@ -2122,7 +2250,7 @@ struct Grids {
     using Fn = void (*)(StepArgs<R, NF>);
     int spmv, iter, rhs, stream, refine;
     size_t smem_init, smem_iter, smem_refine = 0;
-    Fn refine_k = k_refine<R, NF, kRowLanes, K::kRefineStages>;
+    Fn refine_k = k_refine<R, NF, kRowLanes, K::kPassStages>;
     explicit Grids(const StepArgs<R, NF>& a) {
         const int64_t N = a.N;
         smem_init = K::smem_init(a);
@@ -2133,8 +2261,8 @@ struct Grids {
         rhs = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, (kBlock / kRowLanes))));
         stream = (int)std::min<int64_t>(max_grid_blocks(), std::max<int64_t>(1, ceil_div(N, kBlock)));
         refine = rhs;
-        if constexpr (K::kRefineStages > 0) {
-            smem_refine = ring_smem_bytes<R, NF>(a.emax, a.hmax, K::kRefineStages);
+        if constexpr (K::kPassStages > 0) {
+            smem_refine = ring_smem_bytes<R, NF>(a.emax, a.hmax, K::kPassStages);
             refine = wave_grid(refine_k, ceil_div(N, kTileRows), smem_refine);
         }
     }
@@ -2190,7 +2318,7 @@ void build_graph_t(StepGraph& G, const StepArgs<R, NF>& base, LoopFlags* lf) {
     add_kernel(top, n, k_final_check<R, NF, EQ>, g.stream, kBlock, L.a);
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a1.cond, step_body, 0, 0));
     FEA_CUDA_TRY(cudaGraphConditionalHandleCreate(&L.a2.cond, step_body, 0, 0));
-    const RhsKernel<R, NF, EQ> rk(base);
+    const RhsKernel<R, NF, EQ> rk(base, K::kPassStages);
     cudaGraphNode_t s = add_kernel(step_body, nullptr, rk.fn, rk.grid, kBlock, L.a1, rk.smem);
     s = add_kernel(step_body, s, K::init, g.spmv, kBlock, L.a1, g.smem_init);
     cudaGraph_t body1, body2;
@@ -2220,9 +2348,9 @@ int read_flag(const int* d, cudaStream_t st) {
 template <typename R, int NF, int EQ, int WCH>
 void run_stream_t(const StepArgs<R, NF>& base, LoopFlags* lf, cudaStream_t st) {
     LoopArgs<R, NF> L(base, lf, 0);
-    const Grids<R, NF, WCH> g(base);
-    const RhsKernel<R, NF, EQ> rk(base);
     using K = CgKernels<R, NF, WCH>;
+    const Grids<R, NF, WCH> g(base);
+    const RhsKernel<R, NF, EQ> rk(base, K::kPassStages);
     k_start<R, NF><<<1, 1, 0, st>>>(L.a);
     FEA_CHECK_LAUNCH();
     while (read_flag(&lf->step, st)) {

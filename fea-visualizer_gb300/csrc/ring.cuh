@@ -72,23 +72,25 @@ __device__ __forceinline__ T ld_keep(const T* p, uint64_t pol) {
 // warp stages about the same share of a tile's halo.
 __device__ __forceinline__ int halo_slot(int t) { return (t & 7) * 32 + (t >> 3); }
 
-// One stage of the ring: a tile's operator entries, then its local columns.
+// One stage of the ring: a tile's operator entries, then (mv > 0) its mass
+// entries of mv bytes each, then its local columns.
 struct RingStage {
-    size_t A, L, bytes;
-    __host__ __device__ RingStage(int emax, size_t fv) {
+    size_t A, M, L, bytes;
+    __host__ __device__ RingStage(int emax, size_t fv, size_t mv = 0) {
         auto al = [](size_t x) { return (x + 127) & ~(size_t)127; };
         A = 0;
-        L = al(fv * (size_t)emax);
+        M = al(fv * (size_t)emax);
+        L = al(M + mv * (size_t)emax);
         bytes = al(L + 2 * (size_t)emax);
     }
 };
 
 // Dynamic shared memory of the single-mesh ring kernels: the ring (which the
 // end-of-launch reduction reuses once every copy has landed); the two u'
-// buffers follow it.
+// buffers follow it.  mv: bytes of a mass entry in the stages (0: none).
 template <typename R, int NF>
-__host__ __device__ size_t ring_bytes(int emax, int stages) {
-    const size_t ring = (size_t)stages * RingStage(emax, sizeof(FV<R, NF>)).bytes;
+__host__ __device__ size_t ring_bytes(int emax, int stages, size_t mv = 0) {
+    const size_t ring = (size_t)stages * RingStage(emax, sizeof(FV<R, NF>), mv).bytes;
     const size_t red = (size_t)3 * NF * kBlock * sizeof(typename Acc<R>::Packed);
     return (ring > red ? ring : red + 127) & ~(size_t)127;
 }
