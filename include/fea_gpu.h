@@ -190,9 +190,10 @@ int fea_clear_values(fea_solver* s);
  * set copies values[idx] of unknown points in (get_surface_value_vector,
  * CPUSolver.cpp:13-21), get writes every point, Dirichlet points as 0
  * (map_vector_to_surface, CPUSolver.cpp:28-37).  Both return once the
- * values are in place.  A page-locked host buffer (cudaHostAlloc,
- * cudaHostRegister) is read or written in place by the device; other host
- * memory goes through a staging copy. */
+ * values are in place.  A page-locked host buffer that the device can map
+ * (cudaHostAlloc, cudaHostRegister with cudaHostRegisterMapped) is read or
+ * written in place by the device; other host memory goes through a staging
+ * copy. */
 int fea_set_values(fea_solver* s, const float* values);
 int fea_get_values(fea_solver* s, float* values);
 
