@@ -12,8 +12,9 @@ u = 1, v = 0 with 20 squares of side 0.05 at u = 0.5, v = 0.25, plus U(-0.01,
 Prints one JSON line (rank 0).  `value` times each step on the device with
 CUDA events on the solver's stream, with the L2 cache flushed (256 MiB write)
 before every timed step; `e2e` times set_values (host -> device) +
-advance_time(1) + get_values (device -> host) through the C ABI with
-page-locked host buffers.  With --gpus N > 1 (torchrun) every rank steps its
+advance_time(1) + get_values (device -> host) through the C ABI with a
+page-locked host buffer, over the same steps (same start state and
+extrapolation history).  With --gpus N > 1 (torchrun) every rank steps its
 own replica of the workload: the path does not shard across GPUs.
 """
 from __future__ import annotations
